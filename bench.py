@@ -1,0 +1,344 @@
+"""Benchmark of the MLFMA solve on GB300: FP64 MLFMA matvecs/s and time-to-RCS.
+
+Workload (default): PEC sphere of radius 6 lambda at lambda = 1 m, icosphere
+subdivided 6 times (81920 triangles, 122880 RWG unknowns), octree leaves
+criterio_ladomax = 0.25 lambda (7 levels, L 51/31/20/13/9), plain FP64
+MLFMA matvec as in the reference.  Synthetic mesh, seeded random
+complex-Gaussian input vectors.  A step is one matvec over one right-hand
+side; the working set (1.27 GB of radiation patterns, 0.58 GB of fields,
+0.15 GB of near field) is far larger than L2, so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's algorithm
+(the reference itself is Fortran with no compiler here) on the host cores
+with all threads, on the same workload, and prints the same JSON line.
+Under torchrun each rank runs an independent replica (the solve does not
+shard); value = matvecs of all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time-to-RCS & MLFMA matvec/s at 123k RWG, rel.res 1e-4, ≤0.1 dB vs FP64 plain"
+WORKLOADS = {
+    "sphere6": dict(level=6, radius=6.0, lam=1.0, ladomax=0.25,
+                    name="PEC sphere r=6 lambda, icosphere-6 (81920 tri, 122880 RWG), leaf 0.25 lambda, FP64"),
+    "sphere5": dict(level=5, radius=3.0, lam=1.0, ladomax=0.25,
+                    name="PEC sphere r=3 lambda, icosphere-5 (20480 tri, 30720 RWG), leaf 0.25 lambda, FP64"),
+}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    lrank = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, lrank
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 rate of this GPU: cuBLAS DGEMM 4096^3, best of 5 (library roof, like the
+    copy and bf16 GEMM roofs of the measured-peaks file)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def build_problem(wl):
+    from lywell_gb300 import meshes
+    return meshes.icosphere(wl["level"], wl["radius"])
+
+
+def run_reference(args, wl):
+    """CPU restatement of the reference (oracle/), all host threads, bounded sample."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    from oracle import core
+    from oracle.rwg import RWG as ORWG
+    ncores = os.cpu_count() or 1
+    core.set_threads(ncores)
+    tris = build_problem(wl)
+    t0 = time.time()
+    o = core.OracleMLFMA(ORWG(tris), lam=wl["lam"], ladomax=wl["ladomax"])
+    setup = time.time() - t0
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(o.N) + 1j * rng.standard_normal(o.N)
+    for _ in range(max(1, min(args.warmup, 1))):
+        o.matvec(x)
+    steps = max(1, min(args.steps, 3))
+    t0 = time.time()
+    for _ in range(steps):
+        o.matvec(x)
+    dt = (time.time() - t0) / steps
+    v = 1.0 / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "matvec/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": 1, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": wl["name"], "N": o.N, "levels": o.nlev},
+            "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": core.get_threads(), "kind": "port",
+                             "sample": f"{steps} FP64 MLFMA matvecs after {setup:.1f}s set-up"},
+            "e2e": {"value": v, "unit": "matvec/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(wl, budget_steps=2):
+    from oracle import core
+    from oracle.rwg import RWG as ORWG
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    core.set_threads(os.cpu_count() or 1)
+    tris = build_problem(wl)
+    t0 = time.time()
+    o = core.OracleMLFMA(ORWG(tris), lam=wl["lam"], ladomax=wl["ladomax"])
+    setup = time.time() - t0
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(o.N) + 1j * rng.standard_normal(o.N)
+    o.matvec(x)
+    t0 = time.time()
+    for _ in range(budget_steps):
+        o.matvec(x)
+    dt = (time.time() - t0) / budget_steps
+    return {"value": 1.0 / dt, "unit": "matvec/s", "cores": core.get_threads(), "kind": "port",
+            "sample": f"{budget_steps} FP64 MLFMA matvecs of the same workload after a {setup:.1f}s set-up"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="sphere6", choices=list(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-time-to-rcs", action="store_true")
+    ap.add_argument("--rcs-maxit", type=int, default=1500)
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+        return
+
+    import torch
+    ws, rank, lrank = _dist()
+    torch.cuda.set_device(lrank)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", lrank))
+    from lywell_gb300 import MLFMA, RWG, ajustar_polariz, direction
+
+    tris = build_problem(wl)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    rwg = RWG(tris)
+    m = MLFMA(rwg, lam=wl["lam"], ladomax=wl["ladomax"])
+    torch.cuda.synchronize()
+    setup_s = time.time() - t0
+    N = m.N
+    rng = np.random.default_rng(rank)
+    xh = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    x = torch.from_numpy(xh).to("cuda")
+    y = torch.empty_like(x)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def step():
+        m.matvec_device(x.data_ptr(), y.data_ptr(), 1, stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    cnt = m.algorithmic_counts()
+    clocks = ClockSampler(lrank)
+    clocks.start()
+    time.sleep(0.3)
+    m.set_profiling(True)
+    stage = np.zeros(5)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+        stage += m.stage_times()
+    e1.record()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    m.set_profiling(False)
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    if ws > 1:
+        tt = torch.tensor([t], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    value = ws * args.steps / t
+    stage_ms = stage / args.steps
+
+    # end to end through the public host API: pinned host x -> device -> host y
+    xp = torch.from_numpy(xh).pin_memory()
+    yp = torch.empty_like(xp).pin_memory()
+    import ctypes
+    from lywell_gb300 import _capi
+    lib = _capi.load()
+    for _ in range(2):
+        lib.mlf_matvec(m.handle, ctypes.c_void_p(xp.data_ptr()), ctypes.c_void_p(yp.data_ptr()), 1, N)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc = lib.mlf_matvec(m.handle, ctypes.c_void_p(xp.data_ptr()), ctypes.c_void_p(yp.data_ptr()), 1, N)
+        assert rc == 0
+    t_e2e = time.perf_counter() - t0
+    e2e = ws * args.steps / t_e2e if ws == 1 else args.steps / t_e2e * ws
+
+    # roofline of the dominant stage (translation) against the FP64 roof, HBM beside it
+    fp64 = fp64_peak_tflops(torch)
+    hbm, hbm_kind = measured_peaks()
+    tr_s = stage_ms[2] / 1e3
+    tr_flops = cnt["flops"]["translation"]
+    achieved = tr_flops / tr_s / 1e12
+    total_tflops = cnt["flops_total"] / (t / args.steps * ws) / 1e12
+    roof = {"bound": "fp64", "kernel": "k_translate (5 launches/matvec)", "achieved": achieved, "peak": fp64,
+            "unit": "TFLOP/s", "frac": achieved / fp64, "traffic": None,
+            "peak_source": "measured here: cuBLAS DGEMM 4096^3 (GB300 FP64 pipe)",
+            "algorithmic_flops_per_matvec": tr_flops,
+            "hbm": {"achieved_gbs": cnt["translation_bytes"] / tr_s / 1e9, "peak_gbs": hbm,
+                    "peak_source": hbm_kind,
+                    "frac": cnt["translation_bytes"] / tr_s / 1e9 / hbm},
+            "matvec": {"flops": cnt["flops_total"], "bytes": cnt["bytes_total"],
+                       "achieved_tflops": total_tflops, "frac_fp64": total_tflops / fp64,
+                       "achieved_gbs": cnt["bytes_total"] / (t / args.steps * ws) / 1e9,
+                       "frac_hbm": cnt["bytes_total"] / (t / args.steps * ws) / 1e9 / hbm},
+            "stage_ms": {"aggregation": stage_ms[0], "interpolation": stage_ms[1], "translation": stage_ms[2],
+                         "anterpolation": stage_ms[3], "receive_near": stage_ms[4]}}
+
+    # time to RCS: set-up + CGS to 1e-4 + bistatic RCS cuts (phi = 0 and 90 deg, theta 0..180 step 1)
+    ttr = None
+    if not args.no_time_to_rcs:
+        torch.cuda.synchronize()
+        t0 = time.time()
+        m2 = MLFMA(RWG(tris), lam=wl["lam"], ladomax=wl["ladomax"])
+        t_setup = time.time() - t0
+        d = np.array([0.0, 0.0, 1.0])      # x-polarised wave incident from -z (propagating along +z)
+        pol = np.array([1.0, 0, 0], dtype=np.complex128)
+        t1 = time.time()
+        b = m2.excitation(d, pol)
+        out = m2.cgs(b, errmax=1e-4, maxit=args.rcs_maxit)
+        t_solve = time.time() - t1
+        th = np.deg2rad(np.arange(0, 181, 1.0))
+        t2 = time.time()
+        s0 = m2.rcs(out["x"], pol, th, np.zeros_like(th))
+        s9 = m2.rcs(out["x"], pol, th, np.full_like(th, np.pi / 2))
+        t_rcs = time.time() - t2
+        ttr = {"seconds": t_setup + t_solve + t_rcs, "setup_s": t_setup, "solve_s": t_solve, "rcs_s": t_rcs,
+               "cgs_iters": out["iters"], "cgs_status": out["status"], "relres": out["relres"],
+               "precond": "none", "rcs_angles": int(2 * th.size),
+               "rcs_db_phi0_mid": float(10 * np.log10(s0[90])), "rcs_db_phi90_mid": float(10 * np.log10(s9[90]))}
+        m2.close()
+
+    launches_per_matvec = 1 + (m.nlev - 3) + (m.nlev - 2) + (m.nlev - 3) + 1
+    line = {"metric": METRIC, "value": value, "unit": "matvec/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": wl["name"], "N": N, "levels": m.nlev,
+                       "samples_per_level": [m.levels[l]["K"] for l in range(3, m.nlev + 1)],
+                       "near_nnz": m.nnz, "parallelism": f"replicas x{ws}",
+                       "l2": "inputs larger than L2 (patterns 1.27 GB streamed per matvec)"},
+            "e2e": {"value": e2e, "unit": "matvec/s", "h2d_bytes_per_step": N * 16, "d2h_bytes_per_step": N * 16},
+            "roofline": roof, "clocks": clk, "gpu_launches": launches_per_matvec * args.steps,
+            "setup_s": setup_s, "time_to_rcs": ttr}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(wl)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    m.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+/*
+ * lywell_mlfma.h — C ABI of the GB300 (sm_103a) MLFMA iterative solve.
+ *
+ * A drop-in for MLFMAxwell's solve path (gabsantamaria/lywell, Fortran 90):
+ * the MLFMA matvec of modMLFMA, CGS + ILU0 of modIterativo and the RCS
+ * far-field sum of modRCS.  Every entry point takes plain pointers and sizes
+ * (no torch or CUDA types), returns an int status (MLF_OK = 0) and never
+ * prints.  A Fortran host binds these with ISO_C_BINDING; the interface
+ * module is shipped as lywell_gb300/fortran/lywell_mlfma_cabi.f90.
+ *
+ * Conventions
+ *  - Complex numbers are interleaved (re, im) doubles: a complex(8) array of
+ *    length n is `double[2n]`, exactly Fortran's complex(kind=8) layout.
+ *  - Geometry arrays are Fortran column-major, e.g. e_centro(3, N) is
+ *    `double[3*N]` with the three coordinates of edge i at [3i .. 3i+2].
+ *  - Index arrays are 1-based int32, matching Fortran integer(4).
+ *  - Multi-RHS blocks are column-major (n x nrhs) with leading dimension ld.
+ *  - A context is bound to the CUDA device that was current at mlf_init and
+ *    owns one CUDA stream; calls on one context must not overlap.
+ */
+#ifndef LYWELL_MLFMA_H
+#define LYWELL_MLFMA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mlf_ctx mlf_ctx;
+
+enum {
+    MLF_OK = 0,
+    MLF_E_ARG = -1,        /* invalid argument */
+    MLF_E_TOO_SMALL = -2,  /* nivel_max <= 3: the reference stops here (modMLFMA.f90:195-198) */
+    MLF_E_CUDA = -3,       /* CUDA runtime error (message in mlf_last_error) */
+    MLF_E_NOMEM = -4,
+    MLF_E_TABLE = -5,      /* more than 316 distinct translation vectors on a level */
+    MLF_E_STATE = -6,      /* e.g. ILU0 apply before a successful mlf_ilu0 */
+    MLF_E_NOT_FINITE = -7, /* NaN/Inf met in the solver */
+    MLF_E_NO_DEVICE = -8
+};
+
+/* mlf_cgs outcome codes (written to *status_out) */
+enum {
+    MLF_CGS_CONVERGED = 0,
+    MLF_CGS_MAXIT = 1,
+    MLF_CGS_BREAKDOWN = 2,   /* rho == 0: the reference exits silently (modIterativo.f90:392-395) */
+    MLF_CGS_NOT_FINITE = 3,
+    MLF_CGS_STAGNATED = 4    /* no progress over the stagnation window */
+};
+
+/* mlf_init flags */
+enum {
+    MLF_FLAG_LEGENDRE_RECURRENCE = 1 /* P_l by the three-term recurrence instead of the
+                                        reference's explicit binomial sum */
+};
+
+/* Build the RWG basis from a triangle soup, reproducing the reference's
+ * edge order (modRWG.f90:8-174, modReadStl.f90:1444-1533) and triangle
+ * geometry (modRWG.f90:270-328).  Call once with all outputs NULL to get
+ * *N_out and *P_out, then again with arrays of these sizes:
+ *   p_coord(3,P) t_p(3,T) e_p(2,N) e_t(2,N) e_po(2,N) e_long(N) e_centro(3,N)
+ *   t_area(T) t_baric(3,T) t_baric_sub(3,9,T)        (index arrays 1-based)
+ * tris: double[T*9], triangle-major, vertex, xyz (the order of an STL file).
+ * Replaces: cap_geom (main.f90:1430-1468) -> obtener_p_t, parametros_rwg,
+ * hallar_geometria_rwg. */
+int mlf_rwg_build(const double* tris, int T, int* N_out, int* P_out,
+                  double* p_coord, int* t_p, int* e_p, int* e_t, int* e_po,
+                  double* e_long, double* e_centro, double* t_area,
+                  double* t_baric, double* t_baric_sub);
+
+/* Set up the octree, sampling, interpolation and translation tables,
+ * radiation patterns and the complex(4) near-field CSR on the current CUDA
+ * device.  Copies what it needs; the caller keeps ownership of the arrays.
+ * lambda: wavelength in metres (global `lambda`, setlambda in
+ * modGlobalParam.f90:52-61); ladomax: conf%criterio_ladomax.
+ * t_area, t_p, e_p and t_normal are accepted for signature parity and not
+ * needed (t_normal only enters the reference through (1-alphaCFIE) = 0).
+ * Replaces: inicializar_MLFMA (modMLFMA.f90:113-275). */
+int mlf_init(mlf_ctx** ctx, const double* e_centro, int N, const int* e_t, const int* e_po,
+             const double* e_long, const double* t_area, const double* t_baric,
+             const double* t_baric_sub, const double* p_coord, const int* t_p, const int* e_p,
+             int P, int T, const double* t_normal, double lambda, double ladomax, int flags);
+
+/* Release the context.  Replaces: destruir_MLFMA (modMLFMA.f90:85-110). */
+void mlf_free(mlf_ctx* ctx);
+
+/* Last error message of the context (or of the last failed mlf_init when
+ * ctx is NULL). */
+const char* mlf_last_error(const mlf_ctx* ctx);
+
+/* y = Z_MLFMA x for nrhs columns, host arrays (complex(8), n x nrhs, ld >= N).
+ * Includes the host<->device copies.
+ * Replaces: MatxVec_MLFMA (modMLFMA.f90:1901-1946). */
+int mlf_matvec(mlf_ctx* ctx, const double* x, double* y, int nrhs, int ld);
+
+/* Same on device-resident arrays; stream NULL = the context's stream. */
+int mlf_matvec_device(mlf_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, int ld,
+                      void* stream);
+
+/* Near-field block in CSR (1-based), values complex(4) interleaved floats.
+ * Call with a/ja/ia NULL to get *nnz.  Replaces the public module data
+ * Zesparcida_MLFMA, ja_MLFMA, ia_MLFMA, n_esparcida_MLFMA (modMLFMA.f90:12, 30-32). */
+int mlf_near_csr(mlf_ctx* ctx, long long* nnz, float* a, int* ja, int* ia);
+
+/* ILU(0) of the near-field block, complex(4) factors kept on the device.
+ * *ierr_row = 0 on success, k > 0 when a zero pivot was met at row k.
+ * Replaces: crear_precond ILU0 branch (main.f90:851-902) -> ilu0C
+ * (modIterativo.f90:1805-1976). */
+int mlf_ilu0(mlf_ctx* ctx, int* ierr_row);
+
+/* Export the ILU0 factors in the reference's MSR layout (alu: complex(4)
+ * interleaved, nnz+1 entries; jlu: nnz+1; ju: N; 1-based). */
+int mlf_ilu0_factors(mlf_ctx* ctx, float* alu, int* jlu, int* ju);
+
+/* x = (LU)^-1 y for nrhs host columns.  Replaces: lusol0C
+ * (modIterativo.f90:504-560). */
+int mlf_ilu0_solve(mlf_ctx* ctx, const double* y, double* x, int nrhs);
+
+/* Right-preconditioned CGS on the MLFMA operator, one or more right-hand
+ * sides (each solved with its own scalars; converged columns retire).
+ * b, x0, x: host complex(8) n x nrhs (ld = N).  x0 may be NULL (zero guess).
+ * precond_kind: 0 none, 1 ILU0 (mlf_ilu0 must have succeeded).
+ * maxit: iteration cap (the reference has none).  Per column outputs:
+ * iters[nrhs], relres[nrhs] (true-recursion residual ||r||/||b||),
+ * status_out[nrhs] (MLF_CGS_*).
+ * Replaces: CGSold (modIterativo.f90:331-493). */
+int mlf_cgs(mlf_ctx* ctx, const double* b, const double* x0, double tol, int maxit, int nrhs,
+            double* x, int* iters, double* relres, int precond_kind, int* status_out);
+
+/* Plane-wave excitation b(N) for nrhs waves: dirs(3,nrhs) propagation
+ * directions, pols(3,nrhs) complex polarisations, ctte complex amplitude.
+ * Replaces: generar_onda (main.f90:1488-1525). */
+int mlf_excitation(mlf_ctx* ctx, const double* dirs, const double* pols, double ctte_re,
+                   double ctte_im, int nrhs, double* b);
+
+/* sigma(theta_a, phi_a) (linear, m^2) of the current I(N) for nang angles,
+ * polarisation pol(3) complex and amplitude ctte as given to
+ * inicializar_RCS.  Replaces: inicializar_RCS + sigmaRCS + calc_RCS +
+ * calc_E (modRCS.f90:23-153). */
+int mlf_rcs(mlf_ctx* ctx, const double* I, const double* pol, double ctte_re, double ctte_im,
+            const double* theta, const double* phi, int nang, double* sigma);
+
+/* Octree summary for hosts and tests: out[0] = number of levels, out[1] = N;
+ * for level l (1-based) out[5l .. 5l+4] = boxes, multipoles L, samples K,
+ * distinct translation vectors, far-interaction pairs.  out must hold
+ * 5*(levels+1) ints (160 always suffices). */
+int mlf_info(mlf_ctx* ctx, int* out, long long* nnz_near);
+
+/* Per-stage device timings of the last mlf_matvec[_device] in ms:
+ * out[0] aggregation, [1] interpolation, [2] translation, [3] anterpolation,
+ * [4] receive + near.  Only filled when profiling is on (mlf_set_profiling). */
+int mlf_set_profiling(mlf_ctx* ctx, int on);
+int mlf_stage_times(mlf_ctx* ctx, float* out5);
+
+/* Copy the C / B / A field of one level (complex(8), K x 2 x boxes,
+ * the reference's campoC/campoB/campoA layout) after the last matvec.
+ * which: 0 = C, 1 = B, 2 = A.  For parity checks of single stages. */
+int mlf_debug_field(mlf_ctx* ctx, int level, int which, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

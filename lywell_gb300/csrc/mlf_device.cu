@@ -1,0 +1,618 @@
+// Device side of the MLFMA solve on one GB300 (sm_103a).
+//
+// GB300 runs FP64 at about 1/64 of its FP32 rate, so the plain-FP64 matvec is
+// bound by the FP64 pipe, not by HBM.  The kernels therefore keep every
+// double-precision instruction that is not part of the algorithm's own
+// arithmetic off the hot path: phase shifts between levels come from
+// precomputed per-octant tables (no sincos), indices are integer, reductions
+// use warp shuffles, and each complex multiply-add is four DFMA.
+//
+// Set-up kernels (once per context):
+//   k_patterns      radiation patterns R (calcRad, modMLFMA.f90:584-703)
+//   k_translation   T_n(k) per distinct displacement (calc_functransf,
+//                   modMLFMA.f90:964-994), Legendre sum in IEEE round-to-nearest
+//                   steps in the oracle's order
+//   k_near          complex(4) near-field block (Zmn_MoM, modMoM.f90:85-128)
+// Matvec kernels (MatxVec_MLFMA, modMLFMA.f90:1901-1946):
+//   k_aggregate     leaf C = sum_n R_n x_n                (:1805-1811)
+//   k_interp_up     parent C += shift * Interpolar(child C) (:1818-1831)
+//   k_translate     B = w * sum_far C_src T                (:1838-1853)
+//   k_anterp_down   A = B + Anterpolar(shift* parent A|B)  (:1857-1897)
+//   k_receive_near  y = fac sum conj(R) A + Znear x        (:1915-1942)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "mlf_internal.h"
+
+namespace mlf {
+
+bool cuda_ok(Ctx* c, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    c->err = buf;
+    return false;
+}
+
+#define CK(call)                                   \
+    do {                                           \
+        if (!cuda_ok(c, (call), #call)) return MLF_E_CUDA; \
+    } while (0)
+
+template <class T>
+static int upload(Ctx* c, T** dst, const std::vector<T>& v) {
+    const size_t n = std::max<size_t>(v.size(), 1);
+    CK(cudaMalloc((void**)dst, n * sizeof(T)));
+    if (!v.empty()) CK(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return MLF_OK;
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ void cmac(double2& acc, double2 a, double2 b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+
+// ---------------------------------------------------------------------------
+// set-up kernels
+// ---------------------------------------------------------------------------
+
+// R[j][p][k], j = position in the leaf-box-sorted basis list.
+__global__ void k_patterns(int K, const int* __restrict__ bases, const int* __restrict__ box_of_sorted,
+                           const double* __restrict__ centres, const double* __restrict__ t_baric,
+                           const double* __restrict__ p_coord, const int* __restrict__ e_t,
+                           const int* __restrict__ e_po, const double* __restrict__ e_long,
+                           const double* __restrict__ kap, const double* __restrict__ ath,
+                           const double* __restrict__ aph, double ka, double2* __restrict__ R) {
+    const int j = blockIdx.y;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const int n = bases[j];
+    const double* C = centres + 3 * box_of_sorted[j];
+    const double* bp = t_baric + 3 * e_t[2 * n];
+    const double* vp = p_coord + 3 * e_po[2 * n];
+    const double* bm = t_baric + 3 * e_t[2 * n + 1];
+    const double* vm = p_coord + 3 * e_po[2 * n + 1];
+    const double lon = e_long[n];
+    const double* kk = kap + 3 * k;
+    const double ap = ka * (kk[0] * (bp[0] - C[0]) + kk[1] * (bp[1] - C[1]) + kk[2] * (bp[2] - C[2]));
+    const double am = ka * (kk[0] * (bm[0] - C[0]) + kk[1] * (bm[1] - C[1]) + kk[2] * (bm[2] - C[2]));
+    double sp, cp, sm, cm;
+    sincos(ap, &sp, &cp);
+    sincos(am, &sm, &cm);
+    double2 v0 = make_double2(0, 0), v1 = make_double2(0, 0);
+    const double* at = ath + 3 * k;
+    const double* af = aph + 3 * k;
+    for (int d = 0; d < 3; ++d) {
+        const double rp = bp[d] - vp[d], rm = vm[d] - bm[d];
+        const double vr = ((cp * rp + cm * rm) * lon) * 0.5;
+        const double vi = ((sp * rp + sm * rm) * lon) * 0.5;
+        v0.x += vr * at[d]; v0.y += vi * at[d];
+        v1.x += vr * af[d]; v1.y += vi * af[d];
+    }
+    R[(size_t)j * 2 * K + k] = v0;
+    R[(size_t)j * 2 * K + K + k] = v1;
+}
+
+// T[t][k] = s * sum_{l<=Lt} c_l P_l(khat_k . u_t), c_l = (-j)^(l+1) (2l+1) h_l(kD).
+// Legendre by the explicit binomial-square sum with round-to-nearest
+// intrinsics (no contraction), or by the three-term recurrence.
+__global__ void k_translation(int K, const double* __restrict__ kap, const double* __restrict__ u,
+                              const int* __restrict__ Lt, const double2* __restrict__ coef, int ldc,
+                              const double* __restrict__ binom2, int ldb, double scale, int mode,
+                              double2* __restrict__ T) {
+    const int t = blockIdx.y;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const double* kk = kap + 3 * k;
+    const double* ut = u + 3 * t;
+    const double x = __dadd_rn(__dadd_rn(__dmul_rn(kk[0], ut[0]), __dmul_rn(kk[1], ut[1])),
+                               __dmul_rn(kk[2], ut[2]));
+    const int L = Lt[t];
+    const double2* cf = coef + (size_t)t * ldc;
+    double vr = 0., vi = 0.;
+    if (mode == 1) {
+        double pm = 1.0, pc = x;
+        for (int l = 0; l <= L; ++l) {
+            const double P = l == 0 ? 1.0 : pc;
+            vr = __dadd_rn(vr, __dmul_rn(cf[l].x, P));
+            vi = __dadd_rn(vi, __dmul_rn(cf[l].y, P));
+            if (l >= 1) {
+                const double nx = ((2.0 * l + 1.0) * x * pc - l * pm) / (l + 1.0);
+                pm = pc;
+                pc = nx;
+            }
+        }
+    } else {
+        double pa[128], pb[128];
+        const double a = __dadd_rn(x, 1.0), b = __dadd_rn(x, -1.0);
+        pa[0] = 1.0; pb[0] = 1.0;
+        for (int q = 1; q <= L; ++q) { pa[q] = __dmul_rn(pa[q - 1], a); pb[q] = __dmul_rn(pb[q - 1], b); }
+        for (int l = 0; l <= L; ++l) {
+            const double* bn = binom2 + (size_t)l * ldb;
+            double r = 0.;
+            for (int i = 0; i <= l; ++i) r = __dadd_rn(r, __dmul_rn(__dmul_rn(bn[i], pa[l - i]), pb[i]));
+            const double P = ldexp(r, -l);
+            vr = __dadd_rn(vr, __dmul_rn(cf[l].x, P));
+            vi = __dadd_rn(vi, __dmul_rn(cf[l].y, P));
+        }
+    }
+    T[(size_t)t * K + k] = make_double2(__dmul_rn(vr, scale), __dmul_rn(vi, scale));
+}
+
+__device__ __forceinline__ double2 green(double w_smue, const double* a, const double* b) {
+    const double d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2];
+    const double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    double s, co;
+    sincos(w_smue * r, &s, &co);
+    const double ir = 1.0 / r;
+    return make_double2(co * ir, -s * ir);
+}
+
+// One block per row m, threads over the row's near columns.
+__global__ void k_near(const int* __restrict__ ia, const int* __restrict__ ja,
+                       const double* __restrict__ t_baric, const double* __restrict__ t_baric_sub,
+                       const double* __restrict__ p_coord, const int* __restrict__ e_t,
+                       const int* __restrict__ e_po, const double* __restrict__ e_long, double w,
+                       double w_smue, double c72, float2* __restrict__ Z) {
+    const int m = blockIdx.x;
+    const int beg = ia[m], end = ia[m + 1];
+    const double* cpm = t_baric + 3 * e_t[2 * m];
+    const double* cmm = t_baric + 3 * e_t[2 * m + 1];
+    const double* vpm = p_coord + 3 * e_po[2 * m];
+    const double* vmm = p_coord + 3 * e_po[2 * m + 1];
+    const double lm = e_long[m];
+    for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
+        const int n = ja[q];
+        const int tpn = e_t[2 * n], tmn = e_t[2 * n + 1];
+        const double* vpn = p_coord + 3 * e_po[2 * n];
+        const double* vmn = p_coord + 3 * e_po[2 * n + 1];
+        double2 AP[3] = {{0, 0}, {0, 0}, {0, 0}}, AM[3] = {{0, 0}, {0, 0}, {0, 0}};
+        double2 PhiP = {0, 0}, PhiM = {0, 0};
+        for (int i = 0; i < 9; ++i) {
+            const double* sp = t_baric_sub + 27 * (size_t)tpn + 3 * i;
+            const double* sm = t_baric_sub + 27 * (size_t)tmn + 3 * i;
+            const double2 g11 = green(w_smue, cpm, sp), g12 = green(w_smue, cpm, sm);
+            const double2 g21 = green(w_smue, cmm, sp), g22 = green(w_smue, cmm, sm);
+            for (int d = 0; d < 3; ++d) {
+                const double r1 = sp[d] - vpn[d], r2 = vmn[d] - sm[d];
+                AP[d].x += g11.x * r1 + g12.x * r2; AP[d].y += g11.y * r1 + g12.y * r2;
+                AM[d].x += g21.x * r1 + g22.x * r2; AM[d].y += g21.y * r1 + g22.y * r2;
+            }
+            PhiP.x += g11.x - g12.x; PhiP.y += g11.y - g12.y;
+            PhiM.x += g21.x - g22.x; PhiM.y += g21.y - g22.y;
+        }
+        const double ln = e_long[n];
+        const double fa = ((MU / PI) * c72) * ln;
+        const double den = ((36 * PI) * w) * EPSI;
+        // Phi = -Phi*l_n / (j den) = (-Im*l_n/den... ) written out
+        const double tPx = -PhiP.x * ln, tPy = -PhiP.y * ln, tMx = -PhiM.x * ln, tMy = -PhiM.y * ln;
+        const double2 P2 = make_double2(tPy / den, -tPx / den), M2 = make_double2(tMy / den, -tMx / den);
+        double2 s = {0, 0};
+        for (int d = 0; d < 3; ++d) {
+            const double a1 = cpm[d] - vpm[d], a2 = -cmm[d] + vmm[d];
+            s.x += AP[d].x * fa * a1 + AM[d].x * fa * a2;
+            s.y += AP[d].y * fa * a1 + AM[d].y * fa * a2;
+        }
+        const double fz = (0.5 * w) * lm;
+        const double2 PintA = make_double2(-fz * s.y, fz * s.x);
+        const double2 PintPhi = make_double2(lm * (M2.x - P2.x), lm * (M2.y - P2.y));
+        Z[q] = make_float2((float)(PintPhi.x + PintA.x), (float)(PintPhi.y + PintA.y));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// matvec kernels.  Fields carry nrhs columns: F[(box*nrhs + r)*2K + p*K + k].
+// ---------------------------------------------------------------------------
+
+// blockIdx.x = box*nrhs + r
+__global__ void k_aggregate(int K, int nrhs, int ld, const int* __restrict__ box_ptr,
+                            const int* __restrict__ perm, const double2* __restrict__ R,
+                            const double2* __restrict__ x, double2* __restrict__ C) {
+    const int b = blockIdx.x / nrhs, r = blockIdx.x % nrhs;
+    const int j0 = box_ptr[b], j1 = box_ptr[b + 1];
+    const double2* xr = x + (size_t)r * ld;
+    for (int q = threadIdx.x; q < 2 * K; q += blockDim.x) {
+        double2 acc = make_double2(0, 0);
+        for (int j = j0; j < j1; ++j) cmac(acc, R[(size_t)j * 2 * K + q], xr[perm[j]]);
+        C[((size_t)b * nrhs + r) * 2 * K + q] = acc;
+    }
+}
+
+// parent level (coarse) Kp samples, child level Kc; blockIdx.x = (parent*nrhs + r)*nchunk + chunk
+__global__ void k_interp_up(int Kp, int Kc, int nrhs, int nchunk, const int* __restrict__ child_ptr,
+                            const int* __restrict__ octant, const double* __restrict__ iw,
+                            const int* __restrict__ iidx, const double2* __restrict__ shift,
+                            const double2* __restrict__ Cc, double2* __restrict__ Cp) {
+    const int chunk = blockIdx.x % nchunk;
+    const int pr = blockIdx.x / nchunk;
+    const int P = pr / nrhs, r = pr % nrhs;
+    const int q = chunk * blockDim.x + threadIdx.x;
+    if (q >= 2 * Kp) return;
+    const int pol = q >= Kp, m = q - pol * Kp;
+    double w9[9];
+    int i9[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) { w9[t] = iw[9 * m + t]; i9[t] = iidx[9 * m + t] + pol * Kc; }
+    double2 acc = make_double2(0, 0);
+    for (int cb = child_ptr[P]; cb < child_ptr[P + 1]; ++cb) {
+        const double2* src = Cc + ((size_t)cb * nrhs + r) * 2 * Kc;
+        double2 v = make_double2(0, 0);
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            const double2 s = src[i9[t]];
+            v.x = fma(w9[t], s.x, v.x);
+            v.y = fma(w9[t], s.y, v.y);
+        }
+        cmac(acc, v, shift[octant[cb] * Kp + m]);
+    }
+    Cp[((size_t)P * nrhs + r) * 2 * Kp + q] = acc;
+}
+
+// blockIdx.x = (box*nrhs + r)*nchunk + chunk
+__global__ void k_translate(int K, int nrhs, int nchunk, const int* __restrict__ far_ptr,
+                            const int* __restrict__ far_src, const int* __restrict__ far_tid,
+                            const double2* __restrict__ T, const double* __restrict__ wq,
+                            const double2* __restrict__ C, double2* __restrict__ B) {
+    const int chunk = blockIdx.x % nchunk;
+    const int br = blockIdx.x / nchunk;
+    const int b = br / nrhs, r = br % nrhs;
+    const int q = chunk * blockDim.x + threadIdx.x;
+    if (q >= 2 * K) return;
+    const int k = q >= K ? q - K : q;
+    double2 acc = make_double2(0, 0);
+    const int f1 = far_ptr[b + 1];
+    for (int f = far_ptr[b]; f < f1; ++f) {
+        const double2 cs = C[((size_t)far_src[f] * nrhs + r) * 2 * K + q];
+        cmac(acc, cs, T[(size_t)far_tid[f] * K + k]);
+    }
+    const double wk = wq[k];
+    B[((size_t)b * nrhs + r) * 2 * K + q] = make_double2(acc.x * wk, acc.y * wk);
+}
+
+// child level (fine) Kc, parent level Kp. One block per (child, rhs): stage
+// D = P(parent) * conj(shift_oct) in shared memory, then gather the
+// transposed interpolation taps.  Dynamic smem: 2*Kp double2.
+__global__ void k_anterp_down(int Kp, int Kc, int nrhs, const int* __restrict__ parent,
+                              const int* __restrict__ octant, const int* __restrict__ ant_ptr,
+                              const int* __restrict__ ant_row, const double* __restrict__ ant_w,
+                              const double2* __restrict__ shift, const double2* __restrict__ Psrc,
+                              const double2* __restrict__ Bc, double2* __restrict__ Ac) {
+    extern __shared__ double2 D[];
+    const int cb = blockIdx.x / nrhs, r = blockIdx.x % nrhs;
+    const int P = parent[cb];
+    const double2* sh = shift + (size_t)octant[cb] * Kp;
+    const double2* src = Psrc + ((size_t)P * nrhs + r) * 2 * Kp;
+    for (int q = threadIdx.x; q < 2 * Kp; q += blockDim.x) {
+        const int m = q >= Kp ? q - Kp : q;
+        const double2 s = sh[m];
+        const double2 v = src[q];
+        D[q] = make_double2(v.x * s.x + v.y * s.y, v.y * s.x - v.x * s.y);   // v * conj(s)
+    }
+    __syncthreads();
+    const size_t off = ((size_t)cb * nrhs + r) * 2 * Kc;
+    for (int q = threadIdx.x; q < 2 * Kc; q += blockDim.x) {
+        const int pol = q >= Kc, k = q - pol * Kc;
+        double2 acc = make_double2(0, 0);
+        const int e1 = ant_ptr[k + 1];
+        for (int e = ant_ptr[k]; e < e1; ++e) {
+            const double w = ant_w[e];
+            const double2 d = D[ant_row[e] + pol * Kp];
+            acc.x = fma(w, d.x, acc.x);
+            acc.y = fma(w, d.y, acc.y);
+        }
+        const double2 bv = Bc[off + q];
+        Ac[off + q] = make_double2(bv.x + acc.x, bv.y + acc.y);
+    }
+}
+
+// One warp per (sorted basis j, rhs): y[perm[j]] = fac * sum conj(R_j) A_box + sum_near Z x.
+__global__ void k_receive_near(int K, int N, int nrhs, int ld, const int* __restrict__ perm,
+                               const int* __restrict__ box_of_sorted, const double2* __restrict__ R,
+                               const double2* __restrict__ A, const int* __restrict__ ia,
+                               const int* __restrict__ ja, const float2* __restrict__ Z,
+                               const double2* __restrict__ x, double facy, double2* __restrict__ y) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= N * nrhs) return;
+    const int j = gw / nrhs, r = gw % nrhs;
+    const int n = perm[j], b = box_of_sorted[j];
+    const double2* Rj = R + (size_t)j * 2 * K;
+    const double2* Ab = A + ((size_t)b * nrhs + r) * 2 * K;
+    double sr = 0, si = 0;
+    for (int q = lane; q < 2 * K; q += 32) {
+        const double2 a = Rj[q], v = Ab[q];
+        // conj(a) * v
+        sr = fma(a.x, v.x, sr); sr = fma(a.y, v.y, sr);
+        si = fma(a.x, v.y, si); si = fma(-a.y, v.x, si);
+    }
+    const double2* xr = x + (size_t)r * ld;
+    double nr = 0, ni = 0;
+    for (int q = ia[n] + lane; q < ia[n + 1]; q += 32) {
+        const float2 z = Z[q];
+        const double2 xv = xr[ja[q]];
+        nr = fma(xv.x, (double)z.x, nr); nr = fma(-xv.y, (double)z.y, nr);
+        ni = fma(xv.x, (double)z.y, ni); ni = fma(xv.y, (double)z.x, ni);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffff, sr, o);
+        si += __shfl_xor_sync(0xffffffff, si, o);
+        nr += __shfl_xor_sync(0xffffffff, nr, o);
+        ni += __shfl_xor_sync(0xffffffff, ni, o);
+    }
+    if (lane == 0) {
+        // (s) * (j*facy) = (-facy*si, facy*sr)
+        y[(size_t)r * ld + n] = make_double2(-facy * si + nr, facy * sr + ni);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// set-up driver
+// ---------------------------------------------------------------------------
+
+static int launch_check(Ctx* c, const char* what) {
+    return cuda_ok(c, cudaGetLastError(), what) ? MLF_OK : MLF_E_CUDA;
+}
+
+int ensure_fields(Ctx* c, int nrhs) {
+    for (int n = 3; n <= c->nlev; ++n) {
+        Level& L = c->lv[n];
+        if (L.fcap >= nrhs) continue;
+        cudaFree(L.dC); cudaFree(L.dB); cudaFree(L.dA);
+        L.dC = L.dB = L.dA = nullptr;
+        const size_t fsz = (size_t)L.nb * nrhs * 2 * L.K;
+        CK(cudaMalloc(&L.dC, fsz * sizeof(double2)));
+        CK(cudaMalloc(&L.dB, fsz * sizeof(double2)));
+        CK(cudaMalloc(&L.dA, fsz * sizeof(double2)));
+        L.fcap = nrhs;
+    }
+    return MLF_OK;
+}
+
+int fetch_near_values(Ctx* c, std::vector<float2>& out) {
+    out.resize(c->nnz);
+    CK(cudaMemcpy(out.data(), c->dZ, c->nnz * sizeof(float2), cudaMemcpyDeviceToHost));
+    return MLF_OK;
+}
+
+int device_setup(Ctx* c) {
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 8; ++i) CK(cudaEventCreate(&c->ev[i]));
+    const int nl = c->nlev;
+    const int N = c->N;
+    int st;
+    if ((st = upload(c, &c->dp_coord, c->p_coord))) return st;
+    if ((st = upload(c, &c->dt_baric, c->t_baric))) return st;
+    if ((st = upload(c, &c->dt_baric_sub, c->t_baric_sub))) return st;
+    if ((st = upload(c, &c->de_long, c->e_long))) return st;
+    if ((st = upload(c, &c->de_centro, c->e_centro))) return st;
+    if ((st = upload(c, &c->de_t, c->e_t))) return st;
+    if ((st = upload(c, &c->de_po, c->e_po))) return st;
+    Level& leaf = c->lv[nl];
+    std::vector<int> box_of_sorted(N);
+    for (int b = 0; b < leaf.nb; ++b)
+        for (int j = c->box_ptr[b]; j < c->box_ptr[b + 1]; ++j) box_of_sorted[j] = b;
+    if ((st = upload(c, &c->dperm, c->box_bases))) return st;
+    if ((st = upload(c, &c->dbox_ptr, c->box_ptr))) return st;
+    if ((st = upload(c, &c->dbox_of_sorted, box_of_sorted))) return st;
+    if ((st = upload(c, &c->dia, c->ia))) return st;
+    if ((st = upload(c, &c->dja, c->ja))) return st;
+    if ((st = ensure_fields(c, 1))) return st;
+    for (int n = 3; n <= nl; ++n) {
+        Level& L = c->lv[n];
+        if ((st = upload(c, &L.dwq, L.wq))) return st;
+        if ((st = upload(c, &L.dkap, L.kap))) return st;
+        if ((st = upload(c, &L.dath, L.ath))) return st;
+        if ((st = upload(c, &L.daph, L.aph))) return st;
+        if ((st = upload(c, &L.dcentre, L.centre))) return st;
+        if ((st = upload(c, &L.dfar_ptr, L.far_ptr))) return st;
+        if ((st = upload(c, &L.dfar_src, L.far_src))) return st;
+        if ((st = upload(c, &L.dfar_tid, L.far_tid))) return st;
+        if ((st = upload(c, &L.dparent, L.parent))) return st;
+        if ((st = upload(c, &L.doctant, L.octant))) return st;
+        if (n < nl) {
+            if ((st = upload(c, &L.dchild_ptr, L.child_ptr))) return st;
+            if ((st = upload(c, &L.diw, L.iw))) return st;
+            if ((st = upload(c, &L.diidx, L.iidx))) return st;
+            if ((st = upload(c, &L.dant_ptr, L.ant_ptr))) return st;
+            if ((st = upload(c, &L.dant_row, L.ant_row))) return st;
+            if ((st = upload(c, &L.dant_w, L.ant_w))) return st;
+            // phase tables of this (parent) level for the 8 child octants:
+            // exp(+j k khat . r), r = (+-q, +-q, +-q), q = side/4
+            std::vector<double2> sh(8 * (size_t)L.K);
+            static const int sx[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+            static const int sy[8] = {-1, 1, -1, 1, -1, 1, -1, 1};
+            static const int sz[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+            const double q = L.side / 4., k0 = (2. * PI) / c->ph.lambda;
+            for (int o = 0; o < 8; ++o)
+                for (int m = 0; m < L.K; ++m) {
+                    const double* kk = &L.kap[3 * (size_t)m];
+                    const double kr = kk[0] * (sx[o] * q) + kk[1] * (sy[o] * q) + kk[2] * (sz[o] * q);
+                    const double a = k0 * kr;
+                    sh[(size_t)o * L.K + m] = make_double2(std::cos(a), std::sin(a));
+                }
+            if ((st = upload(c, &L.dshift, sh))) return st;
+        }
+    }
+    // translation tables
+    int Lmax = 0;
+    for (int n = 3; n <= nl; ++n) Lmax = std::max(Lmax, c->lv[n].L);
+    const int mode = (c->flags & MLF_FLAG_LEGENDRE_RECURRENCE) ? 1 : 0;
+    if (Lmax > 127 && mode == 0) {
+        c->err = "explicit Legendre sum limited to L <= 127; use MLF_FLAG_LEGENDRE_RECURRENCE";
+        return MLF_E_ARG;
+    }
+    std::vector<double> b2;
+    binomial_squares(Lmax, b2);
+    double* db2 = nullptr;
+    if ((st = upload(c, &db2, b2))) return st;
+    for (int n = 3; n <= nl; ++n) {
+        Level& L = c->lv[n];
+        const int nt = L.ntrans;
+        const int ldc = L.L + 1;
+        std::vector<double> u(3 * (size_t)std::max(nt, 1));
+        std::vector<int> Lt(std::max(nt, 1));
+        std::vector<double2> coef((size_t)std::max(nt, 1) * ldc, make_double2(0, 0));
+        std::vector<double> jb(L.L + 2), yb(L.L + 2);
+        for (int t = 0; t < nt; ++t) {
+            const double* rab = &L.rab[3 * (size_t)t];
+            const double mod = std::sqrt(rab[0] * rab[0] + rab[1] * rab[1] + rab[2] * rab[2]);
+            const double kD = (2. * PI / c->ph.lambda) * mod;
+            int Ltrue = L.L;
+            const int kDint = (int)kD;
+            if (kDint < Ltrue) Ltrue = kDint;   // multipole clipping (modMLFMA.f90:976-982)
+            Lt[t] = Ltrue;
+            for (int d = 0; d < 3; ++d) u[3 * t + d] = rab[d] / mod;
+            sph_bessel(Ltrue, kD, jb.data(), yb.data());
+            for (int l = 0; l <= Ltrue; ++l) {
+                // ((-j)^(l+1) (2l+1)) * (j_l - j y_l): one factor component is zero
+                const double f = 2. * l + 1;
+                const double hr = jb[l], hi = -yb[l];
+                double ar = 0, ai = 0;
+                switch ((l + 1) & 3) {
+                    case 0: ar = f; break;
+                    case 1: ai = -f; break;
+                    case 2: ar = -f; break;
+                    default: ai = f; break;
+                }
+                coef[(size_t)t * ldc + l] = make_double2(ar * hr - ai * hi, ar * hi + ai * hr);
+            }
+        }
+        double* du = nullptr;
+        int* dLt = nullptr;
+        double2* dcoef = nullptr;
+        if ((st = upload(c, &du, u))) return st;
+        if ((st = upload(c, &dLt, Lt))) return st;
+        if ((st = upload(c, &dcoef, coef))) return st;
+        CK(cudaMalloc(&L.dT, std::max<size_t>((size_t)nt * L.K, 1) * sizeof(double2)));
+        const double scale = (2. * PI / c->ph.lambda) / (4. * PI);
+        if (nt > 0) {
+            dim3 grid((L.K + 127) / 128, nt);
+            k_translation<<<grid, 128, 0, c->stream>>>(L.K, L.dkap, du, dLt, dcoef, ldc, db2, Lmax + 1,
+                                                       scale, mode, L.dT);
+            if ((st = launch_check(c, "k_translation"))) return st;
+        }
+        CK(cudaStreamSynchronize(c->stream));
+        cudaFree(du);
+        cudaFree(dLt);
+        cudaFree(dcoef);
+    }
+    cudaFree(db2);
+    // radiation patterns in box order
+    CK(cudaMalloc(&c->dR, (size_t)N * 2 * leaf.K * sizeof(double2)));
+    {
+        dim3 grid((leaf.K + 127) / 128, N);
+        k_patterns<<<grid, 128, 0, c->stream>>>(leaf.K, c->dperm, c->dbox_of_sorted, leaf.dcentre,
+                                                c->dt_baric, c->dp_coord, c->de_t, c->de_po, c->de_long,
+                                                leaf.dkap, leaf.dath, leaf.daph, (2. * PI) / c->ph.lambda,
+                                                c->dR);
+        if ((st = launch_check(c, "k_patterns"))) return st;
+    }
+    // near field
+    CK(cudaMalloc(&c->dZ, std::max<long long>(c->nnz, 1) * sizeof(float2)));
+    {
+        const double c72 = (double)(1.0f / 72.0f);
+        k_near<<<N, 128, 0, c->stream>>>(c->dia, c->dja, c->dt_baric, c->dt_baric_sub, c->dp_coord,
+                                         c->de_t, c->de_po, c->de_long, c->ph.w, c->ph.w * c->ph.smue,
+                                         c72, c->dZ);
+        if ((st = launch_check(c, "k_near"))) return st;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return MLF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// matvec driver
+// ---------------------------------------------------------------------------
+
+static inline int chunks(int n, int bd) { return (n + bd - 1) / bd; }
+
+int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s) {
+    int st;
+    if ((st = ensure_fields(c, nrhs))) return st;
+    c->last_nrhs = nrhs;
+    const int nl = c->nlev;
+    Level& leaf = c->lv[nl];
+    const bool prof = c->profiling != 0;
+    if (prof) cudaEventRecord(c->ev[0], s);
+    k_aggregate<<<leaf.nb * nrhs, 256, 0, s>>>(leaf.K, nrhs, ld, c->dbox_ptr, c->dperm, c->dR, x, leaf.dC);
+    if (prof) cudaEventRecord(c->ev[1], s);
+    for (int n = nl; n >= 4; --n) {
+        Level& Lc = c->lv[n];
+        Level& Lp = c->lv[n - 1];
+        const int bd = 256, nch = chunks(2 * Lp.K, bd);
+        k_interp_up<<<Lp.nb * nrhs * nch, bd, 0, s>>>(Lp.K, Lc.K, nrhs, nch, Lp.dchild_ptr, Lc.doctant,
+                                                      Lp.diw, Lp.diidx, Lp.dshift, Lc.dC, Lp.dC);
+    }
+    if (prof) cudaEventRecord(c->ev[2], s);
+    for (int n = 3; n <= nl; ++n) {
+        Level& L = c->lv[n];
+        const int bd = 128, nch = chunks(2 * L.K, bd);
+        k_translate<<<L.nb * nrhs * nch, bd, 0, s>>>(L.K, nrhs, nch, L.dfar_ptr, L.dfar_src, L.dfar_tid,
+                                                     L.dT, L.dwq, L.dC, L.dB);
+    }
+    if (prof) cudaEventRecord(c->ev[3], s);
+    for (int n = 4; n <= nl; ++n) {
+        Level& Lc = c->lv[n];
+        Level& Lp = c->lv[n - 1];
+        const double2* Psrc = (n == 4) ? Lp.dB : Lp.dA;
+        const size_t smem = 2 * (size_t)Lp.K * sizeof(double2);
+        k_anterp_down<<<Lc.nb * nrhs, 256, smem, s>>>(Lp.K, Lc.K, nrhs, Lc.dparent, Lc.doctant, Lp.dant_ptr,
+                                                      Lp.dant_row, Lp.dant_w, Lp.dshift, Psrc, Lc.dB, Lc.dA);
+    }
+    if (prof) cudaEventRecord(c->ev[4], s);
+    {
+        const int warps = c->N * nrhs;
+        const double facy = c->ph.w * MU / (4. * PI);
+        k_receive_near<<<chunks(warps * 32, 256), 256, 0, s>>>(leaf.K, c->N, nrhs, ld, c->dperm,
+                                                                c->dbox_of_sorted, c->dR, leaf.dA, c->dia,
+                                                                c->dja, c->dZ, x, facy, y);
+    }
+    if (prof) cudaEventRecord(c->ev[5], s);
+    if ((st = launch_check(c, "matvec"))) return st;
+    if (prof) {
+        CK(cudaEventSynchronize(c->ev[5]));
+        for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&c->stage_ms[i], c->ev[i], c->ev[i + 1]);
+    }
+    return MLF_OK;
+}
+
+// anterpolation smem: the largest parent grid decides; opt in above 48 KB
+int configure_kernels(Ctx* c) {
+    size_t mx = 0;
+    for (int n = 3; n < c->nlev; ++n) mx = std::max(mx, 2 * (size_t)c->lv[n].K * sizeof(double2));
+    if (mx > 227 * 1024) {
+        c->err = "parent sampling grid too large for the shared-memory anterpolation stage";
+        return MLF_E_ARG;
+    }
+    CK(cudaFuncSetAttribute(k_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    return MLF_OK;
+}
+
+void device_free(Ctx* c) {
+    auto F = [](void* p) { if (p) cudaFree(p); };
+    for (int n = 1; n <= c->nlev && n < 32; ++n) {
+        Level& L = c->lv[n];
+        F(L.dC); F(L.dB); F(L.dA); F(L.dT); F(L.dwq); F(L.dfar_ptr); F(L.dfar_src); F(L.dfar_tid);
+        F(L.diw); F(L.diidx); F(L.dant_ptr); F(L.dant_row); F(L.dant_w); F(L.dshift);
+        F(L.dchild_ptr); F(L.dparent); F(L.doctant); F(L.dkap); F(L.dath); F(L.daph); F(L.dcentre);
+    }
+    F(c->dR); F(c->dperm); F(c->dbox_ptr); F(c->dbox_of_sorted); F(c->dia); F(c->dja); F(c->dZ);
+    F(c->dp_coord); F(c->dt_baric); F(c->dt_baric_sub); F(c->de_long); F(c->de_centro); F(c->de_t);
+    F(c->de_po); F(c->dalu); F(c->djlu); F(c->dju); F(c->dlvl_rows_f); F(c->dlvl_rows_b);
+    F(c->dwork); F(c->dscal); F(c->dflags); F(c->dx_io); F(c->dy_io);
+    for (int i = 0; i < 8; ++i)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+}  // namespace mlf

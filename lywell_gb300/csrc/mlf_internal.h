@@ -1,0 +1,146 @@
+// Internal state of an MLFMA context: host tables built once at set-up and
+// their device copies.  Layouts (all device arrays in HBM, box-major):
+//   fields  C/B/A of level n : double2[nb_n][2][K_n]   (reference campoC/B/A is
+//                                (K,2,nb) column-major: the same bytes)
+//   patterns R               : double2[N][2][K_leaf] in leaf-box order
+//                                (basis j of the box-sorted list = perm[j])
+//   translation tables T     : double2[ntrans_n][K_n]
+//   near field               : CSR rows in basis order, float2 values
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/lywell_mlfma.h"
+
+namespace mlf {
+
+constexpr double PI = 3.141592653589793;
+constexpr double MU = 1.2566370614E-6;
+constexpr double EPSI = 8.8541878176E-12;
+
+struct Phys {
+    double lambda, w, kappa, vp, smue;
+};
+Phys phys_from_lambda(double lambda);
+
+struct Level {
+    int nb = 0, L = 0, K = 0, nth = 0, nph = 0;
+    double side = 0;
+    std::vector<double> centre;   // nb*3
+    std::vector<int> parent;      // nb (0-based, -1 at level 1)
+    std::vector<int> child_ptr;   // nb+1 (children at level+1 are contiguous)
+    std::vector<int> octant;      // nb: 0..7 position relative to the parent centre
+    // sampling (level >= 3)
+    std::vector<double> kap, ath, aph, ang, wq;
+    // far interactions (level >= 3)
+    std::vector<int> far_ptr, far_src, far_tid;
+    int ntrans = 0;
+    std::vector<double> rab;      // ntrans*3
+    // interpolation from level+1 (fine) to this level (coarse), 3 <= level < nlev
+    std::vector<double> iw;       // K*9
+    std::vector<int> iidx;        // K*9 (0-based fine sample)
+    // transposed table for anterpolation: for fine sample q, entries
+    // [ant_ptr[q], ant_ptr[q+1]) of (coarse sample, weight) in (row, tap) order
+    std::vector<int> ant_ptr, ant_row;
+    std::vector<double> ant_w;
+
+    // device
+    double2 *dC = nullptr, *dB = nullptr, *dA = nullptr;
+    double2* dT = nullptr;
+    double* dwq = nullptr;
+    int *dfar_ptr = nullptr, *dfar_src = nullptr, *dfar_tid = nullptr;
+    double* diw = nullptr;
+    int* diidx = nullptr;
+    int *dant_ptr = nullptr, *dant_row = nullptr;
+    double* dant_w = nullptr;
+    double2* dshift = nullptr;    // 8*K: exp(+j k khat . r_oct) for the 8 child octants
+    int *dchild_ptr = nullptr, *dparent = nullptr, *doctant = nullptr;
+    double *dkap = nullptr, *dath = nullptr, *daph = nullptr, *dcentre = nullptr;
+    int fcap = 0;                 // right-hand sides the field buffers hold
+};
+
+struct Ctx {
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    Phys ph{};
+    double ladomax = 0.5;
+    int flags = 0;
+    int N = 0, T = 0, P = 0;
+    // geometry (host, 0-based indices)
+    std::vector<double> p_coord, t_baric, t_baric_sub, e_long, e_centro;
+    std::vector<int> e_t, e_po;
+    int nlev = 0;
+    Level lv[32];
+    double root_centre[3]{}, root_side = 0;
+    // leaf boxes
+    std::vector<int> box_ptr, box_bases, box_of;
+    std::vector<int> near_ptr, near_bases;
+    long long nnz = 0;
+    std::vector<int> ia, ja;          // 0-based CSR
+    // device: leaf
+    double2* dR = nullptr;            // patterns, box order
+    int *dperm = nullptr, *dbox_ptr = nullptr, *dbox_of_sorted = nullptr;
+    int *dia = nullptr, *dja = nullptr;
+    float2* dZ = nullptr;
+    // device geometry for set-up kernels and RCS
+    double *dp_coord = nullptr, *dt_baric = nullptr, *dt_baric_sub = nullptr, *de_long = nullptr,
+           *de_centro = nullptr;
+    int *de_t = nullptr, *de_po = nullptr;
+    // ILU0 (MSR layout, 1-based content like the reference)
+    int ilu_ok = 0;
+    std::vector<float2> alu;
+    std::vector<int> jlu, ju;
+    float2* dalu = nullptr;
+    int *djlu = nullptr, *dju = nullptr;
+    // level schedule of the triangular solves
+    std::vector<int> lvl_ptr_f, lvl_rows_f, lvl_ptr_b, lvl_rows_b;
+    int *dlvl_rows_f = nullptr, *dlvl_rows_b = nullptr;
+    // scratch vectors for the solver (grown on demand)
+    size_t work_cap = 0;
+    double2* dwork = nullptr;
+    double* dscal = nullptr;          // device scalars
+    size_t scal_cap = 0;
+    int* dflags = nullptr;
+    size_t io_cap = 0;
+    double2 *dx_io = nullptr, *dy_io = nullptr;
+    // profiling
+    int last_nrhs = 1;
+    int profiling = 0;
+    cudaEvent_t ev[8]{};
+    float stage_ms[5]{};
+};
+
+// host set-up (mlf_setup.cpp)
+int fetch_near_values(Ctx* c, std::vector<float2>& out);  // device near values -> host
+int build_octree(Ctx* c);          // levels, boxes, lists, interpolation tables
+void sph_bessel(int nmax, double x, double* j, double* y);
+void binomial_squares(int nmax, std::vector<double>& out);  // (n!/(i!(n-i)!))^2, [n*(nmax+1)+i]
+int ilu0_factor(Ctx* c);           // host ILU(0), fills alu/jlu/ju, returns ierr
+void ilu_levels(Ctx* c);           // level schedules of the forward/backward sweeps
+
+// device set-up and operators (mlf_device.cu)
+int device_setup(Ctx* c);          // uploads tables, computes T, patterns, near field
+void device_free(Ctx* c);
+int ensure_fields(Ctx* c, int nrhs);
+int configure_kernels(Ctx* c);
+int ensure_work(Ctx* c, size_t n_double2);
+int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s);
+int device_ilu_upload(Ctx* c);
+int device_ilu_solve(Ctx* c, const double2* y, double2* x, cudaStream_t s);
+int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs,
+               double2* x, int* iters, double* relres, int precond, int* status);
+int device_excitation(Ctx* c, const double* dirs, const double2* pols, double2 ctte, int nrhs,
+                      double2* b);
+int device_rcs(Ctx* c, const double2* I, const double2* pol, double2 ctte, const double* th,
+               const double* ph, int nang, double* sigma);
+
+bool cuda_ok(Ctx* c, cudaError_t e, const char* what);
+
+}  // namespace mlf
+
+struct mlf_ctx {
+    mlf::Ctx c;
+};

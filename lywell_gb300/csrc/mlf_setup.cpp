@@ -1,0 +1,697 @@
+// Host-side set-up of the MLFMA solve: RWG basis, octree, sampling grids,
+// far/near interaction lists, interpolation tables, ILU(0) factorisation and
+// the level schedule of its triangular sweeps.
+//
+// Everything here is combinatorial or O(N log N); the O(N^2) searches of the
+// reference (node dedup, shared-edge search, box-pair scans) are replaced by
+// hashing with identical outcomes.  Floating-point steps that decide box
+// membership or table values keep the reference's operation order, including
+// its single-precision literals.  Compiled with -ffp-contract=off.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <unordered_map>
+
+#include "mlf_internal.h"
+
+namespace mlf {
+
+Phys phys_from_lambda(double lambda) {
+    // setlambda, modGlobalParam.f90:52-61
+    Phys p;
+    p.vp = 1.0 / std::sqrt(MU * EPSI);
+    p.lambda = lambda;
+    p.w = 2. * PI * p.vp / lambda;
+    p.kappa = 2. * PI / lambda;
+    p.smue = std::sqrt(MU * EPSI);
+    return p;
+}
+
+// ---------------------------------------------------------------------------
+// special functions
+// ---------------------------------------------------------------------------
+
+// Spherical Bessel j_n and y_n, n = 0..nmax, x > 0.  y_n by upward recurrence.
+// j_n by upward recurrence when nmax <= x, else by Miller's backward
+// recurrence started above max(nmax, x) and scaled to j_0 (or j_1 when j_0 is
+// the smaller of the two, i.e. near a zero of sin x).
+void sph_bessel(int nmax, double x, double* j, double* y) {
+    const double sx = std::sin(x), cx = std::cos(x);
+    const double j0 = sx / x, j1 = sx / (x * x) - cx / x;
+    y[0] = -cx / x;
+    if (nmax >= 1) y[1] = -cx / (x * x) - sx / x;
+    for (int n = 1; n < nmax; ++n) y[n + 1] = (2.0 * n + 1.0) / x * y[n] - y[n - 1];
+    if ((double)nmax <= x) {
+        j[0] = j0;
+        if (nmax >= 1) j[1] = j1;
+        for (int n = 1; n < nmax; ++n) j[n + 1] = (2.0 * n + 1.0) / x * j[n] - j[n - 1];
+        return;
+    }
+    const int start = std::max(nmax, (int)x) + 30 + (int)(10.0 * std::cbrt(x + 1.0));
+    double hi = 0.0, cur = 1e-280;
+    for (int n = start; n >= 1; --n) {
+        const double lo = (2.0 * n + 1.0) / x * cur - hi;
+        hi = cur;
+        cur = lo;
+        if (n - 1 <= nmax) j[n - 1] = cur;
+        if (std::fabs(cur) > 1e250) {
+            cur *= 1e-250;
+            hi *= 1e-250;
+            for (int q = std::max(n - 1, 0); q <= nmax; ++q) j[q] *= 1e-250;
+        }
+    }
+    const double s = std::fabs(j0) > std::fabs(j1) ? j0 / j[0] : j1 / j[1];
+    for (int n = 0; n <= nmax; ++n) j[n] *= s;
+}
+
+// (n! / (i! (n-i)!))^2 with the factorials formed as sequential double
+// products, the way legendre/factorial do it (modGlobalMetod.f90:988-1015).
+void binomial_squares(int nmax, std::vector<double>& out) {
+    std::vector<double> fact(nmax + 1);
+    for (int x = 0; x <= nmax; ++x) {
+        double r = 1.;
+        for (int i = 1; i <= x; ++i) r = r * i;
+        fact[x] = r;
+    }
+    out.assign((size_t)(nmax + 1) * (nmax + 1), 0.0);
+    for (int n = 0; n <= nmax; ++n)
+        for (int i = 0; i <= n; ++i) {
+            const double c = fact[n] / (fact[i] * fact[n - i]);
+            out[(size_t)n * (nmax + 1) + i] = c * c;
+        }
+}
+
+// ---------------------------------------------------------------------------
+// RWG basis
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct Vec3Hash {
+    size_t operator()(const std::array<uint64_t, 3>& k) const {
+        uint64_t h = k[0] * 0x9E3779B97F4A7C15ull;
+        h ^= k[1] + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+        h ^= k[2] + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+        return (size_t)h;
+    }
+};
+
+uint64_t dbits(double v) {
+    v = v + 0.0;  // -0.0 -> +0.0: exact equality as in the reference's comparisons
+    uint64_t u;
+    std::memcpy(&u, &v, 8);
+    return u;
+}
+
+}  // namespace
+
+}  // namespace mlf
+
+using namespace mlf;
+
+extern "C" int mlf_rwg_build(const double* tris, int T, int* N_out, int* P_out, double* p_coord,
+                             int* t_p, int* e_p, int* e_t, int* e_po, double* e_long,
+                             double* e_centro, double* t_area, double* t_baric,
+                             double* t_baric_sub) {
+    if (!tris || T <= 0 || !N_out || !P_out) return MLF_E_ARG;
+    // node deduplication by exact coordinates (limpiarnodos,
+    // modReadStl.f90:1444-1533); ids in first-occurrence order
+    std::unordered_map<std::array<uint64_t, 3>, int, Vec3Hash> nodes;
+    nodes.reserve((size_t)T * 2);
+    std::vector<int> tp((size_t)3 * T);
+    std::vector<double> pc;
+    for (int t = 0; t < T; ++t)
+        for (int k = 0; k < 3; ++k) {
+            const double* v = tris + 9 * (size_t)t + 3 * k;
+            std::array<uint64_t, 3> key{dbits(v[0]), dbits(v[1]), dbits(v[2])};
+            auto it = nodes.find(key);
+            int id;
+            if (it == nodes.end()) {
+                id = (int)(pc.size() / 3);
+                nodes.emplace(key, id);
+                pc.insert(pc.end(), {v[0], v[1], v[2]});
+            } else {
+                id = it->second;
+            }
+            tp[3 * (size_t)t + k] = id;
+        }
+    const int P = (int)(pc.size() / 3);
+    // edge list (llenar_lados, modRWG.f90:8-29): per triangle (1,2),(1,3),(2,3);
+    // an edge is made at the first occurrence of a pair that occurs again
+    // (Buscar_L_Comun / llenar_todo, modRWG.f90:32-131)
+    const int M = 3 * T;
+    std::vector<int> la(M), lb(M);
+    for (int t = 0; t < T; ++t) {
+        la[3 * t] = tp[3 * t]; lb[3 * t] = tp[3 * t + 1];
+        la[3 * t + 1] = tp[3 * t]; lb[3 * t + 1] = tp[3 * t + 2];
+        la[3 * t + 2] = tp[3 * t + 1]; lb[3 * t + 2] = tp[3 * t + 2];
+    }
+    std::vector<int> order(M);
+    for (int i = 0; i < M; ++i) order[i] = i;
+    auto key = [&](int i) {
+        const uint64_t a = (uint64_t)std::min(la[i], lb[i]), b = (uint64_t)std::max(la[i], lb[i]);
+        return (a << 32) | b;
+    };
+    std::sort(order.begin(), order.end(), [&](int x, int y) {
+        const uint64_t kx = key(x), ky = key(y);
+        return kx != ky ? kx < ky : x < y;
+    });
+    std::vector<std::pair<int, int>> pairs;
+    for (int s = 0; s < M;) {
+        int e = s;
+        while (e + 1 < M && key(order[e + 1]) == key(order[s])) ++e;
+        for (int q = s; q + 1 <= e; q += 2) pairs.emplace_back(order[q], order[q + 1]);
+        s = e + 1;
+    }
+    std::sort(pairs.begin(), pairs.end());
+    const int N = (int)pairs.size();
+    *N_out = N;
+    *P_out = P;
+    if (!p_coord) return MLF_OK;
+    std::memcpy(p_coord, pc.data(), sizeof(double) * pc.size());
+    for (int i = 0; i < 3 * T; ++i) t_p[i] = tp[i] + 1;
+    for (int e = 0; e < N; ++e) {
+        const int i = pairs[e].first, j = pairs[e].second;
+        const int x = i / 3, y = j / 3;
+        const int p1 = la[i], p2 = lb[i];
+        e_p[2 * e] = p1 + 1;
+        e_p[2 * e + 1] = p2 + 1;
+        e_t[2 * e] = x + 1;
+        e_t[2 * e + 1] = y + 1;
+        for (int s = 0; s < 2; ++s) {
+            const int tri = s == 0 ? x : y;
+            const int* t3 = &tp[3 * (size_t)tri];
+            int o;
+            if (t3[0] != p1 && t3[0] != p2) o = t3[0];
+            else if (t3[1] != p1 && t3[1] != p2) o = t3[1];
+            else o = t3[2];
+            e_po[2 * e + s] = o + 1;
+        }
+        // parametros_rwg, modRWG.f90:161-164
+        const double* a = &pc[3 * (size_t)p1];
+        const double* b = &pc[3 * (size_t)p2];
+        const double d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2];
+        e_long[e] = std::sqrt((d0 * d0 + d1 * d1) + d2 * d2);
+        for (int k = 0; k < 3; ++k) e_centro[3 * e + k] = 0.5 * (a[k] + b[k]);
+    }
+    // hallar_geometria_rwg, modRWG.f90:270-328 (single-precision 1/3, 2/3)
+    const double f13 = (double)(1.0f / 3.0f), f23 = (double)(2.0f / 3.0f);
+    static const int trip[9][3] = {{1, 4, 9}, {4, 5, 10}, {5, 2, 6}, {6, 10, 7}, {7, 8, 3},
+                                   {7, 8, 10}, {8, 9, 10}, {9, 4, 10}, {5, 6, 10}};
+    for (int t = 0; t < T; ++t) {
+        const double* p1 = &pc[3 * (size_t)tp[3 * t]];
+        const double* p2 = &pc[3 * (size_t)tp[3 * t + 1]];
+        const double* p3 = &pc[3 * (size_t)tp[3 * t + 2]];
+        double v[11][3];
+        for (int k = 0; k < 3; ++k) {
+            const double bc = f13 * ((p1[k] + p2[k]) + p3[k]);
+            t_baric[3 * t + k] = bc;
+            v[1][k] = p1[k]; v[2][k] = p2[k]; v[3][k] = p3[k];
+            v[4][k] = p1[k] + f13 * (p2[k] - p1[k]);
+            v[5][k] = p1[k] + f23 * (p2[k] - p1[k]);
+            v[6][k] = p2[k] + f13 * (p3[k] - p2[k]);
+            v[7][k] = p2[k] + f23 * (p3[k] - p2[k]);
+            v[8][k] = p3[k] + f13 * (p1[k] - p3[k]);
+            v[9][k] = p3[k] + f23 * (p1[k] - p3[k]);
+            v[10][k] = bc;
+        }
+        for (int s = 0; s < 9; ++s)
+            for (int k = 0; k < 3; ++k)
+                t_baric_sub[27 * (size_t)t + 3 * s + k] =
+                    f13 * ((v[trip[s][0]][k] + v[trip[s][1]][k]) + v[trip[s][2]][k]);
+        double ba[3], ca[3];
+        for (int k = 0; k < 3; ++k) { ba[k] = p1[k] - p2[k]; ca[k] = p1[k] - p3[k]; }
+        const double c0 = ba[1] * ca[2] - ba[2] * ca[1];
+        const double c1 = ba[2] * ca[0] - ba[0] * ca[2];
+        const double c2 = ba[0] * ca[1] - ba[1] * ca[0];
+        t_area[t] = 0.5 * std::sqrt((c0 * c0 + c1 * c1) + c2 * c2);
+    }
+    return MLF_OK;
+}
+
+namespace mlf {
+
+// ---------------------------------------------------------------------------
+// octree
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// llenar_kappas, modMLFMA.f90:453-495: midpoint theta (L) x phi (2L), theta
+// fastest; weight (cos((k-1)dth) - cos(k dth)) dphi.
+void sampling(Level& L) {
+    const int K = L.K;
+    L.kap.resize(3 * (size_t)K); L.ath.resize(3 * (size_t)K); L.aph.resize(3 * (size_t)K);
+    L.ang.resize(2 * (size_t)K); L.wq.resize(K);
+    const double dphi = 2. * PI / L.nph, dth = PI / L.nth;
+    int q = 0;
+    for (int j = 1; j <= L.nph; ++j) {
+        const double phi = (dphi / 2.) * ((2 * j) - 1);
+        const double sp = std::sin(phi), cp = std::cos(phi);
+        for (int k = 1; k <= L.nth; ++k, ++q) {
+            const double th = (dth / 2.) * ((2 * k) - 1);
+            const double st = std::sin(th), ct = std::cos(th);
+            L.kap[3 * q] = st * cp; L.kap[3 * q + 1] = st * sp; L.kap[3 * q + 2] = ct;
+            L.ath[3 * q] = ct * cp; L.ath[3 * q + 1] = ct * sp; L.ath[3 * q + 2] = -st;
+            L.aph[3 * q] = -sp; L.aph[3 * q + 1] = cp; L.aph[3 * q + 2] = 0.;
+            L.ang[2 * q] = th; L.ang[2 * q + 1] = phi;
+            L.wq[q] = (std::cos((k - 1) * dth) - std::cos(k * dth)) * dphi;
+        }
+    }
+}
+
+// Nearest sample index (1-based) on an increasing midpoint grid by the
+// reference's bisection, then its two neighbours with wrap-around at both
+// ends (hallarKcercanos, modMLFMA.f90:1096-1315).
+void nearest3(const double* grid, int stride, int n, double x, long out[3]) {
+    auto g = [&](long i) { return grid[(size_t)(i - 1) * stride]; };
+    long lo = 1, hi = n, mid;
+    for (;;) {
+        mid = (lo + hi) / 2;
+        const double v = g(mid);
+        if (mid == lo || mid == hi) {
+            mid = std::fabs(x - g(lo)) < std::fabs(x - g(hi)) ? lo : hi;
+            break;
+        }
+        if (v == x) break;
+        if (v > x) hi = mid;
+        else if (v < x) lo = mid;
+    }
+    long below, above;
+    if (mid == 1) { below = n; above = 2; }
+    else if (mid == n) { below = n - 1; above = 1; }
+    else { below = mid - 1; above = mid + 1; }
+    out[0] = mid; out[1] = below; out[2] = above;
+}
+
+// 3-point Lagrange weights (Wlagrange3, modMLFMA.f90:1318-1341)
+void lagrange3(double x, const double m[3], double W[3]) {
+    for (int i = 0; i < 3; ++i) {
+        double w = 1.;
+        for (int j = 0; j < 3; ++j)
+            if (j != i) w = w * ((x - m[j]) / (m[i] - m[j]));
+        W[i] = w;
+    }
+}
+
+// llenarMinterp, modMLFMA.f90:998-1092: 9 taps per coarse sample, weight
+// Wtheta(m2) * Wphi(m1) on child sample (phi_m1, theta_m2).
+void interp_table(const Level& Lc /*coarse*/, const Level& Lf /*fine*/, std::vector<double>& iw,
+                  std::vector<int>& iidx) {
+    iw.resize(9 * (size_t)Lc.K);
+    iidx.resize(9 * (size_t)Lc.K);
+    const int nth = Lf.nth;
+    for (int i = 0; i < Lc.K; ++i) {
+        const double xt = Lc.ang[2 * i], xp = Lc.ang[2 * i + 1];
+        long ph[3], th[3];
+        nearest3(&Lf.ang[1], 2 * nth, Lf.nph, xp, ph);   // phi of sample (p-1)*nth+1
+        nearest3(&Lf.ang[0], 2, nth, xt, th);            // theta of sample t
+        const double mt[3] = {Lf.ang[2 * (th[0] - 1)], Lf.ang[2 * (th[1] - 1)], Lf.ang[2 * (th[2] - 1)]};
+        const double mp[3] = {Lf.ang[2 * ((ph[0] - 1) * nth) + 1], Lf.ang[2 * ((ph[1] - 1) * nth) + 1],
+                              Lf.ang[2 * ((ph[2] - 1) * nth) + 1]};
+        double Wt[3], Wp[3];
+        lagrange3(xt, mt, Wt);
+        lagrange3(xp, mp, Wp);
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                iw[9 * (size_t)i + 3 * a + b] = Wt[b] * Wp[a];
+                iidx[9 * (size_t)i + 3 * a + b] = (int)(nth * (ph[a] - 1) + th[b]) - 1;
+            }
+    }
+}
+
+struct Builder {
+    Ctx* c;
+    std::vector<int> leaf_bases, leaf_ptr;
+    std::vector<int> work;
+
+    // geomMLFMA / dividir_en_8_hijos / buscarFuncBases (modMLFMA.f90:497-833):
+    // a basis goes to the first child, in the fixed child order, whose closed
+    // box holds its edge centre; empty children are not stored.
+    void split(const double centre[3], double side, std::vector<int>& bases, int level) {
+        if (level == c->nlev) return;
+        static const int sx[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+        static const int sy[8] = {-1, 1, -1, 1, -1, 1, -1, 1};
+        static const int sz[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+        const double half = side / 2., quarter = side / 4.;
+        Level& ch = c->lv[level + 1];
+        std::vector<int> rest;
+        rest.reserve(bases.size());
+        for (int i = 0; i < 8; ++i) {
+            double cc[3];
+            cc[0] = sx[i] < 0 ? centre[0] - quarter : centre[0] + quarter;
+            cc[1] = sy[i] < 0 ? centre[1] - quarter : centre[1] + quarter;
+            cc[2] = sz[i] < 0 ? centre[2] - quarter : centre[2] + quarter;
+            const double q = half / 2.;
+            const double xmax = cc[0] + q, xmin = cc[0] - q, ymax = cc[1] + q, ymin = cc[1] - q;
+            const double zmax = cc[2] + q, zmin = cc[2] - q;
+            std::vector<int> found;
+            rest.clear();
+            for (int b : bases) {
+                const double* e = &c->e_centro[3 * (size_t)b];
+                if (e[0] <= xmax && e[0] >= xmin && e[1] <= ymax && e[1] >= ymin && e[2] <= zmax &&
+                    e[2] >= zmin)
+                    found.push_back(b);
+                else
+                    rest.push_back(b);
+            }
+            if (found.empty()) continue;
+            ch.centre.insert(ch.centre.end(), cc, cc + 3);
+            ch.parent.push_back(cur_parent[level]);
+            ch.octant.push_back(i);
+            ch.nb++;
+            if (level + 1 == c->nlev) {
+                leaf_bases.insert(leaf_bases.end(), found.begin(), found.end());
+                leaf_ptr.push_back((int)leaf_bases.size());
+            }
+            const int saved = cur_parent[level + 1];
+            cur_parent[level + 1] = ch.nb - 1;
+            split(cc, half, found, level + 1);
+            cur_parent[level + 1] = saved;
+            bases.swap(rest);
+        }
+    }
+    int cur_parent[33]{};
+};
+
+inline long long cell_key(int a, int b, int cc) {
+    return ((long long)(a + 1) << 42) | ((long long)(b + 1) << 21) | (long long)(cc + 1);
+}
+
+}  // namespace
+
+int build_octree(Ctx* c) {
+    const int N = c->N;
+    const double lambda = c->ph.lambda;
+    // root cube: bounding box of edge centres (limites_dispersor,
+    // modGlobalMetod.f90:386-434) plus lambda/10000 (modMLFMA.f90:160-188)
+    int lim[6] = {0, 0, 0, 0, 0, 0};
+    const double* ec = c->e_centro.data();
+    for (int i = 1; i < N; ++i) {
+        const double* p = ec + 3 * i;
+        if (p[0] > ec[3 * lim[0]]) lim[0] = i;
+        if (p[0] < ec[3 * lim[1]]) lim[1] = i;
+        if (p[1] > ec[3 * lim[2] + 1]) lim[2] = i;
+        if (p[1] < ec[3 * lim[3] + 1]) lim[3] = i;
+        if (p[2] > ec[3 * lim[4] + 2]) lim[4] = i;
+        if (p[2] < ec[3 * lim[5] + 2]) lim[5] = i;
+    }
+    const double maxX = ec[3 * lim[0]], minX = ec[3 * lim[1]];
+    const double maxY = ec[3 * lim[2] + 1], minY = ec[3 * lim[3] + 1];
+    const double maxZ = ec[3 * lim[4] + 2], minZ = ec[3 * lim[5] + 2];
+    const double dX = maxX - minX, dY = maxY - minY, dZ = maxZ - minZ;
+    double side;
+    if (dX >= dY && dX >= dZ) side = dX;
+    else if (dY >= dX && dY >= dZ) side = dY;
+    else side = dZ;
+    side = side + lambda / 10000.;
+    c->root_centre[0] = 0.5 * (maxX + minX);
+    c->root_centre[1] = 0.5 * (maxY + minY);
+    c->root_centre[2] = 0.5 * (maxZ + minZ);
+    c->root_side = side;
+    // nivel_max = ceiling(1 + log10(side/(ladomax*lambda))/log10(2.)), with
+    // log10(2.) of a single-precision argument (modMLFMA.f90:189)
+    const double log10_2f = (double)std::log10(2.0f);
+    const int nl = (int)std::ceil(1. + (std::log10(side / (c->ladomax * lambda)) / log10_2f));
+    c->nlev = nl;
+    if (nl <= 3) {
+        c->err = "body too small electrically for MLFMA (nivel_max <= 3)";
+        return MLF_E_TOO_SMALL;
+    }
+    if (nl > 20) {
+        c->err = "more than 20 octree levels";
+        return MLF_E_ARG;
+    }
+    // per-level multipoles L = floor(kd + 6 (kd)^(1/3)), d = sqrt(3.) side with
+    // sqrt(3.) and 1./3. in single precision (modMLFMA.f90:200-218)
+    const double s3 = (double)std::sqrt(3.0f), third = (double)(1.0f / 3.0f);
+    for (int i = 1; i <= nl; ++i) {
+        Level& L = c->lv[i];
+        L.side = side / std::ldexp(1.0, i - 1);
+        const double kd = (2. * PI / lambda) * (s3 * L.side);
+        L.L = (int)std::floor(kd + 6 * std::pow(kd, third));
+        L.nth = L.L;
+        L.nph = 2 * L.L;
+        L.K = L.nth * L.nph;
+        if (i >= 3) sampling(L);
+    }
+    // boxes
+    Builder B;
+    B.c = c;
+    Level& root = c->lv[1];
+    root.nb = 1;
+    root.centre.assign(c->root_centre, c->root_centre + 3);
+    root.parent.push_back(-1);
+    root.octant.push_back(0);
+    std::vector<int> all(N);
+    for (int i = 0; i < N; ++i) all[i] = i;
+    B.leaf_ptr.push_back(0);
+    B.cur_parent[1] = 0;
+    B.split(c->root_centre, side, all, 1);
+    c->box_bases = std::move(B.leaf_bases);
+    c->box_ptr = std::move(B.leaf_ptr);
+    Level& leaf = c->lv[nl];
+    c->box_of.assign(N, -1);
+    for (int b = 0; b < leaf.nb; ++b)
+        for (int t = c->box_ptr[b]; t < c->box_ptr[b + 1]; ++t) c->box_of[c->box_bases[t]] = b;
+    for (int i = 1; i < nl; ++i) {
+        Level& L = c->lv[i];
+        const Level& Lc = c->lv[i + 1];
+        L.child_ptr.assign(L.nb + 1, 0);
+        for (int b = 0; b < Lc.nb; ++b) L.child_ptr[Lc.parent[b] + 1]++;
+        for (int b = 0; b < L.nb; ++b) L.child_ptr[b + 1] += L.child_ptr[b];
+    }
+    // far / near lists (llenar_functransf, modMLFMA.f90:835-960).  Candidate
+    // partners of box i are the children of the 27 neighbours of i's parent;
+    // they are visited in ascending box index, as the reference's j loop, and
+    // classified with its tests |dc_parent| < 2 s_p - tol, |dc| >= 2 s - tol.
+    const double tol = lambda / 100.;
+    const double ox = c->root_centre[0] - side / 2., oy = c->root_centre[1] - side / 2.,
+                 oz = c->root_centre[2] - side / 2.;
+    std::vector<std::vector<int>> cells(nl + 1);
+    for (int n = 2; n <= nl; ++n) {
+        Level& L = c->lv[n];
+        cells[n].resize(3 * (size_t)L.nb);
+        for (int b = 0; b < L.nb; ++b) {
+            cells[n][3 * b] = (int)std::floor((L.centre[3 * b] - ox) / L.side);
+            cells[n][3 * b + 1] = (int)std::floor((L.centre[3 * b + 1] - oy) / L.side);
+            cells[n][3 * b + 2] = (int)std::floor((L.centre[3 * b + 2] - oz) / L.side);
+        }
+    }
+    c->near_ptr.assign(1, 0);
+    c->near_bases.clear();
+    for (int n = 3; n <= nl; ++n) {
+        Level& L = c->lv[n];
+        const Level& Lp = c->lv[n - 1];
+        std::unordered_map<long long, int> pcell;
+        pcell.reserve(2 * (size_t)Lp.nb);
+        for (int b = 0; b < Lp.nb; ++b)
+            pcell[cell_key(cells[n - 1][3 * b], cells[n - 1][3 * b + 1], cells[n - 1][3 * b + 2])] = b;
+        std::unordered_map<long long, int> tid_of;
+        L.far_ptr.assign(1, 0);
+        L.far_src.clear();
+        L.far_tid.clear();
+        L.rab.clear();
+        std::vector<int> cand;
+        for (int i = 0; i < L.nb; ++i) {
+            const int ip = L.parent[i];
+            cand.clear();
+            const int* pc = &cells[n - 1][3 * ip];
+            for (int dx = -1; dx <= 1; ++dx)
+                for (int dy = -1; dy <= 1; ++dy)
+                    for (int dz = -1; dz <= 1; ++dz) {
+                        auto it = pcell.find(cell_key(pc[0] + dx, pc[1] + dy, pc[2] + dz));
+                        if (it == pcell.end()) continue;
+                        for (int j = Lp.child_ptr[it->second]; j < Lp.child_ptr[it->second + 1]; ++j)
+                            cand.push_back(j);
+                    }
+            std::sort(cand.begin(), cand.end());
+            const size_t near_start = c->near_bases.size();
+            for (int j : cand) {
+                const int jp = L.parent[j];
+                double rp[3], rh[3];
+                for (int d = 0; d < 3; ++d) rp[d] = Lp.centre[3 * ip + d] - Lp.centre[3 * jp + d];
+                const double np_ = std::sqrt(rp[0] * rp[0] + rp[1] * rp[1] + rp[2] * rp[2]);
+                if (!(np_ < (2 * Lp.side - tol))) continue;
+                for (int d = 0; d < 3; ++d) rh[d] = L.centre[3 * i + d] - L.centre[3 * j + d];
+                const double nh = std::sqrt(rh[0] * rh[0] + rh[1] * rh[1] + rh[2] * rh[2]);
+                if (nh >= (2 * L.side - tol)) {
+                    const long long k = cell_key(cells[n][3 * i] - cells[n][3 * j] + 8,
+                                                 cells[n][3 * i + 1] - cells[n][3 * j + 1] + 8,
+                                                 cells[n][3 * i + 2] - cells[n][3 * j + 2] + 8);
+                    auto it = tid_of.find(k);
+                    int tid;
+                    if (it == tid_of.end()) {
+                        tid = (int)(L.rab.size() / 3);
+                        if (tid >= 316) {
+                            c->err = "more than 316 distinct translation vectors on a level";
+                            return MLF_E_TABLE;
+                        }
+                        tid_of.emplace(k, tid);
+                        L.rab.insert(L.rab.end(), rh, rh + 3);
+                    } else {
+                        tid = it->second;
+                    }
+                    L.far_src.push_back(j);
+                    L.far_tid.push_back(tid);
+                } else if (n == nl) {
+                    c->near_bases.insert(c->near_bases.end(), c->box_bases.begin() + c->box_ptr[j],
+                                         c->box_bases.begin() + c->box_ptr[j + 1]);
+                }
+            }
+            L.far_ptr.push_back((int)L.far_src.size());
+            if (n == nl) {
+                std::sort(c->near_bases.begin() + near_start, c->near_bases.end());
+                c->near_ptr.push_back((int)c->near_bases.size());
+            }
+        }
+        L.ntrans = (int)(L.rab.size() / 3);
+    }
+    // near CSR rows in basis order (llenarZesparcida, modMLFMA.f90:1594-1634)
+    c->ia.assign(N + 1, 0);
+    for (int m = 0; m < N; ++m) {
+        const int b = c->box_of[m];
+        c->ia[m + 1] = c->ia[m] + (c->near_ptr[b + 1] - c->near_ptr[b]);
+    }
+    c->nnz = c->ia[N];
+    c->ja.resize(c->nnz);
+    for (int m = 0; m < N; ++m) {
+        const int b = c->box_of[m];
+        std::copy(c->near_bases.begin() + c->near_ptr[b], c->near_bases.begin() + c->near_ptr[b + 1],
+                  c->ja.begin() + c->ia[m]);
+    }
+    // interpolation tables and their transposes
+    for (int n = 3; n < nl; ++n) {
+        Level& L = c->lv[n];
+        const Level& Lf = c->lv[n + 1];
+        interp_table(L, Lf, L.iw, L.iidx);
+        L.ant_ptr.assign(Lf.K + 1, 0);
+        for (int e = 0; e < 9 * L.K; ++e) L.ant_ptr[L.iidx[e] + 1]++;
+        for (int q = 0; q < Lf.K; ++q) L.ant_ptr[q + 1] += L.ant_ptr[q];
+        L.ant_row.resize(9 * (size_t)L.K);
+        L.ant_w.resize(9 * (size_t)L.K);
+        std::vector<int> fill(L.ant_ptr.begin(), L.ant_ptr.end() - 1);
+        for (int e = 0; e < 9 * L.K; ++e) {   // (row, tap) ascending: the scatter order of Anterpolar
+            const int q = L.iidx[e];
+            L.ant_row[fill[q]] = e / 9;
+            L.ant_w[fill[q]] = L.iw[e];
+            fill[q]++;
+        }
+    }
+    return MLF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// ILU(0)
+// ---------------------------------------------------------------------------
+
+namespace {
+inline float2 mulf(float2 a, float2 b) {
+    // complex(4) * complex(4) in single precision
+    const float p1 = a.x * b.x, p2 = a.y * b.y, p3 = a.x * b.y, p4 = a.y * b.x;
+    return make_float2(p1 - p2, p3 + p4);
+}
+}  // namespace
+
+// ilu0C, modIterativo.f90:1805-1976 (Saad's ILU(0), IKJ on the CSR pattern).
+// MSR output with 1-based content: alu[1..n] inverted diagonal, jlu[1] = n+2,
+// row i of L then U in [jlu[i], jlu[i+1]), ju[i] = start of U.  Factors are
+// complex(4); the update alu(jw) - tl*alu(jj) runs in double, tl = alu(j) *
+// alu(jrow) in single, as in the reference.  Returns 0 or the zero-pivot row.
+int ilu0_factor(Ctx* c) {
+    const int n = c->N;
+    const long long nnz = c->nnz;
+    c->alu.assign(nnz + 2, make_float2(0.f, 0.f));
+    c->jlu.assign(nnz + 2, 0);
+    c->ju.assign(n + 1, 0);
+    std::vector<float2> zf;
+    if (fetch_near_values(c, zf) != MLF_OK) return -1;
+    std::vector<int> iw(n + 1, 0);
+    float2* alu = c->alu.data();
+    int* jlu = c->jlu.data();
+    int* ju = c->ju.data();
+    long long ju0 = n + 2;
+    jlu[1] = (int)ju0;
+    for (int ii = 1; ii <= n; ++ii) {
+        const long long js = ju0;
+        for (long long j = c->ia[ii - 1]; j < c->ia[ii]; ++j) {
+            const int jcol = c->ja[j] + 1;
+            if (jcol == ii) {
+                alu[ii] = zf[j];
+                iw[jcol] = ii;
+                ju[ii] = (int)ju0;
+            } else {
+                alu[ju0] = zf[j];
+                jlu[ju0] = jcol;
+                iw[jcol] = (int)ju0;
+                ++ju0;
+            }
+        }
+        jlu[ii + 1] = (int)ju0;
+        const long long jf = ju0 - 1;
+        const long long jm = ju[ii] - 1;
+        for (long long j = js; j <= jm; ++j) {
+            const int jrow = jlu[j];
+            const float2 tlf = mulf(alu[j], alu[jrow]);
+            alu[j] = tlf;
+            const double tr = tlf.x, ti = tlf.y;
+            for (long long jj = ju[jrow]; jj < jlu[jrow + 1]; ++jj) {
+                const int jw = iw[jlu[jj]];
+                if (jw != 0) {
+                    const double ar = alu[jj].x, ai = alu[jj].y;
+                    const double rr = (double)alu[jw].x - (tr * ar - ti * ai);
+                    const double ri = (double)alu[jw].y - (tr * ai + ti * ar);
+                    alu[jw] = make_float2((float)rr, (float)ri);
+                }
+            }
+        }
+        if (alu[ii].x == 0.0f && alu[ii].y == 0.0f) return ii;
+        const double dr = alu[ii].x, di = alu[ii].y, den = dr * dr + di * di;
+        alu[ii] = make_float2((float)(dr / den), (float)(-di / den));
+        iw[ii] = 0;
+        for (long long i = js; i <= jf; ++i) iw[jlu[i]] = 0;
+    }
+    return 0;
+}
+
+// Level schedules: forward row i waits on the L columns of row i, backward
+// row i on its U columns.  Rows of one level are independent.
+void ilu_levels(Ctx* c) {
+    const int n = c->N;
+    std::vector<int> lev(n + 1, 0);
+    int maxl = 0;
+    for (int i = 1; i <= n; ++i) {
+        int l = 0;
+        for (int k = c->jlu[i]; k < c->ju[i]; ++k) l = std::max(l, lev[c->jlu[k]] + 1);
+        lev[i] = l;
+        maxl = std::max(maxl, l);
+    }
+    c->lvl_ptr_f.assign(maxl + 2, 0);
+    for (int i = 1; i <= n; ++i) c->lvl_ptr_f[lev[i] + 1]++;
+    for (int l = 0; l <= maxl; ++l) c->lvl_ptr_f[l + 1] += c->lvl_ptr_f[l];
+    c->lvl_rows_f.assign(n, 0);
+    {
+        std::vector<int> f(c->lvl_ptr_f.begin(), c->lvl_ptr_f.end() - 1);
+        for (int i = 1; i <= n; ++i) c->lvl_rows_f[f[lev[i]]++] = i;
+    }
+    std::fill(lev.begin(), lev.end(), 0);
+    maxl = 0;
+    for (int i = n; i >= 1; --i) {
+        int l = 0;
+        for (int k = c->ju[i]; k < c->jlu[i + 1]; ++k) l = std::max(l, lev[c->jlu[k]] + 1);
+        lev[i] = l;
+        maxl = std::max(maxl, l);
+    }
+    c->lvl_ptr_b.assign(maxl + 2, 0);
+    for (int i = 1; i <= n; ++i) c->lvl_ptr_b[lev[i] + 1]++;
+    for (int l = 0; l <= maxl; ++l) c->lvl_ptr_b[l + 1] += c->lvl_ptr_b[l];
+    c->lvl_rows_b.assign(n, 0);
+    {
+        std::vector<int> f(c->lvl_ptr_b.begin(), c->lvl_ptr_b.end() - 1);
+        for (int i = n; i >= 1; --i) c->lvl_rows_b[f[lev[i]]++] = i;
+    }
+}
+
+}  // namespace mlf

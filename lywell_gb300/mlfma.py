@@ -1,0 +1,291 @@
+"""Host-side mirror of MLFMAxwell's solve interface over the C ABI.
+
+Names follow the reference so that a driver written against it reads the
+same:
+
+==========================  ============================================  =========================
+reference (Fortran)          here                                           C ABI
+==========================  ============================================  =========================
+cap_geom -> parametros_rwg   ``RWG(tris)``                                  mlf_rwg_build
+inicializar_MLFMA            ``MLFMA(rwg, lam, ladomax)``                   mlf_init
+MatxVec_MLFMA                ``MLFMA.MatxVec_MLFMA(x)`` / ``matvec``        mlf_matvec
+Zesparcida_MLFMA, ia, ja     ``MLFMA.near_csr()``                           mlf_near_csr
+crear_precond -> ilu0C       ``MLFMA.ilu0C()`` (returns ierr)               mlf_ilu0
+lusol0C                      ``MLFMA.lusol0C(y)``                           mlf_ilu0_solve
+CGSold                       ``MLFMA.CGSold(b, guess, errmax, ...)``        mlf_cgs
+generar_onda                 ``MLFMA.generar_onda(dir, pol, ctte)``         mlf_excitation
+inicializar_RCS + sigmaRCS   ``MLFMA.sigmaRCS(I, pol, theta, phi, ctte)``   mlf_rcs
+destruir_MLFMA               ``MLFMA.close()``                              mlf_free
+==========================  ============================================  =========================
+
+Errors the reference only prints (ILU zero pivot, CGS breakdown) are
+returned as values; invalid calls raise :class:`MLFError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._capi import CGS_STATUS, FLAG_LEGENDRE_RECURRENCE, MLFError, load
+
+__all__ = ["RWG", "MLFMA", "MLFError", "FLAG_LEGENDRE_RECURRENCE", "ajustar_polariz", "direction"]
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _check(code, h=None):
+    if code != 0:
+        msg = load().mlf_last_error(h)
+        raise MLFError(code, msg.decode() if msg else "")
+
+
+class RWG:
+    """RWG basis of a triangle soup ``tris[T, 3, 3]`` in the reference's edge order.
+
+    Arrays are 0-based numpy views for Python users; ``fortran()`` gives the
+    1-based arrays the C ABI takes.
+    """
+
+    def __init__(self, tris):
+        tris = np.ascontiguousarray(tris, dtype=np.float64).reshape(-1, 3, 3)
+        L = load()
+        T = tris.shape[0]
+        N = C.c_int()
+        P = C.c_int()
+        _check(L.mlf_rwg_build(_p(tris), T, C.byref(N), C.byref(P), *([None] * 10)))
+        N, P = N.value, P.value
+        self.N, self.P, self.T = N, P, T
+        self.p_coord = np.zeros((P, 3))
+        self.t_p = np.zeros((T, 3), dtype=np.int32)
+        self.e_p = np.zeros((N, 2), dtype=np.int32)
+        self.e_t = np.zeros((N, 2), dtype=np.int32)
+        self.e_po = np.zeros((N, 2), dtype=np.int32)
+        self.e_long = np.zeros(N)
+        self.e_centro = np.zeros((N, 3))
+        self.t_area = np.zeros(T)
+        self.t_baric = np.zeros((T, 3))
+        self.t_baric_sub = np.zeros((T, 9, 3))
+        _check(L.mlf_rwg_build(_p(tris), T, C.byref(C.c_int()), C.byref(C.c_int()), _p(self.p_coord),
+                               _p(self.t_p), _p(self.e_p), _p(self.e_t), _p(self.e_po), _p(self.e_long),
+                               _p(self.e_centro), _p(self.t_area), _p(self.t_baric), _p(self.t_baric_sub)))
+        # 0-based views
+        self.t_p -= 1
+        self.e_p -= 1
+        self.e_t -= 1
+        self.e_po -= 1
+
+    def fortran(self):
+        return dict(e_t=np.ascontiguousarray(self.e_t + 1), e_po=np.ascontiguousarray(self.e_po + 1),
+                    t_p=np.ascontiguousarray(self.t_p + 1), e_p=np.ascontiguousarray(self.e_p + 1))
+
+
+def direction(theta_deg: float, phi_deg: float) -> np.ndarray:
+    """Incidence direction as the driver builds it (main.f90:97-99)."""
+    f180 = float(np.float32(180.0))
+    t = theta_deg * np.pi / f180
+    p = phi_deg * np.pi / f180
+    return np.array([np.sin(t) * np.cos(p), np.sin(t) * np.sin(p), np.cos(t)])
+
+
+def ajustar_polariz(d, kind: str) -> np.ndarray:
+    """VV -> z, HH -> d x z normalised (ajustar_polariz, main.f90:828-849)."""
+    if kind == "VV":
+        return np.array([0, 0, 1], dtype=np.complex128)
+    v = np.array([d[1], -d[0], 0.0])
+    return (v / np.sqrt(np.sum(v * v))).astype(np.complex128)
+
+
+class MLFMA:
+    """One MLFMA operator on the current CUDA device (inicializar_MLFMA)."""
+
+    def __init__(self, rwg: RWG, lam: float = 1.0, ladomax: float = 0.5, flags: int = 0):
+        L = load()
+        self.rwg = rwg
+        self.lam = float(lam)
+        self.N = rwg.N
+        f = rwg.fortran()
+        h = C.c_void_p()
+        code = L.mlf_init(C.byref(h), _p(np.ascontiguousarray(rwg.e_centro)), rwg.N, _p(f["e_t"]),
+                          _p(f["e_po"]), _p(np.ascontiguousarray(rwg.e_long)),
+                          _p(np.ascontiguousarray(rwg.t_area)), _p(np.ascontiguousarray(rwg.t_baric)),
+                          _p(np.ascontiguousarray(rwg.t_baric_sub)), _p(np.ascontiguousarray(rwg.p_coord)),
+                          _p(f["t_p"]), _p(f["e_p"]), rwg.P, rwg.T, None, self.lam, float(ladomax), int(flags))
+        if code != 0:
+            msg = L.mlf_last_error(None)
+            raise MLFError(code, msg.decode() if msg else "")
+        self._h = h
+        info = np.zeros(160, dtype=np.int32)
+        nnz = C.c_longlong()
+        _check(L.mlf_info(self._h, _p(info), C.byref(nnz)), self._h)
+        self.nlev = int(info[0])
+        self.nnz = int(nnz.value)
+        self.levels = {l: dict(nb=int(info[5 * l]), L=int(info[5 * l + 1]), K=int(info[5 * l + 2]),
+                               ntrans=int(info[5 * l + 3]), nfar=int(info[5 * l + 4]))
+                       for l in range(1, self.nlev + 1)}
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            load().mlf_free(self._h)
+            self._h = None
+
+    destruir_MLFMA = close
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- operator
+    def matvec(self, x):
+        x = np.asarray(x, dtype=np.complex128)
+        single = x.ndim == 1
+        X = np.asfortranarray(x.reshape(self.N, -1))
+        Y = np.zeros_like(X)
+        _check(load().mlf_matvec(self._h, _p(X), _p(Y), X.shape[1], self.N), self._h)
+        return Y[:, 0] if single else Y
+
+    MatxVec_MLFMA = matvec
+
+    def matvec_device(self, x_ptr: int, y_ptr: int, nrhs: int = 1, stream: int = 0):
+        _check(load().mlf_matvec_device(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), nrhs, self.N,
+                                        C.c_void_p(stream) if stream else None), self._h)
+
+    def near_csr(self):
+        """(ia, ja, a) with 1-based ia/ja and complex64 values (Zesparcida_MLFMA)."""
+        nnz = C.c_longlong()
+        _check(load().mlf_near_csr(self._h, C.byref(nnz), None, None, None), self._h)
+        a = np.zeros(nnz.value, dtype=np.complex64)
+        ja = np.zeros(nnz.value, dtype=np.int32)
+        ia = np.zeros(self.N + 1, dtype=np.int32)
+        _check(load().mlf_near_csr(self._h, C.byref(nnz), _p(a), _p(ja), _p(ia)), self._h)
+        return ia, ja, a
+
+    # -- preconditioner
+    def ilu0(self) -> int:
+        ierr = C.c_int()
+        _check(load().mlf_ilu0(self._h, C.byref(ierr)), self._h)
+        return int(ierr.value)
+
+    ilu0C = ilu0
+
+    def ilu0_factors(self):
+        alu = np.zeros(self.nnz + 1, dtype=np.complex64)
+        jlu = np.zeros(self.nnz + 1, dtype=np.int32)
+        ju = np.zeros(self.N, dtype=np.int32)
+        _check(load().mlf_ilu0_factors(self._h, _p(alu), _p(jlu), _p(ju)), self._h)
+        return alu, jlu, ju
+
+    def lusol0(self, y):
+        y = np.asarray(y, dtype=np.complex128)
+        single = y.ndim == 1
+        Y = np.asfortranarray(y.reshape(self.N, -1))
+        X = np.zeros_like(Y)
+        _check(load().mlf_ilu0_solve(self._h, _p(Y), _p(X), Y.shape[1]), self._h)
+        return X[:, 0] if single else X
+
+    lusol0C = lusol0
+
+    # -- solver
+    def cgs(self, b, guess=None, errmax=1e-4, maxit=1000, precond: int = 0):
+        """Returns dict(x, iters, relres, status) per column."""
+        b = np.asarray(b, dtype=np.complex128)
+        single = b.ndim == 1
+        B = np.asfortranarray(b.reshape(self.N, -1))
+        nrhs = B.shape[1]
+        G = None if guess is None else np.asfortranarray(np.asarray(guess, dtype=np.complex128).reshape(self.N, -1))
+        X = np.zeros_like(B)
+        it = np.zeros(nrhs, dtype=np.int32)
+        rr = np.zeros(nrhs)
+        st = np.zeros(nrhs, dtype=np.int32)
+        _check(load().mlf_cgs(self._h, _p(B), None if G is None else _p(G), float(errmax), int(maxit), nrhs,
+                              _p(X), _p(it), _p(rr), int(precond), _p(st)), self._h)
+        if single:
+            return dict(x=X[:, 0], iters=int(it[0]), relres=float(rr[0]), status=CGS_STATUS[int(st[0])])
+        return dict(x=X, iters=it, relres=rr, status=[CGS_STATUS[int(s)] for s in st])
+
+    def CGSold(self, b, guess, errmax, prec=False, maxit=100000):
+        return self.cgs(b, guess, errmax, maxit, 1 if prec else 0)
+
+    # -- excitation and RCS
+    def excitation(self, dirs, pols, ctte=1.0):
+        dirs = np.ascontiguousarray(np.atleast_2d(dirs), dtype=np.float64)
+        pols = np.ascontiguousarray(np.atleast_2d(pols), dtype=np.complex128)
+        nrhs = dirs.shape[0]
+        Bm = np.zeros((nrhs, self.N), dtype=np.complex128)
+        _check(load().mlf_excitation(self._h, _p(dirs), _p(pols), float(np.real(ctte)), float(np.imag(ctte)),
+                                     nrhs, _p(Bm)), self._h)
+        return Bm[0] if nrhs == 1 else Bm.T.copy()
+
+    def generar_onda(self, direccion, polarizacion, ctte=1.0):
+        return self.excitation(direccion, polarizacion, ctte)
+
+    def rcs(self, current, pol, theta, phi, ctte=1.0):
+        """Linear sigma for each (theta, phi) pair in radians."""
+        th, ph = np.broadcast_arrays(np.atleast_1d(np.asarray(theta, dtype=np.float64)),
+                                     np.atleast_1d(np.asarray(phi, dtype=np.float64)))
+        th = np.ascontiguousarray(th.ravel())
+        ph = np.ascontiguousarray(ph.ravel())
+        cur = np.ascontiguousarray(current, dtype=np.complex128)
+        pol = np.ascontiguousarray(pol, dtype=np.complex128)
+        out = np.zeros(th.size)
+        _check(load().mlf_rcs(self._h, _p(cur), _p(pol), float(np.real(ctte)), float(np.imag(ctte)), _p(th), _p(ph),
+                              th.size, _p(out)), self._h)
+        return out
+
+    def sigmaRCS(self, current, pol, theta, phi, ctte=1.0):
+        return self.rcs(current, pol, theta, phi, ctte)
+
+    # -- diagnostics
+    def set_profiling(self, on=True):
+        _check(load().mlf_set_profiling(self._h, 1 if on else 0), self._h)
+
+    def stage_times(self):
+        out = np.zeros(5, dtype=np.float32)
+        _check(load().mlf_stage_times(self._h, _p(out)), self._h)
+        return out
+
+    def algorithmic_counts(self):
+        """Per-matvec algorithmic FLOPs and HBM bytes (1 RHS), by stage.
+
+        FLOPs: complex MAC = 8, real x complex MAC = 4, complex multiply = 6.
+        Bytes: patterns read at aggregation and at receive, near CSR
+        (complex(4) values + int32 columns + row pointers), each field level
+        written/read once per pass (C write+read, B write, A write+read),
+        x read twice and y written once.
+        """
+        nl = self.nlev
+        lv = self.levels
+        Kl, N = lv[nl]["K"], self.N
+        trans = sum(16.0 * lv[n]["nfar"] * lv[n]["K"] for n in range(3, nl + 1))
+        rows = sum(lv[n - 1]["K"] * lv[n]["nb"] for n in range(4, nl + 1))
+        flops = dict(translation=trans, aggregation=16.0 * Kl * N, receive=16.0 * Kl * N,
+                     interpolation=4.0 * 9 * 2 * rows + 6.0 * 2 * rows,
+                     anterpolation=4.0 * 9 * 2 * rows + 6.0 * 2 * rows, near=8.0 * self.nnz)
+        field = sum(2.0 * lv[n]["K"] * lv[n]["nb"] * 16 for n in range(3, nl + 1))
+        byt = dict(patterns=2 * 2.0 * Kl * N * 16, near=self.nnz * 12.0 + (N + 1) * 4.0, fields=5 * field,
+                   vectors=3.0 * N * 16)
+        trans_bytes = sum(2.0 * 2 * lv[n]["K"] * lv[n]["nb"] * 16 + lv[n]["ntrans"] * lv[n]["K"] * 16.0
+                          for n in range(3, nl + 1))
+        return dict(flops=flops, bytes=byt, flops_total=sum(flops.values()), bytes_total=sum(byt.values()),
+                    translation_bytes=trans_bytes)
+
+    def debug_field(self, level, which):
+        lv = self.levels[level]
+        out = np.zeros((lv["nb"], 2, lv["K"]), dtype=np.complex128)
+        _check(load().mlf_debug_field(self._h, int(level), int(which), _p(out)), self._h)
+        return out

@@ -187,6 +187,12 @@ class OracleMLFMA:
         lib().ora_near(C.c_void_p(self._h), _p(ia), _p(ja), _p(z))
         return ia, ja, z
 
+    def set_near(self, z):
+        z = np.ascontiguousarray(z, dtype=np.complex64)
+        assert z.size == self.nnz
+        self._z_keep = z
+        lib().ora_set_near(C.c_void_p(self._h), _p(z))
+
     def root(self):
         c = np.zeros(3)
         side = lib().ora_root(self._h, _p(c))

@@ -1179,6 +1179,9 @@ void ora_ilu_factors(Ctx* c, cplxf* alu, int* jlu, int* ju) {
     memcpy(jlu, c->jlu, sizeof(int) * (c->nnz + 2));
     memcpy(ju, c->ju, sizeof(int) * (c->N + 1));
 }
+/* replace the near-field values (same CSR pattern), e.g. with values computed
+ * elsewhere, so that later stages can be compared in isolation */
+void ora_set_near(Ctx* c, const cplxf* z) { memcpy(c->zn, z, sizeof(cplxf) * c->nnz); }
 double ora_root(Ctx* c, double* centre) { memcpy(centre, c->root_centre, sizeof(double) * 3); return c->root_side; }
 void ora_set_threads(int n) {
 #ifdef _OPENMP

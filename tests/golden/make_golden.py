@@ -51,12 +51,12 @@ CASES = {
                     "run=mlfma"], 600),
     # same body, dense MoM (the near-field entries are Zmn_MoM).
     "ico3_mom": (lambda: meshes.icosphere(3, 1.0, quantum=QUANTUM),
-                 ["lambda=1", "precond=no", "errsolver=1e-10",
+                 ["lambda=1", "precond=no", "errsolver=1e-8",
                   "rcsmono.active=false", "rcsbi.ntheta=5", "rcsbi.nphi=8",
                   "run=mom"], 900),
     # same body, CGS + ILU0 preconditioner.
     "ico3_ilu0": (lambda: meshes.icosphere(3, 1.0, quantum=QUANTUM),
-                  ["lambda=1", "ladomax=0.3", "precond=ilu0", "errsolver=1e-6",
+                  ["lambda=1", "ladomax=0.3", "precond=ilu0", "errsolver=1e-3",
                    "rcsmono.active=false", "rcsbi.ntheta=5", "rcsbi.nphi=8",
                    "run=mlfma"], 900),
     # monostatic sweep, 4 angles of phi, VV, warm-started CGS.
@@ -96,13 +96,22 @@ def _run_case(name, build, script, timeout):
     t0 = time.time()
     # The program exits with a Fortran end-of-file error once stdin is
     # exhausted; that is its normal end in script mode.
-    proc = subprocess.run(["./MLFMAxwell"], input="\n".join(lines) + "\n", cwd=work,
-                          capture_output=True, text=True, timeout=timeout)
+    try:
+        proc = subprocess.run(["./MLFMAxwell"], input="\n".join(lines) + "\n", cwd=work,
+                              capture_output=True, text=True, timeout=timeout)
+        log = proc.stdout
+        timed_out = False
+    except subprocess.TimeoutExpired as exc:
+        log = exc.stdout.decode() if isinstance(exc.stdout, bytes) else (exc.stdout or "")
+        timed_out = True
     dt = time.time() - t0
-    out = {"tris": tris, "script": np.array("\n".join(lines)), "wall_s": np.array(dt)}
-    log = proc.stdout
-    iters = [int(l.split()[1]) for l in log.splitlines() if l.strip().startswith("Iterac:")]
-    out["iterations"] = np.array(iters[-1] if iters else -1)
+    out = {"tris": tris, "script": np.array("\n".join(lines)), "wall_s": np.array(dt),
+           "timed_out": np.array(timed_out)}
+    iters = [l.split() for l in log.splitlines() if l.strip().startswith("Iterac:")]
+    out["iterations"] = np.array(int(iters[-1][1]) if iters else -1)
+    # per-iteration residual history "Iterac: i residuo r de b - time"
+    out["res_hist"] = np.array([float(w[3]) for w in iters]) if iters else np.zeros(0)
+    out["bnorm"] = np.array(float(iters[-1][5]) if iters else 0.0)
     for fn, key in (("T_IMLFMA.dat", "I"), ("T_IMoM.dat", "I"),
                     ("T_RCSBI_FMM-MLFMA.dat", "rcsbi"), ("T_RCSBI_MoM.dat", "rcsbi"),
                     ("T_RCSMONOVV.dat", "rcsmono")):
@@ -120,7 +129,8 @@ def _run_case(name, build, script, timeout):
         out["W_vals"] = w[out["W_rows"], out["W_cols"]]
         out["W_shape"] = np.array(w.shape)
     shutil.rmtree(work)
-    print(f"{name}: {dt:.1f}s, iterations={int(out['iterations'])}, keys={sorted(out)}")
+    print(f"{name}: {dt:.1f}s, timed_out={timed_out}, iterations={int(out['iterations'])}, "
+          f"keys={sorted(out)}", flush=True)
     return out
 
 
