@@ -71,9 +71,9 @@ __global__ void k_patterns(int K, const int* __restrict__ bases, const int* __re
                            const double* __restrict__ p_coord, const int* __restrict__ e_t,
                            const int* __restrict__ e_po, const double* __restrict__ e_long,
                            const double* __restrict__ kap, const double* __restrict__ ath,
-                           const double* __restrict__ aph, double ka, double2* __restrict__ R) {
-    const int j = blockIdx.y;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+                           const double* __restrict__ aph, double ka, int nchunk, double2* __restrict__ R) {
+    const int j = blockIdx.x / nchunk;
+    const int k = (blockIdx.x % nchunk) * blockDim.x + threadIdx.x;
     if (k >= K) return;
     const int n = bases[j];
     const double* C = centres + 3 * box_of_sorted[j];
@@ -510,11 +510,11 @@ int device_setup(Ctx* c) {
     // radiation patterns in box order
     CK(cudaMalloc(&c->dR, (size_t)N * 2 * leaf.K * sizeof(double2)));
     {
-        dim3 grid((leaf.K + 127) / 128, N);
-        k_patterns<<<grid, 128, 0, c->stream>>>(leaf.K, c->dperm, c->dbox_of_sorted, leaf.dcentre,
-                                                c->dt_baric, c->dp_coord, c->de_t, c->de_po, c->de_long,
-                                                leaf.dkap, leaf.dath, leaf.daph, (2. * PI) / c->ph.lambda,
-                                                c->dR);
+        const int nch = (leaf.K + 127) / 128;
+        k_patterns<<<N * nch, 128, 0, c->stream>>>(leaf.K, c->dperm, c->dbox_of_sorted, leaf.dcentre,
+                                                   c->dt_baric, c->dp_coord, c->de_t, c->de_po, c->de_long,
+                                                   leaf.dkap, leaf.dath, leaf.daph, (2. * PI) / c->ph.lambda,
+                                                   nch, c->dR);
         if ((st = launch_check(c, "k_patterns"))) return st;
     }
     // near field

@@ -83,7 +83,10 @@ def test_interpolation_dump_of_binary_run(ico3):
     assert np.abs(W - Wb).max() < 1e-7          # f16.8 print precision
     orig = np.stack([g["orig_t"].T.ravel(), g["orig_p"].T.ravel()], axis=1)
     inter = np.stack([g["inter_t"].T.ravel(), g["inter_p"].T.ravel()], axis=1)
-    np.testing.assert_allclose(W @ orig, inter, atol=5e-7 * np.abs(orig).max() * 9)
+    # orig and inter are printed in f16.8 (half-ulp 5e-9): the bound is that
+    # print error carried through the 9 weights plus the print of inter
+    bound = 5e-9 * (np.abs(W).sum(axis=1, keepdims=True) + 1.0) * np.sqrt(2.0) * 1.01
+    assert np.all(np.abs(W @ orig - inter) <= bound)
 
 
 def test_interpolation_kat_reference_files():
