@@ -127,6 +127,11 @@ int mlf_ilu0_solve(mlf_ctx* ctx, const double* y, double* x, int nrhs);
 int mlf_cgs(mlf_ctx* ctx, const double* b, const double* x0, double tol, int maxit, int nrhs,
             double* x, int* iters, double* relres, int precond_kind, int* status_out);
 
+/* Residual history ||r_i||/||b|| of column col of the last mlf_cgs call
+ * (the per-iteration line CGSold prints, modIterativo.f90:446-465).
+ * *n = number of iterations recorded; up to cap values are copied. */
+int mlf_cgs_history(mlf_ctx* ctx, int col, double* hist, int cap, int* n);
+
 /* Plane-wave excitation b(N) for nrhs waves: dirs(3,nrhs) propagation
  * directions, pols(3,nrhs) complex polarisations, ctte complex amplitude.
  * Replaces: generar_onda (main.f90:1488-1525). */

@@ -27,6 +27,7 @@ SIGNATURES = {
     "mlf_ilu0_factors": (C.c_int, [vp, vp, vp, vp]),
     "mlf_ilu0_solve": (C.c_int, [vp, vp, vp, C.c_int]),
     "mlf_cgs": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp]),
+    "mlf_cgs_history": (C.c_int, [vp, C.c_int, vp, C.c_int, ip]),
     "mlf_excitation": (C.c_int, [vp, vp, vp, C.c_double, C.c_double, C.c_int, vp]),
     "mlf_rcs": (C.c_int, [vp, vp, vp, C.c_double, C.c_double, vp, vp, C.c_int, vp]),
     "mlf_info": (C.c_int, [vp, vp, C.POINTER(C.c_longlong)]),

@@ -227,6 +227,18 @@ int mlf_cgs(mlf_ctx* h, const double* b, const double* x0, double tol, int maxit
     return st;
 }
 
+int mlf_cgs_history(mlf_ctx* h, int col, double* hist, int cap, int* n) {
+    if (!h || !n) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    const int nr = std::max(c->cgs_hist_nrhs, 1);
+    if (col < 0 || col >= nr) return MLF_E_ARG;
+    const int total = (int)(c->cgs_hist.size() / nr);
+    *n = total;
+    if (hist)
+        for (int i = 0; i < std::min(cap, total); ++i) hist[i] = c->cgs_hist[(size_t)i * nr + col];
+    return MLF_OK;
+}
+
 int mlf_excitation(mlf_ctx* h, const double* dirs, const double* pols, double ctte_re, double ctte_im, int nrhs,
                    double* b) {
     if (!h || !dirs || !pols || !b || nrhs <= 0) return MLF_E_ARG;

@@ -108,6 +108,8 @@ struct Ctx {
     double2 *dx_io = nullptr, *dy_io = nullptr;
     // profiling
     int last_nrhs = 1;
+    std::vector<double> cgs_hist;     // ||r||/||b|| per iteration, [it * nrhs + col]
+    int cgs_hist_nrhs = 0;
     int profiling = 0;
     cudaEvent_t ev[8]{};
     float stage_ms[5]{};

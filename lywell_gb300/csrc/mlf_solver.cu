@@ -383,6 +383,8 @@ int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxi
     const double tol2 = tol * tol;
     std::vector<int> hflags((size_t)nrhs * F_NFLAG);
     std::vector<double> hscal((size_t)nrhs * S_NSCAL);
+    c->cgs_hist.clear();
+    c->cgs_hist_nrhs = nrhs;
     int it = 0;
     for (; it < maxit; ++it) {
         k_dot_partial<<<rg, RED_THREADS, 0, s>>>(N, r, Rt, 0, flags, partials);
@@ -400,7 +402,12 @@ int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxi
         k_dot_partial<<<rg, RED_THREADS, 0, s>>>(N, r, r, 1, flags, partials);
         k_finalize<<<nrhs, RED_THREADS, 0, s>>>(3, RED_BLOCKS, partials, scal, flags, tol2);
         CK(cudaMemcpyAsync(hflags.data(), flags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(hscal.data(), scal, hscal.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
+        for (int col = 0; col < nrhs; ++col) {
+            const double bb = hscal[col * S_NSCAL + S_BB];
+            c->cgs_hist.push_back(bb > 0 ? std::sqrt(hscal[col * S_NSCAL + S_RR] / bb) : 0.0);
+        }
         bool all = true;
         for (int col = 0; col < nrhs; ++col) all = all && hflags[col * F_NFLAG + F_DONE];
         if (all) break;

@@ -218,6 +218,13 @@ class MLFMA:
             return dict(x=X[:, 0], iters=int(it[0]), relres=float(rr[0]), status=CGS_STATUS[int(st[0])])
         return dict(x=X, iters=it, relres=rr, status=[CGS_STATUS[int(s)] for s in st])
 
+    def cgs_history(self, col: int = 0):
+        n = C.c_int()
+        _check(load().mlf_cgs_history(self._h, int(col), None, 0, C.byref(n)), self._h)
+        h = np.zeros(n.value)
+        _check(load().mlf_cgs_history(self._h, int(col), _p(h), n.value, C.byref(n)), self._h)
+        return h
+
     def CGSold(self, b, guess, errmax, prec=False, maxit=100000):
         return self.cgs(b, guess, errmax, maxit, 1 if prec else 0)
 

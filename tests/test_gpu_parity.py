@@ -176,12 +176,27 @@ def test_cgs_ilu0_matches_oracle(ico3):
     b = m.excitation(d, ajustar_polariz(d, "VV"))
     # ILU0-preconditioned CGS is erratic on this body (as in the reference), so
     # rounding differences grow along the iteration: compare the first steps
-    for k in (1, 2, 4):
+    # (measured growth: ~1e-16 at k = 1, ~1e-7 at k = 4)
+    for k, tol in ((1, 1e-10), (2, 1e-9), (4, 1e-6)):
         out = m.cgs(b, errmax=1e-12, maxit=k, precond=1)
         ref = o.cgs(b, tol=1e-12, maxit=k, prec=True)
         assert out["iters"] == ref["iters"] == k
-        assert _rel(out["x"], ref["x"]) < 1e-9, k
-        assert abs(out["relres"] - ref["relres"]) < 1e-8 * ref["relres"], k
+        assert _rel(out["x"], ref["x"]) < tol, k
+        assert abs(out["relres"] - ref["relres"]) < tol * ref["relres"], k
+
+
+def test_cgs_ilu0_against_binary_run(ico3):
+    """The binary's precond=ilu0, errsolver=1e-3 run on the same mesh."""
+    _, m, _ = ico3
+    g = load_golden("bin_ico3_ilu0.npz")
+    assert m.ilu0() == 0
+    d = direction(90.0, 180.0)
+    b = m.excitation(d, ajustar_polariz(d, "VV"))
+    out = m.cgs(b, errmax=1e-3, maxit=3000, precond=1)
+    assert out["status"] == "converged"
+    assert abs(out["iters"] - int(g["iterations"])) <= 0.1 * int(g["iterations"])
+    assert np.linalg.norm(m.matvec(g["I"]) - b) / np.linalg.norm(b) < 1e-3
+    assert _rel(out["x"], g["I"]) < 1e-2
 
 
 def test_cgs_multi_rhs_per_column(ico3):
