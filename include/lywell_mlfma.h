@@ -97,6 +97,21 @@ int mlf_matvec(mlf_ctx* ctx, const double* x, double* y, int nrhs, int ld);
 int mlf_matvec_device(mlf_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, int ld,
                       void* stream);
 
+/* Allocation-free variant of mlf_matvec_device for one right-hand side
+ * (x, y: device arrays of N complex(8)).  It has no counterpart in the
+ * reference.  It is for callers that must not allocate device memory
+ * while they solve: hosts that record their iteration into a CUDA graph,
+ * or hosts whose device memory belongs to another runtime or a fixed
+ * pool.  It runs the same kernels as mlf_matvec_device but keeps the
+ * multipole fields in one fixed 64 MiB device array inside the library
+ * (held by every GPU that loads it, until exit) and never calls
+ * cudaMalloc/cudaFree.  Octrees whose C, B and A fields together exceed
+ * 4,194,304 complex values are rejected with MLF_E_ARG.  The first call on
+ * a device looks up the array's address; make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race.
+ * stream NULL = the context's stream. */
+int mlf_matvec_device_noalloc(mlf_ctx* ctx, const void* x_dev, void* y_dev, void* stream);
+
 /* Near-field block in CSR (1-based), values complex(4) interleaved floats.
  * Call with a/ja/ia NULL to get *nnz.  Replaces the public module data
  * Zesparcida_MLFMA, ja_MLFMA, ia_MLFMA, n_esparcida_MLFMA (modMLFMA.f90:12, 30-32). */

@@ -22,6 +22,7 @@ SIGNATURES = {
     "mlf_last_error": (C.c_char_p, [vp]),
     "mlf_matvec": (C.c_int, [vp, vp, vp, C.c_int, C.c_int]),
     "mlf_matvec_device": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, vp]),
+    "mlf_matvec_device_noalloc": (C.c_int, [vp, vp, vp, vp]),
     "mlf_near_csr": (C.c_int, [vp, C.POINTER(C.c_longlong), vp, vp, vp]),
     "mlf_ilu0": (C.c_int, [vp, ip]),
     "mlf_ilu0_factors": (C.c_int, [vp, vp, vp, vp]),

@@ -165,6 +165,14 @@ class MLFMA:
         _check(load().mlf_matvec_device(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), nrhs, self.N,
                                         C.c_void_p(stream) if stream else None), self._h)
 
+    def matvec_device_noalloc(self, x_ptr: int, y_ptr: int, stream: int = 0):
+        """One-column matvec on device arrays that allocates nothing: the
+        multipole fields live in the library's fixed 64 MiB device scratch
+        (for hosts that cannot allocate mid-solve); raises MLFError when the
+        octree's fields do not fit."""
+        _check(load().mlf_matvec_device_noalloc(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr),
+                                                C.c_void_p(stream) if stream else None), self._h)
+
     def near_csr(self):
         """(ia, ja, a) with 1-based ia/ja and complex64 values (Zesparcida_MLFMA)."""
         nnz = C.c_longlong()
