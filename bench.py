@@ -196,7 +196,7 @@ def main():
     ap.add_argument("--workload", default="sphere6", choices=list(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-time-to-rcs", action="store_true")
-    ap.add_argument("--rcs-maxit", type=int, default=1500)
+    ap.add_argument("--rcs-maxit", type=int, default=4000)
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -296,29 +296,41 @@ def main():
             "stage_ms": {"aggregation": stage_ms[0], "interpolation": stage_ms[1], "translation": stage_ms[2],
                          "anterpolation": stage_ms[3], "receive_near": stage_ms[4]}}
 
-    # time to RCS: set-up + CGS to 1e-4 + bistatic RCS cuts (phi = 0 and 90 deg, theta 0..180 step 1)
+    # time to RCS: set-up (octree, tables, patterns, near field, preconditioner) + solve to
+    # 1e-4 + two bistatic cuts (phi = 0, 90 deg; theta = 0..180 deg step 1)
     ttr = None
     if not args.no_time_to_rcs:
-        torch.cuda.synchronize()
-        t0 = time.time()
-        m2 = MLFMA(RWG(tris), lam=wl["lam"], ladomax=wl["ladomax"])
-        t_setup = time.time() - t0
         d = np.array([0.0, 0.0, 1.0])      # x-polarised wave incident from -z (propagating along +z)
         pol = np.array([1.0, 0, 0], dtype=np.complex128)
-        t1 = time.time()
-        b = m2.excitation(d, pol)
-        out = m2.cgs(b, errmax=1e-4, maxit=args.rcs_maxit)
-        t_solve = time.time() - t1
         th = np.deg2rad(np.arange(0, 181, 1.0))
-        t2 = time.time()
-        s0 = m2.rcs(out["x"], pol, th, np.zeros_like(th))
-        s9 = m2.rcs(out["x"], pol, th, np.full_like(th, np.pi / 2))
-        t_rcs = time.time() - t2
-        ttr = {"seconds": t_setup + t_solve + t_rcs, "setup_s": t_setup, "solve_s": t_solve, "rcs_s": t_rcs,
-               "cgs_iters": out["iters"], "cgs_status": out["status"], "relres": out["relres"],
-               "precond": "none", "rcs_angles": int(2 * th.size),
-               "rcs_db_phi0_mid": float(10 * np.log10(s0[90])), "rcs_db_phi90_mid": float(10 * np.log10(s9[90]))}
-        m2.close()
+        ttr = {}
+        rcs_ref = None
+        for label, mixed in (("fp64_cgs_nearinv", False), ("mixed_gmres_ir_nearinv", True)):
+            torch.cuda.synchronize()
+            t0 = time.time()
+            m2 = MLFMA(RWG(tris), lam=wl["lam"], ladomax=wl["ladomax"])
+            bad = m2.nearinv()
+            t_setup = time.time() - t0
+            t1 = time.time()
+            b = m2.excitation(d, pol)
+            out = m2.solve(b, errmax=1e-4, maxit=args.rcs_maxit, precond="nearinv", mixed=mixed)
+            t_solve = time.time() - t1
+            t2 = time.time()
+            s0 = m2.rcs(out["x"], pol, th, np.zeros_like(th))
+            s9 = m2.rcs(out["x"], pol, th, np.full_like(th, np.pi / 2))
+            t_rcs = time.time() - t2
+            true_res = float(np.linalg.norm(m2.matvec(out["x"]) - b) / np.linalg.norm(b))
+            db = 10 * np.log10(np.concatenate([s0, s9]))
+            ent = {"seconds": t_setup + t_solve + t_rcs, "setup_s": t_setup, "solve_s": t_solve, "rcs_s": t_rcs,
+                   "iters": out["iters"], "outer": out.get("outer", 0), "status": out["status"],
+                   "relres_fp64": true_res, "nearinv_bad_box": bad, "rcs_angles": int(db.size)}
+            if rcs_ref is None:
+                rcs_ref = db
+            else:
+                ent["rcs_db_maxdiff_vs_fp64"] = float(np.abs(db - rcs_ref).max())
+            ttr[label] = ent
+            m2.close()
+        ttr["speedup_mixed_vs_fp64"] = ttr["fp64_cgs_nearinv"]["seconds"] / ttr["mixed_gmres_ir_nearinv"]["seconds"]
 
     launches_per_matvec = 1 + (m.nlev - 3) + (m.nlev - 2) + (m.nlev - 3) + 1
     line = {"metric": METRIC, "value": value, "unit": "matvec/s", "n_gpus": ws, "steps": args.steps,

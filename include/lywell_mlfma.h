@@ -48,6 +48,13 @@ enum {
     MLF_CGS_STAGNATED = 4    /* no progress over the stagnation window */
 };
 
+/* mlf_cgs preconditioners */
+enum {
+    MLF_PRECOND_NONE = 0,
+    MLF_PRECOND_ILU0 = 1,     /* ilu0C + lusol0C, as the reference */
+    MLF_PRECOND_NEARINV = 2   /* neighbourhood inverse (mlf_nearinv); no counterpart in the reference */
+};
+
 /* mlf_init flags */
 enum {
     MLF_FLAG_LEGENDRE_RECURRENCE = 1 /* P_l by the three-term recurrence instead of the
@@ -134,13 +141,51 @@ int mlf_ilu0_solve(mlf_ctx* ctx, const double* y, double* x, int nrhs);
 /* Right-preconditioned CGS on the MLFMA operator, one or more right-hand
  * sides (each solved with its own scalars; converged columns retire).
  * b, x0, x: host complex(8) n x nrhs (ld = N).  x0 may be NULL (zero guess).
- * precond_kind: 0 none, 1 ILU0 (mlf_ilu0 must have succeeded).
+ * precond_kind: MLF_PRECOND_NONE, MLF_PRECOND_ILU0 (mlf_ilu0 must have
+ * succeeded) or MLF_PRECOND_NEARINV (mlf_nearinv must have succeeded).
  * maxit: iteration cap (the reference has none).  Per column outputs:
  * iters[nrhs], relres[nrhs] (true-recursion residual ||r||/||b||),
  * status_out[nrhs] (MLF_CGS_*).
  * Replaces: CGSold (modIterativo.f90:331-493). */
 int mlf_cgs(mlf_ctx* ctx, const double* b, const double* x0, double tol, int maxit, int nrhs,
             double* x, int* iters, double* relres, int precond_kind, int* status_out);
+
+/* Solve Z_MLFMA x = b for nrhs columns.  mode 0: CGS on the FP64 operator
+ * (exactly mlf_cgs).  mode 1: mixed precision — iterative refinement whose
+ * residual r = b - Z x is formed with the FP64 operator and whose
+ * corrections come from one right-preconditioned GMRES(m) cycle (m = 400 by
+ * default, mlf_set_gmres_restart) on the FP32
+ * operator (patterns, translations, interpolation and fields in float;
+ * complex(4) near field), stopped when its residual estimate drops below
+ * inner_tol ||b|| (<= 0: tol/2).  Stops when the FP64 residual satisfies
+ * ||b - Z x|| < tol ||b||, the same test as CGSold (modIterativo.f90:472).
+ * iters: inner GMRES steps (FP32 matvecs) per column; *outer: refinement
+ * steps (FP64 matvecs).  No counterpart in the reference for mode 1. */
+int mlf_solve(mlf_ctx* ctx, const double* b, const double* x0, double tol, int maxit, int nrhs,
+              int precond_kind, int mode, double inner_tol, double* x, int* iters, double* relres,
+              int* status_out, int* outer);
+
+/* Restart length m of mode 1's GMRES cycles (4..2000; memory (m+1) N nrhs
+ * complex(8) values). */
+int mlf_set_gmres_restart(mlf_ctx* ctx, int m);
+
+/* y = Z_MLFMA x with the FP32 operator of mode 1 (host or device arrays);
+ * inputs and outputs complex(8). */
+int mlf_matvec32(mlf_ctx* ctx, const double* x, double* y, int nrhs, int ld);
+int mlf_matvec32_device(mlf_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, int ld, void* stream);
+
+/* Neighbourhood-inverse preconditioner: for every leaf box, the rows of the
+ * inverse of its near-field neighbourhood block (the box's near list x
+ * itself, entries from the near CSR) that belong to the box's own bases;
+ * M has the near CSR's pattern.  No counterpart in the reference, which
+ * offers ILU0/ILUT (modIterativo.f90:1805-1976, 2432-2883); on the bodies
+ * measured here ILU0 makes CGS diverge while this one cuts the iteration
+ * count several-fold.  *bad_box = 0 on success, b+1 when box b's block is
+ * singular. */
+int mlf_nearinv(mlf_ctx* ctx, int* bad_box);
+
+/* Values of M (complex(8), interleaved) in the order of mlf_near_csr. */
+int mlf_nearinv_values(mlf_ctx* ctx, double* vals);
 
 /* Residual history ||r_i||/||b|| of column col of the last mlf_cgs call
  * (the per-iteration line CGSold prints, modIterativo.f90:446-465).
@@ -159,6 +204,20 @@ int mlf_excitation(mlf_ctx* ctx, const double* dirs, const double* pols, double 
  * calc_E (modRCS.f90:23-153). */
 int mlf_rcs(mlf_ctx* ctx, const double* I, const double* pol, double ctte_re, double ctte_im,
             const double* theta, const double* phi, int nang, double* sigma);
+
+/* Monostatic RCS sweep.  Replaces: gen_rcs_monostatica (main.f90:967-1089).
+ * nang angles phi_a (radians; phis NULL = the reference's grid
+ * (a-1) pi / nang), incidence d = (-cos phi, -sin phi, 0), polarisation VV
+ * (hh = 0) or HH (hh = 1), backscatter sigma(pi/2, phi_a) (linear) into
+ * sigma[nang]; iters/status_out per angle.
+ * mode 0: the reference's sequential sweep, CGS on the FP64 operator,
+ *         warm start = previous currents x exp(-j k (d_a - d_{a-1}) . r_edge).
+ * mode 1: batched, blocks of `block` angles as one multi-RHS FP64 CGS.
+ * mode 2: batched mixed precision (mlf_solve mode 1 per block).
+ * Modes 1 and 2 have no counterpart in the reference. */
+int mlf_monostatic(mlf_ctx* ctx, int nang, const double* phis, int hh, double ctte_re, double ctte_im,
+                   double tol, int maxit, int precond_kind, int mode, int block, double* sigma, int* iters,
+                   int* status_out);
 
 /* Octree summary for hosts and tests: out[0] = number of levels, out[1] = N;
  * for level l (1-based) out[5l .. 5l+4] = boxes, multipoles L, samples K,

@@ -28,10 +28,19 @@ SIGNATURES = {
     "mlf_ilu0_factors": (C.c_int, [vp, vp, vp, vp]),
     "mlf_ilu0_solve": (C.c_int, [vp, vp, vp, C.c_int]),
     "mlf_cgs": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp]),
+    "mlf_nearinv": (C.c_int, [vp, ip]),
+    "mlf_solve": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp, vp,
+                            vp, ip]),
+    "mlf_matvec32": (C.c_int, [vp, vp, vp, C.c_int, C.c_int]),
+    "mlf_set_gmres_restart": (C.c_int, [vp, C.c_int]),
+    "mlf_matvec32_device": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, vp]),
+    "mlf_nearinv_values": (C.c_int, [vp, vp]),
     "mlf_cgs_history": (C.c_int, [vp, C.c_int, vp, C.c_int, ip]),
     "mlf_excitation": (C.c_int, [vp, vp, vp, C.c_double, C.c_double, C.c_int, vp]),
     "mlf_rcs": (C.c_int, [vp, vp, vp, C.c_double, C.c_double, vp, vp, C.c_int, vp]),
     "mlf_info": (C.c_int, [vp, vp, C.POINTER(C.c_longlong)]),
+    "mlf_monostatic": (C.c_int, [vp, C.c_int, vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                                 C.c_int, C.c_int, vp, vp, vp]),
     "mlf_set_profiling": (C.c_int, [vp, C.c_int]),
     "mlf_stage_times": (C.c_int, [vp, vp]),
     "mlf_debug_field": (C.c_int, [vp, C.c_int, C.c_int, vp]),
@@ -41,6 +50,7 @@ STATUS = {0: "MLF_OK", -1: "MLF_E_ARG", -2: "MLF_E_TOO_SMALL", -3: "MLF_E_CUDA",
           -5: "MLF_E_TABLE", -6: "MLF_E_STATE", -7: "MLF_E_NOT_FINITE", -8: "MLF_E_NO_DEVICE"}
 CGS_STATUS = {0: "converged", 1: "maxit", 2: "breakdown", 3: "not_finite", 4: "stagnated"}
 FLAG_LEGENDRE_RECURRENCE = 1
+PRECOND = {"none": 0, "ilu0": 1, "nearinv": 2}
 
 _lib = None
 

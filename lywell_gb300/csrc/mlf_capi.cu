@@ -206,8 +206,12 @@ int mlf_cgs(mlf_ctx* h, const double* b, const double* x0, double tol, int maxit
     if (!h || !b || !x || !iters || !relres || !status_out || nrhs <= 0 || maxit <= 0 || !(tol > 0))
         return MLF_E_ARG;
     Ctx* c = &h->c;
-    if (precond_kind != 0 && precond_kind != 1) return MLF_E_ARG;
+    if (precond_kind < 0 || precond_kind > 2) return MLF_E_ARG;
     if (precond_kind == 1 && !c->ilu_ok) { c->err = "ILU0 requested but not factorised"; return MLF_E_STATE; }
+    if (precond_kind == 2 && !c->nearinv_ok) {
+        c->err = "neighbourhood inverse requested but not built";
+        return MLF_E_STATE;
+    }
     if (!bind_device(c)) return MLF_E_CUDA;
     const size_t n = (size_t)c->N * nrhs;
     double2 *db = nullptr, *dx = nullptr, *dx0 = nullptr;
@@ -225,6 +229,57 @@ int mlf_cgs(mlf_ctx* h, const double* b, const double* x0, double tol, int maxit
     cudaFree(dx);
     if (dx0) cudaFree(dx0);
     return st;
+}
+
+int mlf_solve(mlf_ctx* h, const double* b, const double* x0, double tol, int maxit, int nrhs, int precond_kind,
+              int mode, double inner_tol, double* x, int* iters, double* relres, int* status_out, int* outer) {
+    if (!h || !b || !x || !iters || !relres || !status_out || nrhs <= 0 || maxit <= 0 || !(tol > 0)) return MLF_E_ARG;
+    if (mode != 0 && mode != 1) return MLF_E_ARG;
+    if (mode == 0) {
+        if (outer) *outer = 0;
+        return mlf_cgs(h, b, x0, tol, maxit, nrhs, x, iters, relres, precond_kind, status_out);
+    }
+    Ctx* c = &h->c;
+    if (precond_kind < 0 || precond_kind > 2) return MLF_E_ARG;
+    if ((precond_kind == 1 && !c->ilu_ok) || (precond_kind == 2 && !c->nearinv_ok)) {
+        c->err = "requested preconditioner not built";
+        return MLF_E_STATE;
+    }
+    if (!bind_device(c)) return MLF_E_CUDA;
+    const size_t n = (size_t)c->N * nrhs;
+    double2 *db = nullptr, *dx = nullptr, *dx0 = nullptr;
+    CK(cudaMalloc(&db, n * sizeof(double2)));
+    CK(cudaMalloc(&dx, n * sizeof(double2)));
+    int st = h2d_cols(c, db, b, nrhs, c->N);
+    if (!st && x0) {
+        CK(cudaMalloc(&dx0, n * sizeof(double2)));
+        st = h2d_cols(c, dx0, x0, nrhs, c->N);
+    }
+    int outer_k = 0;
+    if (!st)
+        st = device_solve_mixed(c, db, dx0, tol, maxit, nrhs, dx, iters, relres, precond_kind, status_out,
+                                inner_tol > 0 ? inner_tol : 0.5 * tol, &outer_k);
+    if (outer) *outer = outer_k;
+    if (!st) st = d2h_cols(c, x, dx, nrhs, c->N);
+    if (!st) CK(cudaStreamSynchronize(c->stream));
+    cudaFree(db);
+    cudaFree(dx);
+    if (dx0) cudaFree(dx0);
+    return st;
+}
+
+int mlf_matvec32(mlf_ctx* h, const double* x, double* y, int nrhs, int ld) {
+    if (!h || !x || !y || nrhs <= 0 || ld < h->c.N) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    if (!bind_device(c)) return MLF_E_CUDA;
+    const size_t n = (size_t)c->N * nrhs;
+    int st;
+    if ((st = ensure_io(c, n))) return st;
+    if ((st = h2d_cols(c, c->dx_io, x, nrhs, ld))) return st;
+    if ((st = device_matvec32(c, c->dx_io, c->dy_io, nrhs, c->N, c->stream))) return st;
+    if ((st = d2h_cols(c, y, c->dy_io, nrhs, ld))) return st;
+    CK(cudaStreamSynchronize(c->stream));
+    return MLF_OK;
 }
 
 int mlf_cgs_history(mlf_ctx* h, int col, double* hist, int cap, int* n) {

@@ -537,6 +537,7 @@ int device_setup(Ctx* c) {
 static inline int chunks(int n, int bd) { return (n + bd - 1) / bd; }
 
 int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s) {
+    if (c->mv_prec == 1) return device_matvec32(c, x, y, nrhs, ld, s);
     int st;
     if ((st = ensure_fields(c, nrhs))) return st;
     c->last_nrhs = nrhs;
@@ -609,7 +610,8 @@ void device_free(Ctx* c) {
     F(c->dR); F(c->dperm); F(c->dbox_ptr); F(c->dbox_of_sorted); F(c->dia); F(c->dja); F(c->dZ);
     F(c->dp_coord); F(c->dt_baric); F(c->dt_baric_sub); F(c->de_long); F(c->de_centro); F(c->de_t);
     F(c->de_po); F(c->dalu); F(c->djlu); F(c->dju); F(c->dlvl_rows_f); F(c->dlvl_rows_b);
-    F(c->dwork); F(c->dscal); F(c->dflags); F(c->dx_io); F(c->dy_io);
+    F(c->dwork); F(c->dscal); F(c->dflags); F(c->dx_io); F(c->dy_io); F(c->dMinv);
+    mixed_free(c);
     for (int i = 0; i < 8; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);

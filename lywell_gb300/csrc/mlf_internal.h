@@ -61,8 +61,22 @@ struct Level {
     int fcap = 0;                 // right-hand sides the field buffers hold
 };
 
+// FP32 copies of the operator tables and FP32 fields (mixed-precision solve)
+struct Mixed32 {
+    int ready = 0, fcap = 0;
+    float2* R = nullptr;
+    float2* xf = nullptr;
+    struct Lv {
+        float2 *T = nullptr, *shift = nullptr, *C = nullptr, *B = nullptr, *A = nullptr;
+        float *wq = nullptr, *iw = nullptr, *ant_w = nullptr;
+    } lv[32];
+};
+
 struct Ctx {
     int dev = 0;
+    int mv_prec = 0;                  // operator precision used by device_matvec: 0 FP64, 1 FP32
+    int gmres_m = 400;                // restart length of the mixed-precision GMRES cycles
+    Mixed32 m32;
     cudaStream_t stream = nullptr;
     std::string err;
     Phys ph{};
@@ -95,6 +109,9 @@ struct Ctx {
     std::vector<int> jlu, ju;
     float2* dalu = nullptr;
     int *djlu = nullptr, *dju = nullptr;
+    // neighbourhood-inverse preconditioner (near CSR pattern)
+    double2* dMinv = nullptr;
+    int nearinv_ok = 0;
     // level schedule of the triangular solves
     std::vector<int> lvl_ptr_f, lvl_rows_f, lvl_ptr_b, lvl_rows_b;
     int *dlvl_rows_f = nullptr, *dlvl_rows_b = nullptr;
@@ -134,6 +151,12 @@ int device_ilu_upload(Ctx* c);
 int device_ilu_solve(Ctx* c, const double2* y, double2* x, cudaStream_t s);
 int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs,
                double2* x, int* iters, double* relres, int precond, int* status);
+int device_nearinv_setup(Ctx* c, int* bad_box);
+int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s);
+void mixed_free(Ctx* c);
+int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
+                       int* iters, double* relres, int precond, int* status, double inner_tol, int* outer);
+int device_nearinv_apply(Ctx* c, const double2* y, double2* x, int nrhs, cudaStream_t s);
 int device_excitation(Ctx* c, const double* dirs, const double2* pols, double2 ctte, int nrhs,
                       double2* b);
 int device_rcs(Ctx* c, const double2* I, const double2* pol, double2 ctte, const double* th,

@@ -1,0 +1,598 @@
+// Mixed-precision solve: FP32 MLFMA matvec inside an FP64 iterative-refinement
+// loop.  (An addition of this library: the reference runs its whole matvec
+// with complex(8) fields, modMLFMA.f90:1783-1946.)
+//
+// FP32 operator: radiation patterns, translation tables, interpolation and
+// anterpolation weights, phase-shift tables and all C/B/A fields are float;
+// every stage accumulates in FP32 on the CUDA cores, which GB300 runs 64x
+// faster than FP64; the near field is the reference's complex(4) block
+// itself.  Input and output vectors stay complex(8).
+//
+// Refinement (mode 1 of mlf_solve): r = b - A64 x in FP64; one restart cycle
+// of right-preconditioned GMRES(m) on the FP32 operator (FP64 vectors and
+// Arnoldi) solves A d = r until its residual estimate drops below
+// inner_tol ||b|| or m steps; x += M^-1 V y; stop when the FP64 residual
+// ||b - A64 x|| < tol ||b||.  The FP64 residual is the judge, so the result
+// meets the same stopping test as the plain FP64 solve.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mlf_internal.h"
+
+namespace mlf {
+
+#define CK(call)                                             \
+    do {                                                     \
+        if (!cuda_ok(c, (call), #call)) return MLF_E_CUDA;   \
+    } while (0)
+
+__device__ __forceinline__ void fmac(float2& acc, float2 a, float2 b) {
+    acc.x = fmaf(a.x, b.x, acc.x);
+    acc.x = fmaf(-a.y, b.y, acc.x);
+    acc.y = fmaf(a.x, b.y, acc.y);
+    acc.y = fmaf(a.y, b.x, acc.y);
+}
+
+__global__ void k32_from64(size_t n, const double2* __restrict__ a, float2* __restrict__ b) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+// x (FP64, ld) -> packed FP32 columns
+__global__ void k32_pack_x(int N, int nrhs, int ld, const double2* __restrict__ x, float2* __restrict__ xf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y;
+    if (i < N) {
+        const double2 v = x[(size_t)r * ld + i];
+        xf[(size_t)r * N + i] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+__global__ void k32_aggregate(int K, int nrhs, int N, const int* __restrict__ box_ptr, const int* __restrict__ perm,
+                              const float2* __restrict__ R, const float2* __restrict__ xf, float2* __restrict__ C) {
+    const int b = blockIdx.x / nrhs, r = blockIdx.x % nrhs;
+    const int j0 = box_ptr[b], j1 = box_ptr[b + 1];
+    const float2* xr = xf + (size_t)r * N;
+    for (int q = threadIdx.x; q < 2 * K; q += blockDim.x) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int j = j0; j < j1; ++j) fmac(acc, R[(size_t)j * 2 * K + q], xr[perm[j]]);
+        C[((size_t)b * nrhs + r) * 2 * K + q] = acc;
+    }
+}
+
+__global__ void k32_interp_up(int Kp, int Kc, int nrhs, int nchunk, const int* __restrict__ child_ptr,
+                              const int* __restrict__ octant, const float* __restrict__ iw,
+                              const int* __restrict__ iidx, const float2* __restrict__ shift,
+                              const float2* __restrict__ Cc, float2* __restrict__ Cp) {
+    const int chunk = blockIdx.x % nchunk;
+    const int pr = blockIdx.x / nchunk;
+    const int P = pr / nrhs, r = pr % nrhs;
+    const int q = chunk * blockDim.x + threadIdx.x;
+    if (q >= 2 * Kp) return;
+    const int pol = q >= Kp, m = q - pol * Kp;
+    float w9[9];
+    int i9[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) { w9[t] = iw[9 * m + t]; i9[t] = iidx[9 * m + t] + pol * Kc; }
+    float2 acc = make_float2(0.f, 0.f);
+    for (int cb = child_ptr[P]; cb < child_ptr[P + 1]; ++cb) {
+        const float2* src = Cc + ((size_t)cb * nrhs + r) * 2 * Kc;
+        float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < 9; ++t) {
+            const float2 s = src[i9[t]];
+            v.x = fmaf(w9[t], s.x, v.x);
+            v.y = fmaf(w9[t], s.y, v.y);
+        }
+        fmac(acc, v, shift[octant[cb] * Kp + m]);
+    }
+    Cp[((size_t)P * nrhs + r) * 2 * Kp + q] = acc;
+}
+
+__global__ void k32_translate(int K, int nrhs, int nchunk, const int* __restrict__ far_ptr,
+                              const int* __restrict__ far_src, const int* __restrict__ far_tid,
+                              const float2* __restrict__ T, const float* __restrict__ wq,
+                              const float2* __restrict__ C, float2* __restrict__ B) {
+    const int chunk = blockIdx.x % nchunk;
+    const int br = blockIdx.x / nchunk;
+    const int b = br / nrhs, r = br % nrhs;
+    const int q = chunk * blockDim.x + threadIdx.x;
+    if (q >= 2 * K) return;
+    const int k = q >= K ? q - K : q;
+    float2 acc = make_float2(0.f, 0.f);
+    const int f1 = far_ptr[b + 1];
+    for (int f = far_ptr[b]; f < f1; ++f)
+        fmac(acc, C[((size_t)far_src[f] * nrhs + r) * 2 * K + q], T[(size_t)far_tid[f] * K + k]);
+    const float wk = wq[k];
+    B[((size_t)b * nrhs + r) * 2 * K + q] = make_float2(acc.x * wk, acc.y * wk);
+}
+
+__global__ void k32_anterp_down(int Kp, int Kc, int nrhs, const int* __restrict__ parent,
+                                const int* __restrict__ octant, const int* __restrict__ ant_ptr,
+                                const int* __restrict__ ant_row, const float* __restrict__ ant_w,
+                                const float2* __restrict__ shift, const float2* __restrict__ Psrc,
+                                const float2* __restrict__ Bc, float2* __restrict__ Ac) {
+    extern __shared__ float2 D32[];
+    const int cb = blockIdx.x / nrhs, r = blockIdx.x % nrhs;
+    const int P = parent[cb];
+    const float2* sh = shift + (size_t)octant[cb] * Kp;
+    const float2* src = Psrc + ((size_t)P * nrhs + r) * 2 * Kp;
+    for (int q = threadIdx.x; q < 2 * Kp; q += blockDim.x) {
+        const int m = q >= Kp ? q - Kp : q;
+        const float2 s = sh[m];
+        const float2 v = src[q];
+        D32[q] = make_float2(v.x * s.x + v.y * s.y, v.y * s.x - v.x * s.y);
+    }
+    __syncthreads();
+    const size_t off = ((size_t)cb * nrhs + r) * 2 * Kc;
+    for (int q = threadIdx.x; q < 2 * Kc; q += blockDim.x) {
+        const int pol = q >= Kc, k = q - pol * Kc;
+        float2 acc = make_float2(0.f, 0.f);
+        const int e1 = ant_ptr[k + 1];
+        for (int e = ant_ptr[k]; e < e1; ++e) {
+            const float w = ant_w[e];
+            const float2 d = D32[ant_row[e] + pol * Kp];
+            acc.x = fmaf(w, d.x, acc.x);
+            acc.y = fmaf(w, d.y, acc.y);
+        }
+        const float2 bv = Bc[off + q];
+        Ac[off + q] = make_float2(bv.x + acc.x, bv.y + acc.y);
+    }
+}
+
+__global__ void k32_receive_near(int K, int N, int nrhs, int ld, const int* __restrict__ perm,
+                                 const int* __restrict__ box_of_sorted, const float2* __restrict__ R,
+                                 const float2* __restrict__ A, const int* __restrict__ ia, const int* __restrict__ ja,
+                                 const float2* __restrict__ Z, const float2* __restrict__ xf, float facy,
+                                 double2* __restrict__ y) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= N * nrhs) return;
+    const int j = gw / nrhs, r = gw % nrhs;
+    const int n = perm[j], b = box_of_sorted[j];
+    const float2* Rj = R + (size_t)j * 2 * K;
+    const float2* Ab = A + ((size_t)b * nrhs + r) * 2 * K;
+    float sr = 0.f, si = 0.f;
+    for (int q = lane; q < 2 * K; q += 32) {
+        const float2 a = Rj[q], v = Ab[q];
+        sr = fmaf(a.x, v.x, sr); sr = fmaf(a.y, v.y, sr);
+        si = fmaf(a.x, v.y, si); si = fmaf(-a.y, v.x, si);
+    }
+    const float2* xr = xf + (size_t)r * N;
+    float nr = 0.f, ni = 0.f;
+    for (int q = ia[n] + lane; q < ia[n + 1]; q += 32) {
+        const float2 z = Z[q];
+        const float2 xv = xr[ja[q]];
+        nr = fmaf(xv.x, z.x, nr); nr = fmaf(-xv.y, z.y, nr);
+        ni = fmaf(xv.x, z.y, ni); ni = fmaf(xv.y, z.x, ni);
+    }
+    float tr = fmaf(-facy, si, nr), ti = fmaf(facy, sr, ni);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        tr += __shfl_xor_sync(0xffffffff, tr, o);
+        ti += __shfl_xor_sync(0xffffffff, ti, o);
+    }
+    if (lane == 0) y[(size_t)r * ld + n] = make_double2((double)tr, (double)ti);
+}
+
+// ---------------------------------------------------------------------------
+
+static int up32(Ctx* c, float** dst, const std::vector<double>& v) {
+    std::vector<float> f(v.begin(), v.end());
+    CK(cudaMalloc(dst, std::max<size_t>(f.size(), 1) * sizeof(float)));
+    if (!f.empty()) CK(cudaMemcpy(*dst, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return MLF_OK;
+}
+
+static int conv32(Ctx* c, float2** dst, const double2* src, size_t n) {
+    CK(cudaMalloc(dst, std::max<size_t>(n, 1) * sizeof(float2)));
+    if (n) k32_from64<<<(unsigned)std::min<size_t>((n + 255) / 256, 65535), 256, 0, c->stream>>>(n, src, *dst);
+    CK(cudaGetLastError());
+    return MLF_OK;
+}
+
+int mixed_setup(Ctx* c) {
+    if (c->m32.ready) return MLF_OK;
+    const int nl = c->nlev;
+    int st;
+    if ((st = conv32(c, &c->m32.R, c->dR, (size_t)c->N * 2 * c->lv[nl].K))) return st;
+    for (int n = 3; n <= nl; ++n) {
+        Level& L = c->lv[n];
+        Mixed32::Lv& M = c->m32.lv[n];
+        if ((st = conv32(c, &M.T, L.dT, (size_t)L.ntrans * L.K))) return st;
+        if ((st = up32(c, &M.wq, L.wq))) return st;
+        if (n < nl) {
+            if ((st = up32(c, &M.iw, L.iw))) return st;
+            if ((st = up32(c, &M.ant_w, L.ant_w))) return st;
+            std::vector<double2> sh(8 * (size_t)L.K);
+            CK(cudaMemcpy(sh.data(), L.dshift, sh.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+            std::vector<float2> s32(sh.size());
+            for (size_t i = 0; i < sh.size(); ++i) s32[i] = make_float2((float)sh[i].x, (float)sh[i].y);
+            CK(cudaMalloc(&M.shift, s32.size() * sizeof(float2)));
+            CK(cudaMemcpy(M.shift, s32.data(), s32.size() * sizeof(float2), cudaMemcpyHostToDevice));
+        }
+    }
+    size_t mx = 0;
+    for (int n = 3; n < nl; ++n) mx = std::max(mx, 2 * (size_t)c->lv[n].K * sizeof(float2));
+    CK(cudaFuncSetAttribute(k32_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    CK(cudaStreamSynchronize(c->stream));
+    c->m32.ready = 1;
+    return MLF_OK;
+}
+
+static int ensure_fields32(Ctx* c, int nrhs) {
+    if (c->m32.fcap >= nrhs && c->m32.xf) return MLF_OK;
+    for (int n = 3; n <= c->nlev; ++n) {
+        Mixed32::Lv& M = c->m32.lv[n];
+        if (M.C) cudaFree(M.C);
+        if (M.B) cudaFree(M.B);
+        if (M.A) cudaFree(M.A);
+        const size_t f = (size_t)c->lv[n].nb * nrhs * 2 * c->lv[n].K;
+        CK(cudaMalloc(&M.C, f * sizeof(float2)));
+        CK(cudaMalloc(&M.B, f * sizeof(float2)));
+        CK(cudaMalloc(&M.A, f * sizeof(float2)));
+    }
+    if (c->m32.xf) cudaFree(c->m32.xf);
+    CK(cudaMalloc(&c->m32.xf, (size_t)c->N * nrhs * sizeof(float2)));
+    c->m32.fcap = nrhs;
+    return MLF_OK;
+}
+
+int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s) {
+    int st;
+    if ((st = mixed_setup(c))) return st;
+    if ((st = ensure_fields32(c, nrhs))) return st;
+    const int nl = c->nlev;
+    Level& leaf = c->lv[nl];
+    const bool prof = c->profiling != 0;
+    if (prof) cudaEventRecord(c->ev[0], s);
+    k32_pack_x<<<dim3((c->N + 255) / 256, nrhs), 256, 0, s>>>(c->N, nrhs, ld, x, c->m32.xf);
+    k32_aggregate<<<leaf.nb * nrhs, 256, 0, s>>>(leaf.K, nrhs, c->N, c->dbox_ptr, c->dperm, c->m32.R, c->m32.xf,
+                                                 c->m32.lv[nl].C);
+    if (prof) cudaEventRecord(c->ev[1], s);
+    for (int n = nl; n >= 4; --n) {
+        Level& Lc = c->lv[n];
+        Level& Lp = c->lv[n - 1];
+        const int bd = 256, nch = (2 * Lp.K + bd - 1) / bd;
+        k32_interp_up<<<Lp.nb * nrhs * nch, bd, 0, s>>>(Lp.K, Lc.K, nrhs, nch, Lp.dchild_ptr, Lc.doctant,
+                                                        c->m32.lv[n - 1].iw, Lp.diidx, c->m32.lv[n - 1].shift,
+                                                        c->m32.lv[n].C, c->m32.lv[n - 1].C);
+    }
+    if (prof) cudaEventRecord(c->ev[2], s);
+    for (int n = 3; n <= nl; ++n) {
+        Level& L = c->lv[n];
+        const int bd = 128, nch = (2 * L.K + bd - 1) / bd;
+        k32_translate<<<L.nb * nrhs * nch, bd, 0, s>>>(L.K, nrhs, nch, L.dfar_ptr, L.dfar_src, L.dfar_tid,
+                                                       c->m32.lv[n].T, c->m32.lv[n].wq, c->m32.lv[n].C,
+                                                       c->m32.lv[n].B);
+    }
+    if (prof) cudaEventRecord(c->ev[3], s);
+    for (int n = 4; n <= nl; ++n) {
+        Level& Lc = c->lv[n];
+        Level& Lp = c->lv[n - 1];
+        const float2* Psrc = (n == 4) ? c->m32.lv[n - 1].B : c->m32.lv[n - 1].A;
+        const size_t smem = 2 * (size_t)Lp.K * sizeof(float2);
+        k32_anterp_down<<<Lc.nb * nrhs, 256, smem, s>>>(Lp.K, Lc.K, nrhs, Lc.dparent, Lc.doctant, Lp.dant_ptr,
+                                                        Lp.dant_row, c->m32.lv[n - 1].ant_w, c->m32.lv[n - 1].shift,
+                                                        Psrc, c->m32.lv[n].B, c->m32.lv[n].A);
+    }
+    if (prof) cudaEventRecord(c->ev[4], s);
+    {
+        const long long warps = (long long)c->N * nrhs;
+        const float facy = (float)(c->ph.w * MU / (4. * PI));
+        k32_receive_near<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+            leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, c->m32.lv[nl].A, c->dia, c->dja, c->dZ,
+            c->m32.xf, facy, y);
+    }
+    if (prof) cudaEventRecord(c->ev[5], s);
+    if (!cuda_ok(c, cudaGetLastError(), "matvec32")) return MLF_E_CUDA;
+    if (prof) {
+        CK(cudaEventSynchronize(c->ev[5]));
+        for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&c->stage_ms[i], c->ev[i], c->ev[i + 1]);
+    }
+    return MLF_OK;
+}
+
+void mixed_free(Ctx* c) {
+    auto F = [](void* p) { if (p) cudaFree(p); };
+    F(c->m32.R); F(c->m32.xf);
+    for (int n = 0; n < 32; ++n) {
+        Mixed32::Lv& M = c->m32.lv[n];
+        F(M.T); F(M.wq); F(M.iw); F(M.ant_w); F(M.shift); F(M.C); F(M.B); F(M.A);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// GMRES-IR: FP64 iterative refinement, each step one right-preconditioned
+// GMRES(m) cycle on the FP32 operator (classical Gram-Schmidt applied twice).
+// The reference's CGS (kept as mode 0) is too erratic to tolerate an
+// operator perturbed at the 1e-7 level; GMRES minimises the residual over
+// the Krylov space and cannot diverge.
+// ---------------------------------------------------------------------------
+
+constexpr int GM_BLOCKS = 128;
+
+__global__ void k_resid(size_t n, const double2* __restrict__ b, const double2* __restrict__ Ax,
+                        double2* __restrict__ r) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        r[i] = make_double2(b[i].x - Ax[i].x, b[i].y - Ax[i].y);
+}
+__global__ void k_axpy1(size_t n, const double2* __restrict__ d, double2* __restrict__ x) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        x[i].x += d[i].x;
+        x[i].y += d[i].y;
+    }
+}
+
+// partial[(i*nrhs + col)*GM_BLOCKS + blk] = sum conj(V_i) w   (grid: GM_BLOCKS, nrhs, nvec)
+// or, with V == nullptr, sum |w|^2 in the real part (nvec = 1).
+__global__ void k_mdot(int N, int nrhs, const double2* __restrict__ V, size_t vstride, const double2* __restrict__ w,
+                       double2* __restrict__ partial) {
+    const int col = blockIdx.y, i = blockIdx.z;
+    const double2* wc = w + (size_t)col * N;
+    const double2* vc = V ? V + i * vstride + (size_t)col * N : nullptr;
+    double sr = 0, si = 0;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+        const double2 b = wc[e];
+        if (vc) {
+            const double2 a = vc[e];   // conj(a) * b
+            sr = fma(a.x, b.x, sr); sr = fma(a.y, b.y, sr);
+            si = fma(a.x, b.y, si); si = fma(-a.y, b.x, si);
+        } else {
+            sr = fma(b.x, b.x, sr); sr = fma(b.y, b.y, sr);
+        }
+    }
+    __shared__ double rs[256], is[256];
+    rs[threadIdx.x] = sr;
+    is[threadIdx.x] = si;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) { rs[threadIdx.x] += rs[threadIdx.x + s]; is[threadIdx.x] += is[threadIdx.x + s]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[((size_t)i * nrhs + col) * gridDim.x + blockIdx.x] = make_double2(rs[0], is[0]);
+}
+
+// out[k] = sum_b partial[k*GM_BLOCKS + b], fixed order
+__global__ void k_reduce_partials(int nk, const double2* __restrict__ partial, double2* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    double2 s = make_double2(0, 0);
+    for (int b = 0; b < GM_BLOCKS; ++b) {
+        s.x += partial[(size_t)k * GM_BLOCKS + b].x;
+        s.y += partial[(size_t)k * GM_BLOCKS + b].y;
+    }
+    out[k] = s;
+}
+
+// w -= sum_{i<nvec} h[i*nrhs+col] V_i
+__global__ void k_gs_update(int N, int nrhs, int nvec, const double2* __restrict__ V, size_t vstride,
+                            const double2* __restrict__ h, double2* __restrict__ w) {
+    const int col = blockIdx.y;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+        double2 acc = w[(size_t)col * N + e];
+        for (int i = 0; i < nvec; ++i) {
+            const double2 hv = h[i * nrhs + col];
+            const double2 v = V[i * vstride + (size_t)col * N + e];
+            acc.x -= hv.x * v.x - hv.y * v.y;
+            acc.y -= hv.x * v.y + hv.y * v.x;
+        }
+        w[(size_t)col * N + e] = acc;
+    }
+}
+
+// dst[col] = src[col] * s[col] (real scale per column)
+__global__ void k_colscale(int N, const double2* __restrict__ src, const double* __restrict__ s, double2* __restrict__ dst) {
+    const int col = blockIdx.y;
+    const double f = s[col];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+        const double2 v = src[(size_t)col * N + e];
+        dst[(size_t)col * N + e] = make_double2(v.x * f, v.y * f);
+    }
+}
+
+// d[col] = sum_{i<nvec} y[i*nrhs+col] V_i[col]
+__global__ void k_combine(int N, int nrhs, int nvec, const double2* __restrict__ V, size_t vstride,
+                          const double2* __restrict__ y, double2* __restrict__ d) {
+    const int col = blockIdx.y;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+        double2 acc = make_double2(0, 0);
+        for (int i = 0; i < nvec; ++i) {
+            const double2 yv = y[i * nrhs + col];
+            const double2 v = V[i * vstride + (size_t)col * N + e];
+            acc.x += yv.x * v.x - yv.y * v.y;
+            acc.y += yv.x * v.y + yv.y * v.x;
+        }
+        d[(size_t)col * N + e] = acc;
+    }
+}
+
+namespace {
+struct Cx {
+    double r, i;
+};
+inline Cx cx(double r, double i) { return {r, i}; }
+inline Cx operator+(Cx a, Cx b) { return {a.r + b.r, a.i + b.i}; }
+inline Cx operator-(Cx a, Cx b) { return {a.r - b.r, a.i - b.i}; }
+inline Cx operator*(Cx a, Cx b) { return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; }
+inline Cx conjx(Cx a) { return {a.r, -a.i}; }
+inline double absx(Cx a) { return std::hypot(a.r, a.i); }
+inline Cx divx(Cx a, Cx b) {
+    const double d = b.r * b.r + b.i * b.i;
+    return {(a.r * b.r + a.i * b.i) / d, (a.i * b.r - a.r * b.i) / d};
+}
+}  // namespace
+
+static int col_norms(Ctx* c, int nrhs, const double2* w, double2* partial, double2* dred, std::vector<double2>& h,
+                     std::vector<double>& out, cudaStream_t s) {
+    k_mdot<<<dim3(GM_BLOCKS, nrhs, 1), 256, 0, s>>>(c->N, nrhs, nullptr, 0, w, partial);
+    k_reduce_partials<<<(nrhs + 127) / 128, 128, 0, s>>>(nrhs, partial, dred);
+    CK(cudaMemcpyAsync(h.data(), dred, nrhs * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int col = 0; col < nrhs; ++col) out[col] = std::sqrt(h[col].x);
+    return MLF_OK;
+}
+
+int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
+                       int* iters, double* relres, int precond, int* status, double inner_tol, int* outer) {
+    const int N = c->N;
+    const int m = std::max(4, std::min(c->gmres_m, 2000));
+    const size_t V1 = (size_t)N * nrhs;
+    cudaStream_t s = c->stream;
+    double2 *V = nullptr, *w = nullptr, *t = nullptr, *r = nullptr, *partial = nullptr, *dred = nullptr;
+    double* dscale = nullptr;
+    CK(cudaMalloc(&V, (size_t)(m + 1) * V1 * sizeof(double2)));
+    CK(cudaMalloc(&w, V1 * sizeof(double2)));
+    CK(cudaMalloc(&t, V1 * sizeof(double2)));
+    CK(cudaMalloc(&r, V1 * sizeof(double2)));
+    CK(cudaMalloc(&partial, (size_t)(m + 1) * nrhs * GM_BLOCKS * sizeof(double2)));
+    CK(cudaMalloc(&dred, (size_t)(m + 1) * nrhs * sizeof(double2)));
+    CK(cudaMalloc(&dscale, nrhs * sizeof(double)));
+    if (x0) CK(cudaMemcpyAsync(x, x0, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    else CK(cudaMemsetAsync(x, 0, V1 * sizeof(double2), s));
+    const unsigned g = (unsigned)std::min<size_t>((N + 255) / 256, 2048);
+    const dim3 gc(g, nrhs);
+    std::vector<double2> hbuf((size_t)(m + 1) * nrhs);
+    std::vector<double> bn(nrhs), beta(nrhs), scl(nrhs);
+    if (int st = col_norms(c, nrhs, b, partial, dred, hbuf, bn, s)) return st;
+    std::fill(iters, iters + nrhs, 0);
+    std::vector<int> done(nrhs, 0);
+    // per column: Hessenberg (column-major (m+1) x m), Givens (cs, sn), rhs g
+    std::vector<Cx> H((size_t)nrhs * (m + 1) * m), G((size_t)nrhs * (m + 1)), CS((size_t)nrhs * m), SN((size_t)nrhs * m);
+    auto Hc = [&](int col, int i, int j) -> Cx& { return H[((size_t)col * m + j) * (m + 1) + i]; };
+    int st = MLF_OK, k = 0;
+    const int max_outer = 1000;
+    for (; k < max_outer; ++k) {
+        c->mv_prec = 0;
+        if ((st = device_matvec(c, x, t, nrhs, N, s))) break;
+        k_resid<<<4096, 256, 0, s>>>(V1, b, t, r);
+        if ((st = col_norms(c, nrhs, r, partial, dred, hbuf, beta, s))) break;
+        bool all = true, budget = false;
+        for (int col = 0; col < nrhs; ++col) {
+            relres[col] = bn[col] > 0 ? beta[col] / bn[col] : 0.0;
+            if (!done[col] && (relres[col] < tol || bn[col] == 0)) { done[col] = 1; status[col] = MLF_CGS_CONVERGED; }
+            if (!std::isfinite(relres[col]) && !done[col]) { done[col] = 1; status[col] = MLF_CGS_NOT_FINITE; }
+            all = all && done[col];
+            budget = budget || (!done[col] && iters[col] < maxit);
+        }
+        if (all || !budget) break;
+        for (int col = 0; col < nrhs; ++col) scl[col] = (!done[col] && beta[col] > 0) ? 1.0 / beta[col] : 0.0;
+        CK(cudaMemcpyAsync(dscale, scl.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
+        k_colscale<<<gc, 256, 0, s>>>(N, r, dscale, V);
+        std::fill(H.begin(), H.end(), cx(0, 0));
+        std::fill(G.begin(), G.end(), cx(0, 0));
+        for (int col = 0; col < nrhs; ++col) G[(size_t)col * (m + 1)] = cx(done[col] ? 0.0 : beta[col], 0);
+        std::vector<int> jcol(nrhs, 0);   // Krylov dimension reached per column
+        std::vector<int> live(nrhs, 0);
+        for (int col = 0; col < nrhs; ++col) live[col] = !done[col];
+        int j = 0;
+        for (; j < m; ++j) {
+            bool any = false;
+            for (int col = 0; col < nrhs; ++col) any = any || live[col];
+            if (!any) break;
+            const double2* vj = V + (size_t)j * V1;
+            if (precond == 2) { if ((st = device_nearinv_apply(c, vj, t, nrhs, s))) break; }
+            else if (precond == 1) {
+                for (int col = 0; col < nrhs && !st; ++col)
+                    st = device_ilu_solve(c, vj + (size_t)col * N, t + (size_t)col * N, s);
+                if (st) break;
+            } else CK(cudaMemcpyAsync(t, vj, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+            c->mv_prec = 1;
+            st = device_matvec(c, t, w, nrhs, N, s);
+            c->mv_prec = 0;
+            if (st) break;
+            std::vector<double2> hsum((size_t)(j + 1) * nrhs, make_double2(0, 0));
+            for (int pass = 0; pass < 2; ++pass) {
+                k_mdot<<<dim3(GM_BLOCKS, nrhs, j + 1), 256, 0, s>>>(N, nrhs, V, V1, w, partial);
+                k_reduce_partials<<<((j + 1) * nrhs + 127) / 128, 128, 0, s>>>((j + 1) * nrhs, partial, dred);
+                k_gs_update<<<gc, 256, 0, s>>>(N, nrhs, j + 1, V, V1, dred, w);
+                CK(cudaMemcpyAsync(hbuf.data(), dred, (size_t)(j + 1) * nrhs * sizeof(double2), cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                for (size_t q = 0; q < (size_t)(j + 1) * nrhs; ++q) { hsum[q].x += hbuf[q].x; hsum[q].y += hbuf[q].y; }
+            }
+            std::vector<double> hn(nrhs);
+            if ((st = col_norms(c, nrhs, w, partial, dred, hbuf, hn, s))) break;
+            for (int col = 0; col < nrhs; ++col) scl[col] = (live[col] && hn[col] > 1e-300) ? 1.0 / hn[col] : 0.0;
+            CK(cudaMemcpyAsync(dscale, scl.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
+            k_colscale<<<gc, 256, 0, s>>>(N, w, dscale, V + (size_t)(j + 1) * V1);
+            for (int col = 0; col < nrhs; ++col) {
+                if (!live[col]) continue;
+                for (int i = 0; i <= j; ++i) Hc(col, i, j) = cx(hsum[(size_t)i * nrhs + col].x, hsum[(size_t)i * nrhs + col].y);
+                Hc(col, j + 1, j) = cx(hn[col], 0);
+                // apply previous rotations, then a new one that zeroes H(j+1, j)
+                for (int i = 0; i < j; ++i) {
+                    const Cx a = Hc(col, i, j), bq = Hc(col, i + 1, j);
+                    const Cx c_ = CS[(size_t)col * m + i], s_ = SN[(size_t)col * m + i];
+                    Hc(col, i, j) = conjx(c_) * a + conjx(s_) * bq;
+                    Hc(col, i + 1, j) = cx(0, 0) - s_ * a + c_ * bq;
+                }
+                const Cx a = Hc(col, j, j), bq = Hc(col, j + 1, j);
+                const double nrm = std::hypot(absx(a), absx(bq));
+                Cx c_ = cx(1, 0), s_ = cx(0, 0);
+                if (nrm > 0) { c_ = divx(a, cx(nrm, 0)); s_ = divx(bq, cx(nrm, 0)); }
+                CS[(size_t)col * m + j] = c_;
+                SN[(size_t)col * m + j] = s_;
+                Hc(col, j, j) = cx(nrm, 0);
+                Hc(col, j + 1, j) = cx(0, 0);
+                const Cx gj = G[(size_t)col * (m + 1) + j];
+                G[(size_t)col * (m + 1) + j] = conjx(c_) * gj;
+                G[(size_t)col * (m + 1) + j + 1] = cx(0, 0) - s_ * gj;
+                jcol[col] = j + 1;
+                iters[col] += 1;
+                const double est = absx(G[(size_t)col * (m + 1) + j + 1]);
+                if (est < inner_tol * bn[col] || hn[col] <= 1e-300 * bn[col] || iters[col] >= maxit) live[col] = 0;
+            }
+        }
+        if (st) break;
+        // y = H^-1 g per column, d = V y, x += M^-1 d
+        std::vector<double2> y((size_t)(m + 1) * nrhs, make_double2(0, 0));
+        int jmax = 0;
+        for (int col = 0; col < nrhs; ++col) {
+            const int jj = jcol[col];
+            jmax = std::max(jmax, jj);
+            std::vector<Cx> yy(jj);
+            for (int i = jj - 1; i >= 0; --i) {
+                Cx acc = G[(size_t)col * (m + 1) + i];
+                for (int q = i + 1; q < jj; ++q) acc = acc - Hc(col, i, q) * yy[q];
+                yy[i] = Hc(col, i, i).r != 0 || Hc(col, i, i).i != 0 ? divx(acc, Hc(col, i, i)) : cx(0, 0);
+            }
+            for (int i = 0; i < jj; ++i) y[(size_t)i * nrhs + col] = make_double2(yy[i].r, yy[i].i);
+        }
+        if (jmax == 0) break;
+        CK(cudaMemcpyAsync(dred, y.data(), (size_t)jmax * nrhs * sizeof(double2), cudaMemcpyHostToDevice, s));
+        k_combine<<<gc, 256, 0, s>>>(N, nrhs, jmax, V, V1, dred, w);
+        if (precond == 2) { if ((st = device_nearinv_apply(c, w, t, nrhs, s))) break; }
+        else if (precond == 1) {
+            for (int col = 0; col < nrhs && !st; ++col) st = device_ilu_solve(c, w + (size_t)col * N, t + (size_t)col * N, s);
+            if (st) break;
+        } else CK(cudaMemcpyAsync(t, w, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        k_axpy1<<<4096, 256, 0, s>>>(V1, t, x);
+        CK(cudaGetLastError());
+    }
+    c->mv_prec = 0;
+    for (int col = 0; col < nrhs; ++col)
+        if (!done[col]) status[col] = MLF_CGS_MAXIT;
+    *outer = k;
+    cudaFree(V); cudaFree(w); cudaFree(t); cudaFree(r); cudaFree(partial); cudaFree(dred); cudaFree(dscale);
+    return st;
+}
+
+}  // namespace mlf
+
+using namespace mlf;
+
+extern "C" int mlf_set_gmres_restart(mlf_ctx* h, int m) {
+    if (!h || m < 4 || m > 2000) return MLF_E_ARG;
+    h->c.gmres_m = m;
+    return MLF_OK;
+}
+
+extern "C" int mlf_matvec32_device(mlf_ctx* h, const void* x, void* y, int nrhs, int ld, void* stream) {
+    if (!h || !x || !y || nrhs <= 0 || ld < h->c.N) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
+    return device_matvec32(c, (const double2*)x, (double2*)y, nrhs, ld, stream ? (cudaStream_t)stream : c->stream);
+}

@@ -1,0 +1,256 @@
+// Neighbourhood-inverse preconditioner (an addition of this library; the
+// reference offers ILU0/ILUT, modIterativo.f90:1805-1976, 2432-2883).
+//
+// For each leaf box b with neighbourhood S (the sorted near list of b, i.e.
+// the column set of every row of b in the near-field CSR) take
+// A = Znear[S, S] (entries absent from the CSR are zero) and keep the rows of
+// A^-1 that belong to b's own bases.  Stacked, these rows form M with the
+// near CSR's own sparsity pattern; M is fixed and linear, so
+// right-preconditioned CGS stays valid.  Rows of A^-1 solve A^T X = E_own.
+//
+// Set-up: one CTA per box, Gaussian elimination with partial pivoting
+// (largest |a|^2, first row on ties) in FP64 on a per-CTA workspace slab.
+// Apply: a warp-per-row SpMV with the near CSR pattern.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "mlf_internal.h"
+
+namespace mlf {
+
+#define CK(call)                                             \
+    do {                                                     \
+        if (!cuda_ok(c, (call), #call)) return MLF_E_CUDA;   \
+    } while (0)
+
+__device__ __forceinline__ int bsearch_sorted(const int* S, int n, int v) {
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int s = S[mid];
+        if (s == v) return mid;
+        if (s < v) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ double2 zdiv(double2 a, double2 b) {
+    const double d = b.x * b.x + b.y * b.y;
+    return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+constexpr int NBI_THREADS = 256;
+
+__global__ void __launch_bounds__(NBI_THREADS)
+k_nbhd_inverse(int b0, int nb, const int* __restrict__ box_ptr, const int* __restrict__ box_bases,
+               const int* __restrict__ ia, const int* __restrict__ ja, const float2* __restrict__ Z,
+               size_t slab, double2* __restrict__ work, double2* __restrict__ M, int* __restrict__ bad) {
+    const int b = b0 + blockIdx.x;
+    if (b >= nb) return;
+    const int tid = threadIdx.x, bd = blockDim.x;
+    const int m0 = box_bases[box_ptr[b]];
+    const int n = ia[m0 + 1] - ia[m0];
+    const int* S = ja + ia[m0];
+    const int nown = box_ptr[b + 1] - box_ptr[b];
+    double2* At = work + (size_t)blockIdx.x * slab;   // n x n, row-major, holds A^T
+    double2* X = At + (size_t)n * n;                   // n x nown
+    for (int i = tid; i < n * n; i += bd) At[i] = make_double2(0, 0);
+    for (int i = tid; i < n * nown; i += bd) X[i] = make_double2(0, 0);
+    __syncthreads();
+    for (int r = tid; r < n; r += bd) {
+        const int m = S[r];
+        for (int q = ia[m]; q < ia[m + 1]; ++q) {
+            const int pos = bsearch_sorted(S, n, ja[q]);
+            if (pos >= 0) At[(size_t)pos * n + r] = make_double2((double)Z[q].x, (double)Z[q].y);
+        }
+    }
+    for (int i = tid; i < nown; i += bd) {
+        const int pos = bsearch_sorted(S, n, box_bases[box_ptr[b] + i]);
+        X[(size_t)pos * nown + i] = make_double2(1.0, 0.0);
+    }
+    __shared__ double s_val[NBI_THREADS / 32];
+    __shared__ int s_idx[NBI_THREADS / 32];
+    __shared__ int s_piv;
+    __shared__ int s_sing;
+    if (tid == 0) s_sing = 0;
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        // pivot: largest |a|^2 in column k at or below the diagonal, first on ties
+        double best = -1.0;
+        int bi = n;
+        for (int i = k + tid; i < n; i += bd) {
+            const double2 a = At[(size_t)i * n + k];
+            const double v = a.x * a.x + a.y * a.y;
+            if (v > best) { best = v; bi = i; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffff, best, o);
+            const int oi = __shfl_xor_sync(0xffffffff, bi, o);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if ((tid & 31) == 0) { s_val[tid >> 5] = best; s_idx[tid >> 5] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+            double bv = s_val[0];
+            int bx = s_idx[0];
+            for (int w = 1; w < bd / 32; ++w)
+                if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bx)) { bv = s_val[w]; bx = s_idx[w]; }
+            s_piv = bx;
+            if (!(bv > 0.0)) s_sing = 1;
+        }
+        __syncthreads();
+        if (s_sing) break;
+        const int piv = s_piv;
+        if (piv != k) {
+            for (int j = tid; j < n; j += bd) {
+                const double2 t = At[(size_t)k * n + j];
+                At[(size_t)k * n + j] = At[(size_t)piv * n + j];
+                At[(size_t)piv * n + j] = t;
+            }
+            for (int j = tid; j < nown; j += bd) {
+                const double2 t = X[(size_t)k * nown + j];
+                X[(size_t)k * nown + j] = X[(size_t)piv * nown + j];
+                X[(size_t)piv * nown + j] = t;
+            }
+        }
+        __syncthreads();
+        const double2 d = At[(size_t)k * n + k];
+        for (int i = k + 1 + tid; i < n; i += bd) At[(size_t)i * n + k] = zdiv(At[(size_t)i * n + k], d);
+        __syncthreads();
+        const int rows = n - k - 1, wcols = (n - k - 1) + nown;
+        for (int e = tid; e < rows * wcols; e += bd) {
+            const int i = k + 1 + e / wcols, jj = e % wcols;
+            const double2 f = At[(size_t)i * n + k];
+            double2* dst;
+            double2 src;
+            if (jj < n - k - 1) {
+                dst = &At[(size_t)i * n + k + 1 + jj];
+                src = At[(size_t)k * n + k + 1 + jj];
+            } else {
+                dst = &X[(size_t)i * nown + (jj - (n - k - 1))];
+                src = X[(size_t)k * nown + (jj - (n - k - 1))];
+            }
+            double2 v = *dst;
+            v.x -= f.x * src.x - f.y * src.y;
+            v.y -= f.x * src.y + f.y * src.x;
+            *dst = v;
+        }
+        __syncthreads();
+    }
+    if (s_sing) {
+        if (tid == 0) atomicMin(bad, b + 1);
+        return;
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        const double2 d = At[(size_t)k * n + k];
+        for (int j = tid; j < nown; j += bd) X[(size_t)k * nown + j] = zdiv(X[(size_t)k * nown + j], d);
+        __syncthreads();
+        for (int e = tid; e < k * nown; e += bd) {
+            const int i = e / nown, j = e % nown;
+            const double2 f = At[(size_t)i * n + k];
+            const double2 s = X[(size_t)k * nown + j];
+            double2 v = X[(size_t)i * nown + j];
+            v.x -= f.x * s.x - f.y * s.y;
+            v.y -= f.x * s.y + f.y * s.x;
+            X[(size_t)i * nown + j] = v;
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < nown * n; e += bd) {
+        const int i = e / n, j = e % n;
+        const int g = box_bases[box_ptr[b] + i];
+        M[(size_t)ia[g] + j] = X[(size_t)j * nown + i];
+    }
+}
+
+// y[:, col] = M x[:, col], one warp per (row, column), near CSR pattern
+__global__ void k_spmv_z(int N, int nrhs, const int* __restrict__ ia, const int* __restrict__ ja,
+                         const double2* __restrict__ M, const double2* __restrict__ x, double2* __restrict__ y) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (gw >= N * nrhs) return;
+    const int m = gw % N, col = gw / N;
+    const double2* xc = x + (size_t)col * N;
+    double sr = 0, si = 0;
+    for (int q = ia[m] + lane; q < ia[m + 1]; q += 32) {
+        const double2 a = M[q], v = xc[ja[q]];
+        sr = fma(a.x, v.x, sr); sr = fma(-a.y, v.y, sr);
+        si = fma(a.x, v.y, si); si = fma(a.y, v.x, si);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffff, sr, o);
+        si += __shfl_xor_sync(0xffffffff, si, o);
+    }
+    if (lane == 0) y[(size_t)col * N + m] = make_double2(sr, si);
+}
+
+int device_nearinv_setup(Ctx* c, int* bad_box) {
+    const int nl = c->nlev;
+    const Level& leaf = c->lv[nl];
+    int nmax = 0, nownmax = 0;
+    for (int b = 0; b < leaf.nb; ++b) {
+        nmax = std::max(nmax, c->near_ptr[b + 1] - c->near_ptr[b]);
+        nownmax = std::max(nownmax, c->box_ptr[b + 1] - c->box_ptr[b]);
+    }
+    const size_t slab = (size_t)nmax * nmax + (size_t)nmax * nownmax;
+    int batch = (int)std::min<size_t>(leaf.nb, std::max<size_t>(1, ((size_t)1 << 30) / (slab * sizeof(double2))));
+    batch = std::min(batch, 4096);
+    if (c->dMinv) cudaFree(c->dMinv);
+    c->dMinv = nullptr;
+    c->nearinv_ok = 0;
+    CK(cudaMalloc(&c->dMinv, std::max<long long>(c->nnz, 1) * sizeof(double2)));
+    double2* work = nullptr;
+    int* dbad = nullptr;
+    int* dbases = nullptr;
+    CK(cudaMalloc(&work, slab * batch * sizeof(double2)));
+    CK(cudaMalloc(&dbad, sizeof(int)));
+    const int big = 0x7fffffff;
+    CK(cudaMemcpy(dbad, &big, sizeof(int), cudaMemcpyHostToDevice));
+    dbases = c->dperm;   // the box-sorted basis list
+    for (int b0 = 0; b0 < leaf.nb; b0 += batch) {
+        k_nbhd_inverse<<<std::min(batch, leaf.nb - b0), NBI_THREADS, 0, c->stream>>>(
+            b0, leaf.nb, c->dbox_ptr, dbases, c->dia, c->dja, c->dZ, slab, work, c->dMinv, dbad);
+        CK(cudaGetLastError());
+    }
+    int hbad = 0;
+    CK(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(work);
+    cudaFree(dbad);
+    *bad_box = hbad == big ? 0 : hbad;
+    c->nearinv_ok = *bad_box == 0;
+    return MLF_OK;
+}
+
+int device_nearinv_apply(Ctx* c, const double2* y, double2* x, int nrhs, cudaStream_t s) {
+    if (!c->nearinv_ok) {
+        c->err = "neighbourhood-inverse preconditioner not built (mlf_nearinv has not succeeded)";
+        return MLF_E_STATE;
+    }
+    const long long warps = (long long)c->N * nrhs;
+    k_spmv_z<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(c->N, nrhs, c->dia, c->dja, c->dMinv, y, x);
+    return cuda_ok(c, cudaGetLastError(), "k_spmv_z") ? MLF_OK : MLF_E_CUDA;
+}
+
+}  // namespace mlf
+
+using namespace mlf;
+
+extern "C" int mlf_nearinv(mlf_ctx* h, int* bad_box) {
+    if (!h || !bad_box) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
+    return device_nearinv_setup(c, bad_box);
+}
+
+extern "C" int mlf_nearinv_values(mlf_ctx* h, double* vals) {
+    if (!h || !vals) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    if (!c->nearinv_ok) { c->err = "neighbourhood-inverse preconditioner not built"; return MLF_E_STATE; }
+    if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
+    CK(cudaMemcpy(vals, c->dMinv, c->nnz * sizeof(double2), cudaMemcpyDeviceToHost));
+    return MLF_OK;
+}

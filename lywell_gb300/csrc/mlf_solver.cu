@@ -333,6 +333,7 @@ static int precond_apply(Ctx* c, int precond, int nrhs, const double2* y, double
         CK(cudaMemcpyAsync(x, y, (size_t)nrhs * c->N * sizeof(double2), cudaMemcpyDeviceToDevice, s));
         return MLF_OK;
     }
+    if (precond == 2) return device_nearinv_apply(c, y, x, nrhs, s);
     for (int r = 0; r < nrhs; ++r) {
         const int st = device_ilu_solve(c, y + (size_t)r * c->N, x + (size_t)r * c->N, s);
         if (st) return st;

@@ -27,7 +27,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._capi import CGS_STATUS, FLAG_LEGENDRE_RECURRENCE, MLFError, load
+from ._capi import CGS_STATUS, FLAG_LEGENDRE_RECURRENCE, PRECOND, MLFError, load
 
 __all__ = ["RWG", "MLFMA", "MLFError", "FLAG_LEGENDRE_RECURRENCE", "ajustar_polariz", "direction"]
 
@@ -208,9 +208,23 @@ class MLFMA:
 
     lusol0C = lusol0
 
+    def nearinv(self) -> int:
+        """Build the neighbourhood-inverse preconditioner; 0 or (singular box + 1)."""
+        bad = C.c_int()
+        _check(load().mlf_nearinv(self._h, C.byref(bad)), self._h)
+        return int(bad.value)
+
+    def nearinv_values(self):
+        out = np.zeros(self.nnz, dtype=np.complex128)
+        _check(load().mlf_nearinv_values(self._h, _p(out)), self._h)
+        return out
+
     # -- solver
-    def cgs(self, b, guess=None, errmax=1e-4, maxit=1000, precond: int = 0):
-        """Returns dict(x, iters, relres, status) per column."""
+    def cgs(self, b, guess=None, errmax=1e-4, maxit=1000, precond=0):
+        """Returns dict(x, iters, relres, status) per column.  precond: 0/'none',
+        1/'ilu0', 2/'nearinv'."""
+        if isinstance(precond, str):
+            precond = PRECOND[precond]
         b = np.asarray(b, dtype=np.complex128)
         single = b.ndim == 1
         B = np.asfortranarray(b.reshape(self.N, -1))
@@ -232,6 +246,40 @@ class MLFMA:
         h = np.zeros(n.value)
         _check(load().mlf_cgs_history(self._h, int(col), _p(h), n.value, C.byref(n)), self._h)
         return h
+
+    def solve(self, b, guess=None, errmax=1e-4, maxit=1000, precond=0, mixed=False, inner_tol=0.0):
+        """mlf_solve: mixed=False is CGS on the FP64 operator; mixed=True is FP64
+        iterative refinement around CGS on the FP32 operator."""
+        if isinstance(precond, str):
+            precond = PRECOND[precond]
+        b = np.asarray(b, dtype=np.complex128)
+        single = b.ndim == 1
+        B = np.asfortranarray(b.reshape(self.N, -1))
+        nrhs = B.shape[1]
+        G = None if guess is None else np.asfortranarray(np.asarray(guess, dtype=np.complex128).reshape(self.N, -1))
+        X = np.zeros_like(B)
+        it = np.zeros(nrhs, dtype=np.int32)
+        rr = np.zeros(nrhs)
+        st = np.zeros(nrhs, dtype=np.int32)
+        outer = C.c_int()
+        _check(load().mlf_solve(self._h, _p(B), None if G is None else _p(G), float(errmax), int(maxit), nrhs,
+                                int(precond), 1 if mixed else 0, float(inner_tol), _p(X), _p(it), _p(rr), _p(st),
+                                C.byref(outer)), self._h)
+        if single:
+            return dict(x=X[:, 0], iters=int(it[0]), relres=float(rr[0]), status=CGS_STATUS[int(st[0])],
+                        outer=outer.value)
+        return dict(x=X, iters=it, relres=rr, status=[CGS_STATUS[int(s)] for s in st], outer=outer.value)
+
+    def set_gmres_restart(self, m: int):
+        _check(load().mlf_set_gmres_restart(self._h, int(m)), self._h)
+
+    def matvec32(self, x):
+        x = np.asarray(x, dtype=np.complex128)
+        single = x.ndim == 1
+        X = np.asfortranarray(x.reshape(self.N, -1))
+        Y = np.zeros_like(X)
+        _check(load().mlf_matvec32(self._h, _p(X), _p(Y), X.shape[1], self.N), self._h)
+        return Y[:, 0] if single else Y
 
     def CGSold(self, b, guess, errmax, prec=False, maxit=100000):
         return self.cgs(b, guess, errmax, maxit, 1 if prec else 0)
@@ -264,6 +312,25 @@ class MLFMA:
 
     def sigmaRCS(self, current, pol, theta, phi, ctte=1.0):
         return self.rcs(current, pol, theta, phi, ctte)
+
+    def monostatic(self, nang, phis=None, pol="VV", errmax=1e-3, maxit=5000, precond=0, mode=0, block=32,
+                   ctte=1.0):
+        """Monostatic sweep (gen_rcs_monostatica).  Returns dict(phi, sigma_db, iters, status).
+        mode 0: the reference's warm-started sequential sweep; 1: batched FP64 CGS;
+        2: batched mixed precision."""
+        if isinstance(precond, str):
+            precond = PRECOND[precond]
+        ph = None if phis is None else np.ascontiguousarray(phis, dtype=np.float64)
+        sig = np.zeros(nang)
+        it = np.zeros(nang, dtype=np.int32)
+        st = np.zeros(nang, dtype=np.int32)
+        _check(load().mlf_monostatic(self._h, int(nang), None if ph is None else _p(ph), 1 if pol == "HH" else 0,
+                                     float(np.real(ctte)), float(np.imag(ctte)), float(errmax), int(maxit),
+                                     int(precond), int(mode), int(block), _p(sig), _p(it), _p(st)), self._h)
+        phi = ph if ph is not None else np.arange(nang) * (np.pi / nang)
+        return dict(phi=phi, sigma_db=10 * np.log10(sig), iters=it, status=[CGS_STATUS[int(s)] for s in st])
+
+    gen_rcs_monostatica = monostatic
 
     # -- diagnostics
     def set_profiling(self, on=True):

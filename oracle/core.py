@@ -221,6 +221,20 @@ class OracleMLFMA:
         lib().ora_lusol0(self._h, _p(y), _p(x))
         return x
 
+    def nearinv(self) -> int:
+        return int(lib().ora_nearinv(C.c_void_p(self._h)))
+
+    def nearinv_values(self):
+        out = np.zeros(self.nnz, dtype=np.complex128)
+        lib().ora_nearinv_values(C.c_void_p(self._h), _p(out))
+        return out
+
+    def nearinv_apply(self, y):
+        y = np.ascontiguousarray(y, dtype=np.complex128)
+        x = np.zeros(self.N, dtype=np.complex128)
+        lib().ora_nearinv_apply(C.c_void_p(self._h), _p(y), _p(x))
+        return x
+
     def cgs(self, b, guess=None, tol=1e-4, maxit=1000, prec=False, history=False):
         b = np.ascontiguousarray(b, dtype=np.complex128)
         g = np.zeros(self.N, dtype=np.complex128) if guess is None else np.ascontiguousarray(guess, dtype=np.complex128)
@@ -228,7 +242,7 @@ class OracleMLFMA:
         it = C.c_int()
         rr = C.c_double()
         hist = np.zeros(maxit)
-        st = lib().ora_cgs(self._h, _p(b), _p(g), float(tol), int(maxit), 1 if prec else 0, _p(x),
+        st = lib().ora_cgs(self._h, _p(b), _p(g), float(tol), int(maxit), int(prec), _p(x),
                            C.byref(it), C.byref(rr), _p(hist))
         out = dict(x=x, status=int(st), iters=it.value, relres=rr.value)
         if history:
@@ -284,6 +298,31 @@ def direction_from_angles(theta_deg, phi_deg):
     t = theta_deg * PI / f180
     p = phi_deg * PI / f180
     return np.array([np.sin(t) * np.cos(p), np.sin(t) * np.sin(p), np.cos(t)])
+
+
+def monostatic_sweep(o: "OracleMLFMA", nang, pol="VV", tol=1e-3, maxit=5000, prec=0):
+    """gen_rcs_monostatica (main.f90:967-1089): sequential angles phi = (a-1) pi/nang,
+    incidence (-cos, -sin, 0), warm start = previous currents x exp(-j k dR . r_edge),
+    backscatter sigma(pi/2, phi).  Returns (phi, sigma_dB, iterations)."""
+    r = o.rwg
+    kappa = 2. * PI / o.lam
+    dephi = 1. * PI / nang
+    guess = np.zeros(o.N, dtype=np.complex128)
+    prev = np.array([-1., 0., 0.])
+    phis, out_db, its = [], [], []
+    for a in range(1, nang + 1):
+        phi = (a - 1) * dephi
+        d = np.array([-np.cos(phi), -np.sin(phi), 0.])
+        dR = d - prev
+        guess = guess * np.exp((-1j) * kappa * (r.e_centro @ dR))
+        pol_v = ajustar_polariz(d, pol)
+        b = generar_onda(r, o.lam, d, pol_v)
+        res = o.cgs(b, guess=guess, tol=tol, maxit=maxit, prec=prec)
+        s = sigma_rcs(r, o.lam, res["x"], pol_v, PI / 2., phi)[0]
+        phis.append(phi); out_db.append(10 * np.log10(s)); its.append(res["iters"])
+        guess = res["x"]
+        prev = d
+    return np.array(phis), np.array(out_db), np.array(its)
 
 
 def ilu0_raw(n, a, ja, ia):

@@ -184,6 +184,7 @@ typedef struct {
     int* jlu;
     int* ju;
     int ilu_status;        /* -1 not built */
+    cplx* minv;            /* neighbourhood-inverse preconditioner, near CSR pattern */
     int nthreads;
 } Ctx;
 
@@ -640,6 +641,7 @@ void ora_free(Ctx* c) {
     for (int n = 1; n <= c->nlev && n < 32; n++) free_level(&c->lv[n]);
     free(c->box_ptr); free(c->box_bases); free(c->box_of); free(c->near_ptr); free(c->near_bases);
     free(c->frad); free(c->ia); free(c->ja); free(c->zn); free(c->alu); free(c->jlu); free(c->ju);
+    free(c->minv);
     free(c);
 }
 
@@ -972,6 +974,106 @@ int ora_ilu0(Ctx* c) {
 void ora_lusol0(Ctx* c, const cplx* y, cplx* x) { lusol0(c->N, y, x, c->alu, c->jlu, c->ju); }
 
 /* ------------------------------------------------------------------ */
+/* neighbourhood-inverse preconditioner                                 */
+/* ------------------------------------------------------------------ */
+
+/* For every leaf box b with neighbourhood S (the sorted near list of b, the
+ * column set of each of b's rows in the near CSR), A = Znear[S, S] (entries
+ * absent from the CSR are zero).  The rows of A^-1 that belong to b's own
+ * bases become the rows of M, so M has the near CSR's pattern and
+ * M x = sum over boxes of (A^-1 x_S)[own].  Rows of A^-1 solve
+ * A^T X = E_own (Gaussian elimination with partial pivoting, largest |a|^2,
+ * first index on ties, in double).  This preconditioner is an addition of
+ * this build (the reference offers ILU0/ILUT only); it is linear and fixed,
+ * so right-preconditioned CGS stays valid.  Returns 0 or the first box whose
+ * block is singular (+1). */
+int ora_nearinv(Ctx* c) {
+    Level* leaf = &c->lv[c->nlev];
+    free(c->minv);
+    c->minv = xcalloc(c->nnz, sizeof(cplx));
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int b = 0; b < leaf->nb; b++) {
+        int m0 = c->box_bases[c->box_ptr[b]];
+        int n = c->ia[m0 + 1] - c->ia[m0];
+        const int* S = c->ja + c->ia[m0];
+        int nown = c->box_ptr[b + 1] - c->box_ptr[b];
+        cplx* At = xcalloc((size_t)n * n, sizeof(cplx));
+        cplx* X = xcalloc((size_t)n * nown, sizeof(cplx));
+        for (int r = 0; r < n; r++) {
+            int m = S[r];
+            for (int q = c->ia[m]; q < c->ia[m + 1]; q++) {
+                int col = c->ja[q];
+                int lo = 0, hi = n - 1, pos = -1;
+                while (lo <= hi) {
+                    int mid = (lo + hi) / 2;
+                    if (S[mid] == col) { pos = mid; break; }
+                    if (S[mid] < col) lo = mid + 1; else hi = mid - 1;
+                }
+                if (pos >= 0) At[(size_t)pos * n + r] = (double)crealf(c->zn[q]) + I * (double)cimagf(c->zn[q]);
+            }
+        }
+        for (int i = 0; i < nown; i++) {
+            int g = c->box_bases[c->box_ptr[b] + i];
+            for (int j = 0; j < n; j++) if (S[j] == g) X[(size_t)j * nown + i] = 1.0;
+        }
+        int sing = 0;
+        for (int k = 0; k < n && !sing; k++) {
+            int piv = k;
+            double best = -1.0;
+            for (int i = k; i < n; i++) {
+                cplx a = At[(size_t)i * n + k];
+                double v = creal(a) * creal(a) + cimag(a) * cimag(a);
+                if (v > best) { best = v; piv = i; }
+            }
+            if (best == 0.0) { sing = 1; break; }
+            if (piv != k) {
+                for (int j = 0; j < n; j++) { cplx t = At[(size_t)k * n + j]; At[(size_t)k * n + j] = At[(size_t)piv * n + j]; At[(size_t)piv * n + j] = t; }
+                for (int j = 0; j < nown; j++) { cplx t = X[(size_t)k * nown + j]; X[(size_t)k * nown + j] = X[(size_t)piv * nown + j]; X[(size_t)piv * nown + j] = t; }
+            }
+            cplx d = At[(size_t)k * n + k];
+            for (int i = k + 1; i < n; i++) {
+                cplx f = At[(size_t)i * n + k] / d;
+                if (f == 0) continue;
+                for (int j = k + 1; j < n; j++) At[(size_t)i * n + j] -= f * At[(size_t)k * n + j];
+                for (int j = 0; j < nown; j++) X[(size_t)i * nown + j] -= f * X[(size_t)k * nown + j];
+            }
+        }
+        if (sing) {
+#pragma omp critical
+            { if (!bad || b + 1 < bad) bad = b + 1; }
+        } else {
+            for (int k = n - 1; k >= 0; k--) {
+                cplx d = At[(size_t)k * n + k];
+                for (int j = 0; j < nown; j++) X[(size_t)k * nown + j] /= d;
+                for (int i = 0; i < k; i++) {
+                    cplx f = At[(size_t)i * n + k];
+                    for (int j = 0; j < nown; j++) X[(size_t)i * nown + j] -= f * X[(size_t)k * nown + j];
+                }
+            }
+            for (int i = 0; i < nown; i++) {
+                int g = c->box_bases[c->box_ptr[b] + i];
+                for (int j = 0; j < n; j++) c->minv[c->ia[g] + j] = X[(size_t)j * nown + i];
+            }
+        }
+        free(At); free(X);
+    }
+    return bad;
+}
+
+static void nearinv_apply(Ctx* c, const cplx* y, cplx* x) {
+#pragma omp parallel for schedule(static)
+    for (int m = 0; m < c->N; m++) {
+        cplx s = 0;
+        for (int q = c->ia[m]; q < c->ia[m + 1]; q++) s = s + c->minv[q] * y[c->ja[q]];
+        x[m] = s;
+    }
+}
+
+void ora_nearinv_apply(Ctx* c, const cplx* y, cplx* x) { nearinv_apply(c, y, x); }
+void ora_nearinv_values(Ctx* c, cplx* out) { memcpy(out, c->minv, sizeof(cplx) * c->nnz); }
+
+/* ------------------------------------------------------------------ */
 /* CGS                                                                  */
 /* ------------------------------------------------------------------ */
 
@@ -983,7 +1085,8 @@ static double nrm2(const cplx* v, int n) {
 
 /* CGSold, modIterativo.f90:331-493, with an iteration cap added.
  * matvec: this context's MLFMA matvec.  prec: 1 = ILU0 factors of the
- * context (ora_ilu0 must have succeeded).  Returns 0 converged, 1 maxit,
+ * context (ora_ilu0 must have succeeded), 2 = neighbourhood inverse
+ * (ora_nearinv must have succeeded).  Returns 0 converged, 1 maxit,
  * 2 breakdown (rho == 0), 3 non-finite. */
 int ora_cgs(Ctx* c, const cplx* b, const cplx* guess, double errmax, int maxit, int prec,
             cplx* x, int* iters, double* relres, double* hist) {
@@ -1014,14 +1117,16 @@ int ora_cgs(Ctx* c, const cplx* b, const cplx* guess, double errmax, int maxit, 
                 p[i] = u[i] + (beta * (q[i] + (beta * p[i])));
             }
         }
-        if (prec) lusol0(n, p, P_, c->alu, c->jlu, c->ju);
+        if (prec == 1) lusol0(n, p, P_, c->alu, c->jlu, c->ju);
+        else if (prec == 2) nearinv_apply(c, p, P_);
         else memcpy(P_, p, sizeof(cplx) * n);
         ora_matvec(c, P_, V_);
         cplx sv = 0;
         for (int i = 0; i < n; i++) sv = sv + R_[i] * V_[i];
         cplx alfa = rho1 / sv;
         for (int i = 0; i < n; i++) { q[i] = u[i] - (alfa * V_[i]); tmp[i] = u[i] + q[i]; }
-        if (prec) lusol0(n, tmp, U_, c->alu, c->jlu, c->ju);
+        if (prec == 1) lusol0(n, tmp, U_, c->alu, c->jlu, c->ju);
+        else if (prec == 2) nearinv_apply(c, tmp, U_);
         else memcpy(U_, tmp, sizeof(cplx) * n);
         for (int i = 0; i < n; i++) x[i] = x[i] + (alfa * U_[i]);
         ora_matvec(c, U_, Q_);

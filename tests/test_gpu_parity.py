@@ -223,3 +223,41 @@ def test_cfg2_sphere_matvec_vs_oracle(gpu_lib):
     for x in _vectors(m.N, [0, 1]):
         assert _rel(m.matvec(x), o.matvec(x)) < 1e-12
     m.close()
+
+
+def test_monostatic_reference_sweep(ico3):
+    """mlf_monostatic mode 0 against the oracle's sweep and the binary's RCSMONO file."""
+    tris, m, o = ico3
+    _, _, a = m.near_csr()
+    o.set_near(a)
+    out = m.monostatic(4, pol="VV", errmax=1e-8, maxit=3000, mode=0)
+    phi, db, its = core.monostatic_sweep(o, 4, "VV", tol=1e-8)
+    assert all(s == "converged" for s in out["status"])
+    assert np.abs(out["sigma_db"] - db).max() < 1e-6
+    assert np.all(np.abs(out["iters"] - its) <= 2)
+    g = load_golden("bin_ico3_mono.npz")
+    assert np.abs(out["sigma_db"] - g["rcsmono"][:, 1]).max() < 1e-5
+
+
+def test_monostatic_batched_modes(ico3):
+    _, m, _ = ico3
+    ref = m.monostatic(12, pol="HH", errmax=1e-6, maxit=3000, mode=0)
+    b1 = m.monostatic(12, pol="HH", errmax=1e-6, maxit=3000, mode=1, block=5)
+    b2 = m.monostatic(12, pol="HH", errmax=1e-6, maxit=3000, mode=2, block=5)
+    for out in (b1, b2):
+        assert all(s == "converged" for s in out["status"])
+        assert np.abs(out["sigma_db"] - ref["sigma_db"]).max() < 0.01
+
+
+def test_five_level_octree_against_binary(gpu_lib):
+    g = load_golden("bin_ico4_mlfma.npz")
+    m = MLFMA(RWG(g["tris"]), lam=0.5, ladomax=0.3)
+    assert m.nlev == 5
+    d = direction(90.0, 180.0)
+    pol = ajustar_polariz(d, "VV")
+    b = m.excitation(d, pol)
+    assert np.linalg.norm(m.matvec(g["I"]) - b) / np.linalg.norm(b) < 5e-5
+    out = m.cgs(b, errmax=1e-7, maxit=3000)
+    assert out["status"] == "converged"
+    assert abs(out["iters"] - int(g["iterations"])) <= 0.05 * int(g["iterations"])
+    m.close()

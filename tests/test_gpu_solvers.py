@@ -1,0 +1,113 @@
+"""Preconditioner and mixed-precision paths on the GPU (no counterpart in the
+reference; checked against the oracle's restatement of the same algorithm
+and against the FP64 path).  Needs a GB300.
+
+Tolerances: neighbourhood-inverse rows 1e-11 relative (FP64 elimination
+with partial pivoting on both sides, different rounding order); the FP32
+operator agrees with the FP64 one to 2e-5 relative; a mixed-precision solve
+meets the FP64 residual test and its RCS lies within 0.1 dB of the FP64
+solve's.
+"""
+import numpy as np
+import pytest
+
+from lywell_gb300 import MLFMA, RWG, ajustar_polariz, direction, meshes
+from oracle import core
+from oracle.rwg import RWG as ORWG
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.ravel(a - b)) / np.linalg.norm(np.ravel(b)))
+
+
+@pytest.fixture(scope="module")
+def ico4(gpu_lib):
+    tris = meshes.icosphere(4, 1.5)
+    m = MLFMA(RWG(tris), lam=1.0, ladomax=0.25)
+    o = core.OracleMLFMA(ORWG(tris), lam=1.0, ladomax=0.25)
+    _, _, a = m.near_csr()
+    o.set_near(a)
+    yield tris, m, o
+    m.close()
+
+
+def test_nearinv_rows_match_oracle(ico4):
+    _, m, o = ico4
+    assert m.nearinv() == 0
+    assert o.nearinv() == 0
+    assert _rel(m.nearinv_values(), o.nearinv_values()) < 1e-11
+
+
+def test_nearinv_is_local_inverse(ico4):
+    """Row block of box b times Znear[S, S] gives the identity rows of b."""
+    _, m, o = ico4
+    ia, ja, z = m.near_csr()
+    ia0, ja0 = ia - 1, ja - 1
+    Mv = m.nearinv_values()
+    ptr, bases = o.leaf_boxes()
+    import scipy.sparse as sps
+    Z = sps.csr_matrix((z.astype(np.complex128), ja0, ia0), shape=(m.N, m.N))
+    for b in (0, len(ptr) // 2, len(ptr) - 2):
+        own = bases[ptr[b]:ptr[b + 1]]
+        S = ja0[ia0[own[0]]:ia0[own[0] + 1]]
+        A = Z[S][:, S].toarray()
+        rows = np.stack([Mv[ia0[g]:ia0[g + 1]] for g in own])
+        E = rows @ A
+        target = (S[None, :] == own[:, None]).astype(float)
+        assert np.abs(E - target).max() < 1e-8
+
+
+def test_cgs_nearinv_matches_oracle(ico4):
+    _, m, o = ico4
+    assert m.nearinv() == 0 and o.nearinv() == 0
+    b = m.excitation(np.array([0, 0, 1.0]), np.array([1, 0, 0], complex))
+    out = m.cgs(b, errmax=1e-4, maxit=2000, precond="nearinv")
+    ref = o.cgs(b, tol=1e-4, maxit=2000, prec=2)
+    assert out["status"] == "converged" and ref["status"] == 0
+    assert abs(out["iters"] - ref["iters"]) <= max(3, 0.05 * ref["iters"])
+    none = m.cgs(b, errmax=1e-4, maxit=3000)
+    assert out["iters"] < 0.5 * none["iters"]
+    res = np.linalg.norm(m.matvec(out["x"]) - b) / np.linalg.norm(b)
+    assert res < 1.01e-4
+
+
+def test_fp32_operator_close_to_fp64(ico4):
+    _, m, _ = ico4
+    rng = np.random.default_rng(3)
+    for _ in range(3):
+        x = rng.standard_normal(m.N) + 1j * rng.standard_normal(m.N)
+        assert _rel(m.matvec32(x), m.matvec(x)) < 2e-5
+
+
+def test_mixed_solve_meets_fp64_test_and_rcs(ico4):
+    _, m, _ = ico4
+    assert m.nearinv() == 0
+    d = np.array([0, 0, 1.0])
+    pol = np.array([1, 0, 0], complex)
+    b = m.excitation(d, pol)
+    ref = m.solve(b, errmax=1e-4, maxit=3000, precond="nearinv", mixed=False)
+    mix = m.solve(b, errmax=1e-4, maxit=3000, precond="nearinv", mixed=True)
+    assert ref["status"] == "converged" and mix["status"] == "converged"
+    res = np.linalg.norm(m.matvec(mix["x"]) - b) / np.linalg.norm(b)
+    assert res < 1e-4
+    assert abs(res - mix["relres"]) < 1e-9
+    th = np.deg2rad(np.arange(0, 181, 2.0))
+    for phi in (0.0, np.pi / 2):
+        s_ref = 10 * np.log10(m.rcs(ref["x"], pol, th, np.full_like(th, phi)))
+        s_mix = 10 * np.log10(m.rcs(mix["x"], pol, th, np.full_like(th, phi)))
+        assert np.abs(s_ref - s_mix).max() < 0.1
+
+
+def test_mixed_multi_rhs(ico4):
+    _, m, _ = ico4
+    assert m.nearinv() == 0
+    dirs = np.stack([direction(90.0, a) for a in (0.0, 45.0, 90.0)])
+    pols = np.stack([ajustar_polariz(d, "VV") for d in dirs])
+    B = m.excitation(dirs, pols)
+    out = m.solve(B, errmax=1e-4, maxit=3000, precond="nearinv", mixed=True)
+    for k in range(3):
+        assert out["status"][k] == "converged"
+        r = np.linalg.norm(m.matvec(out["x"][:, k]) - B[:, k]) / np.linalg.norm(B[:, k])
+        assert r < 1e-4

@@ -215,3 +215,30 @@ def test_ilu0_cgs_against_binary_run():
     np.testing.assert_allclose(out["history"][:5], hist[:5], rtol=2e-5)
     assert np.linalg.norm(o.matvec(g["I"]) - b) / np.linalg.norm(b) < 1e-3
     assert np.linalg.norm(out["x"] - g["I"]) / np.linalg.norm(g["I"]) < 1e-2
+
+
+def test_monostatic_sweep_matches_binary():
+    """gen_rcs_monostatica (main.f90:967-1089): 4 angles, VV, warm-started CGS to 1e-8."""
+    g = load_golden("bin_ico3_mono.npz")
+    r = RWG(g["tris"])
+    o = core.OracleMLFMA(r, lam=1.0, ladomax=0.3)
+    phi, db, its = core.monostatic_sweep(o, 4, "VV", tol=1e-8)
+    np.testing.assert_allclose(np.rad2deg(phi), g["rcsmono"][:, 0], atol=1e-9)
+    assert np.abs(db - g["rcsmono"][:, 1]).max() < 1e-6
+    assert its[-1] == int(g["iterations"])
+    assert abs(int(its.sum()) - len(g["res_hist"])) <= 10
+
+
+def test_five_level_octree_against_binary():
+    """icosphere-4 at lambda = 0.5 (7680 RWG, 5 levels): the binary's converged currents."""
+    g = load_golden("bin_ico4_mlfma.npz")
+    r = RWG(g["tris"])
+    o = core.OracleMLFMA(r, lam=0.5, ladomax=0.3)
+    assert o.nlev == 5
+    d = core.direction_from_angles(90.0, 180.0)
+    pol = core.ajustar_polariz(d, "VV")
+    b = core.generar_onda(r, 0.5, d, pol)
+    assert np.linalg.norm(o.matvec(g["I"]) - b) / np.linalg.norm(b) < 5e-5
+    th, ph = _bistatic_grid(5, 8)
+    rcs = 10 * np.log10(core.sigma_rcs(r, 0.5, g["I"], pol, th, ph)).reshape(5, 8)
+    assert np.abs(rcs - g["rcsbi"]).max() < 1e-4
