@@ -119,6 +119,19 @@ def fp64_peak_tflops(torch):
     return 2.0 * n ** 3 / best / 1e12
 
 
+def replica_rate(steps: int, t_local: float, ws: int, device="cpu"):
+    """Replicas only: every rank times its own `steps` matvecs; the job rate is
+    all ranks' matvecs over the slowest rank's time (max over ranks)."""
+    t = float(t_local)
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([t], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    return ws * steps / t, t
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -251,12 +264,7 @@ def main():
         torch.distributed.barrier()
     m.set_profiling(False)
     clk = clocks.stop()
-    t = e0.elapsed_time(e1) / 1e3
-    if ws > 1:
-        tt = torch.tensor([t], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
-    value = ws * args.steps / t
+    value, t = replica_rate(args.steps, e0.elapsed_time(e1) / 1e3, ws, "cuda")
     stage_ms = stage / args.steps
 
     # end to end through the public host API: pinned host x -> device -> host y

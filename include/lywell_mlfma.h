@@ -130,8 +130,19 @@ int mlf_near_csr(mlf_ctx* ctx, long long* nnz, float* a, int* ja, int* ia);
  * (modIterativo.f90:1805-1976). */
 int mlf_ilu0(mlf_ctx* ctx, int* ierr_row);
 
-/* Export the ILU0 factors in the reference's MSR layout (alu: complex(4)
- * interleaved, nnz+1 entries; jlu: nnz+1; ju: N; 1-based). */
+/* ILUT (dual threshold) of the near-field block, the reference's default
+ * preconditioner: lfil = ceiling(0.01 fill_in_prc N), drop tolerance
+ * droptol (ilut.fillin / ilut.droptol; defaults 5 and 1e-3).  The factors
+ * replace any ILU0 factors and are applied by mlf_ilu0_solve / precond kind
+ * MLF_PRECOND_ILU0.  *ierr as ilutC: 0, zero-pivot row k > 0, or -1..-5.
+ * Replaces: crear_precond ILUT branch (main.f90:904-960) -> ilutC
+ * (modIterativo.f90:2432-2883). */
+int mlf_ilut(mlf_ctx* ctx, double fill_in_prc, double droptol, int* ierr);
+
+/* Export the ILU0 / ILUT factors in the reference's MSR layout (alu:
+ * complex(4) interleaved, jlu: same length = jlu(N+1)-1 entries, nnz+1 for
+ * ILU0; ju: N; 1-based).  mlf_ilu_size gives that length. */
+int mlf_ilu_size(mlf_ctx* ctx, long long* len);
 int mlf_ilu0_factors(mlf_ctx* ctx, float* alu, int* jlu, int* ju);
 
 /* x = (LU)^-1 y for nrhs host columns.  Replaces: lusol0C

@@ -26,6 +26,8 @@ SIGNATURES = {
     "mlf_near_csr": (C.c_int, [vp, C.POINTER(C.c_longlong), vp, vp, vp]),
     "mlf_ilu0": (C.c_int, [vp, ip]),
     "mlf_ilu0_factors": (C.c_int, [vp, vp, vp, vp]),
+    "mlf_ilut": (C.c_int, [vp, C.c_double, C.c_double, ip]),
+    "mlf_ilu_size": (C.c_int, [vp, C.POINTER(C.c_longlong)]),
     "mlf_ilu0_solve": (C.c_int, [vp, vp, vp, C.c_int]),
     "mlf_cgs": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp]),
     "mlf_nearinv": (C.c_int, [vp, ip]),

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -173,12 +174,38 @@ int mlf_ilu0(mlf_ctx* h, int* ierr_row) {
     return MLF_OK;
 }
 
+int mlf_ilut(mlf_ctx* h, double fill_in_prc, double droptol, int* ierr_out) {
+    if (!h || !ierr_out || fill_in_prc < 0 || droptol < 0) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    if (!bind_device(c)) return MLF_E_CUDA;
+    c->ilu_ok = 0;
+    // crear_precond (main.f90:904-906): lfil = ceiling(0.01 * fill_in_prc * N)
+    const int lfil = (int)std::ceil(0.01 * fill_in_prc * c->N);
+    const int ierr = ilut_factor(c, lfil, droptol);
+    if (ierr == -100) return MLF_E_CUDA;
+    *ierr_out = ierr;
+    if (ierr != 0) return MLF_OK;
+    ilu_levels(c);
+    const int st = device_ilu_upload(c);
+    if (st) return st;
+    c->ilu_ok = 1;
+    return MLF_OK;
+}
+
+int mlf_ilu_size(mlf_ctx* h, long long* len) {
+    if (!h || !len) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    if (!c->ilu_ok) { c->err = "no ILU factors"; return MLF_E_STATE; }
+    *len = (long long)c->jlu[c->N + 1] - 1;
+    return MLF_OK;
+}
+
 int mlf_ilu0_factors(mlf_ctx* h, float* alu, int* jlu, int* ju) {
     if (!h || !alu || !jlu || !ju) return MLF_E_ARG;
     Ctx* c = &h->c;
     if (!c->ilu_ok) { c->err = "ILU0 factors not available"; return MLF_E_STATE; }
     // MSR arrays are 1-based: element k of the Fortran array is index k here
-    const long long n1 = c->nnz + 1;
+    const long long n1 = (long long)c->jlu[c->N + 1] - 1;
     std::memcpy(alu, c->alu.data() + 1, n1 * sizeof(float2));
     std::memcpy(jlu, c->jlu.data() + 1, n1 * sizeof(int));
     std::memcpy(ju, c->ju.data() + 1, (size_t)c->N * sizeof(int));

@@ -138,6 +138,7 @@ int build_octree(Ctx* c);          // levels, boxes, lists, interpolation tables
 void sph_bessel(int nmax, double x, double* j, double* y);
 void binomial_squares(int nmax, std::vector<double>& out);  // (n!/(i!(n-i)!))^2, [n*(nmax+1)+i]
 int ilu0_factor(Ctx* c);           // host ILU(0), fills alu/jlu/ju, returns ierr
+int ilut_factor(Ctx* c, int lfil, double tol);  // host ILUT, same MSR layout
 void ilu_levels(Ctx* c);           // level schedules of the forward/backward sweeps
 
 // device set-up and operators (mlf_device.cu)

@@ -656,6 +656,148 @@ int ilu0_factor(Ctx* c) {
     return 0;
 }
 
+// ilutC, modIterativo.f90:2432-2883 (Saad's dual-threshold ILUT as adapted
+// to complex in the reference) with bsort2C (:1673-1748).  Row ii: entries
+// with |a| >= tol*tnorm (tnorm = mean |a| of the row) are unpacked into an L
+// and a U work row; rows jrow < ii are eliminated in increasing column order,
+// a multiplier fact = wl*alu(jrow) is dropped when |fact| * unorm(jrow) <=
+// tol*tnorm, small fill-ins are dropped; then the len = min(nl, lenl0+lfil)
+// largest multipliers (bubble-sorted by modulus) form the L row and the
+// diagonal plus the len-1 largest of the rest form the U row; unorm(ii) =
+// sum |U offdiag kept| / (len+1).  Factors are complex(4) (rounded on store),
+// work rows complex(8).  When the diagonal is not the first U entry the
+// reference swaps with a stale index (wu(j) = wu(idiag)); this restatement
+// swaps into position 1, the evident intent.  Returns ierr as the reference:
+// 0, the zero-pivot row, or -5 for a zero U diagonal.
+int ilut_factor(Ctx* c, int lfil, double tol) {
+    const int n = c->N;
+    std::vector<float2> zf;
+    if (fetch_near_values(c, zf) != MLF_OK) return -100;
+    std::vector<float2> alu(n + 2);
+    std::vector<int> jlu(n + 2), ju(n + 1, 0);
+    std::vector<int> jr(n + 1, 0), jwl(n + 1), jwu(n + 1);
+    std::vector<double> wlr(n + 2), wli(n + 2), wur(n + 2), wui(n + 2), unorm(n + 2, 0.0);
+    long long ju0 = n + 2;
+    jlu[1] = (int)ju0;
+    auto cab = [](double r, double i) { return std::hypot(r, i); };
+    auto bsort = [&](double* wr, double* wi, int* ind, int nn, int ncut) {
+        int i = 1;
+        for (;;) {
+            bool test = false;
+            for (int j = nn - 1; j >= i; --j) {
+                if (cab(wr[j - 1], wi[j - 1]) < cab(wr[j], wi[j])) {
+                    std::swap(wr[j - 1], wr[j]);
+                    std::swap(wi[j - 1], wi[j]);
+                    std::swap(ind[j - 1], ind[j]);
+                    test = true;
+                }
+            }
+            ++i;
+            if (!test || ncut < i) break;
+        }
+    };
+    for (int ii = 1; ii <= n; ++ii) {
+        const long long j1 = c->ia[ii - 1], j2 = c->ia[ii] - 1;
+        int lenu = 0, lenl = 0;
+        double tnorm = 0.0;
+        for (long long k = j1; k <= j2; ++k) tnorm = tnorm + cab(zf[k].x, zf[k].y);
+        tnorm = tnorm / (double)(j2 - j1 + 1);
+        for (long long j = j1; j <= j2; ++j) {
+            const int k = c->ja[j] + 1;
+            const double tr = zf[j].x, ti = zf[j].y;
+            if (tol * tnorm <= cab(tr, ti)) {
+                if (k < ii) {
+                    ++lenl; jwl[lenl] = k; wlr[lenl] = tr; wli[lenl] = ti; jr[k] = lenl;
+                } else {
+                    ++lenu; jwu[lenu] = k; wur[lenu] = tr; wui[lenu] = ti; jr[k] = lenu;
+                }
+            }
+        }
+        const int lenl0 = lenl, lenu0 = lenu;
+        int jjj = 0, nl = 0;
+        for (;;) {
+            ++jjj;
+            if (lenl < jjj) break;
+            int jrow = jwl[jjj], kk = jjj;
+            for (int j = jjj + 1; j <= lenl; ++j)
+                if (jwl[j] < jrow) { jrow = jwl[j]; kk = j; }
+            const int jold = jwl[jjj];
+            jwl[jjj] = jrow; jwl[kk] = jold;
+            jr[jrow] = jjj; jr[jold] = kk;
+            std::swap(wlr[kk], wlr[jjj]);
+            std::swap(wli[kk], wli[jjj]);
+            if (ii <= jrow) break;
+            // fact = wl(jjj) * alu(jrow): complex(8) x complex(4)
+            const double ar = alu[jrow].x, ai = alu[jrow].y;
+            const double fr = wlr[jjj] * ar - wli[jjj] * ai, fi = wlr[jjj] * ai + wli[jjj] * ar;
+            jr[jrow] = 0;
+            if (cab(fr, fi) * unorm[jrow] <= tol * tnorm) continue;
+            for (int k = ju[jrow]; k < jlu[jrow + 1]; ++k) {
+                const double sr = fr * alu[k].x - fi * alu[k].y, si = fr * alu[k].y + fi * alu[k].x;
+                const int j = jlu[k];
+                const int jpos = jr[j];
+                if (cab(sr, si) < tol * tnorm && jpos == 0) continue;
+                if (ii <= j) {
+                    if (jpos == 0) {
+                        ++lenu;
+                        if (n < lenu) return -1;
+                        jwu[lenu] = j; jr[j] = lenu; wur[lenu] = -sr; wui[lenu] = -si;
+                    } else {
+                        wur[jpos] = wur[jpos] - sr; wui[jpos] = wui[jpos] - si;
+                    }
+                } else {
+                    if (jpos == 0) {
+                        ++lenl;
+                        if (n < lenl) return -1;
+                        jwl[lenl] = j; jr[j] = lenl; wlr[lenl] = -sr; wli[lenl] = -si;
+                    } else {
+                        wlr[jpos] = wlr[jpos] - sr; wli[jpos] = wli[jpos] - si;
+                    }
+                }
+            }
+            ++nl;
+            wlr[nl] = fr; wli[nl] = fi; jwl[nl] = jrow;
+        }
+        int len = std::min(nl, lenl0 + lfil);
+        bsort(&wlr[1], &wli[1], &jwl[1], nl, len);
+        for (int k = 1; k <= len; ++k) {
+            alu.push_back(make_float2((float)wlr[k], (float)wli[k]));
+            jlu.push_back(jwl[k]);
+            ++ju0;
+        }
+        ju[ii] = (int)ju0;
+        for (int k = jjj; k <= lenl; ++k) jr[jwl[k]] = 0;
+        const int idiag = jr[ii];
+        if (idiag == 0) return ii;
+        if (idiag != 1) {
+            std::swap(wur[1], wur[idiag]);
+            std::swap(wui[1], wui[idiag]);
+            std::swap(jwu[1], jwu[idiag]);
+        }
+        len = std::min(lenu, lenu0 + lfil);
+        bsort(&wur[2], &wui[2], &jwu[2], lenu - 1, len);
+        double t = 0.0;
+        for (int k = 2; k <= len; ++k) {
+            jlu.push_back(jwu[k]);
+            alu.push_back(make_float2((float)wur[k], (float)wui[k]));
+            t = t + cab(wur[k], wui[k]);
+            ++ju0;
+        }
+        unorm[ii] = t / (double)(len + 1);
+        if (cab(wur[1], wui[1]) == 0.0) return -5;
+        const double dr = wur[1], di = wui[1], den = dr * dr + di * di;
+        alu[ii] = make_float2((float)(dr / den), (float)(-di / den));
+        jlu[ii + 1] = (int)ju0;
+        for (int k = 1; k <= lenu; ++k) jr[jwu[k]] = 0;
+    }
+    c->alu.swap(alu);
+    c->jlu.swap(jlu);
+    c->ju.swap(ju);
+    c->alu.push_back(make_float2(0, 0));
+    c->jlu.push_back(0);
+    return 0;
+}
+
 // Level schedules: forward row i waits on the L columns of row i, backward
 // row i on its U columns.  Rows of one level are independent.
 void ilu_levels(Ctx* c) {

@@ -191,9 +191,19 @@ class MLFMA:
 
     ilu0C = ilu0
 
+    def ilut(self, fill_in_prc=5.0, droptol=1e-3) -> int:
+        """ILUT of the near field (crear_precond ILUT branch); returns ilutC's ierr."""
+        ierr = C.c_int()
+        _check(load().mlf_ilut(self._h, float(fill_in_prc), float(droptol), C.byref(ierr)), self._h)
+        return int(ierr.value)
+
+    ilutC = ilut
+
     def ilu0_factors(self):
-        alu = np.zeros(self.nnz + 1, dtype=np.complex64)
-        jlu = np.zeros(self.nnz + 1, dtype=np.int32)
+        n = C.c_longlong()
+        _check(load().mlf_ilu_size(self._h, C.byref(n)), self._h)
+        alu = np.zeros(n.value, dtype=np.complex64)
+        jlu = np.zeros(n.value, dtype=np.int32)
         ju = np.zeros(self.N, dtype=np.int32)
         _check(load().mlf_ilu0_factors(self._h, _p(alu), _p(jlu), _p(ju)), self._h)
         return alu, jlu, ju

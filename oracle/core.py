@@ -208,9 +208,15 @@ class OracleMLFMA:
     def ilu0(self) -> int:
         return int(lib().ora_ilu0(self._h))
 
+    def ilut(self, fill_in_prc=5.0, droptol=1e-3) -> int:
+        lfil = int(np.ceil(0.01 * fill_in_prc * self.N))
+        return int(lib().ora_ilut(C.c_void_p(self._h), C.c_int(lfil), C.c_double(droptol)))
+
     def ilu_factors(self):
-        alu = np.zeros(self.nnz + 2, dtype=np.complex64)
-        jlu = np.zeros(self.nnz + 2, dtype=np.int32)
+        lib().ora_ilu_len.restype = C.c_int64
+        n = int(lib().ora_ilu_len(C.c_void_p(self._h)))
+        alu = np.zeros(n + 2, dtype=np.complex64)
+        jlu = np.zeros(n + 2, dtype=np.int32)
         ju = np.zeros(self.N + 1, dtype=np.int32)
         lib().ora_ilu_factors(C.c_void_p(self._h), _p(alu), _p(jlu), _p(ju))
         return alu, jlu, ju

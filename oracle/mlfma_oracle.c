@@ -953,6 +953,159 @@ void ora_lusol0_raw(int n, const cplx* y, cplx* x, const cplxf* alu, const int* 
     lusol0(n, y, x, alu, jlu, ju);
 }
 
+/* bsort2C, modIterativo.f90:1673-1748: bubble passes moving the largest
+ * moduli to the front until ncut positions are settled */
+static void bsort2(cplx* w, int* ind, int n, int ncut) {
+    int i = 1;
+    for (;;) {
+        int test = 0;
+        for (int j = n - 1; j >= i; j--) {
+            if (cabs(w[j - 1]) < cabs(w[j])) {
+                cplx t = w[j - 1]; w[j - 1] = w[j]; w[j] = t;
+                int q = ind[j - 1]; ind[j - 1] = ind[j]; ind[j] = q;
+                test = 1;
+            }
+        }
+        i++;
+        if (!test || ncut < i) break;
+    }
+}
+
+/* ilutC, modIterativo.f90:2432-2883 (dual threshold ILU as adapted to
+ * complex by the reference; factors complex(4), work rows complex(8)).  The
+ * reference's diagonal swap writes through a stale index (wu(j)); here the
+ * diagonal is swapped into position 1.  Arrays 1-based like ora_ilu0_raw;
+ * alu/jlu are grown as needed (returned through pointers). */
+int ora_ilut_raw(int n, const cplxf* a, const int* ja, const int* ia, int lfil, double tol,
+                 cplxf** alu_out, int** jlu_out, int* ju) {
+    if (lfil < 0) return -4;
+    size_t cap = (size_t)n + 2 + (size_t)ia[n + 1] * 2 + 16;
+    cplxf* alu = xcalloc(cap, sizeof(cplxf));
+    int* jlu = xcalloc(cap, sizeof(int));
+    int* jr = xcalloc(n + 2, sizeof(int));
+    int* jwl = xcalloc(n + 2, sizeof(int));
+    int* jwu = xcalloc(n + 2, sizeof(int));
+    cplx* wl = xcalloc(n + 2, sizeof(cplx));
+    cplx* wu = xcalloc(n + 2, sizeof(cplx));
+    double* unorm = xcalloc(n + 2, sizeof(double));
+    long ju0 = n + 2;
+    jlu[1] = (int)ju0;
+    int ierr = 0;
+    for (int ii = 1; ii <= n && !ierr; ii++) {
+        int j1 = ia[ii], j2 = ia[ii + 1] - 1;
+        int lenu = 0, lenl = 0;
+        double tnorm = 0.0;
+        for (int k = j1; k <= j2; k++) tnorm = tnorm + cabs((cplx)a[k]);
+        tnorm = tnorm / (double)(j2 - j1 + 1);
+        for (int j = j1; j <= j2; j++) {
+            int k = ja[j];
+            cplx t = (double)crealf(a[j]) + I * (double)cimagf(a[j]);
+            if (tol * tnorm <= cabs(t)) {
+                if (k < ii) { lenl++; jwl[lenl] = k; wl[lenl] = t; jr[k] = lenl; }
+                else { lenu++; jwu[lenu] = k; wu[lenu] = t; jr[k] = lenu; }
+            }
+        }
+        int lenl0 = lenl, lenu0 = lenu, jjj = 0, nl = 0;
+        for (;;) {
+            jjj++;
+            if (lenl < jjj) break;
+            int jrow = jwl[jjj], kk = jjj;
+            for (int j = jjj + 1; j <= lenl; j++) if (jwl[j] < jrow) { jrow = jwl[j]; kk = j; }
+            int jold = jwl[jjj];
+            jwl[jjj] = jrow; jwl[kk] = jold;
+            jr[jrow] = jjj; jr[jold] = kk;
+            cplx sw = wl[kk]; wl[kk] = wl[jjj]; wl[jjj] = sw;
+            if (ii <= jrow) break;
+            cplx al = (double)crealf(alu[jrow]) + I * (double)cimagf(alu[jrow]);
+            double fr = creal(wl[jjj]) * creal(al) - cimag(wl[jjj]) * cimag(al);
+            double fi = creal(wl[jjj]) * cimag(al) + cimag(wl[jjj]) * creal(al);
+            cplx fact = fr + I * fi;
+            jr[jrow] = 0;
+            if (cabs(fact) * unorm[jrow] <= tol * tnorm) continue;
+            for (int k = ju[jrow]; k <= jlu[jrow + 1] - 1; k++) {
+                double ar = crealf(alu[k]), ai = cimagf(alu[k]);
+                cplx s = (fr * ar - fi * ai) + I * (fr * ai + fi * ar);
+                int j = jlu[k];
+                int jpos = jr[j];
+                if (cabs(s) < tol * tnorm && jpos == 0) continue;
+                if (ii <= j) {
+                    if (jpos == 0) {
+                        lenu++;
+                        if (n < lenu) { ierr = -1; break; }
+                        jwu[lenu] = j; jr[j] = lenu; wu[lenu] = -s;
+                    } else wu[jpos] = wu[jpos] - s;
+                } else {
+                    if (jpos == 0) {
+                        lenl++;
+                        if (n < lenl) { ierr = -1; break; }
+                        jwl[lenl] = j; jr[j] = lenl; wl[lenl] = -s;
+                    } else wl[jpos] = wl[jpos] - s;
+                }
+            }
+            if (ierr) break;
+            nl++;
+            wl[nl] = fact; jwl[nl] = jrow;
+        }
+        if (ierr) break;
+        int len = nl < lenl0 + lfil ? nl : lenl0 + lfil;
+        bsort2(wl + 1, jwl + 1, nl, len);
+        if ((size_t)ju0 + len + lenu + 2 >= cap) {
+            cap = 2 * cap + len + lenu + 16;
+            alu = realloc(alu, cap * sizeof(cplxf));
+            jlu = realloc(jlu, cap * sizeof(int));
+        }
+        for (int k = 1; k <= len; k++) {
+            alu[ju0] = (float)creal(wl[k]) + I * (float)cimag(wl[k]);
+            jlu[ju0] = jwl[k];
+            ju0++;
+        }
+        ju[ii] = (int)ju0;
+        for (int k = jjj; k <= lenl; k++) jr[jwl[k]] = 0;
+        int idiag = jr[ii];
+        if (idiag == 0) { ierr = ii; break; }
+        if (idiag != 1) {
+            cplx t = wu[1]; wu[1] = wu[idiag]; wu[idiag] = t;
+            int q = jwu[1]; jwu[1] = jwu[idiag]; jwu[idiag] = q;
+        }
+        len = lenu < lenu0 + lfil ? lenu : lenu0 + lfil;
+        bsort2(wu + 2, jwu + 2, lenu - 1, len);
+        double t = 0.0;
+        for (int k = 2; k <= len; k++) {
+            jlu[ju0] = jwu[k];
+            alu[ju0] = (float)creal(wu[k]) + I * (float)cimag(wu[k]);
+            t = t + cabs(wu[k]);
+            ju0++;
+        }
+        unorm[ii] = t / (double)(len + 1);
+        if (cabs(wu[1]) == 0.0) { ierr = -5; break; }
+        double dr = creal(wu[1]), di = cimag(wu[1]), den = dr * dr + di * di;
+        alu[ii] = (float)(dr / den) + I * (float)(-di / den);
+        jlu[ii + 1] = (int)ju0;
+        for (int k = 1; k <= lenu; k++) jr[jwu[k]] = 0;
+    }
+    free(jr); free(jwl); free(jwu); free(wl); free(wu); free(unorm);
+    *alu_out = alu;
+    *jlu_out = jlu;
+    return ierr;
+}
+
+int ora_ilut(Ctx* c, int lfil, double tol) {
+    int n = c->N;
+    int64_t nnz = c->nnz;
+    cplxf* a1 = xcalloc(nnz + 1, sizeof(cplxf));
+    int* ja1 = xcalloc(nnz + 1, sizeof(int));
+    int* ia1 = xcalloc(n + 2, sizeof(int));
+    for (int64_t q = 0; q < nnz; q++) { a1[q + 1] = c->zn[q]; ja1[q + 1] = c->ja[q] + 1; }
+    for (int i = 0; i <= n; i++) ia1[i + 1] = c->ia[i] + 1;
+    free(c->alu); free(c->jlu); free(c->ju);
+    c->ju = xcalloc(n + 1, sizeof(int));
+    c->ilu_status = ora_ilut_raw(n, a1, ja1, ia1, lfil, tol, &c->alu, &c->jlu, c->ju);
+    free(a1); free(ja1); free(ia1);
+    return c->ilu_status;
+}
+
+int64_t ora_ilu_len(Ctx* c) { return (int64_t)c->jlu[c->N + 1] - 1; }
+
 /* crear_precond, ILU0 branch (main.f90:851-902) on the near CSR */
 int ora_ilu0(Ctx* c) {
     int n = c->N;
@@ -1280,8 +1433,9 @@ void ora_near(Ctx* c, int* ia, int* ja, cplxf* z) {
     memcpy(z, c->zn, sizeof(cplxf) * c->nnz);
 }
 void ora_ilu_factors(Ctx* c, cplxf* alu, int* jlu, int* ju) {
-    memcpy(alu, c->alu, sizeof(cplxf) * (c->nnz + 2));
-    memcpy(jlu, c->jlu, sizeof(int) * (c->nnz + 2));
+    int64_t len = (int64_t)c->jlu[c->N + 1] + 1;
+    memcpy(alu, c->alu, sizeof(cplxf) * len);
+    memcpy(jlu, c->jlu, sizeof(int) * len);
     memcpy(ju, c->ju, sizeof(int) * (c->N + 1));
 }
 /* replace the near-field values (same CSR pattern), e.g. with values computed

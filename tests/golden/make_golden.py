@@ -59,6 +59,11 @@ CASES = {
                   ["lambda=1", "ladomax=0.3", "precond=ilu0", "errsolver=1e-3",
                    "rcsmono.active=false", "rcsbi.ntheta=5", "rcsbi.nphi=8",
                    "run=mlfma"], 900),
+    # same body, CGS + ILUT (the reference default: fill-in 5 %, drop 1e-3).
+    "ico3_ilut": (lambda: meshes.icosphere(3, 1.0, quantum=QUANTUM),
+                  ["lambda=1", "ladomax=0.3", "precond=ilut", "ilut.fillin=5", "ilut.droptol=0.001",
+                   "errsolver=1e-6", "rcsmono.active=false", "rcsbi.ntheta=5", "rcsbi.nphi=8",
+                   "run=mlfma"], 900),
     # monostatic sweep, 4 angles of phi, VV, warm-started CGS.
     "ico3_mono": (lambda: meshes.icosphere(3, 1.0, quantum=QUANTUM),
                   ["lambda=1", "ladomax=0.3", "precond=no", "errsolver=1e-8",
@@ -168,7 +173,7 @@ def _reference_kats():
 
 def main(argv):
     names = argv[1:] or list(CASES)
-    if "kat" in names or not argv[1:]:
+    if "kat" in names or not argv[1:]:  # reference known-answer files
         _reference_kats()
     for name in names:
         if name in CASES:

@@ -261,3 +261,24 @@ def test_five_level_octree_against_binary(gpu_lib):
     assert out["status"] == "converged"
     assert abs(out["iters"] - int(g["iterations"])) <= 0.05 * int(g["iterations"])
     m.close()
+
+
+def test_ilut_bitexact_and_cgs(ico3):
+    """ILUT (the reference default, fill-in 5 %, drop 1e-3) against the oracle's ilutC."""
+    _, m, o = ico3
+    _, _, a = m.near_csr()
+    o.set_near(a)
+    assert m.ilut(5.0, 1e-3) == 0
+    assert o.ilut(5.0, 1e-3) == 0
+    alu, jlu, ju = m.ilu0_factors()
+    oalu, ojlu, oju = o.ilu_factors()
+    n1 = alu.size
+    assert np.array_equal(jlu, ojlu[1:n1 + 1]) and np.array_equal(ju, oju[1:m.N + 1])
+    assert np.array_equal(alu.view(np.uint32), oalu[1:n1 + 1].view(np.uint32))
+    d = direction(90.0, 180.0)
+    b = m.excitation(d, ajustar_polariz(d, "VV"))
+    out = m.cgs(b, errmax=1e-6, maxit=500, precond=1)
+    ref = o.cgs(b, tol=1e-6, maxit=500, prec=True)
+    assert out["status"] == "converged" and ref["status"] == 0
+    assert abs(out["iters"] - ref["iters"]) <= 2
+    assert _rel(out["x"], ref["x"]) < 1e-5
