@@ -282,3 +282,16 @@ def test_ilut_bitexact_and_cgs(ico3):
     assert out["status"] == "converged" and ref["status"] == 0
     assert abs(out["iters"] - ref["iters"]) <= 2
     assert _rel(out["x"], ref["x"]) < 1e-5
+
+
+def test_ilut_against_binary_run(gpu_lib):
+    g = load_golden("bin_ico3_ilut.npz")
+    m = MLFMA(RWG(g["tris"]), lam=1.0, ladomax=0.3)
+    assert m.ilut(5.0, 1e-3) == 0
+    d = direction(90.0, 180.0)
+    b = m.excitation(d, ajustar_polariz(d, "VV"))
+    out = m.cgs(b, errmax=1e-6, maxit=500, precond=1)
+    assert out["status"] == "converged"
+    assert abs(out["iters"] - int(g["iterations"])) <= 2
+    assert _rel(out["x"], g["I"]) < 1e-5
+    m.close()

@@ -242,3 +242,20 @@ def test_five_level_octree_against_binary():
     th, ph = _bistatic_grid(5, 8)
     rcs = 10 * np.log10(core.sigma_rcs(r, 0.5, g["I"], pol, th, ph)).reshape(5, 8)
     assert np.abs(rcs - g["rcsbi"]).max() < 1e-4
+
+
+def test_ilut_cgs_against_binary_run():
+    """crear_precond ILUT (fill-in 5 %, drop 1e-3; ilutC + bsort2C) + CGSold
+    against the binary's precond=ilut run: same iteration count, same
+    residual history to the printed digits, same currents."""
+    g = load_golden("bin_ico3_ilut.npz")
+    r = RWG(g["tris"])
+    o = core.OracleMLFMA(r, lam=1.0, ladomax=0.3)
+    assert o.ilut(5.0, 1e-3) == 0
+    d = core.direction_from_angles(90.0, 180.0)
+    b = core.generar_onda(r, 1.0, d, core.ajustar_polariz(d, "VV"))
+    out = o.cgs(b, tol=1e-6, maxit=3000, prec=True, history=True)
+    assert out["status"] == 0 and out["iters"] == int(g["iterations"])
+    hist = g["res_hist"] / float(g["bnorm"])
+    np.testing.assert_allclose(out["history"][:20], hist[:20], rtol=2e-5)
+    assert np.linalg.norm(out["x"] - g["I"]) / np.linalg.norm(g["I"]) < 1e-5
