@@ -195,6 +195,11 @@ int mlf_matvec32_device(mlf_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, 
  * singular. */
 int mlf_nearinv(mlf_ctx* ctx, int* bad_box);
 
+/* Same with each box's own bases as the neighbourhood (block Jacobi on the
+ * near field): cheaper where leaf boxes hold many bases and near lists run
+ * into the thousands.  Replaces any previous mlf_nearinv result. */
+int mlf_nearinv_own(mlf_ctx* ctx, int* bad_box);
+
 /* Values of M (complex(8), interleaved) in the order of mlf_near_csr. */
 int mlf_nearinv_values(mlf_ctx* ctx, double* vals);
 

@@ -31,6 +31,7 @@ SIGNATURES = {
     "mlf_ilu0_solve": (C.c_int, [vp, vp, vp, C.c_int]),
     "mlf_cgs": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp]),
     "mlf_nearinv": (C.c_int, [vp, ip]),
+    "mlf_nearinv_own": (C.c_int, [vp, ip]),
     "mlf_solve": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp, vp,
                             vp, ip]),
     "mlf_matvec32": (C.c_int, [vp, vp, vp, C.c_int, C.c_int]),

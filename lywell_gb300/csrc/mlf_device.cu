@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "mlf_internal.h"
+#include "mlf_sep.cuh"
 
 namespace mlf {
 
@@ -426,6 +427,16 @@ int device_setup(Ctx* c) {
             if ((st = upload(c, &L.dant_ptr, L.ant_ptr))) return st;
             if ((st = upload(c, &L.dant_row, L.ant_row))) return st;
             if ((st = upload(c, &L.dant_w, L.ant_w))) return st;
+            if ((st = upload(c, &L.dsth, L.sth))) return st;
+            if ((st = upload(c, &L.dsph, L.sph))) return st;
+            if ((st = upload(c, &L.dwth, L.wth))) return st;
+            if ((st = upload(c, &L.dwph, L.wph))) return st;
+            if ((st = upload(c, &L.dthT_ptr, L.thT_ptr))) return st;
+            if ((st = upload(c, &L.dthT_row, L.thT_row))) return st;
+            if ((st = upload(c, &L.dthT_w, L.thT_w))) return st;
+            if ((st = upload(c, &L.dphT_ptr, L.phT_ptr))) return st;
+            if ((st = upload(c, &L.dphT_row, L.phT_row))) return st;
+            if ((st = upload(c, &L.dphT_w, L.phT_w))) return st;
             // phase tables of this (parent) level for the 8 child octants:
             // exp(+j k khat . r), r = (+-q, +-q, +-q), q = side/4
             std::vector<double2> sh(8 * (size_t)L.K);
@@ -550,9 +561,11 @@ int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaSt
     for (int n = nl; n >= 4; --n) {
         Level& Lc = c->lv[n];
         Level& Lp = c->lv[n - 1];
-        const int bd = 256, nch = chunks(2 * Lp.K, bd);
-        k_interp_up<<<Lp.nb * nrhs * nch, bd, 0, s>>>(Lp.K, Lc.K, nrhs, nch, Lp.dchild_ptr, Lc.doctant,
-                                                      Lp.diw, Lp.diidx, Lp.dshift, Lc.dC, Lp.dC);
+        const int slab = SEP_SLAB, nslab = chunks(Lp.L, slab);
+        const size_t smem = (size_t)slab * 2 * Lc.L * sizeof(double2);
+        k_interp_sep<double2><<<Lp.nb * nrhs * 2 * nslab, 256, smem, s>>>(
+            Lp.L, Lc.L, nrhs, slab, nslab, Lp.dchild_ptr, Lc.doctant, Lp.dsth, Lp.dwth, Lp.dsph, Lp.dwph, Lp.dshift,
+            Lc.dC, Lp.dC);
     }
     if (prof) cudaEventRecord(c->ev[2], s);
     for (int n = 3; n <= nl; ++n) {
@@ -566,9 +579,10 @@ int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaSt
         Level& Lc = c->lv[n];
         Level& Lp = c->lv[n - 1];
         const double2* Psrc = (n == 4) ? Lp.dB : Lp.dA;
-        const size_t smem = 2 * (size_t)Lp.K * sizeof(double2);
-        k_anterp_down<<<Lc.nb * nrhs, 256, smem, s>>>(Lp.K, Lc.K, nrhs, Lc.dparent, Lc.doctant, Lp.dant_ptr,
-                                                      Lp.dant_row, Lp.dant_w, Lp.dshift, Psrc, Lc.dB, Lc.dA);
+        const size_t smem = ((size_t)Lp.K + (size_t)Lp.L * 2 * Lc.L) * sizeof(double2);
+        k_anterp_sep<double2><<<Lc.nb * nrhs * 2, 256, smem, s>>>(
+            Lp.L, Lc.L, nrhs, Lc.dparent, Lc.doctant, Lp.dthT_ptr, Lp.dthT_row, Lp.dthT_w, Lp.dphT_ptr,
+            Lp.dphT_row, Lp.dphT_w, Lp.dshift, Psrc, Lc.dB, Lc.dA);
     }
     if (prof) cudaEventRecord(c->ev[4], s);
     {
@@ -589,13 +603,19 @@ int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaSt
 
 // anterpolation smem: the largest parent grid decides; opt in above 48 KB
 int configure_kernels(Ctx* c) {
-    size_t mx = 0;
-    for (int n = 3; n < c->nlev; ++n) mx = std::max(mx, 2 * (size_t)c->lv[n].K * sizeof(double2));
-    if (mx > 227 * 1024) {
+    size_t mx = 0, mx2 = 0, mx3 = 0;
+    for (int n = 3; n < c->nlev; ++n) {
+        mx = std::max(mx, 2 * (size_t)c->lv[n].K * sizeof(double2));
+        mx2 = std::max(mx2, ((size_t)c->lv[n].K + (size_t)c->lv[n].L * 2 * c->lv[n + 1].L) * sizeof(double2));
+        mx3 = std::max(mx3, (size_t)SEP_SLAB * 2 * c->lv[n + 1].L * sizeof(double2));
+    }
+    if (mx > 227 * 1024 || mx2 > 227 * 1024) {
         c->err = "parent sampling grid too large for the shared-memory anterpolation stage";
         return MLF_E_ARG;
     }
     CK(cudaFuncSetAttribute(k_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    CK(cudaFuncSetAttribute(k_anterp_sep<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx2));
+    CK(cudaFuncSetAttribute(k_interp_sep<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx3));
     return MLF_OK;
 }
 
@@ -606,6 +626,8 @@ void device_free(Ctx* c) {
         F(L.dC); F(L.dB); F(L.dA); F(L.dT); F(L.dwq); F(L.dfar_ptr); F(L.dfar_src); F(L.dfar_tid);
         F(L.diw); F(L.diidx); F(L.dant_ptr); F(L.dant_row); F(L.dant_w); F(L.dshift);
         F(L.dchild_ptr); F(L.dparent); F(L.doctant); F(L.dkap); F(L.dath); F(L.daph); F(L.dcentre);
+        F(L.dsth); F(L.dsph); F(L.dwth); F(L.dwph); F(L.dthT_ptr); F(L.dthT_row); F(L.dthT_w); F(L.dphT_ptr);
+        F(L.dphT_row); F(L.dphT_w);
     }
     F(c->dR); F(c->dperm); F(c->dbox_ptr); F(c->dbox_of_sorted); F(c->dia); F(c->dja); F(c->dZ);
     F(c->dp_coord); F(c->dt_baric); F(c->dt_baric_sub); F(c->de_long); F(c->de_centro); F(c->de_t);

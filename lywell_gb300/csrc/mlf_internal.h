@@ -19,6 +19,7 @@ namespace mlf {
 constexpr double PI = 3.141592653589793;
 constexpr double MU = 1.2566370614E-6;
 constexpr double EPSI = 8.8541878176E-12;
+constexpr int SEP_SLAB = 8;   // coarse theta rows per CTA in the separable upward pass
 
 struct Phys {
     double lambda, w, kappa, vp, smue;
@@ -45,6 +46,14 @@ struct Level {
     // [ant_ptr[q], ant_ptr[q+1]) of (coarse sample, weight) in (row, tap) order
     std::vector<int> ant_ptr, ant_row;
     std::vector<double> ant_w;
+    // the same stencil in separable form: 3 fine theta rows per coarse theta,
+    // 3 fine phi columns per coarse phi, and the transposed lists
+    std::vector<int> sth, sph;          // L*3, 2L*3 (0-based fine indices)
+    std::vector<double> wth, wph;       // L*3, 2L*3
+    std::vector<int> thT_ptr, thT_row;  // per fine theta: coarse rows
+    std::vector<double> thT_w;
+    std::vector<int> phT_ptr, phT_row;  // per fine phi: coarse columns
+    std::vector<double> phT_w;
 
     // device
     double2 *dC = nullptr, *dB = nullptr, *dA = nullptr;
@@ -55,6 +64,9 @@ struct Level {
     int* diidx = nullptr;
     int *dant_ptr = nullptr, *dant_row = nullptr;
     double* dant_w = nullptr;
+    int *dsth = nullptr, *dsph = nullptr, *dthT_ptr = nullptr, *dthT_row = nullptr, *dphT_ptr = nullptr,
+        *dphT_row = nullptr;
+    double *dwth = nullptr, *dwph = nullptr, *dthT_w = nullptr, *dphT_w = nullptr;
     double2* dshift = nullptr;    // 8*K: exp(+j k khat . r_oct) for the 8 child octants
     int *dchild_ptr = nullptr, *dparent = nullptr, *doctant = nullptr;
     double *dkap = nullptr, *dath = nullptr, *daph = nullptr, *dcentre = nullptr;
@@ -69,6 +81,7 @@ struct Mixed32 {
     struct Lv {
         float2 *T = nullptr, *shift = nullptr, *C = nullptr, *B = nullptr, *A = nullptr;
         float *wq = nullptr, *iw = nullptr, *ant_w = nullptr;
+        float *wth = nullptr, *wph = nullptr, *thT_w = nullptr, *phT_w = nullptr;
     } lv[32];
 };
 
@@ -152,7 +165,7 @@ int device_ilu_upload(Ctx* c);
 int device_ilu_solve(Ctx* c, const double2* y, double2* x, cudaStream_t s);
 int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs,
                double2* x, int* iters, double* relres, int precond, int* status);
-int device_nearinv_setup(Ctx* c, int* bad_box);
+int device_nearinv_setup(Ctx* c, int* bad_box, int own_only);
 int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s);
 void mixed_free(Ctx* c);
 int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,

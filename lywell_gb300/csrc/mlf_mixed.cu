@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "mlf_internal.h"
+#include "mlf_sep.cuh"
 
 namespace mlf {
 
@@ -207,6 +208,10 @@ int mixed_setup(Ctx* c) {
         if (n < nl) {
             if ((st = up32(c, &M.iw, L.iw))) return st;
             if ((st = up32(c, &M.ant_w, L.ant_w))) return st;
+            if ((st = up32(c, &M.wth, L.wth))) return st;
+            if ((st = up32(c, &M.wph, L.wph))) return st;
+            if ((st = up32(c, &M.thT_w, L.thT_w))) return st;
+            if ((st = up32(c, &M.phT_w, L.phT_w))) return st;
             std::vector<double2> sh(8 * (size_t)L.K);
             CK(cudaMemcpy(sh.data(), L.dshift, sh.size() * sizeof(double2), cudaMemcpyDeviceToHost));
             std::vector<float2> s32(sh.size());
@@ -215,9 +220,15 @@ int mixed_setup(Ctx* c) {
             CK(cudaMemcpy(M.shift, s32.data(), s32.size() * sizeof(float2), cudaMemcpyHostToDevice));
         }
     }
-    size_t mx = 0;
-    for (int n = 3; n < nl; ++n) mx = std::max(mx, 2 * (size_t)c->lv[n].K * sizeof(float2));
+    size_t mx = 0, mx2 = 0, mx3 = 0;
+    for (int n = 3; n < nl; ++n) {
+        mx = std::max(mx, 2 * (size_t)c->lv[n].K * sizeof(float2));
+        mx2 = std::max(mx2, ((size_t)c->lv[n].K + (size_t)c->lv[n].L * 2 * c->lv[n + 1].L) * sizeof(float2));
+        mx3 = std::max(mx3, (size_t)SEP_SLAB * 2 * c->lv[n + 1].L * sizeof(float2));
+    }
     CK(cudaFuncSetAttribute(k32_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+    CK(cudaFuncSetAttribute(k_anterp_sep<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx2));
+    CK(cudaFuncSetAttribute(k_interp_sep<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx3));
     CK(cudaStreamSynchronize(c->stream));
     c->m32.ready = 1;
     return MLF_OK;
@@ -256,10 +267,11 @@ int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cuda
     for (int n = nl; n >= 4; --n) {
         Level& Lc = c->lv[n];
         Level& Lp = c->lv[n - 1];
-        const int bd = 256, nch = (2 * Lp.K + bd - 1) / bd;
-        k32_interp_up<<<Lp.nb * nrhs * nch, bd, 0, s>>>(Lp.K, Lc.K, nrhs, nch, Lp.dchild_ptr, Lc.doctant,
-                                                        c->m32.lv[n - 1].iw, Lp.diidx, c->m32.lv[n - 1].shift,
-                                                        c->m32.lv[n].C, c->m32.lv[n - 1].C);
+        const int slab = SEP_SLAB, nslab = (Lp.L + slab - 1) / slab;
+        const size_t smem = (size_t)slab * 2 * Lc.L * sizeof(float2);
+        k_interp_sep<float2><<<Lp.nb * nrhs * 2 * nslab, 256, smem, s>>>(
+            Lp.L, Lc.L, nrhs, slab, nslab, Lp.dchild_ptr, Lc.doctant, Lp.dsth, c->m32.lv[n - 1].wth, Lp.dsph,
+            c->m32.lv[n - 1].wph, c->m32.lv[n - 1].shift, c->m32.lv[n].C, c->m32.lv[n - 1].C);
     }
     if (prof) cudaEventRecord(c->ev[2], s);
     for (int n = 3; n <= nl; ++n) {
@@ -274,10 +286,10 @@ int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cuda
         Level& Lc = c->lv[n];
         Level& Lp = c->lv[n - 1];
         const float2* Psrc = (n == 4) ? c->m32.lv[n - 1].B : c->m32.lv[n - 1].A;
-        const size_t smem = 2 * (size_t)Lp.K * sizeof(float2);
-        k32_anterp_down<<<Lc.nb * nrhs, 256, smem, s>>>(Lp.K, Lc.K, nrhs, Lc.dparent, Lc.doctant, Lp.dant_ptr,
-                                                        Lp.dant_row, c->m32.lv[n - 1].ant_w, c->m32.lv[n - 1].shift,
-                                                        Psrc, c->m32.lv[n].B, c->m32.lv[n].A);
+        const size_t smem = ((size_t)Lp.K + (size_t)Lp.L * 2 * Lc.L) * sizeof(float2);
+        k_anterp_sep<float2><<<Lc.nb * nrhs * 2, 256, smem, s>>>(
+            Lp.L, Lc.L, nrhs, Lc.dparent, Lc.doctant, Lp.dthT_ptr, Lp.dthT_row, c->m32.lv[n - 1].thT_w, Lp.dphT_ptr,
+            Lp.dphT_row, c->m32.lv[n - 1].phT_w, c->m32.lv[n - 1].shift, Psrc, c->m32.lv[n].B, c->m32.lv[n].A);
     }
     if (prof) cudaEventRecord(c->ev[4], s);
     {
@@ -302,6 +314,7 @@ void mixed_free(Ctx* c) {
     for (int n = 0; n < 32; ++n) {
         Mixed32::Lv& M = c->m32.lv[n];
         F(M.T); F(M.wq); F(M.iw); F(M.ant_w); F(M.shift); F(M.C); F(M.B); F(M.A);
+        F(M.wth); F(M.wph); F(M.thT_w); F(M.phT_w);
     }
 }
 

@@ -46,15 +46,17 @@ constexpr int NBI_THREADS = 256;
 
 __global__ void __launch_bounds__(NBI_THREADS)
 k_nbhd_inverse(int b0, int nb, const int* __restrict__ box_ptr, const int* __restrict__ box_bases,
-               const int* __restrict__ ia, const int* __restrict__ ja, const float2* __restrict__ Z,
-               size_t slab, double2* __restrict__ work, double2* __restrict__ M, int* __restrict__ bad) {
+               const int* __restrict__ own_sorted, int own_only, const int* __restrict__ ia,
+               const int* __restrict__ ja, const float2* __restrict__ Z, size_t slab, double2* __restrict__ work,
+               double2* __restrict__ M, int* __restrict__ bad) {
     const int b = b0 + blockIdx.x;
     if (b >= nb) return;
     const int tid = threadIdx.x, bd = blockDim.x;
     const int m0 = box_bases[box_ptr[b]];
-    const int n = ia[m0 + 1] - ia[m0];
-    const int* S = ja + ia[m0];
     const int nown = box_ptr[b + 1] - box_ptr[b];
+    // neighbourhood S: the box's near list, or (own_only) its own bases, sorted
+    const int n = own_only ? nown : ia[m0 + 1] - ia[m0];
+    const int* S = own_only ? own_sorted + box_ptr[b] : ja + ia[m0];
     double2* At = work + (size_t)blockIdx.x * slab;   // n x n, row-major, holds A^T
     double2* X = At + (size_t)n * n;                   // n x nown
     for (int i = tid; i < n * n; i += bd) At[i] = make_double2(0, 0);
@@ -159,10 +161,21 @@ k_nbhd_inverse(int b0, int nb, const int* __restrict__ box_ptr, const int* __res
         }
         __syncthreads();
     }
-    for (int e = tid; e < nown * n; e += bd) {
-        const int i = e / n, j = e % n;
-        const int g = box_bases[box_ptr[b] + i];
-        M[(size_t)ia[g] + j] = X[(size_t)j * nown + i];
+    if (!own_only) {
+        for (int e = tid; e < nown * n; e += bd) {
+            const int i = e / n, j = e % n;
+            const int g = box_bases[box_ptr[b] + i];
+            M[(size_t)ia[g] + j] = X[(size_t)j * nown + i];
+        }
+    } else {
+        // rows of the own-box inverse, placed at the own columns of each CSR row
+        const int rl = ia[m0 + 1] - ia[m0];
+        for (int e = tid; e < nown * rl; e += bd) {
+            const int i = e / rl, q = e % rl;
+            const int g = box_bases[box_ptr[b] + i];
+            const int pos = bsearch_sorted(S, n, ja[ia[g] + q]);
+            M[(size_t)ia[g] + q] = pos >= 0 ? X[(size_t)pos * nown + i] : make_double2(0, 0);
+        }
     }
 }
 
@@ -187,7 +200,7 @@ __global__ void k_spmv_z(int N, int nrhs, const int* __restrict__ ia, const int*
     if (lane == 0) y[(size_t)col * N + m] = make_double2(sr, si);
 }
 
-int device_nearinv_setup(Ctx* c, int* bad_box) {
+int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     const int nl = c->nlev;
     const Level& leaf = c->lv[nl];
     int nmax = 0, nownmax = 0;
@@ -195,6 +208,7 @@ int device_nearinv_setup(Ctx* c, int* bad_box) {
         nmax = std::max(nmax, c->near_ptr[b + 1] - c->near_ptr[b]);
         nownmax = std::max(nownmax, c->box_ptr[b + 1] - c->box_ptr[b]);
     }
+    if (own_only) nmax = nownmax;
     const size_t slab = (size_t)nmax * nmax + (size_t)nmax * nownmax;
     int batch = (int)std::min<size_t>(leaf.nb, std::max<size_t>(1, ((size_t)1 << 30) / (slab * sizeof(double2))));
     batch = std::min(batch, 4096);
@@ -210,11 +224,20 @@ int device_nearinv_setup(Ctx* c, int* bad_box) {
     const int big = 0x7fffffff;
     CK(cudaMemcpy(dbad, &big, sizeof(int), cudaMemcpyHostToDevice));
     dbases = c->dperm;   // the box-sorted basis list
+    int* downs = nullptr;  // each box's own bases, sorted (the box lists are ascending already)
+    if (own_only) {
+        std::vector<int> own(c->box_bases);
+        for (int b = 0; b < leaf.nb; ++b) std::sort(own.begin() + c->box_ptr[b], own.begin() + c->box_ptr[b + 1]);
+        CK(cudaMalloc(&downs, own.size() * sizeof(int)));
+        CK(cudaMemcpy(downs, own.data(), own.size() * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemsetAsync(c->dMinv, 0, std::max<long long>(c->nnz, 1) * sizeof(double2), c->stream));
+    }
     for (int b0 = 0; b0 < leaf.nb; b0 += batch) {
         k_nbhd_inverse<<<std::min(batch, leaf.nb - b0), NBI_THREADS, 0, c->stream>>>(
-            b0, leaf.nb, c->dbox_ptr, dbases, c->dia, c->dja, c->dZ, slab, work, c->dMinv, dbad);
+            b0, leaf.nb, c->dbox_ptr, dbases, downs, own_only, c->dia, c->dja, c->dZ, slab, work, c->dMinv, dbad);
         CK(cudaGetLastError());
     }
+    if (downs) cudaFree(downs);
     int hbad = 0;
     CK(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -243,7 +266,14 @@ extern "C" int mlf_nearinv(mlf_ctx* h, int* bad_box) {
     if (!h || !bad_box) return MLF_E_ARG;
     Ctx* c = &h->c;
     if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
-    return device_nearinv_setup(c, bad_box);
+    return device_nearinv_setup(c, bad_box, 0);
+}
+
+extern "C" int mlf_nearinv_own(mlf_ctx* h, int* bad_box) {
+    if (!h || !bad_box) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
+    return device_nearinv_setup(c, bad_box, 1);
 }
 
 extern "C" int mlf_nearinv_values(mlf_ctx* h, double* vals) {

@@ -322,6 +322,51 @@ void interp_table(const Level& Lc /*coarse*/, const Level& Lf /*fine*/, std::vec
     }
 }
 
+// Separable form of the same stencil: for each coarse theta row the three
+// fine theta rows (posT, posTmen, posTmay) and their Lagrange weights, for
+// each coarse phi column the three fine phi columns and weights; the 9-tap
+// weight of interp_table is exactly wth[a] * wph[b].
+void separable_tables(const Level& Lc, const Level& Lf, Level& out) {
+    const int Lt = Lc.nth, Lp2 = Lc.nph, nth = Lf.nth;
+    out.sth.assign(3 * Lt, 0); out.wth.assign(3 * Lt, 0);
+    out.sph.assign(3 * Lp2, 0); out.wph.assign(3 * Lp2, 0);
+    for (int it = 0; it < Lt; ++it) {
+        const double xt = Lc.ang[2 * it];           // theta of coarse sample it (phi column 0)
+        long th[3];
+        nearest3(&Lf.ang[0], 2, nth, xt, th);
+        const double mt[3] = {Lf.ang[2 * (th[0] - 1)], Lf.ang[2 * (th[1] - 1)], Lf.ang[2 * (th[2] - 1)]};
+        double Wt[3];
+        lagrange3(xt, mt, Wt);
+        for (int a = 0; a < 3; ++a) { out.sth[3 * it + a] = (int)th[a] - 1; out.wth[3 * it + a] = Wt[a]; }
+    }
+    for (int ip = 0; ip < Lp2; ++ip) {
+        const double xp = Lc.ang[2 * ((size_t)ip * Lt) + 1];
+        long ph[3];
+        nearest3(&Lf.ang[1], 2 * nth, Lf.nph, xp, ph);
+        const double mp[3] = {Lf.ang[2 * ((ph[0] - 1) * nth) + 1], Lf.ang[2 * ((ph[1] - 1) * nth) + 1],
+                              Lf.ang[2 * ((ph[2] - 1) * nth) + 1]};
+        double Wp[3];
+        lagrange3(xp, mp, Wp);
+        for (int b = 0; b < 3; ++b) { out.sph[3 * ip + b] = (int)ph[b] - 1; out.wph[3 * ip + b] = Wp[b]; }
+    }
+    auto transpose = [](const std::vector<int>& idx, const std::vector<double>& w, int ncoarse, int nfine,
+                        std::vector<int>& ptr, std::vector<int>& row, std::vector<double>& ww) {
+        ptr.assign(nfine + 1, 0);
+        for (int e = 0; e < 3 * ncoarse; ++e) ptr[idx[e] + 1]++;
+        for (int q = 0; q < nfine; ++q) ptr[q + 1] += ptr[q];
+        row.assign(3 * ncoarse, 0);
+        ww.assign(3 * ncoarse, 0);
+        std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+        for (int e = 0; e < 3 * ncoarse; ++e) {
+            row[fill[idx[e]]] = e / 3;
+            ww[fill[idx[e]]] = w[e];
+            fill[idx[e]]++;
+        }
+    };
+    transpose(out.sth, out.wth, Lt, Lf.nth, out.thT_ptr, out.thT_row, out.thT_w);
+    transpose(out.sph, out.wph, Lp2, Lf.nph, out.phT_ptr, out.phT_row, out.phT_w);
+}
+
 struct Builder {
     Ctx* c;
     std::vector<int> leaf_bases, leaf_ptr;
@@ -567,6 +612,7 @@ int build_octree(Ctx* c) {
         Level& L = c->lv[n];
         const Level& Lf = c->lv[n + 1];
         interp_table(L, Lf, L.iw, L.iidx);
+        separable_tables(L, Lf, L);
         L.ant_ptr.assign(Lf.K + 1, 0);
         for (int e = 0; e < 9 * L.K; ++e) L.ant_ptr[L.iidx[e] + 1]++;
         for (int q = 0; q < Lf.K; ++q) L.ant_ptr[q + 1] += L.ant_ptr[q];

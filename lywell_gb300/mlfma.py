@@ -218,10 +218,12 @@ class MLFMA:
 
     lusol0C = lusol0
 
-    def nearinv(self) -> int:
-        """Build the neighbourhood-inverse preconditioner; 0 or (singular box + 1)."""
+    def nearinv(self, own_only: bool = False) -> int:
+        """Build the neighbourhood-inverse preconditioner (own_only: block Jacobi on each
+        box's own bases); 0 or (singular box + 1)."""
         bad = C.c_int()
-        _check(load().mlf_nearinv(self._h, C.byref(bad)), self._h)
+        f = load().mlf_nearinv_own if own_only else load().mlf_nearinv
+        _check(f(self._h, C.byref(bad)), self._h)
         return int(bad.value)
 
     def nearinv_values(self):
