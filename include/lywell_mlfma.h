@@ -200,8 +200,13 @@ int mlf_nearinv(mlf_ctx* ctx, int* bad_box);
  * into the thousands.  Replaces any previous mlf_nearinv result. */
 int mlf_nearinv_own(mlf_ctx* ctx, int* bad_box);
 
-/* Values of M (complex(8), interleaved) in the order of mlf_near_csr. */
+/* Values of M (complex(8), interleaved) in the order of mlf_near_csr
+ * (full-neighbourhood mode only). */
 int mlf_nearinv_values(mlf_ctx* ctx, double* vals);
+
+/* x = M^-1 y for nrhs host columns with the preconditioner of kind
+ * MLF_PRECOND_ILU0 (lusol0C) or MLF_PRECOND_NEARINV. */
+int mlf_precond_apply(mlf_ctx* ctx, int precond_kind, const double* y, double* x, int nrhs);
 
 /* Residual history ||r_i||/||b|| of column col of the last mlf_cgs call
  * (the per-iteration line CGSold prints, modIterativo.f90:446-465).

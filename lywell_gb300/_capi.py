@@ -32,6 +32,7 @@ SIGNATURES = {
     "mlf_cgs": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp]),
     "mlf_nearinv": (C.c_int, [vp, ip]),
     "mlf_nearinv_own": (C.c_int, [vp, ip]),
+    "mlf_precond_apply": (C.c_int, [vp, C.c_int, vp, vp, C.c_int]),
     "mlf_solve": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp, vp,
                             vp, ip]),
     "mlf_matvec32": (C.c_int, [vp, vp, vp, C.c_int, C.c_int]),

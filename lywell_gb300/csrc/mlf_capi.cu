@@ -321,6 +321,26 @@ int mlf_cgs_history(mlf_ctx* h, int col, double* hist, int cap, int* n) {
     return MLF_OK;
 }
 
+int mlf_precond_apply(mlf_ctx* h, int precond_kind, const double* y, double* x, int nrhs) {
+    if (!h || !y || !x || nrhs <= 0 || precond_kind < 1 || precond_kind > 2) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    if (!bind_device(c)) return MLF_E_CUDA;
+    const size_t n = (size_t)c->N * nrhs;
+    int st;
+    if ((st = ensure_io(c, n))) return st;
+    if ((st = h2d_cols(c, c->dx_io, y, nrhs, c->N))) return st;
+    if (precond_kind == 2) {
+        if ((st = device_nearinv_apply(c, c->dx_io, c->dy_io, nrhs, c->stream))) return st;
+    } else {
+        for (int r = 0; r < nrhs; ++r)
+            if ((st = device_ilu_solve(c, c->dx_io + (size_t)r * c->N, c->dy_io + (size_t)r * c->N, c->stream)))
+                return st;
+    }
+    if ((st = d2h_cols(c, x, c->dy_io, nrhs, c->N))) return st;
+    CK(cudaStreamSynchronize(c->stream));
+    return MLF_OK;
+}
+
 int mlf_excitation(mlf_ctx* h, const double* dirs, const double* pols, double ctte_re, double ctte_im, int nrhs,
                    double* b) {
     if (!h || !dirs || !pols || !b || nrhs <= 0) return MLF_E_ARG;

@@ -356,6 +356,50 @@ __global__ void k_receive_near(int K, int N, int nrhs, int ld, const int* __rest
     }
 }
 
+// Same with the near field held as complex(8): the complex(4) values of the
+// reference converted once at set-up, so the SpMV spends no FP64-pipe slots
+// on float -> double conversions.
+__global__ void k_receive_near_d(int K, int N, int nrhs, int ld, const int* __restrict__ perm,
+                                 const int* __restrict__ box_of_sorted, const double2* __restrict__ R,
+                                 const double2* __restrict__ A, const int* __restrict__ ia,
+                                 const int* __restrict__ ja, const double2* __restrict__ Zd,
+                                 const double2* __restrict__ x, double facy, double2* __restrict__ y) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= N * nrhs) return;
+    const int j = gw / nrhs, r = gw % nrhs;
+    const int n = perm[j], b = box_of_sorted[j];
+    const double2* Rj = R + (size_t)j * 2 * K;
+    const double2* Ab = A + ((size_t)b * nrhs + r) * 2 * K;
+    double sr = 0, si = 0;
+    for (int q = lane; q < 2 * K; q += 32) {
+        const double2 a = Rj[q], v = Ab[q];
+        sr = fma(a.x, v.x, sr); sr = fma(a.y, v.y, sr);
+        si = fma(a.x, v.y, si); si = fma(-a.y, v.x, si);
+    }
+    const double2* xr = x + (size_t)r * ld;
+    double nr = 0, ni = 0;
+    for (int q = ia[n] + lane; q < ia[n + 1]; q += 32) {
+        const double2 z = Zd[q];
+        const double2 xv = xr[ja[q]];
+        nr = fma(xv.x, z.x, nr); nr = fma(-xv.y, z.y, nr);
+        ni = fma(xv.x, z.y, ni); ni = fma(xv.y, z.x, ni);
+    }
+    // combine before the reduction: t = j*facy*s + near
+    double tr = fma(-facy, si, nr), ti = fma(facy, sr, ni);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        tr += __shfl_xor_sync(0xffffffff, tr, o);
+        ti += __shfl_xor_sync(0xffffffff, ti, o);
+    }
+    if (lane == 0) y[(size_t)r * ld + n] = make_double2(tr, ti);
+}
+
+__global__ void k_f2d(size_t n, const float2* __restrict__ a, double2* __restrict__ b) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = make_double2((double)a[i].x, (double)a[i].y);
+}
+
 // ---------------------------------------------------------------------------
 // set-up driver
 // ---------------------------------------------------------------------------
@@ -536,6 +580,9 @@ int device_setup(Ctx* c) {
                                          c->de_t, c->de_po, c->de_long, c->ph.w, c->ph.w * c->ph.smue,
                                          c72, c->dZ);
         if ((st = launch_check(c, "k_near"))) return st;
+        CK(cudaMalloc(&c->dZd, std::max<long long>(c->nnz, 1) * sizeof(double2)));
+        k_f2d<<<4096, 256, 0, c->stream>>>((size_t)c->nnz, c->dZ, c->dZd);
+        if ((st = launch_check(c, "k_f2d"))) return st;
     }
     CK(cudaStreamSynchronize(c->stream));
     return MLF_OK;
@@ -588,9 +635,9 @@ int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaSt
     {
         const int warps = c->N * nrhs;
         const double facy = c->ph.w * MU / (4. * PI);
-        k_receive_near<<<chunks(warps * 32, 256), 256, 0, s>>>(leaf.K, c->N, nrhs, ld, c->dperm,
-                                                                c->dbox_of_sorted, c->dR, leaf.dA, c->dia,
-                                                                c->dja, c->dZ, x, facy, y);
+        k_receive_near_d<<<chunks(warps * 32, 256), 256, 0, s>>>(leaf.K, c->N, nrhs, ld, c->dperm,
+                                                                  c->dbox_of_sorted, c->dR, leaf.dA, c->dia,
+                                                                  c->dja, c->dZd, x, facy, y);
     }
     if (prof) cudaEventRecord(c->ev[5], s);
     if ((st = launch_check(c, "matvec"))) return st;
@@ -632,7 +679,7 @@ void device_free(Ctx* c) {
     F(c->dR); F(c->dperm); F(c->dbox_ptr); F(c->dbox_of_sorted); F(c->dia); F(c->dja); F(c->dZ);
     F(c->dp_coord); F(c->dt_baric); F(c->dt_baric_sub); F(c->de_long); F(c->de_centro); F(c->de_t);
     F(c->de_po); F(c->dalu); F(c->djlu); F(c->dju); F(c->dlvl_rows_f); F(c->dlvl_rows_b);
-    F(c->dwork); F(c->dscal); F(c->dflags); F(c->dx_io); F(c->dy_io); F(c->dMinv);
+    F(c->dwork); F(c->dscal); F(c->dflags); F(c->dx_io); F(c->dy_io); F(c->dMinv); F(c->dZd); F(c->dboff);
     mixed_free(c);
     for (int i = 0; i < 8; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);

@@ -78,6 +78,7 @@ struct Mixed32 {
     int ready = 0, fcap = 0;
     float2* R = nullptr;
     float2* xf = nullptr;
+    float2* xT = nullptr;             // row-major copy of the input block for the near-field tiles
     struct Lv {
         float2 *T = nullptr, *shift = nullptr, *C = nullptr, *B = nullptr, *A = nullptr;
         float *wq = nullptr, *iw = nullptr, *ant_w = nullptr;
@@ -112,6 +113,7 @@ struct Ctx {
     int *dperm = nullptr, *dbox_ptr = nullptr, *dbox_of_sorted = nullptr;
     int *dia = nullptr, *dja = nullptr;
     float2* dZ = nullptr;
+    double2* dZd = nullptr;           // the same near values as complex(8)
     // device geometry for set-up kernels and RCS
     double *dp_coord = nullptr, *dt_baric = nullptr, *dt_baric_sub = nullptr, *de_long = nullptr,
            *de_centro = nullptr;
@@ -123,8 +125,9 @@ struct Ctx {
     float2* dalu = nullptr;
     int *djlu = nullptr, *dju = nullptr;
     // neighbourhood-inverse preconditioner (near CSR pattern)
-    double2* dMinv = nullptr;
-    int nearinv_ok = 0;
+    double2* dMinv = nullptr;         // CSR values, or compact own-box blocks when nearinv_own
+    long long* dboff = nullptr;       // own-box block offsets
+    int nearinv_ok = 0, nearinv_own = 0;
     // level schedule of the triangular solves
     std::vector<int> lvl_ptr_f, lvl_rows_f, lvl_ptr_b, lvl_rows_b;
     int *dlvl_rows_f = nullptr, *dlvl_rows_b = nullptr;

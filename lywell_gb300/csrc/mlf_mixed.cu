@@ -179,6 +179,83 @@ __global__ void k32_receive_near(int K, int N, int nrhs, int ld, const int* __re
     if (lane == 0) y[(size_t)r * ld + n] = make_double2((double)tr, (double)ti);
 }
 
+// Receive-only variant (near field added by k32_near_tiles).
+__global__ void k32_receive(int K, int N, int nrhs, int ld, const int* __restrict__ perm,
+                            const int* __restrict__ box_of_sorted, const float2* __restrict__ R,
+                            const float2* __restrict__ A, float facy, double2* __restrict__ y) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= N * nrhs) return;
+    const int j = gw / nrhs, r = gw % nrhs;
+    const int n = perm[j], b = box_of_sorted[j];
+    const float2* Rj = R + (size_t)j * 2 * K;
+    const float2* Ab = A + ((size_t)b * nrhs + r) * 2 * K;
+    float sr = 0.f, si = 0.f;
+    for (int q = lane; q < 2 * K; q += 32) {
+        const float2 a = Rj[q], v = Ab[q];
+        sr = fmaf(a.x, v.x, sr); sr = fmaf(a.y, v.y, sr);
+        si = fmaf(a.x, v.y, si); si = fmaf(-a.y, v.x, si);
+    }
+    float tr = -facy * si, ti = facy * sr;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        tr += __shfl_xor_sync(0xffffffff, tr, o);
+        ti += __shfl_xor_sync(0xffffffff, ti, o);
+    }
+    if (lane == 0) y[(size_t)r * ld + n] = make_double2((double)tr, (double)ti);
+}
+
+// x (FP64, ld) -> row-major FP32 xT[i][r]
+__global__ void k32_pack_xT(int N, int nrhs, int ld, const double2* __restrict__ x, float2* __restrict__ xT) {
+    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= (size_t)N * nrhs) return;
+    const int i = (int)(e / nrhs), r = (int)(e % nrhs);
+    const double2 v = x[(size_t)r * ld + i];
+    xT[e] = make_float2((float)v.x, (float)v.y);
+}
+
+// y[:, r0:r0+NT] += Znear x for one tile of NT right-hand sides, one warp per
+// row: each complex(4) near value is read once per tile instead of once per
+// column; x is read from the row-major copy so a tile is one contiguous load.
+template <int NT>
+__global__ void k32_near_tiles(int N, int nrhs, int ld, const int* __restrict__ ia, const int* __restrict__ ja,
+                               const float2* __restrict__ Z, const float2* __restrict__ xT, double2* __restrict__ y) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int ntile = (nrhs + NT - 1) / NT;
+    if (gw >= N * ntile) return;
+    const int m = gw / ntile, t = gw % ntile;
+    const int r0 = t * NT, nr = min(NT, nrhs - r0);
+    float2 acc[NT];
+#pragma unroll
+    for (int u = 0; u < NT; ++u) acc[u] = make_float2(0.f, 0.f);
+    for (int q = ia[m] + lane; q < ia[m + 1]; q += 32) {
+        const float2 z = Z[q];
+        const float2* xr = xT + (size_t)ja[q] * nrhs + r0;
+#pragma unroll
+        for (int u = 0; u < NT; ++u)
+            if (u < nr) fmac(acc[u], z, xr[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < NT; ++u) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            acc[u].x += __shfl_xor_sync(0xffffffff, acc[u].x, o);
+            acc[u].y += __shfl_xor_sync(0xffffffff, acc[u].y, o);
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int u = 0; u < NT; ++u) {
+            if (u < nr) {
+                double2* yp = y + (size_t)(r0 + u) * ld + m;
+                const double2 v = *yp;
+                *yp = make_double2(v.x + (double)acc[u].x, v.y + (double)acc[u].y);
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 
 static int up32(Ctx* c, float** dst, const std::vector<double>& v) {
@@ -248,6 +325,8 @@ static int ensure_fields32(Ctx* c, int nrhs) {
     }
     if (c->m32.xf) cudaFree(c->m32.xf);
     CK(cudaMalloc(&c->m32.xf, (size_t)c->N * nrhs * sizeof(float2)));
+    if (c->m32.xT) cudaFree(c->m32.xT);
+    CK(cudaMalloc(&c->m32.xT, (size_t)c->N * nrhs * sizeof(float2)));
     c->m32.fcap = nrhs;
     return MLF_OK;
 }
@@ -295,9 +374,20 @@ int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cuda
     {
         const long long warps = (long long)c->N * nrhs;
         const float facy = (float)(c->ph.w * MU / (4. * PI));
-        k32_receive_near<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-            leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, c->m32.lv[nl].A, c->dia, c->dja, c->dZ,
-            c->m32.xf, facy, y);
+        if (nrhs == 1) {
+            k32_receive_near<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+                leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, c->m32.lv[nl].A, c->dia, c->dja,
+                c->dZ, c->m32.xf, facy, y);
+        } else {
+            k32_receive<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+                leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, c->m32.lv[nl].A, facy, y);
+            const size_t ne = (size_t)c->N * nrhs;
+            k32_pack_xT<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(c->N, nrhs, ld, x, c->m32.xT);
+            constexpr int NT = 16;
+            const long long w2 = (long long)c->N * ((nrhs + NT - 1) / NT);
+            k32_near_tiles<NT><<<(unsigned)((w2 * 32 + 255) / 256), 256, 0, s>>>(c->N, nrhs, ld, c->dia, c->dja,
+                                                                              c->dZ, c->m32.xT, y);
+        }
     }
     if (prof) cudaEventRecord(c->ev[5], s);
     if (!cuda_ok(c, cudaGetLastError(), "matvec32")) return MLF_E_CUDA;
@@ -310,7 +400,7 @@ int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cuda
 
 void mixed_free(Ctx* c) {
     auto F = [](void* p) { if (p) cudaFree(p); };
-    F(c->m32.R); F(c->m32.xf);
+    F(c->m32.R); F(c->m32.xf); F(c->m32.xT);
     for (int n = 0; n < 32; ++n) {
         Mixed32::Lv& M = c->m32.lv[n];
         F(M.T); F(M.wq); F(M.iw); F(M.ant_w); F(M.shift); F(M.C); F(M.B); F(M.A);
@@ -502,6 +592,7 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
         std::vector<int> live(nrhs, 0);
         for (int col = 0; col < nrhs; ++col) live[col] = !done[col];
         int j = 0;
+        cudaGraphExec_t gexec = nullptr;
         for (; j < m; ++j) {
             bool any = false;
             for (int col = 0; col < nrhs; ++col) any = any || live[col];
@@ -513,10 +604,30 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
                     st = device_ilu_solve(c, vj + (size_t)col * N, t + (size_t)col * N, s);
                 if (st) break;
             } else CK(cudaMemcpyAsync(t, vj, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-            c->mv_prec = 1;
-            st = device_matvec(c, t, w, nrhs, N, s);
-            c->mv_prec = 0;
-            if (st) break;
+            // w = A32 t: the first step of a cycle records the FP32 matvec's
+            // launches (fixed buffers t -> w) into a CUDA graph, later steps replay it
+            if (!gexec) {
+                c->mv_prec = 1;
+                st = device_matvec(c, t, w, nrhs, N, s);   // allocates lazily, outside any capture
+                c->mv_prec = 0;
+                if (st) break;
+                cudaGraph_t graph = nullptr;
+                if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                    c->mv_prec = 1;
+                    const int prof = c->profiling;
+                    c->profiling = 0;
+                    const int st2 = device_matvec(c, t, w, nrhs, N, s);
+                    c->profiling = prof;
+                    c->mv_prec = 0;
+                    if (cudaStreamEndCapture(s, &graph) == cudaSuccess && st2 == MLF_OK && graph) {
+                        if (cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) gexec = nullptr;
+                    }
+                    if (graph) cudaGraphDestroy(graph);
+                    cudaGetLastError();
+                }
+            } else {
+                CK(cudaGraphLaunch(gexec, s));
+            }
             std::vector<double2> hsum((size_t)(j + 1) * nrhs, make_double2(0, 0));
             for (int pass = 0; pass < 2; ++pass) {
                 k_mdot<<<dim3(GM_BLOCKS, nrhs, j + 1), 256, 0, s>>>(N, nrhs, V, V1, w, partial);
@@ -559,6 +670,7 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
                 if (est < inner_tol * bn[col] || hn[col] <= 1e-300 * bn[col] || iters[col] >= maxit) live[col] = 0;
             }
         }
+        if (gexec) cudaGraphExecDestroy(gexec);
         if (st) break;
         // y = H^-1 g per column, d = V y, x += M^-1 d
         std::vector<double2> y((size_t)(m + 1) * nrhs, make_double2(0, 0));

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(NBI_THREADS)
 k_nbhd_inverse(int b0, int nb, const int* __restrict__ box_ptr, const int* __restrict__ box_bases,
                const int* __restrict__ own_sorted, int own_only, const int* __restrict__ ia,
                const int* __restrict__ ja, const float2* __restrict__ Z, size_t slab, double2* __restrict__ work,
-               double2* __restrict__ M, int* __restrict__ bad) {
+               double2* __restrict__ M, const long long* __restrict__ boff, int* __restrict__ bad) {
     const int b = b0 + blockIdx.x;
     if (b >= nb) return;
     const int tid = threadIdx.x, bd = blockDim.x;
@@ -168,15 +168,37 @@ k_nbhd_inverse(int b0, int nb, const int* __restrict__ box_ptr, const int* __res
             M[(size_t)ia[g] + j] = X[(size_t)j * nown + i];
         }
     } else {
-        // rows of the own-box inverse, placed at the own columns of each CSR row
-        const int rl = ia[m0 + 1] - ia[m0];
-        for (int e = tid; e < nown * rl; e += bd) {
-            const int i = e / rl, q = e % rl;
-            const int g = box_bases[box_ptr[b] + i];
-            const int pos = bsearch_sorted(S, n, ja[ia[g] + q]);
-            M[(size_t)ia[g] + q] = pos >= 0 ? X[(size_t)pos * nown + i] : make_double2(0, 0);
+        // compact block: row i of the own-box inverse at boff[b] + i*nown
+        for (int e = tid; e < nown * nown; e += bd) {
+            const int i = e / nown, j = e % nown;
+            M[boff[b] + e] = X[(size_t)j * nown + i];
         }
     }
+}
+
+// y[:, col] = blockdiag(M_b) x[:, col]; warp per (box-sorted row p, column)
+__global__ void k_blockdiag_apply(int N, int nrhs, const int* __restrict__ box_ptr,
+                                  const int* __restrict__ box_of_sorted, const int* __restrict__ perm,
+                                  const long long* __restrict__ boff, const double2* __restrict__ M,
+                                  const double2* __restrict__ x, double2* __restrict__ y) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (gw >= N * nrhs) return;
+    const int p = gw % N, col = gw / N;
+    const int b = box_of_sorted[p], j0 = box_ptr[b], n = box_ptr[b + 1] - j0, i = p - j0;
+    const double2* row = M + boff[b] + (size_t)i * n;
+    const double2* xc = x + (size_t)col * N;
+    double sr = 0, si = 0;
+    for (int j = lane; j < n; j += 32) {
+        const double2 a = row[j], v = xc[perm[j0 + j]];
+        sr = fma(a.x, v.x, sr); sr = fma(-a.y, v.y, sr);
+        si = fma(a.x, v.y, si); si = fma(a.y, v.x, si);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffff, sr, o);
+        si += __shfl_xor_sync(0xffffffff, si, o);
+    }
+    if (lane == 0) y[(size_t)col * N + perm[p]] = make_double2(sr, si);
 }
 
 // y[:, col] = M x[:, col], one warp per (row, column), near CSR pattern
@@ -213,9 +235,23 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     int batch = (int)std::min<size_t>(leaf.nb, std::max<size_t>(1, ((size_t)1 << 30) / (slab * sizeof(double2))));
     batch = std::min(batch, 4096);
     if (c->dMinv) cudaFree(c->dMinv);
+    if (c->dboff) cudaFree(c->dboff);
     c->dMinv = nullptr;
+    c->dboff = nullptr;
     c->nearinv_ok = 0;
-    CK(cudaMalloc(&c->dMinv, std::max<long long>(c->nnz, 1) * sizeof(double2)));
+    c->nearinv_own = own_only;
+    long long total = c->nnz;
+    if (own_only) {
+        std::vector<long long> boff(leaf.nb + 1, 0);
+        for (int b = 0; b < leaf.nb; ++b) {
+            const long long n = c->box_ptr[b + 1] - c->box_ptr[b];
+            boff[b + 1] = boff[b] + n * n;
+        }
+        total = boff[leaf.nb];
+        CK(cudaMalloc(&c->dboff, boff.size() * sizeof(long long)));
+        CK(cudaMemcpy(c->dboff, boff.data(), boff.size() * sizeof(long long), cudaMemcpyHostToDevice));
+    }
+    CK(cudaMalloc(&c->dMinv, std::max<long long>(total, 1) * sizeof(double2)));
     double2* work = nullptr;
     int* dbad = nullptr;
     int* dbases = nullptr;
@@ -224,20 +260,13 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     const int big = 0x7fffffff;
     CK(cudaMemcpy(dbad, &big, sizeof(int), cudaMemcpyHostToDevice));
     dbases = c->dperm;   // the box-sorted basis list
-    int* downs = nullptr;  // each box's own bases, sorted (the box lists are ascending already)
-    if (own_only) {
-        std::vector<int> own(c->box_bases);
-        for (int b = 0; b < leaf.nb; ++b) std::sort(own.begin() + c->box_ptr[b], own.begin() + c->box_ptr[b + 1]);
-        CK(cudaMalloc(&downs, own.size() * sizeof(int)));
-        CK(cudaMemcpy(downs, own.data(), own.size() * sizeof(int), cudaMemcpyHostToDevice));
-        CK(cudaMemsetAsync(c->dMinv, 0, std::max<long long>(c->nnz, 1) * sizeof(double2), c->stream));
-    }
+    // each box's own bases in ascending order: the box-sorted list already is
     for (int b0 = 0; b0 < leaf.nb; b0 += batch) {
         k_nbhd_inverse<<<std::min(batch, leaf.nb - b0), NBI_THREADS, 0, c->stream>>>(
-            b0, leaf.nb, c->dbox_ptr, dbases, downs, own_only, c->dia, c->dja, c->dZ, slab, work, c->dMinv, dbad);
+            b0, leaf.nb, c->dbox_ptr, dbases, dbases, own_only, c->dia, c->dja, c->dZ, slab, work, c->dMinv,
+            c->dboff, dbad);
         CK(cudaGetLastError());
     }
-    if (downs) cudaFree(downs);
     int hbad = 0;
     CK(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -254,8 +283,12 @@ int device_nearinv_apply(Ctx* c, const double2* y, double2* x, int nrhs, cudaStr
         return MLF_E_STATE;
     }
     const long long warps = (long long)c->N * nrhs;
-    k_spmv_z<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(c->N, nrhs, c->dia, c->dja, c->dMinv, y, x);
-    return cuda_ok(c, cudaGetLastError(), "k_spmv_z") ? MLF_OK : MLF_E_CUDA;
+    if (c->nearinv_own)
+        k_blockdiag_apply<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+            c->N, nrhs, c->dbox_ptr, c->dbox_of_sorted, c->dperm, c->dboff, c->dMinv, y, x);
+    else
+        k_spmv_z<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(c->N, nrhs, c->dia, c->dja, c->dMinv, y, x);
+    return cuda_ok(c, cudaGetLastError(), "nearinv apply") ? MLF_OK : MLF_E_CUDA;
 }
 
 }  // namespace mlf
@@ -279,7 +312,10 @@ extern "C" int mlf_nearinv_own(mlf_ctx* h, int* bad_box) {
 extern "C" int mlf_nearinv_values(mlf_ctx* h, double* vals) {
     if (!h || !vals) return MLF_E_ARG;
     Ctx* c = &h->c;
-    if (!c->nearinv_ok) { c->err = "neighbourhood-inverse preconditioner not built"; return MLF_E_STATE; }
+    if (!c->nearinv_ok || c->nearinv_own) {
+        c->err = "neighbourhood-inverse values exist for the full-neighbourhood mode only";
+        return MLF_E_STATE;
+    }
     if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
     CK(cudaMemcpy(vals, c->dMinv, c->nnz * sizeof(double2), cudaMemcpyDeviceToHost));
     return MLF_OK;

@@ -226,6 +226,16 @@ class MLFMA:
         _check(f(self._h, C.byref(bad)), self._h)
         return int(bad.value)
 
+    def precond_apply(self, y, precond="nearinv"):
+        if isinstance(precond, str):
+            precond = PRECOND[precond]
+        y = np.asarray(y, dtype=np.complex128)
+        single = y.ndim == 1
+        Y = np.asfortranarray(y.reshape(self.N, -1))
+        X = np.zeros_like(Y)
+        _check(load().mlf_precond_apply(self._h, int(precond), _p(Y), _p(X), Y.shape[1]), self._h)
+        return X[:, 0] if single else X
+
     def nearinv_values(self):
         out = np.zeros(self.nnz, dtype=np.complex128)
         _check(load().mlf_nearinv_values(self._h, _p(out)), self._h)

@@ -111,3 +111,33 @@ def test_mixed_multi_rhs(ico4):
         assert out["status"][k] == "converged"
         r = np.linalg.norm(m.matvec(out["x"][:, k]) - B[:, k]) / np.linalg.norm(B[:, k])
         assert r < 1e-4
+
+
+def test_fp32_multi_rhs_columns(ico4):
+    """The batched FP32 operator (near field in tiles of right-hand sides)
+    against one column at a time."""
+    _, m, _ = ico4
+    rng = np.random.default_rng(11)
+    X = rng.standard_normal((m.N, 20)) + 1j * rng.standard_normal((m.N, 20))
+    Y = m.matvec32(X)
+    for k in (0, 7, 19):
+        assert _rel(Y[:, k], m.matvec32(X[:, k])) < 1e-6
+        assert _rel(Y[:, k], m.matvec(X[:, k])) < 2e-5
+
+
+def test_own_box_inverse_apply(ico4):
+    """Own-box mode: x = blockdiag(Z_bb^-1) y against numpy on the same near field."""
+    _, m, o = ico4
+    assert m.nearinv(own_only=True) == 0
+    ia, ja, z = m.near_csr()
+    import scipy.sparse as sps
+    Z = sps.csr_matrix((z.astype(np.complex128), ja - 1, ia - 1), shape=(m.N, m.N))
+    ptr, bases = o.leaf_boxes()
+    y = np.random.default_rng(4).standard_normal(m.N) + 1j * np.random.default_rng(5).standard_normal(m.N)
+    x = m.precond_apply(y, "nearinv")
+    ref = np.zeros_like(y)
+    for b in range(len(ptr) - 1):
+        own = bases[ptr[b]:ptr[b + 1]]
+        ref[own] = np.linalg.solve(Z[own][:, own].toarray(), y[own])
+    assert _rel(x, ref) < 1e-10
+    assert m.nearinv() == 0   # back to the full neighbourhood for the other tests
