@@ -180,6 +180,21 @@ int mlf_solve(mlf_ctx* ctx, const double* b, const double* x0, double tol, int m
  * complex(8) values). */
 int mlf_set_gmres_restart(mlf_ctx* ctx, int m);
 
+/* Phase times (ms) of the last mixed-precision solve run while profiling was
+ * on (mlf_set_profiling): out4 = {preconditioner, FP32 operator,
+ * orthogonalisation, wall total}.  No counterpart in the reference. */
+int mlf_solve_times(mlf_ctx* ctx, double* out4);
+
+/* Autotuner for batched solves: times the FP32 operator on each candidate
+ * block of right-hand sides (candidates[ncand], 1..4096) with both near-field
+ * tile widths (8 and 32 columns) and returns the smallest block whose time
+ * per right-hand side is within 5 % of the best, with its tile width (0 for a
+ * single column); the tile width is kept for later operator calls.
+ * per_rhs_ms (optional, ncand) receives the best time per right-hand side of
+ * each candidate.  No counterpart in the reference. */
+int mlf_autotune_block(mlf_ctx* ctx, const int* candidates, int ncand, int* best_block, int* best_cols,
+                       float* per_rhs_ms);
+
 /* y = Z_MLFMA x with the FP32 operator of mode 1 (host or device arrays);
  * inputs and outputs complex(8). */
 int mlf_matvec32(mlf_ctx* ctx, const double* x, double* y, int nrhs, int ld);
@@ -235,6 +250,7 @@ int mlf_rcs(mlf_ctx* ctx, const double* I, const double* pol, double ctte_re, do
  *         warm start = previous currents x exp(-j k (d_a - d_{a-1}) . r_edge).
  * mode 1: batched, blocks of `block` angles as one multi-RHS FP64 CGS.
  * mode 2: batched mixed precision (mlf_solve mode 1 per block).
+ * block <= 0 (modes 1, 2): chosen by mlf_autotune_block among 8..128.
  * Modes 1 and 2 have no counterpart in the reference. */
 int mlf_monostatic(mlf_ctx* ctx, int nang, const double* phis, int hh, double ctte_re, double ctte_im,
                    double tol, int maxit, int precond_kind, int mode, int block, double* sigma, int* iters,

@@ -37,6 +37,8 @@ SIGNATURES = {
                             vp, ip]),
     "mlf_matvec32": (C.c_int, [vp, vp, vp, C.c_int, C.c_int]),
     "mlf_set_gmres_restart": (C.c_int, [vp, C.c_int]),
+    "mlf_solve_times": (C.c_int, [vp, vp]),
+    "mlf_autotune_block": (C.c_int, [vp, vp, C.c_int, vp, vp, vp]),
     "mlf_matvec32_device": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, vp]),
     "mlf_nearinv_values": (C.c_int, [vp, vp]),
     "mlf_cgs_history": (C.c_int, [vp, C.c_int, vp, C.c_int, ip]),

@@ -78,7 +78,7 @@ struct Mixed32 {
     int ready = 0, fcap = 0;
     float2* R = nullptr;
     float2* xf = nullptr;
-    float2* xT = nullptr;             // row-major copy of the input block for the near-field tiles
+    float2* xT = nullptr;             // box-sorted row-major copy of the input block (near blocks)
     struct Lv {
         float2 *T = nullptr, *shift = nullptr, *C = nullptr, *B = nullptr, *A = nullptr;
         float *wq = nullptr, *iw = nullptr, *ant_w = nullptr;
@@ -106,6 +106,17 @@ struct Ctx {
     // leaf boxes
     std::vector<int> box_ptr, box_bases, box_of;
     std::vector<int> near_ptr, near_bases;
+    std::vector<int> nbox_ptr, nbox_list;   // near leaf boxes of each leaf box, ascending
+    // near field as dense box-pair blocks (multi-right-hand-side FP32 operator):
+    // block e = (i, nbox_list[e]) holds Z(rows of box i, columns of box j)
+    // column-major at Zblk + blk_off[e]; tiles = (box, first row) of each
+    // 64-row tile of the leaf boxes
+    int blk_ok = 0, nblk_tiles = 0;
+    int blk_cols = 0;                 // near-block tile width: 0 = by nrhs, else 8 or 32 (autotuner)
+    float2* dZblk = nullptr;
+    long long* dblk_off = nullptr;
+    int *dnbox_ptr = nullptr, *dnbox_list = nullptr;
+    int2* dblk_tiles = nullptr;
     long long nnz = 0;
     std::vector<int> ia, ja;          // 0-based CSR
     // device: leaf
@@ -127,6 +138,8 @@ struct Ctx {
     // neighbourhood-inverse preconditioner (near CSR pattern)
     double2* dMinv = nullptr;         // CSR values, or compact own-box blocks when nearinv_own
     long long* dboff = nullptr;       // own-box block offsets
+    float2* dMinv32 = nullptr;        // FP32 copy for the FP32 inner solves
+    long long minv_len = 0;
     int nearinv_ok = 0, nearinv_own = 0;
     // level schedule of the triangular solves
     std::vector<int> lvl_ptr_f, lvl_rows_f, lvl_ptr_b, lvl_rows_b;
@@ -146,6 +159,10 @@ struct Ctx {
     int profiling = 0;
     cudaEvent_t ev[8]{};
     float stage_ms[5]{};
+    // mixed solve phases, accumulated while profiling: preconditioner,
+    // FP32 operator, orthogonalisation, total
+    cudaEvent_t sev[4]{};
+    double solve_ms[4]{};
 };
 
 // host set-up (mlf_setup.cpp)
@@ -170,7 +187,13 @@ int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxi
                double2* x, int* iters, double* relres, int precond, int* status);
 int device_nearinv_setup(Ctx* c, int* bad_box, int own_only);
 int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s);
+int device_matvec32_from32(Ctx* c, const float2* x32, double2* y, int nrhs, cudaStream_t s);
+int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStream_t s);
 void mixed_free(Ctx* c);
+int device_near_blocks32(Ctx* c, const double2* x, const float2* x32, int ld, int nrhs, float2* xs, double2* y,
+                         cudaStream_t s);
+void near_blocks_free(Ctx* c);
+int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* best_cols, float* per_rhs_ms);
 int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
                        int* iters, double* relres, int precond, int* status, double inner_tol, int* outer);
 int device_nearinv_apply(Ctx* c, const double2* y, double2* x, int nrhs, cudaStream_t s);

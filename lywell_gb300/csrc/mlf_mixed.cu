@@ -9,14 +9,15 @@
 // itself.  Input and output vectors stay complex(8).
 //
 // Refinement (mode 1 of mlf_solve): r = b - A64 x in FP64; one restart cycle
-// of right-preconditioned GMRES(m) on the FP32 operator (FP64 vectors and
-// Arnoldi) solves A d = r until its residual estimate drops below
-// inner_tol ||b|| or m steps; x += M^-1 V y; stop when the FP64 residual
-// ||b - A64 x|| < tol ||b||.  The FP64 residual is the judge, so the result
+// of right-preconditioned GMRES(m) solves A d = r with an FP32 inner loop
+// (operator, preconditioner, Krylov basis and Gram-Schmidt in float) until its
+// residual estimate drops below inner_tol ||b|| or m steps; x += M^-1 V y in
+// FP64; stop when the FP64 residual ||b - A64 x|| < tol ||b||.  The FP64 residual is the judge, so the result
 // meets the same stopping test as the plain FP64 solve.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <vector>
 
@@ -205,57 +206,6 @@ __global__ void k32_receive(int K, int N, int nrhs, int ld, const int* __restric
     if (lane == 0) y[(size_t)r * ld + n] = make_double2((double)tr, (double)ti);
 }
 
-// x (FP64, ld) -> row-major FP32 xT[i][r]
-__global__ void k32_pack_xT(int N, int nrhs, int ld, const double2* __restrict__ x, float2* __restrict__ xT) {
-    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (e >= (size_t)N * nrhs) return;
-    const int i = (int)(e / nrhs), r = (int)(e % nrhs);
-    const double2 v = x[(size_t)r * ld + i];
-    xT[e] = make_float2((float)v.x, (float)v.y);
-}
-
-// y[:, r0:r0+NT] += Znear x for one tile of NT right-hand sides, one warp per
-// row: each complex(4) near value is read once per tile instead of once per
-// column; x is read from the row-major copy so a tile is one contiguous load.
-template <int NT>
-__global__ void k32_near_tiles(int N, int nrhs, int ld, const int* __restrict__ ia, const int* __restrict__ ja,
-                               const float2* __restrict__ Z, const float2* __restrict__ xT, double2* __restrict__ y) {
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const int ntile = (nrhs + NT - 1) / NT;
-    if (gw >= N * ntile) return;
-    const int m = gw / ntile, t = gw % ntile;
-    const int r0 = t * NT, nr = min(NT, nrhs - r0);
-    float2 acc[NT];
-#pragma unroll
-    for (int u = 0; u < NT; ++u) acc[u] = make_float2(0.f, 0.f);
-    for (int q = ia[m] + lane; q < ia[m + 1]; q += 32) {
-        const float2 z = Z[q];
-        const float2* xr = xT + (size_t)ja[q] * nrhs + r0;
-#pragma unroll
-        for (int u = 0; u < NT; ++u)
-            if (u < nr) fmac(acc[u], z, xr[u]);
-    }
-#pragma unroll
-    for (int u = 0; u < NT; ++u) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            acc[u].x += __shfl_xor_sync(0xffffffff, acc[u].x, o);
-            acc[u].y += __shfl_xor_sync(0xffffffff, acc[u].y, o);
-        }
-    }
-    if (lane == 0) {
-#pragma unroll
-        for (int u = 0; u < NT; ++u) {
-            if (u < nr) {
-                double2* yp = y + (size_t)(r0 + u) * ld + m;
-                const double2 v = *yp;
-                *yp = make_double2(v.x + (double)acc[u].x, v.y + (double)acc[u].y);
-            }
-        }
-    }
-}
-
 // ---------------------------------------------------------------------------
 
 static int up32(Ctx* c, float** dst, const std::vector<double>& v) {
@@ -331,7 +281,18 @@ static int ensure_fields32(Ctx* c, int nrhs) {
     return MLF_OK;
 }
 
+static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y, int nrhs, int ld, cudaStream_t s);
+
 int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s) {
+    return matvec32_core(c, x, nullptr, y, nrhs, ld, s);
+}
+
+// y (FP64 columns, ld = N) = A32 x32 (FP32 packed columns)
+int device_matvec32_from32(Ctx* c, const float2* x32, double2* y, int nrhs, cudaStream_t s) {
+    return matvec32_core(c, nullptr, x32, y, nrhs, c->N, s);
+}
+
+static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y, int nrhs, int ld, cudaStream_t s) {
     int st;
     if ((st = mixed_setup(c))) return st;
     if ((st = ensure_fields32(c, nrhs))) return st;
@@ -339,8 +300,9 @@ int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cuda
     Level& leaf = c->lv[nl];
     const bool prof = c->profiling != 0;
     if (prof) cudaEventRecord(c->ev[0], s);
-    k32_pack_x<<<dim3((c->N + 255) / 256, nrhs), 256, 0, s>>>(c->N, nrhs, ld, x, c->m32.xf);
-    k32_aggregate<<<leaf.nb * nrhs, 256, 0, s>>>(leaf.K, nrhs, c->N, c->dbox_ptr, c->dperm, c->m32.R, c->m32.xf,
+    const float2* xf = x32 ? x32 : c->m32.xf;
+    if (!x32) k32_pack_x<<<dim3((c->N + 255) / 256, nrhs), 256, 0, s>>>(c->N, nrhs, ld, x, c->m32.xf);
+    k32_aggregate<<<leaf.nb * nrhs, 256, 0, s>>>(leaf.K, nrhs, c->N, c->dbox_ptr, c->dperm, c->m32.R, xf,
                                                  c->m32.lv[nl].C);
     if (prof) cudaEventRecord(c->ev[1], s);
     for (int n = nl; n >= 4; --n) {
@@ -377,16 +339,11 @@ int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cuda
         if (nrhs == 1) {
             k32_receive_near<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
                 leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, c->m32.lv[nl].A, c->dia, c->dja,
-                c->dZ, c->m32.xf, facy, y);
+                c->dZ, xf, facy, y);
         } else {
             k32_receive<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
                 leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, c->m32.lv[nl].A, facy, y);
-            const size_t ne = (size_t)c->N * nrhs;
-            k32_pack_xT<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(c->N, nrhs, ld, x, c->m32.xT);
-            constexpr int NT = 16;
-            const long long w2 = (long long)c->N * ((nrhs + NT - 1) / NT);
-            k32_near_tiles<NT><<<(unsigned)((w2 * 32 + 255) / 256), 256, 0, s>>>(c->N, nrhs, ld, c->dia, c->dja,
-                                                                              c->dZ, c->m32.xT, y);
+            if ((st = device_near_blocks32(c, x, x32, ld, nrhs, c->m32.xT, y, s))) return st;
         }
     }
     if (prof) cudaEventRecord(c->ev[5], s);
@@ -513,6 +470,175 @@ __global__ void k_combine(int N, int nrhs, int nvec, const double2* __restrict__
     }
 }
 
+// FP32 Arnoldi kernels: basis V32 and work vector w32 in float, per-thread
+// sums in float, block and final reductions in double.
+__global__ void k_mdot32(int N, int nrhs, const float2* __restrict__ V, size_t vstride, const float2* __restrict__ w,
+                         double2* __restrict__ partial) {
+    const int col = blockIdx.y, i = blockIdx.z;
+    const float2* wc = w + (size_t)col * N;
+    const float2* vc = V ? V + i * vstride + (size_t)col * N : nullptr;
+    float sr = 0.f, si = 0.f;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+        const float2 b = wc[e];
+        if (vc) {
+            const float2 a = vc[e];
+            sr = fmaf(a.x, b.x, sr); sr = fmaf(a.y, b.y, sr);
+            si = fmaf(a.x, b.y, si); si = fmaf(-a.y, b.x, si);
+        } else {
+            sr = fmaf(b.x, b.x, sr); sr = fmaf(b.y, b.y, sr);
+        }
+    }
+    __shared__ double rs[256], is[256];
+    rs[threadIdx.x] = sr;
+    is[threadIdx.x] = si;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) { rs[threadIdx.x] += rs[threadIdx.x + s]; is[threadIdx.x] += is[threadIdx.x + s]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[((size_t)i * nrhs + col) * gridDim.x + blockIdx.x] = make_double2(rs[0], is[0]);
+}
+
+// Block dot products for the FP32 Arnoldi step: each CTA keeps its slice of
+// w (MD_E values per thread) in registers and streams the nvec basis vectors
+// past it, MD_G vectors per block reduction.
+// partial[(i * nrhs + col) * gridDim.x + blockIdx.x] = sum conj(V_i) w over the slice.
+constexpr int MD_E = 8, MD_G = 4;
+__global__ void __launch_bounds__(256) k_mdot32b(int N, int nrhs, int nvec, const float2* __restrict__ V,
+                                                 size_t vstride, const float2* __restrict__ w,
+                                                 double2* __restrict__ partial) {
+    const int col = blockIdx.y;
+    const size_t base = (size_t)col * N;
+    const int e0 = blockIdx.x * 256 * MD_E + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ float red[8][2 * MD_G];
+    float2 wv[MD_E];
+#pragma unroll
+    for (int u = 0; u < MD_E; ++u) {
+        const int e = e0 + u * 256;
+        wv[u] = e < N ? w[base + e] : make_float2(0.f, 0.f);
+    }
+    for (int i0 = 0; i0 < nvec; i0 += MD_G) {
+        float sacc[2 * MD_G];
+#pragma unroll
+        for (int g = 0; g < MD_G; ++g) {
+            float sr = 0.f, si = 0.f;
+            const int i = i0 + g;
+            if (i < nvec) {
+                const float2* v = V + (size_t)i * vstride + base;
+#pragma unroll
+                for (int u = 0; u < MD_E; ++u) {
+                    const int e = e0 + u * 256;
+                    if (e < N) {
+                        const float2 a = v[e];
+                        sr = fmaf(a.x, wv[u].x, sr); sr = fmaf(a.y, wv[u].y, sr);
+                        si = fmaf(a.x, wv[u].y, si); si = fmaf(-a.y, wv[u].x, si);
+                    }
+                }
+            }
+            sacc[2 * g] = sr;
+            sacc[2 * g + 1] = si;
+        }
+#pragma unroll
+        for (int q = 0; q < 2 * MD_G; ++q)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sacc[q] += __shfl_xor_sync(0xffffffff, sacc[q], o);
+        if (lane == 0)
+#pragma unroll
+            for (int q = 0; q < 2 * MD_G; ++q) red[warp][q] = sacc[q];
+        __syncthreads();
+        if (threadIdx.x < MD_G && i0 + (int)threadIdx.x < nvec) {
+            double tr = 0, ti = 0;
+            for (int wp = 0; wp < 8; ++wp) {
+                tr += red[wp][2 * threadIdx.x];
+                ti += red[wp][2 * threadIdx.x + 1];
+            }
+            partial[((size_t)(i0 + threadIdx.x) * nrhs + col) * gridDim.x + blockIdx.x] = make_double2(tr, ti);
+        }
+        __syncthreads();
+    }
+}
+
+// out[k] = sum_b partial[k * nb + b], fixed order
+__global__ void k_reduce_partials_n(int nk, int nb, const double2* __restrict__ partial, double2* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    double2 s = make_double2(0, 0);
+    for (int b = 0; b < nb; ++b) {
+        s.x += partial[(size_t)k * nb + b].x;
+        s.y += partial[(size_t)k * nb + b].y;
+    }
+    out[k] = s;
+}
+
+__global__ void k_gs_update32(int N, int nrhs, int nvec, const float2* __restrict__ V, size_t vstride,
+                              const double2* __restrict__ h, float2* __restrict__ w) {
+    const int col = blockIdx.y;
+    __shared__ float2 hs[2048];
+    for (int i = threadIdx.x; i < nvec; i += blockDim.x) {
+        const double2 hd = h[(size_t)i * nrhs + col];
+        hs[i] = make_float2((float)hd.x, (float)hd.y);
+    }
+    __syncthreads();
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+        float2 acc = w[(size_t)col * N + e];
+        const float2* v = V + (size_t)col * N + e;
+#pragma unroll 4
+        for (int i = 0; i < nvec; ++i) {
+            const float2 hv = hs[i];
+            const float2 a = v[(size_t)i * vstride];
+            acc.x -= hv.x * a.x - hv.y * a.y;
+            acc.y -= hv.x * a.y + hv.y * a.x;
+        }
+        w[(size_t)col * N + e] = acc;
+    }
+}
+
+__global__ void k_colscale_df(int N, const double2* __restrict__ src, const double* __restrict__ s,
+                              float2* __restrict__ dst) {
+    const int col = blockIdx.y;
+    const double f = s[col];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+        const double2 v = src[(size_t)col * N + e];
+        dst[(size_t)col * N + e] = make_float2((float)(v.x * f), (float)(v.y * f));
+    }
+}
+
+__global__ void k_colscale32(int N, const float2* __restrict__ src, const double* __restrict__ s,
+                             float2* __restrict__ dst) {
+    const int col = blockIdx.y;
+    const float f = (float)s[col];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+        const float2 v = src[(size_t)col * N + e];
+        dst[(size_t)col * N + e] = make_float2(v.x * f, v.y * f);
+    }
+}
+
+// d[col] = sum_i y[i*nrhs+col] V32_i[col] in double (once per cycle)
+__global__ void k_combine32(int N, int nrhs, int nvec, const float2* __restrict__ V, size_t vstride,
+                            const double2* __restrict__ y, double2* __restrict__ d) {
+    const int col = blockIdx.y;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+        double2 acc = make_double2(0, 0);
+        for (int i = 0; i < nvec; ++i) {
+            const double2 yv = y[i * nrhs + col];
+            const float2 v = V[i * vstride + (size_t)col * N + e];
+            acc.x += yv.x * v.x - yv.y * v.y;
+            acc.y += yv.x * v.y + yv.y * v.x;
+        }
+        d[(size_t)col * N + e] = acc;
+    }
+}
+
+__global__ void k_d2f_m(size_t n, const double2* __restrict__ a, float2* __restrict__ b) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+__global__ void k_f2d_m(size_t n, const float2* __restrict__ a, double2* __restrict__ b) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = make_double2((double)a[i].x, (double)a[i].y);
+}
+
 namespace {
 struct Cx {
     double r, i;
@@ -539,19 +665,51 @@ static int col_norms(Ctx* c, int nrhs, const double2* w, double2* partial, doubl
     return MLF_OK;
 }
 
+static int col_norms32(Ctx* c, int nrhs, const float2* w, double2* partial, double2* dred, std::vector<double2>& h,
+                       std::vector<double>& out, cudaStream_t s) {
+    k_mdot32<<<dim3(GM_BLOCKS, nrhs, 1), 256, 0, s>>>(c->N, nrhs, nullptr, 0, w, partial);
+    k_reduce_partials<<<(nrhs + 127) / 128, 128, 0, s>>>(nrhs, partial, dred);
+    CK(cudaMemcpyAsync(h.data(), dred, nrhs * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int col = 0; col < nrhs; ++col) out[col] = std::sqrt(h[col].x);
+    return MLF_OK;
+}
+
+// FP64 M^-1 applied to the correction once per cycle
+static int apply_precond64(Ctx* c, int precond, int nrhs, const double2* in, double2* out, cudaStream_t s) {
+    if (precond == 2) return device_nearinv_apply(c, in, out, nrhs, s);
+    if (precond == 1) {
+        for (int col = 0; col < nrhs; ++col) {
+            const int st = device_ilu_solve(c, in + (size_t)col * c->N, out + (size_t)col * c->N, s);
+            if (st) return st;
+        }
+        return MLF_OK;
+    }
+    CK(cudaMemcpyAsync(out, in, (size_t)c->N * nrhs * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    return MLF_OK;
+}
+
+// Iterative refinement: r = b - A64 x (FP64); one cycle of right-preconditioned
+// GMRES(m) with an all-FP32 inner loop (basis, Gram-Schmidt, preconditioner,
+// operator; Hessenberg and Givens on the host in double); d = V y in double;
+// x += M^-1 d with the FP64 preconditioner.
 int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
                        int* iters, double* relres, int precond, int* status, double inner_tol, int* outer) {
     const int N = c->N;
     const int m = std::max(4, std::min(c->gmres_m, 2000));
     const size_t V1 = (size_t)N * nrhs;
     cudaStream_t s = c->stream;
-    double2 *V = nullptr, *w = nullptr, *t = nullptr, *r = nullptr, *partial = nullptr, *dred = nullptr;
+    float2 *V = nullptr, *w32 = nullptr, *t32 = nullptr;
+    double2 *w = nullptr, *r = nullptr, *t64 = nullptr, *partial = nullptr, *dred = nullptr;
     double* dscale = nullptr;
-    CK(cudaMalloc(&V, (size_t)(m + 1) * V1 * sizeof(double2)));
+    CK(cudaMalloc(&V, (size_t)(m + 1) * V1 * sizeof(float2)));
+    CK(cudaMalloc(&w32, V1 * sizeof(float2)));
+    CK(cudaMalloc(&t32, V1 * sizeof(float2)));
     CK(cudaMalloc(&w, V1 * sizeof(double2)));
-    CK(cudaMalloc(&t, V1 * sizeof(double2)));
     CK(cudaMalloc(&r, V1 * sizeof(double2)));
-    CK(cudaMalloc(&partial, (size_t)(m + 1) * nrhs * GM_BLOCKS * sizeof(double2)));
+    CK(cudaMalloc(&t64, V1 * sizeof(double2)));
+    const int md_chunks = (N + 256 * MD_E - 1) / (256 * MD_E);
+    CK(cudaMalloc(&partial, (size_t)(m + 1) * nrhs * std::max(GM_BLOCKS, md_chunks) * sizeof(double2)));
     CK(cudaMalloc(&dred, (size_t)(m + 1) * nrhs * sizeof(double2)));
     CK(cudaMalloc(&dscale, nrhs * sizeof(double)));
     if (x0) CK(cudaMemcpyAsync(x, x0, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
@@ -563,15 +721,22 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
     if (int st = col_norms(c, nrhs, b, partial, dred, hbuf, bn, s)) return st;
     std::fill(iters, iters + nrhs, 0);
     std::vector<int> done(nrhs, 0);
-    // per column: Hessenberg (column-major (m+1) x m), Givens (cs, sn), rhs g
     std::vector<Cx> H((size_t)nrhs * (m + 1) * m), G((size_t)nrhs * (m + 1)), CS((size_t)nrhs * m), SN((size_t)nrhs * m);
     auto Hc = [&](int col, int i, int j) -> Cx& { return H[((size_t)col * m + j) * (m + 1) + i]; };
     int st = MLF_OK, k = 0;
     const int max_outer = 1000;
+    const bool prof = c->profiling != 0;
+    if (prof) {
+        for (int q = 0; q < 4; ++q) {
+            if (!c->sev[q]) CK(cudaEventCreate(&c->sev[q]));
+            c->solve_ms[q] = 0;
+        }
+    }
+    const auto t_start = std::chrono::steady_clock::now();
     for (; k < max_outer; ++k) {
         c->mv_prec = 0;
-        if ((st = device_matvec(c, x, t, nrhs, N, s))) break;
-        k_resid<<<4096, 256, 0, s>>>(V1, b, t, r);
+        if ((st = device_matvec(c, x, t64, nrhs, N, s))) break;
+        k_resid<<<4096, 256, 0, s>>>(V1, b, t64, r);
         if ((st = col_norms(c, nrhs, r, partial, dred, hbuf, beta, s))) break;
         bool all = true, budget = false;
         for (int col = 0; col < nrhs; ++col) {
@@ -584,41 +749,41 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
         if (all || !budget) break;
         for (int col = 0; col < nrhs; ++col) scl[col] = (!done[col] && beta[col] > 0) ? 1.0 / beta[col] : 0.0;
         CK(cudaMemcpyAsync(dscale, scl.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
-        k_colscale<<<gc, 256, 0, s>>>(N, r, dscale, V);
+        k_colscale_df<<<gc, 256, 0, s>>>(N, r, dscale, V);
         std::fill(H.begin(), H.end(), cx(0, 0));
         std::fill(G.begin(), G.end(), cx(0, 0));
         for (int col = 0; col < nrhs; ++col) G[(size_t)col * (m + 1)] = cx(done[col] ? 0.0 : beta[col], 0);
-        std::vector<int> jcol(nrhs, 0);   // Krylov dimension reached per column
-        std::vector<int> live(nrhs, 0);
+        std::vector<int> jcol(nrhs, 0), live(nrhs, 0);
         for (int col = 0; col < nrhs; ++col) live[col] = !done[col];
-        int j = 0;
         cudaGraphExec_t gexec = nullptr;
-        for (; j < m; ++j) {
+        for (int j = 0; j < m; ++j) {
             bool any = false;
             for (int col = 0; col < nrhs; ++col) any = any || live[col];
             if (!any) break;
-            const double2* vj = V + (size_t)j * V1;
-            if (precond == 2) { if ((st = device_nearinv_apply(c, vj, t, nrhs, s))) break; }
-            else if (precond == 1) {
-                for (int col = 0; col < nrhs && !st; ++col)
-                    st = device_ilu_solve(c, vj + (size_t)col * N, t + (size_t)col * N, s);
-                if (st) break;
-            } else CK(cudaMemcpyAsync(t, vj, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-            // w = A32 t: the first step of a cycle records the FP32 matvec's
-            // launches (fixed buffers t -> w) into a CUDA graph, later steps replay it
+            const float2* vj = V + (size_t)j * V1;
+            if (prof) cudaEventRecord(c->sev[0], s);
+            if (precond == 2) {
+                if ((st = device_nearinv_apply32(c, vj, t32, nrhs, s))) break;
+            } else if (precond == 1) {
+                k_f2d_m<<<4096, 256, 0, s>>>(V1, vj, w);
+                if ((st = apply_precond64(c, 1, nrhs, w, t64, s))) break;
+                k_d2f_m<<<4096, 256, 0, s>>>(V1, t64, t32);
+            } else {
+                CK(cudaMemcpyAsync(t32, vj, V1 * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+            }
+            if (prof) cudaEventRecord(c->sev[1], s);
+            // w32 = float(A32 t32): the first step of a cycle records these
+            // launches (fixed buffers) into a CUDA graph, later steps replay it
             if (!gexec) {
-                c->mv_prec = 1;
-                st = device_matvec(c, t, w, nrhs, N, s);   // allocates lazily, outside any capture
-                c->mv_prec = 0;
-                if (st) break;
+                if ((st = device_matvec32_from32(c, t32, w, nrhs, s))) break;   // allocates lazily, uncaptured
+                k_d2f_m<<<4096, 256, 0, s>>>(V1, w, w32);
                 cudaGraph_t graph = nullptr;
                 if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-                    c->mv_prec = 1;
                     const int prof = c->profiling;
                     c->profiling = 0;
-                    const int st2 = device_matvec(c, t, w, nrhs, N, s);
+                    const int st2 = device_matvec32_from32(c, t32, w, nrhs, s);
+                    k_d2f_m<<<4096, 256, 0, s>>>(V1, w, w32);
                     c->profiling = prof;
-                    c->mv_prec = 0;
                     if (cudaStreamEndCapture(s, &graph) == cudaSuccess && st2 == MLF_OK && graph) {
                         if (cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) gexec = nullptr;
                     }
@@ -628,25 +793,35 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
             } else {
                 CK(cudaGraphLaunch(gexec, s));
             }
+            if (prof) cudaEventRecord(c->sev[2], s);
             std::vector<double2> hsum((size_t)(j + 1) * nrhs, make_double2(0, 0));
             for (int pass = 0; pass < 2; ++pass) {
-                k_mdot<<<dim3(GM_BLOCKS, nrhs, j + 1), 256, 0, s>>>(N, nrhs, V, V1, w, partial);
-                k_reduce_partials<<<((j + 1) * nrhs + 127) / 128, 128, 0, s>>>((j + 1) * nrhs, partial, dred);
-                k_gs_update<<<gc, 256, 0, s>>>(N, nrhs, j + 1, V, V1, dred, w);
+                k_mdot32b<<<dim3(md_chunks, nrhs), 256, 0, s>>>(N, nrhs, j + 1, V, V1, w32, partial);
+                k_reduce_partials_n<<<((j + 1) * nrhs + 127) / 128, 128, 0, s>>>((j + 1) * nrhs, md_chunks, partial,
+                                                                                  dred);
+                k_gs_update32<<<gc, 256, 0, s>>>(N, nrhs, j + 1, V, V1, dred, w32);
                 CK(cudaMemcpyAsync(hbuf.data(), dred, (size_t)(j + 1) * nrhs * sizeof(double2), cudaMemcpyDeviceToHost, s));
                 CK(cudaStreamSynchronize(s));
                 for (size_t q = 0; q < (size_t)(j + 1) * nrhs; ++q) { hsum[q].x += hbuf[q].x; hsum[q].y += hbuf[q].y; }
             }
             std::vector<double> hn(nrhs);
-            if ((st = col_norms(c, nrhs, w, partial, dred, hbuf, hn, s))) break;
+            if ((st = col_norms32(c, nrhs, w32, partial, dred, hbuf, hn, s))) break;
             for (int col = 0; col < nrhs; ++col) scl[col] = (live[col] && hn[col] > 1e-300) ? 1.0 / hn[col] : 0.0;
             CK(cudaMemcpyAsync(dscale, scl.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
-            k_colscale<<<gc, 256, 0, s>>>(N, w, dscale, V + (size_t)(j + 1) * V1);
+            k_colscale32<<<gc, 256, 0, s>>>(N, w32, dscale, V + (size_t)(j + 1) * V1);
+            if (prof) {
+                cudaEventRecord(c->sev[3], s);
+                cudaEventSynchronize(c->sev[3]);
+                float a = 0, b2 = 0, d = 0;
+                cudaEventElapsedTime(&a, c->sev[0], c->sev[1]);
+                cudaEventElapsedTime(&b2, c->sev[1], c->sev[2]);
+                cudaEventElapsedTime(&d, c->sev[2], c->sev[3]);
+                c->solve_ms[0] += a; c->solve_ms[1] += b2; c->solve_ms[2] += d;
+            }
             for (int col = 0; col < nrhs; ++col) {
                 if (!live[col]) continue;
                 for (int i = 0; i <= j; ++i) Hc(col, i, j) = cx(hsum[(size_t)i * nrhs + col].x, hsum[(size_t)i * nrhs + col].y);
                 Hc(col, j + 1, j) = cx(hn[col], 0);
-                // apply previous rotations, then a new one that zeroes H(j+1, j)
                 for (int i = 0; i < j; ++i) {
                     const Cx a = Hc(col, i, j), bq = Hc(col, i + 1, j);
                     const Cx c_ = CS[(size_t)col * m + i], s_ = SN[(size_t)col * m + i];
@@ -672,7 +847,6 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
         }
         if (gexec) cudaGraphExecDestroy(gexec);
         if (st) break;
-        // y = H^-1 g per column, d = V y, x += M^-1 d
         std::vector<double2> y((size_t)(m + 1) * nrhs, make_double2(0, 0));
         int jmax = 0;
         for (int col = 0; col < nrhs; ++col) {
@@ -688,20 +862,21 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
         }
         if (jmax == 0) break;
         CK(cudaMemcpyAsync(dred, y.data(), (size_t)jmax * nrhs * sizeof(double2), cudaMemcpyHostToDevice, s));
-        k_combine<<<gc, 256, 0, s>>>(N, nrhs, jmax, V, V1, dred, w);
-        if (precond == 2) { if ((st = device_nearinv_apply(c, w, t, nrhs, s))) break; }
-        else if (precond == 1) {
-            for (int col = 0; col < nrhs && !st; ++col) st = device_ilu_solve(c, w + (size_t)col * N, t + (size_t)col * N, s);
-            if (st) break;
-        } else CK(cudaMemcpyAsync(t, w, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
-        k_axpy1<<<4096, 256, 0, s>>>(V1, t, x);
+        k_combine32<<<gc, 256, 0, s>>>(N, nrhs, jmax, V, V1, dred, w);
+        if ((st = apply_precond64(c, precond, nrhs, w, t64, s))) break;
+        k_axpy1<<<4096, 256, 0, s>>>(V1, t64, x);
         CK(cudaGetLastError());
     }
     c->mv_prec = 0;
     for (int col = 0; col < nrhs; ++col)
         if (!done[col]) status[col] = MLF_CGS_MAXIT;
     *outer = k;
-    cudaFree(V); cudaFree(w); cudaFree(t); cudaFree(r); cudaFree(partial); cudaFree(dred); cudaFree(dscale);
+    if (prof) {
+        cudaStreamSynchronize(s);
+        c->solve_ms[3] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    }
+    cudaFree(V); cudaFree(w32); cudaFree(t32); cudaFree(w); cudaFree(r); cudaFree(t64); cudaFree(partial);
+    cudaFree(dred); cudaFree(dscale);
     return st;
 }
 
@@ -709,7 +884,13 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
 
 using namespace mlf;
 
-extern "C" int mlf_set_gmres_restart(mlf_ctx* h, int m) {
+extern "C" int mlf_solve_times(mlf_ctx* h, double* out4) {
+    if (!h || !out4) return MLF_E_ARG;
+    for (int q = 0; q < 4; ++q) out4[q] = h->c.solve_ms[q];
+    return MLF_OK;
+}
+
+int mlf_set_gmres_restart(mlf_ctx* h, int m) {
     if (!h || m < 4 || m > 2000) return MLF_E_ARG;
     h->c.gmres_m = m;
     return MLF_OK;

@@ -1,0 +1,223 @@
+// Near field of the FP32 operator for blocks of right-hand sides.
+//
+// The near matrix (llenarZesparcida, modMLFMA.f90:1594-1634) couples every
+// basis of a leaf box with every basis of each near leaf box, so its CSR rows
+// are unions of whole boxes.  For nrhs > 1 it is applied here as dense
+// box-pair blocks: Y_i += Z_ij X_j for each leaf box i and near box j, a
+// complex GEMM per pair with X_j (n_j x nrhs) staged in shared memory and each
+// Z value read once per tile of right-hand sides.  The CSR form stays the one
+// the single-column kernels, ILU and the preconditioners use; the blocks are a
+// second copy of the same complex(4) values, built once on first use.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "mlf_internal.h"
+
+namespace mlf {
+
+#define CK(call)                                             \
+    do {                                                     \
+        if (!cuda_ok(c, (call), #call)) return MLF_E_CUDA;   \
+    } while (0)
+
+constexpr int NBK_ROWS = 64;   // rows of box i per CTA
+constexpr int NBK_KC = 32;     // source bases per shared-memory chunk
+
+// Zblk[blk_off[e] + t * n_i + p] = Z(perm[box_ptr[i] + p], perm[box_ptr[j] + t])
+// for entry e = (i, j); one CTA per entry, the value found by binary search in
+// the (column-sorted) CSR row.
+__global__ void k_blk_fill(const int* __restrict__ entry_box, const int* __restrict__ nbox_list,
+                           const long long* __restrict__ blk_off, const int* __restrict__ box_ptr,
+                           const int* __restrict__ perm, const int* __restrict__ ia, const int* __restrict__ ja,
+                           const float2* __restrict__ Z, float2* __restrict__ Zblk) {
+    const int e = blockIdx.x;
+    const int i = entry_box[e], j = nbox_list[e];
+    const int i0 = box_ptr[i], ni = box_ptr[i + 1] - i0;
+    const int j0 = box_ptr[j], nj = box_ptr[j + 1] - j0;
+    float2* out = Zblk + blk_off[e];
+    for (int q = threadIdx.x; q < ni * nj; q += blockDim.x) {
+        const int t = q / ni, p = q - t * ni;
+        const int m = perm[i0 + p], col = perm[j0 + t];
+        int lo = ia[m], hi = ia[m + 1] - 1;
+        float2 v = make_float2(0.f, 0.f);
+        while (lo <= hi) {
+            const int mid = (lo + hi) >> 1;
+            const int jm = ja[mid];
+            if (jm == col) { v = Z[mid]; break; }
+            if (jm < col) lo = mid + 1; else hi = mid - 1;
+        }
+        out[q] = v;
+    }
+}
+
+// xs[pos * nrhs + r] = x(:, r)[perm[pos]]: box-sorted, row-major copy of the
+// input block (FP32 columns or FP64 columns with leading dimension ld)
+__global__ void k_blk_pack32(int N, int nrhs, const int* __restrict__ perm, const float2* __restrict__ x32,
+                             float2* __restrict__ xs) {
+    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= (size_t)N * nrhs) return;
+    const int pos = (int)(e / nrhs), r = (int)(e % nrhs);
+    xs[e] = x32[(size_t)r * N + perm[pos]];
+}
+
+__global__ void k_blk_pack64(int N, int nrhs, int ld, const int* __restrict__ perm, const double2* __restrict__ x,
+                             float2* __restrict__ xs) {
+    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= (size_t)N * nrhs) return;
+    const int pos = (int)(e / nrhs), r = (int)(e % nrhs);
+    const double2 v = x[(size_t)r * ld + perm[pos]];
+    xs[e] = make_float2((float)v.x, (float)v.y);
+}
+
+// y(:, c0 : c0 + 8 TC) += Z_near x for one 64-row tile of one leaf box.
+// 256 threads: thread (ty = tid / 8, tx = tid % 8) owns rows r0 + 2 ty, +1 and
+// columns c0 + TC tx .. + TC - 1 (2 x TC complex accumulators).
+template <int TC>
+__global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2* __restrict__ tiles,
+                                                    const int* __restrict__ box_ptr, const int* __restrict__ nbox_ptr,
+                                                    const int* __restrict__ nbox_list,
+                                                    const long long* __restrict__ blk_off,
+                                                    const float2* __restrict__ Zblk, const float2* __restrict__ xs,
+                                                    const int* __restrict__ perm, double2* __restrict__ y) {
+    constexpr int NC = 8 * TC;
+    __shared__ __align__(16) float2 Zs[NBK_KC][NBK_ROWS];
+    __shared__ __align__(16) float2 Xs[NBK_KC][NC];
+    const int2 tl = tiles[blockIdx.x];
+    const int i = tl.x, r0 = tl.y;
+    const int c0 = blockIdx.y * NC;
+    const int ni = box_ptr[i + 1] - box_ptr[i];
+    const int tid = threadIdx.x, ty = tid >> 3, tx = tid & 7;
+    float2 acc[2][TC];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int u = 0; u < TC; ++u) acc[a][u] = make_float2(0.f, 0.f);
+    for (int e = nbox_ptr[i]; e < nbox_ptr[i + 1]; ++e) {
+        const int j = nbox_list[e];
+        const int j0 = box_ptr[j], nj = box_ptr[j + 1] - j0;
+        const float2* zb = Zblk + blk_off[e];
+        for (int t0 = 0; t0 < nj; t0 += NBK_KC) {
+            for (int q = tid; q < NBK_KC * NBK_ROWS; q += 256) {
+                const int k = q / NBK_ROWS, p = q - k * NBK_ROWS;
+                const int t = t0 + k, row = r0 + p;
+                Zs[k][p] = (t < nj && row < ni) ? zb[(size_t)t * ni + row] : make_float2(0.f, 0.f);
+            }
+            for (int q = tid; q < NBK_KC * NC; q += 256) {
+                const int k = q / NC, cc = q - k * NC;
+                const int t = t0 + k, col = c0 + cc;
+                Xs[k][cc] = (t < nj && col < nrhs) ? xs[(size_t)(j0 + t) * nrhs + col] : make_float2(0.f, 0.f);
+            }
+            __syncthreads();
+#pragma unroll 8
+            for (int k = 0; k < NBK_KC; ++k) {
+                const float4 zz = *reinterpret_cast<const float4*>(&Zs[k][2 * ty]);
+#pragma unroll
+                for (int u = 0; u < TC; ++u) {
+                    const float2 xv = Xs[k][tx * TC + u];
+                    acc[0][u].x = fmaf(zz.x, xv.x, acc[0][u].x);
+                    acc[0][u].x = fmaf(-zz.y, xv.y, acc[0][u].x);
+                    acc[0][u].y = fmaf(zz.x, xv.y, acc[0][u].y);
+                    acc[0][u].y = fmaf(zz.y, xv.x, acc[0][u].y);
+                    acc[1][u].x = fmaf(zz.z, xv.x, acc[1][u].x);
+                    acc[1][u].x = fmaf(-zz.w, xv.y, acc[1][u].x);
+                    acc[1][u].y = fmaf(zz.z, xv.y, acc[1][u].y);
+                    acc[1][u].y = fmaf(zz.w, xv.x, acc[1][u].y);
+                }
+            }
+            __syncthreads();
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        const int row = r0 + 2 * ty + a;
+        if (row >= ni) continue;
+        const int n = perm[box_ptr[i] + row];
+#pragma unroll
+        for (int u = 0; u < TC; ++u) {
+            const int col = c0 + tx * TC + u;
+            if (col < nrhs) {
+                double2* yp = y + (size_t)col * ld + n;
+                const double2 v = *yp;
+                *yp = make_double2(v.x + (double)acc[a][u].x, v.y + (double)acc[a][u].y);
+            }
+        }
+    }
+}
+
+static int near_blocks_setup(Ctx* c) {
+    if (c->blk_ok) return MLF_OK;
+    const int nb = (int)c->box_ptr.size() - 1;
+    if ((int)c->nbox_ptr.size() != nb + 1) {
+        c->err = "near box lists missing";
+        return MLF_E_STATE;
+    }
+    const int ne = c->nbox_ptr[nb];
+    std::vector<long long> off(ne + 1, 0);
+    std::vector<int> entry_box(ne);
+    std::vector<int2> tiles;
+    for (int i = 0; i < nb; ++i) {
+        const int ni = c->box_ptr[i + 1] - c->box_ptr[i];
+        for (int e = c->nbox_ptr[i]; e < c->nbox_ptr[i + 1]; ++e) {
+            const int j = c->nbox_list[e];
+            entry_box[e] = i;
+            off[e + 1] = off[e] + (long long)ni * (c->box_ptr[j + 1] - c->box_ptr[j]);
+        }
+        for (int r0 = 0; r0 < ni; r0 += NBK_ROWS) tiles.push_back(make_int2(i, r0));
+    }
+    if (off[ne] != c->nnz) {
+        c->err = "near blocks do not cover the near CSR";
+        return MLF_E_STATE;
+    }
+    int* dentry = nullptr;
+    CK(cudaMalloc(&c->dZblk, std::max<long long>(c->nnz, 1) * sizeof(float2)));
+    CK(cudaMalloc(&c->dblk_off, (ne + 1) * sizeof(long long)));
+    CK(cudaMalloc(&c->dnbox_ptr, (nb + 1) * sizeof(int)));
+    CK(cudaMalloc(&c->dnbox_list, std::max(ne, 1) * sizeof(int)));
+    CK(cudaMalloc(&c->dblk_tiles, std::max<size_t>(tiles.size(), 1) * sizeof(int2)));
+    CK(cudaMalloc(&dentry, std::max(ne, 1) * sizeof(int)));
+    CK(cudaMemcpy(c->dblk_off, off.data(), (ne + 1) * sizeof(long long), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->dnbox_ptr, c->nbox_ptr.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->dnbox_list, c->nbox_list.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->dblk_tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dentry, entry_box.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
+    if (ne) k_blk_fill<<<ne, 256, 0, c->stream>>>(dentry, c->dnbox_list, c->dblk_off, c->dbox_ptr, c->dperm, c->dia,
+                                                  c->dja, c->dZ, c->dZblk);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(dentry);
+    c->nblk_tiles = (int)tiles.size();
+    c->blk_ok = 1;
+    return MLF_OK;
+}
+
+// y(:, 0:nrhs) += Z_near x with x given as FP32 columns (x32, ld N) or FP64
+// columns (x, ld); xs is an N x nrhs FP32 scratch.
+int device_near_blocks32(Ctx* c, const double2* x, const float2* x32, int ld, int nrhs, float2* xs, double2* y,
+                         cudaStream_t s) {
+    int st;
+    if ((st = near_blocks_setup(c))) return st;
+    const size_t ne = (size_t)c->N * nrhs;
+    if (x32) k_blk_pack32<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(c->N, nrhs, c->dperm, x32, xs);
+    else k_blk_pack64<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(c->N, nrhs, ld, c->dperm, x, xs);
+    const bool narrow = c->blk_cols ? c->blk_cols == 8 : nrhs <= 8;
+    if (narrow) {
+        k32_near_blk<1><<<dim3(c->nblk_tiles, (nrhs + 7) / 8), 256, 0, s>>>(
+            nrhs, ld, c->dblk_tiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, c->dblk_off, c->dZblk, xs, c->dperm, y);
+    } else {
+        k32_near_blk<4><<<dim3(c->nblk_tiles, (nrhs + 31) / 32), 256, 0, s>>>(
+            nrhs, ld, c->dblk_tiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, c->dblk_off, c->dZblk, xs, c->dperm, y);
+    }
+    return cuda_ok(c, cudaGetLastError(), "near blocks") ? MLF_OK : MLF_E_CUDA;
+}
+
+void near_blocks_free(Ctx* c) {
+    auto F = [](void* p) { if (p) cudaFree(p); };
+    F(c->dZblk); F(c->dblk_off); F(c->dnbox_ptr); F(c->dnbox_list); F(c->dblk_tiles);
+    c->dZblk = nullptr; c->dblk_off = nullptr; c->dnbox_ptr = nullptr; c->dnbox_list = nullptr;
+    c->dblk_tiles = nullptr;
+    c->blk_ok = 0;
+}
+
+}  // namespace mlf

@@ -222,6 +222,74 @@ __global__ void k_spmv_z(int N, int nrhs, const int* __restrict__ ia, const int*
     if (lane == 0) y[(size_t)col * N + m] = make_double2(sr, si);
 }
 
+// FP32 copies of the same operator, for the FP32 inner solves of mlf_solve mode 1
+__global__ void k32_blockdiag_apply(int N, int nrhs, const int* __restrict__ box_ptr,
+                                    const int* __restrict__ box_of_sorted, const int* __restrict__ perm,
+                                    const long long* __restrict__ boff, const float2* __restrict__ M,
+                                    const float2* __restrict__ x, float2* __restrict__ y) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (gw >= N * nrhs) return;
+    const int p = gw % N, col = gw / N;
+    const int b = box_of_sorted[p], j0 = box_ptr[b], n = box_ptr[b + 1] - j0, i = p - j0;
+    const float2* row = M + boff[b] + (size_t)i * n;
+    const float2* xc = x + (size_t)col * N;
+    float sr = 0.f, si = 0.f;
+    for (int j = lane; j < n; j += 32) {
+        const float2 a = row[j], v = xc[perm[j0 + j]];
+        sr = fmaf(a.x, v.x, sr); sr = fmaf(-a.y, v.y, sr);
+        si = fmaf(a.x, v.y, si); si = fmaf(a.y, v.x, si);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffff, sr, o);
+        si += __shfl_xor_sync(0xffffffff, si, o);
+    }
+    if (lane == 0) y[(size_t)col * N + perm[p]] = make_float2(sr, si);
+}
+
+__global__ void k32_spmv_z(int N, int nrhs, const int* __restrict__ ia, const int* __restrict__ ja,
+                           const float2* __restrict__ M, const float2* __restrict__ x, float2* __restrict__ y) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (gw >= N * nrhs) return;
+    const int m = gw % N, col = gw / N;
+    const float2* xc = x + (size_t)col * N;
+    float sr = 0.f, si = 0.f;
+    for (int q = ia[m] + lane; q < ia[m + 1]; q += 32) {
+        const float2 a = M[q], v = xc[ja[q]];
+        sr = fmaf(a.x, v.x, sr); sr = fmaf(-a.y, v.y, sr);
+        si = fmaf(a.x, v.y, si); si = fmaf(a.y, v.x, si);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffff, sr, o);
+        si += __shfl_xor_sync(0xffffffff, si, o);
+    }
+    if (lane == 0) y[(size_t)col * N + m] = make_float2(sr, si);
+}
+
+__global__ void k_d2f(size_t n, const double2* __restrict__ a, float2* __restrict__ b) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStream_t s) {
+    if (!c->nearinv_ok) {
+        c->err = "neighbourhood-inverse preconditioner not built";
+        return MLF_E_STATE;
+    }
+    if (!c->dMinv32) {
+        CK(cudaMalloc(&c->dMinv32, std::max<long long>(c->minv_len, 1) * sizeof(float2)));
+        k_d2f<<<4096, 256, 0, s>>>((size_t)c->minv_len, c->dMinv, c->dMinv32);
+    }
+    const long long warps = (long long)c->N * nrhs;
+    if (c->nearinv_own)
+        k32_blockdiag_apply<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+            c->N, nrhs, c->dbox_ptr, c->dbox_of_sorted, c->dperm, c->dboff, c->dMinv32, y, x);
+    else
+        k32_spmv_z<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(c->N, nrhs, c->dia, c->dja, c->dMinv32, y, x);
+    return cuda_ok(c, cudaGetLastError(), "nearinv apply32") ? MLF_OK : MLF_E_CUDA;
+}
+
 int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     const int nl = c->nlev;
     const Level& leaf = c->lv[nl];
@@ -236,8 +304,10 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     batch = std::min(batch, 4096);
     if (c->dMinv) cudaFree(c->dMinv);
     if (c->dboff) cudaFree(c->dboff);
+    if (c->dMinv32) cudaFree(c->dMinv32);
     c->dMinv = nullptr;
     c->dboff = nullptr;
+    c->dMinv32 = nullptr;
     c->nearinv_ok = 0;
     c->nearinv_own = own_only;
     long long total = c->nnz;
@@ -251,6 +321,7 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
         CK(cudaMalloc(&c->dboff, boff.size() * sizeof(long long)));
         CK(cudaMemcpy(c->dboff, boff.data(), boff.size() * sizeof(long long), cudaMemcpyHostToDevice));
     }
+    c->minv_len = total;
     CK(cudaMalloc(&c->dMinv, std::max<long long>(total, 1) * sizeof(double2)));
     double2* work = nullptr;
     int* dbad = nullptr;

@@ -527,6 +527,8 @@ int build_octree(Ctx* c) {
     }
     c->near_ptr.assign(1, 0);
     c->near_bases.clear();
+    c->nbox_ptr.assign(1, 0);
+    c->nbox_list.clear();
     for (int n = 3; n <= nl; ++n) {
         Level& L = c->lv[n];
         const Level& Lp = c->lv[n - 1];
@@ -582,6 +584,7 @@ int build_octree(Ctx* c) {
                     L.far_src.push_back(j);
                     L.far_tid.push_back(tid);
                 } else if (n == nl) {
+                    c->nbox_list.push_back(j);
                     c->near_bases.insert(c->near_bases.end(), c->box_bases.begin() + c->box_ptr[j],
                                          c->box_bases.begin() + c->box_ptr[j + 1]);
                 }
@@ -590,6 +593,7 @@ int build_octree(Ctx* c) {
             if (n == nl) {
                 std::sort(c->near_bases.begin() + near_start, c->near_bases.end());
                 c->near_ptr.push_back((int)c->near_bases.size());
+                c->nbox_ptr.push_back((int)c->nbox_list.size());
             }
         }
         L.ntrans = (int)(L.rab.size() / 3);

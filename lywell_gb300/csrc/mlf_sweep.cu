@@ -6,6 +6,8 @@
 //   operator warm-started from the previous angle's currents times
 //   exp(-j k (d_a - d_{a-1}) . r_edge) (main.f90:1017-1022), backscatter
 //   sigma(pi/2, phi_a).  The first guess is zero with d_0 = (-1, 0, 0).
+// Blocks hold `block` angles; block <= 0 lets the autotuner choose it
+// (mlf_autotune_block) among 8..128.
 // mode 1 — batched: blocks of `block` angles solved together as one
 //   multi-right-hand-side CGS on the FP64 operator (zero guesses, columns
 //   retire independently).
@@ -105,7 +107,17 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
         cudaFree(g);
         return st;
     }
-    const int bs = std::max(1, std::min(block, nang));
+    int bsel = block;
+    if (bsel <= 0) {
+        // autotuned block: candidates up to the sweep length
+        std::vector<int> cand;
+        for (int b : {8, 16, 32, 64, 128})
+            if (b <= nang) cand.push_back(b);
+        if (cand.empty()) cand.push_back(nang);
+        int cols = 0;
+        if ((st = autotune_block(c, cand.data(), (int)cand.size(), &bsel, &cols, nullptr))) return st;
+    }
+    const int bs = std::max(1, std::min(bsel, nang));
     double2 *b = nullptr, *x = nullptr;
     CK(cudaMalloc(&b, (size_t)N * bs * sizeof(double2)));
     CK(cudaMalloc(&x, (size_t)N * bs * sizeof(double2)));

@@ -292,6 +292,24 @@ class MLFMA:
                         outer=outer.value)
         return dict(x=X, iters=it, relres=rr, status=[CGS_STATUS[int(s)] for s in st], outer=outer.value)
 
+    def autotune_block(self, candidates=(8, 16, 32, 64, 128)):
+        """mlf_autotune_block: block size and near-field tile width for batched
+        solves, with the measured FP32 operator time per right-hand side."""
+        cand = np.ascontiguousarray(candidates, dtype=np.int32)
+        per = np.zeros(cand.size, dtype=np.float32)
+        best, cols = C.c_int(), C.c_int()
+        _check(load().mlf_autotune_block(self._h, _p(cand), cand.size, C.byref(best), C.byref(cols), _p(per)),
+               self._h)
+        return dict(block=best.value, tile_cols=cols.value,
+                    per_rhs_ms={int(b): float(t) for b, t in zip(cand, per)})
+
+    def solve_times(self):
+        """Phase times (ms) of the last mixed solve run with profiling on:
+        preconditioner, FP32 operator, orthogonalisation, total."""
+        out = np.zeros(4)
+        _check(load().mlf_solve_times(self._h, _p(out)), self._h)
+        return dict(zip(("precond", "operator", "orthogonalisation", "total"), out.tolist()))
+
     def set_gmres_restart(self, m: int):
         _check(load().mlf_set_gmres_restart(self._h, int(m)), self._h)
 

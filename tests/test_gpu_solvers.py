@@ -113,14 +113,15 @@ def test_mixed_multi_rhs(ico4):
         assert r < 1e-4
 
 
-def test_fp32_multi_rhs_columns(ico4):
-    """The batched FP32 operator (near field in tiles of right-hand sides)
-    against one column at a time."""
+@pytest.mark.parametrize("nrhs", [5, 20, 40])
+def test_fp32_multi_rhs_columns(ico4, nrhs):
+    """The batched FP32 operator (near field as dense box-pair blocks, 8- and
+    32-column tiles, ragged last tile) against one column at a time."""
     _, m, _ = ico4
-    rng = np.random.default_rng(11)
-    X = rng.standard_normal((m.N, 20)) + 1j * rng.standard_normal((m.N, 20))
+    rng = np.random.default_rng(11 + nrhs)
+    X = rng.standard_normal((m.N, nrhs)) + 1j * rng.standard_normal((m.N, nrhs))
     Y = m.matvec32(X)
-    for k in (0, 7, 19):
+    for k in sorted({0, nrhs // 2, nrhs - 1}):
         assert _rel(Y[:, k], m.matvec32(X[:, k])) < 1e-6
         assert _rel(Y[:, k], m.matvec(X[:, k])) < 2e-5
 
