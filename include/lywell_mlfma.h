@@ -273,6 +273,26 @@ int mlf_stage_times(mlf_ctx* ctx, float* out5);
  * which: 0 = C, 1 = B, 2 = A.  For parity checks of single stages. */
 int mlf_debug_field(mlf_ctx* ctx, int level, int which, double* out);
 
+/* ---- Learned near-field preconditioner: the network ------------------------
+ * A 16 -> 128 -> 128 -> 2 MLP (ReLU) with hand-written CUDA forward, backward
+ * and Adam kernels: BF16 parameters and activations, FP32 accumulation, FP32
+ * master weights.  Parameter vector (mlf_mlp_nparam() floats):
+ * W1[16][128] b1[128] W2[128][128] b2[128] W3[128][2] b3[2]; norm = mu[16],
+ * sd[16] (inputs enter as (x - mu) / sd).  Loss: mean squared error over
+ * tokens and outputs.  X, T, Y are device arrays (row-major [ntok][16],
+ * [ntok][2]).  No counterpart in the reference. */
+typedef struct mlf_mlp mlf_mlp;
+int mlf_mlp_create(mlf_mlp** net, int device, unsigned long long seed);
+void mlf_mlp_free(mlf_mlp* net);
+const char* mlf_mlp_last_error(mlf_mlp* net);
+int mlf_mlp_nparam(void);
+int mlf_mlp_set_params(mlf_mlp* net, const float* params, const float* norm);
+int mlf_mlp_get_params(mlf_mlp* net, float* params, float* norm);
+int mlf_mlp_forward(mlf_mlp* net, const float* X, long long ntok, float* Y, void* stream);
+int mlf_mlp_grad(mlf_mlp* net, const float* X, const float* T, long long ntok, float* grad, double* loss);
+int mlf_mlp_train(mlf_mlp* net, const float* X, const float* T, long long ntok, int steps, int batch, float lr,
+                  unsigned long long seed, float* loss_hist);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,15 @@ SIGNATURES = {
     "mlf_set_gmres_restart": (C.c_int, [vp, C.c_int]),
     "mlf_solve_times": (C.c_int, [vp, vp]),
     "mlf_autotune_block": (C.c_int, [vp, vp, C.c_int, vp, vp, vp]),
+    "mlf_mlp_create": (C.c_int, [vp, C.c_int, C.c_ulonglong]),
+    "mlf_mlp_free": (None, [vp]),
+    "mlf_mlp_last_error": (C.c_char_p, [vp]),
+    "mlf_mlp_nparam": (C.c_int, []),
+    "mlf_mlp_set_params": (C.c_int, [vp, vp, vp]),
+    "mlf_mlp_get_params": (C.c_int, [vp, vp, vp]),
+    "mlf_mlp_forward": (C.c_int, [vp, vp, C.c_longlong, vp, vp]),
+    "mlf_mlp_grad": (C.c_int, [vp, vp, vp, C.c_longlong, vp, vp]),
+    "mlf_mlp_train": (C.c_int, [vp, vp, vp, C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_ulonglong, vp]),
     "mlf_matvec32_device": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, vp]),
     "mlf_nearinv_values": (C.c_int, [vp, vp]),
     "mlf_cgs_history": (C.c_int, [vp, C.c_int, vp, C.c_int, ip]),
