@@ -57,8 +57,18 @@ enum {
 
 /* mlf_init flags */
 enum {
-    MLF_FLAG_LEGENDRE_RECURRENCE = 1 /* P_l by the three-term recurrence instead of the
-                                        reference's explicit binomial sum */
+    MLF_FLAG_LEGENDRE_RECURRENCE = 1, /* P_l by the three-term recurrence instead of the
+                                         reference's explicit binomial sum */
+    MLF_FLAG_DENSE_MOM = 2            /* dense MoM operator (MoM + MatxVec_MoM, modMoM.f90:85-128,
+                                         273-277): the N x N matrix in FP64 on the device, no
+                                         octree (ladomax ignored); matvec, CGS without
+                                         preconditioner, excitation, RCS and the FP64 monostatic
+                                         modes work, octree-based calls return MLF_E_STATE */,
+    MLF_FLAG_FMM = 4                  /* single-level FMM (inicializar_FMM + MatxVec_FMM,
+                                         modFMM.f90:170-268, 904-963) instead of MLFMA: one grid
+                                         level of boxes of side <= ladomax * lambda (the
+                                         reference uses ladomax = 0.5), far pairs translated
+                                         directly, near field and preconditioners as MLFMA's */
 };
 
 /* Build the RWG basis from a triangle soup, reproducing the reference's
@@ -223,6 +233,12 @@ int mlf_nearinv_values(mlf_ctx* ctx, double* vals);
  * MLF_PRECOND_ILU0 (lusol0C) or MLF_PRECOND_NEARINV. */
 int mlf_precond_apply(mlf_ctx* ctx, int precond_kind, const double* y, double* x, int nrhs);
 
+/* x = M32 y: the FP32 copy of the neighbourhood / own-box (or learned)
+ * preconditioner that mode 1 of mlf_solve applies in its inner loop; for
+ * nrhs > 1 the own-box blocks run as per-box GEMMs.  Complex(8) in and out.
+ * No counterpart in the reference. */
+int mlf_precond_apply32(mlf_ctx* ctx, const double* y, double* x, int nrhs);
+
 /* Residual history ||r_i||/||b|| of column col of the last mlf_cgs call
  * (the per-iteration line CGSold prints, modIterativo.f90:446-465).
  * *n = number of iterations recorded; up to cap values are copied. */
@@ -292,6 +308,25 @@ int mlf_mlp_forward(mlf_mlp* net, const float* X, long long ntok, float* Y, void
 int mlf_mlp_grad(mlf_mlp* net, const float* X, const float* T, long long ntok, float* grad, double* loss);
 int mlf_mlp_train(mlf_mlp* net, const float* X, const float* T, long long ntok, int steps, int batch, float lr,
                   unsigned long long seed, float* loss_hist);
+
+/* ---- Learned near-field preconditioner: tokens and installation -----------
+ * A token is one entry (p, q) of a leaf box's own near-field block, in
+ * box-major, row-major block order.  With s_p = 1 / sqrt(Z_pp) and
+ * Zh = S Z S, its 16 features are: Re, Im, |.| of Zh_pq, [p == q], the edge
+ * centre offset r_q - r_p (3) and its length in wavelengths, l_p, l_q in
+ * wavelengths, n_b / 100, the mean |Zh| of row p and of column q, the phase
+ * (Re, Im) of Z_pp, 1.  Targets (2) are Re, Im of M_pq / (s_p s_q) for an
+ * exact preconditioner M: target 1 = the own-box inverse (after
+ * mlf_nearinv_own), 2 = the rows of the neighbourhood inverse restricted to
+ * the box's own columns (after mlf_nearinv); target 0 = features only.
+ * X (16 floats per token), T (2 per token): device arrays of capacity cap
+ * tokens; X = NULL returns the token count only.
+ * mlf_lp_install replaces the context's preconditioner by the network's
+ * prediction, M_pq = s_p net(features)_pq s_q, applied like the own-box
+ * inverse (precond_kind MLF_PRECOND_NEARINV); *nonfinite counts outputs
+ * that were not finite (set to zero).  No counterpart in the reference. */
+int mlf_lp_tokens(mlf_ctx* ctx, int target, float* X, float* T, long long cap, long long* ntok);
+int mlf_lp_install(mlf_ctx* ctx, mlf_mlp* net, int* nonfinite);
 
 #ifdef __cplusplus
 }

@@ -38,6 +38,7 @@ SIGNATURES = {
     "mlf_matvec32": (C.c_int, [vp, vp, vp, C.c_int, C.c_int]),
     "mlf_set_gmres_restart": (C.c_int, [vp, C.c_int]),
     "mlf_solve_times": (C.c_int, [vp, vp]),
+    "mlf_precond_apply32": (C.c_int, [vp, vp, vp, C.c_int]),
     "mlf_autotune_block": (C.c_int, [vp, vp, C.c_int, vp, vp, vp]),
     "mlf_mlp_create": (C.c_int, [vp, C.c_int, C.c_ulonglong]),
     "mlf_mlp_free": (None, [vp]),
@@ -47,6 +48,8 @@ SIGNATURES = {
     "mlf_mlp_get_params": (C.c_int, [vp, vp, vp]),
     "mlf_mlp_forward": (C.c_int, [vp, vp, C.c_longlong, vp, vp]),
     "mlf_mlp_grad": (C.c_int, [vp, vp, vp, C.c_longlong, vp, vp]),
+    "mlf_lp_tokens": (C.c_int, [vp, C.c_int, vp, vp, C.c_longlong, vp]),
+    "mlf_lp_install": (C.c_int, [vp, vp, vp]),
     "mlf_mlp_train": (C.c_int, [vp, vp, vp, C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_ulonglong, vp]),
     "mlf_matvec32_device": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, vp]),
     "mlf_nearinv_values": (C.c_int, [vp, vp]),
@@ -65,6 +68,8 @@ STATUS = {0: "MLF_OK", -1: "MLF_E_ARG", -2: "MLF_E_TOO_SMALL", -3: "MLF_E_CUDA",
           -5: "MLF_E_TABLE", -6: "MLF_E_STATE", -7: "MLF_E_NOT_FINITE", -8: "MLF_E_NO_DEVICE"}
 CGS_STATUS = {0: "converged", 1: "maxit", 2: "breakdown", 3: "not_finite", 4: "stagnated"}
 FLAG_LEGENDRE_RECURRENCE = 1
+FLAG_DENSE_MOM = 2
+FLAG_FMM = 4
 PRECOND = {"none": 0, "ilu0": 1, "nearinv": 2}
 
 _lib = None

@@ -100,9 +100,15 @@ int mlf_init(mlf_ctx** out, const double* e_centro, int N, const int* e_t, const
             return MLF_E_ARG;
         }
     }
-    int st = build_octree(c);
-    if (st == MLF_OK) st = configure_kernels(c);
-    if (st == MLF_OK) st = device_setup(c);
+    int st;
+    if (flags & MLF_FLAG_DENSE_MOM) {
+        c->dense = 1;
+        st = dense_setup(c);
+    } else {
+        st = (flags & MLF_FLAG_FMM) ? build_fmm(c) : build_octree(c);
+        if (st == MLF_OK) st = configure_kernels(c);
+        if (st == MLF_OK) st = device_setup(c);
+    }
     if (st != MLF_OK) {
         g_init_error = c->err;
         device_free(c);
@@ -147,6 +153,7 @@ int mlf_matvec_device(mlf_ctx* h, const void* x, void* y, int nrhs, int ld, void
 int mlf_near_csr(mlf_ctx* h, long long* nnz, float* a, int* ja, int* ia) {
     if (!h || !nnz) return MLF_E_ARG;
     Ctx* c = &h->c;
+    if (need_tree(c)) return MLF_E_STATE;
     *nnz = c->nnz;
     if (!a && !ja && !ia) return MLF_OK;
     if (!bind_device(c)) return MLF_E_CUDA;
@@ -161,6 +168,7 @@ int mlf_near_csr(mlf_ctx* h, long long* nnz, float* a, int* ja, int* ia) {
 int mlf_ilu0(mlf_ctx* h, int* ierr_row) {
     if (!h || !ierr_row) return MLF_E_ARG;
     Ctx* c = &h->c;
+    if (need_tree(c)) return MLF_E_STATE;
     if (!bind_device(c)) return MLF_E_CUDA;
     c->ilu_ok = 0;
     const int ierr = ilu0_factor(c);
@@ -177,6 +185,7 @@ int mlf_ilu0(mlf_ctx* h, int* ierr_row) {
 int mlf_ilut(mlf_ctx* h, double fill_in_prc, double droptol, int* ierr_out) {
     if (!h || !ierr_out || fill_in_prc < 0 || droptol < 0) return MLF_E_ARG;
     Ctx* c = &h->c;
+    if (need_tree(c)) return MLF_E_STATE;
     if (!bind_device(c)) return MLF_E_CUDA;
     c->ilu_ok = 0;
     // crear_precond (main.f90:904-906): lfil = ceiling(0.01 * fill_in_prc * N)
@@ -203,6 +212,7 @@ int mlf_ilu_size(mlf_ctx* h, long long* len) {
 int mlf_ilu0_factors(mlf_ctx* h, float* alu, int* jlu, int* ju) {
     if (!h || !alu || !jlu || !ju) return MLF_E_ARG;
     Ctx* c = &h->c;
+    if (need_tree(c)) return MLF_E_STATE;
     if (!c->ilu_ok) { c->err = "ILU0 factors not available"; return MLF_E_STATE; }
     // MSR arrays are 1-based: element k of the Fortran array is index k here
     const long long n1 = (long long)c->jlu[c->N + 1] - 1;
@@ -215,6 +225,7 @@ int mlf_ilu0_factors(mlf_ctx* h, float* alu, int* jlu, int* ju) {
 int mlf_ilu0_solve(mlf_ctx* h, const double* y, double* x, int nrhs) {
     if (!h || !y || !x || nrhs <= 0) return MLF_E_ARG;
     Ctx* c = &h->c;
+    if (need_tree(c)) return MLF_E_STATE;
     if (!bind_device(c)) return MLF_E_CUDA;
     const size_t n = (size_t)c->N * nrhs;
     int st;
@@ -341,6 +352,41 @@ int mlf_precond_apply(mlf_ctx* h, int precond_kind, const double* y, double* x, 
     return MLF_OK;
 }
 
+namespace {
+__global__ void k_cast_df(size_t n, const double2* __restrict__ a, float2* __restrict__ b) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+__global__ void k_cast_fd(size_t n, const float2* __restrict__ a, double2* __restrict__ b) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = make_double2(a[i].x, a[i].y);
+}
+}  // namespace
+
+int mlf_precond_apply32(mlf_ctx* h, const double* y, double* x, int nrhs) {
+    if (!h || !y || !x || nrhs <= 0) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    if (!bind_device(c)) return MLF_E_CUDA;
+    const size_t n = (size_t)c->N * nrhs;
+    int st;
+    if ((st = ensure_io(c, n))) return st;
+    if ((st = h2d_cols(c, c->dx_io, y, nrhs, c->N))) return st;
+    float2 *a = nullptr, *b = nullptr;
+    CK(cudaMalloc(&a, n * sizeof(float2)));
+    CK(cudaMalloc(&b, n * sizeof(float2)));
+    const unsigned g = (unsigned)((n + 255) / 256);
+    k_cast_df<<<g, 256, 0, c->stream>>>(n, c->dx_io, a);
+    st = device_nearinv_apply32(c, a, b, nrhs, c->stream);
+    if (!st) {
+        k_cast_fd<<<g, 256, 0, c->stream>>>(n, b, c->dy_io);
+        st = d2h_cols(c, x, c->dy_io, nrhs, c->N);
+    }
+    if (!st && !cuda_ok(c, cudaStreamSynchronize(c->stream), "precond32")) st = MLF_E_CUDA;
+    cudaFree(a);
+    cudaFree(b);
+    return st;
+}
+
 int mlf_excitation(mlf_ctx* h, const double* dirs, const double* pols, double ctte_re, double ctte_im, int nrhs,
                    double* b) {
     if (!h || !dirs || !pols || !b || nrhs <= 0) return MLF_E_ARG;
@@ -398,6 +444,7 @@ int mlf_stage_times(mlf_ctx* h, float* out5) {
 int mlf_debug_field(mlf_ctx* h, int level, int which, double* out) {
     if (!h || !out) return MLF_E_ARG;
     Ctx* c = &h->c;
+    if (need_tree(c)) return MLF_E_STATE;
     if (level < 3 || level > c->nlev || which < 0 || which > 2) return MLF_E_ARG;
     if (!bind_device(c)) return MLF_E_CUDA;
     Level& L = c->lv[level];

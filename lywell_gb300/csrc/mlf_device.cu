@@ -28,6 +28,7 @@
 
 #include "mlf_internal.h"
 #include "mlf_sep.cuh"
+#include "mlf_zmn.cuh"
 
 namespace mlf {
 
@@ -149,15 +150,6 @@ __global__ void k_translation(int K, const double* __restrict__ kap, const doubl
     T[(size_t)t * K + k] = make_double2(__dmul_rn(vr, scale), __dmul_rn(vi, scale));
 }
 
-__device__ __forceinline__ double2 green(double w_smue, const double* a, const double* b) {
-    const double d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2];
-    const double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-    double s, co;
-    sincos(w_smue * r, &s, &co);
-    const double ir = 1.0 / r;
-    return make_double2(co * ir, -s * ir);
-}
-
 // One block per row m, threads over the row's near columns.
 __global__ void k_near(const int* __restrict__ ia, const int* __restrict__ ja,
                        const double* __restrict__ t_baric, const double* __restrict__ t_baric_sub,
@@ -166,47 +158,9 @@ __global__ void k_near(const int* __restrict__ ia, const int* __restrict__ ja,
                        double w_smue, double c72, float2* __restrict__ Z) {
     const int m = blockIdx.x;
     const int beg = ia[m], end = ia[m + 1];
-    const double* cpm = t_baric + 3 * e_t[2 * m];
-    const double* cmm = t_baric + 3 * e_t[2 * m + 1];
-    const double* vpm = p_coord + 3 * e_po[2 * m];
-    const double* vmm = p_coord + 3 * e_po[2 * m + 1];
-    const double lm = e_long[m];
     for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
-        const int n = ja[q];
-        const int tpn = e_t[2 * n], tmn = e_t[2 * n + 1];
-        const double* vpn = p_coord + 3 * e_po[2 * n];
-        const double* vmn = p_coord + 3 * e_po[2 * n + 1];
-        double2 AP[3] = {{0, 0}, {0, 0}, {0, 0}}, AM[3] = {{0, 0}, {0, 0}, {0, 0}};
-        double2 PhiP = {0, 0}, PhiM = {0, 0};
-        for (int i = 0; i < 9; ++i) {
-            const double* sp = t_baric_sub + 27 * (size_t)tpn + 3 * i;
-            const double* sm = t_baric_sub + 27 * (size_t)tmn + 3 * i;
-            const double2 g11 = green(w_smue, cpm, sp), g12 = green(w_smue, cpm, sm);
-            const double2 g21 = green(w_smue, cmm, sp), g22 = green(w_smue, cmm, sm);
-            for (int d = 0; d < 3; ++d) {
-                const double r1 = sp[d] - vpn[d], r2 = vmn[d] - sm[d];
-                AP[d].x += g11.x * r1 + g12.x * r2; AP[d].y += g11.y * r1 + g12.y * r2;
-                AM[d].x += g21.x * r1 + g22.x * r2; AM[d].y += g21.y * r1 + g22.y * r2;
-            }
-            PhiP.x += g11.x - g12.x; PhiP.y += g11.y - g12.y;
-            PhiM.x += g21.x - g22.x; PhiM.y += g21.y - g22.y;
-        }
-        const double ln = e_long[n];
-        const double fa = ((MU / PI) * c72) * ln;
-        const double den = ((36 * PI) * w) * EPSI;
-        // Phi = -Phi*l_n / (j den) = (-Im*l_n/den... ) written out
-        const double tPx = -PhiP.x * ln, tPy = -PhiP.y * ln, tMx = -PhiM.x * ln, tMy = -PhiM.y * ln;
-        const double2 P2 = make_double2(tPy / den, -tPx / den), M2 = make_double2(tMy / den, -tMx / den);
-        double2 s = {0, 0};
-        for (int d = 0; d < 3; ++d) {
-            const double a1 = cpm[d] - vpm[d], a2 = -cmm[d] + vmm[d];
-            s.x += AP[d].x * fa * a1 + AM[d].x * fa * a2;
-            s.y += AP[d].y * fa * a1 + AM[d].y * fa * a2;
-        }
-        const double fz = (0.5 * w) * lm;
-        const double2 PintA = make_double2(-fz * s.y, fz * s.x);
-        const double2 PintPhi = make_double2(lm * (M2.x - P2.x), lm * (M2.y - P2.y));
-        Z[q] = make_float2((float)(PintPhi.x + PintA.x), (float)(PintPhi.y + PintA.y));
+        const double2 v = zmn_mom(m, ja[q], t_baric, t_baric_sub, p_coord, e_t, e_po, e_long, w, w_smue, c72);
+        Z[q] = make_float2((float)v.x, (float)v.y);
     }
 }
 
@@ -429,11 +383,13 @@ int fetch_near_values(Ctx* c, std::vector<float2>& out) {
     return MLF_OK;
 }
 
-int device_setup(Ctx* c) {
-    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-    for (int i = 0; i < 8; ++i) CK(cudaEventCreate(&c->ev[i]));
-    const int nl = c->nlev;
-    const int N = c->N;
+int need_tree(Ctx* c) {
+    if (!c->dense) return 0;
+    c->err = "this call needs the MLFMA octree; the context holds the dense MoM operator";
+    return 1;
+}
+
+int upload_geometry(Ctx* c) {
     int st;
     if ((st = upload(c, &c->dp_coord, c->p_coord))) return st;
     if ((st = upload(c, &c->dt_baric, c->t_baric))) return st;
@@ -442,6 +398,16 @@ int device_setup(Ctx* c) {
     if ((st = upload(c, &c->de_centro, c->e_centro))) return st;
     if ((st = upload(c, &c->de_t, c->e_t))) return st;
     if ((st = upload(c, &c->de_po, c->e_po))) return st;
+    return MLF_OK;
+}
+
+int device_setup(Ctx* c) {
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 8; ++i) CK(cudaEventCreate(&c->ev[i]));
+    const int nl = c->nlev;
+    const int N = c->N;
+    int st;
+    if ((st = upload_geometry(c))) return st;
     Level& leaf = c->lv[nl];
     std::vector<int> box_of_sorted(N);
     for (int b = 0; b < leaf.nb; ++b)
@@ -550,10 +516,12 @@ int device_setup(Ctx* c) {
         if ((st = upload(c, &dcoef, coef))) return st;
         CK(cudaMalloc(&L.dT, std::max<size_t>((size_t)nt * L.K, 1) * sizeof(double2)));
         const double scale = (2. * PI / c->ph.lambda) / (4. * PI);
-        if (nt > 0) {
-            dim3 grid((L.K + 127) / 128, nt);
-            k_translation<<<grid, 128, 0, c->stream>>>(L.K, L.dkap, du, dLt, dcoef, ldc, db2, Lmax + 1,
-                                                       scale, mode, L.dT);
+        for (int t0 = 0; t0 < nt; t0 += 65535) {   // grid.y limit (single-level FMM grids have many vectors)
+            const int cnt = std::min(65535, nt - t0);
+            dim3 grid((L.K + 127) / 128, cnt);
+            k_translation<<<grid, 128, 0, c->stream>>>(L.K, L.dkap, du + 3 * (size_t)t0, dLt + t0,
+                                                       dcoef + (size_t)t0 * ldc, ldc, db2, Lmax + 1, scale, mode,
+                                                       L.dT + (size_t)t0 * L.K);
             if ((st = launch_check(c, "k_translation"))) return st;
         }
         CK(cudaStreamSynchronize(c->stream));
@@ -595,6 +563,7 @@ int device_setup(Ctx* c) {
 static inline int chunks(int n, int bd) { return (n + bd - 1) / bd; }
 
 int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s) {
+    if (c->dense) return dense_matvec(c, x, y, nrhs, ld, s);
     if (c->mv_prec == 1) return device_matvec32(c, x, y, nrhs, ld, s);
     int st;
     if ((st = ensure_fields(c, nrhs))) return st;
@@ -636,7 +605,8 @@ int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaSt
         const int warps = c->N * nrhs;
         const double facy = c->ph.w * MU / (4. * PI);
         k_receive_near_d<<<chunks(warps * 32, 256), 256, 0, s>>>(leaf.K, c->N, nrhs, ld, c->dperm,
-                                                                  c->dbox_of_sorted, c->dR, leaf.dA, c->dia,
+                                                                  c->dbox_of_sorted, c->dR,
+                                                                  nl == 3 ? leaf.dB : leaf.dA, c->dia,
                                                                   c->dja, c->dZd, x, facy, y);
     }
     if (prof) cudaEventRecord(c->ev[5], s);
@@ -679,7 +649,7 @@ void device_free(Ctx* c) {
     F(c->dR); F(c->dperm); F(c->dbox_ptr); F(c->dbox_of_sorted); F(c->dia); F(c->dja); F(c->dZ);
     F(c->dp_coord); F(c->dt_baric); F(c->dt_baric_sub); F(c->de_long); F(c->de_centro); F(c->de_t);
     F(c->de_po); F(c->dalu); F(c->djlu); F(c->dju); F(c->dlvl_rows_f); F(c->dlvl_rows_b);
-    F(c->dwork); F(c->dscal); F(c->dflags); F(c->dx_io); F(c->dy_io); F(c->dMinv); F(c->dZd); F(c->dboff); F(c->dMinv32);
+    F(c->dwork); F(c->dscal); F(c->dflags); F(c->dx_io); F(c->dy_io); F(c->dMinv); F(c->dZd); F(c->dboff); F(c->dMinv32); F(c->dpre_xs); F(c->dZdense);
     mixed_free(c);
     near_blocks_free(c);
     for (int i = 0; i < 8; ++i)

@@ -88,6 +88,8 @@ struct Mixed32 {
 
 struct Ctx {
     int dev = 0;
+    int dense = 0;                    // dense MoM operator instead of the octree (MLF_FLAG_DENSE_MOM)
+    double2* dZdense = nullptr;       // N x N row-major, FP64
     int mv_prec = 0;                  // operator precision used by device_matvec: 0 FP64, 1 FP32
     int gmres_m = 400;                // restart length of the mixed-precision GMRES cycles
     Mixed32 m32;
@@ -140,7 +142,10 @@ struct Ctx {
     long long* dboff = nullptr;       // own-box block offsets
     float2* dMinv32 = nullptr;        // FP32 copy for the FP32 inner solves
     long long minv_len = 0;
+    float2* dpre_xs = nullptr;        // box-sorted copy of the preconditioner input (blocks of columns)
+    size_t pre_xs_cap = 0;
     int nearinv_ok = 0, nearinv_own = 0;
+    int learned = 0;                  // own-box blocks installed from the learned network
     // level schedule of the triangular solves
     std::vector<int> lvl_ptr_f, lvl_rows_f, lvl_ptr_b, lvl_rows_b;
     int *dlvl_rows_f = nullptr, *dlvl_rows_b = nullptr;
@@ -168,6 +173,7 @@ struct Ctx {
 // host set-up (mlf_setup.cpp)
 int fetch_near_values(Ctx* c, std::vector<float2>& out);  // device near values -> host
 int build_octree(Ctx* c);          // levels, boxes, lists, interpolation tables
+int build_fmm(Ctx* c);             // single-level FMM grid as a one-level tree (nlev = 3)
 void sph_bessel(int nmax, double x, double* j, double* y);
 void binomial_squares(int nmax, std::vector<double>& out);  // (n!/(i!(n-i)!))^2, [n*(nmax+1)+i]
 int ilu0_factor(Ctx* c);           // host ILU(0), fills alu/jlu/ju, returns ierr
@@ -190,9 +196,20 @@ int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cuda
 int device_matvec32_from32(Ctx* c, const float2* x32, double2* y, int nrhs, cudaStream_t s);
 int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStream_t s);
 void mixed_free(Ctx* c);
-int device_near_blocks32(Ctx* c, const double2* x, const float2* x32, int ld, int nrhs, float2* xs, double2* y,
+int upload_geometry(Ctx* c);
+int dense_setup(Ctx* c);
+int dense_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s);
+int need_tree(Ctx* c);
+int device_blk_pack(Ctx* c, const double2* x, const float2* x32, int ld, int nrhs, float2* xs, cudaStream_t s);
+int device_near_blocks32(Ctx* c, const float2* xs, int ld, int nrhs, double2* y, cudaStream_t s);
+int device_agg_blocks32(Ctx* c, const float2* R, int K, const float2* xs, int nrhs, float2* C, cudaStream_t s);
+int device_recv_blocks32(Ctx* c, const float2* R, int K, const float2* A, float facy, int nrhs, int ld, double2* y,
                          cudaStream_t s);
+int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const float2* xs, int nrhs, float2* out,
+                        cudaStream_t s);
 void near_blocks_free(Ctx* c);
+int near_blocks_ensure(Ctx* c);
+int lp_tokens(Ctx* c, int target, float* X, float* T, long long cap, long long* ntok);
 int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* best_cols, float* per_rhs_ms);
 int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
                        int* iters, double* relres, int precond, int* status, double inner_tol, int* outer);

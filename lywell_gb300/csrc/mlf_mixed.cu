@@ -180,32 +180,6 @@ __global__ void k32_receive_near(int K, int N, int nrhs, int ld, const int* __re
     if (lane == 0) y[(size_t)r * ld + n] = make_double2((double)tr, (double)ti);
 }
 
-// Receive-only variant (near field added by k32_near_tiles).
-__global__ void k32_receive(int K, int N, int nrhs, int ld, const int* __restrict__ perm,
-                            const int* __restrict__ box_of_sorted, const float2* __restrict__ R,
-                            const float2* __restrict__ A, float facy, double2* __restrict__ y) {
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (gw >= N * nrhs) return;
-    const int j = gw / nrhs, r = gw % nrhs;
-    const int n = perm[j], b = box_of_sorted[j];
-    const float2* Rj = R + (size_t)j * 2 * K;
-    const float2* Ab = A + ((size_t)b * nrhs + r) * 2 * K;
-    float sr = 0.f, si = 0.f;
-    for (int q = lane; q < 2 * K; q += 32) {
-        const float2 a = Rj[q], v = Ab[q];
-        sr = fmaf(a.x, v.x, sr); sr = fmaf(a.y, v.y, sr);
-        si = fmaf(a.x, v.y, si); si = fmaf(-a.y, v.x, si);
-    }
-    float tr = -facy * si, ti = facy * sr;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        tr += __shfl_xor_sync(0xffffffff, tr, o);
-        ti += __shfl_xor_sync(0xffffffff, ti, o);
-    }
-    if (lane == 0) y[(size_t)r * ld + n] = make_double2((double)tr, (double)ti);
-}
-
 // ---------------------------------------------------------------------------
 
 static int up32(Ctx* c, float** dst, const std::vector<double>& v) {
@@ -294,6 +268,7 @@ int device_matvec32_from32(Ctx* c, const float2* x32, double2* y, int nrhs, cuda
 
 static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y, int nrhs, int ld, cudaStream_t s) {
     int st;
+    if (need_tree(c)) return MLF_E_STATE;
     if ((st = mixed_setup(c))) return st;
     if ((st = ensure_fields32(c, nrhs))) return st;
     const int nl = c->nlev;
@@ -301,9 +276,15 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
     const bool prof = c->profiling != 0;
     if (prof) cudaEventRecord(c->ev[0], s);
     const float2* xf = x32 ? x32 : c->m32.xf;
-    if (!x32) k32_pack_x<<<dim3((c->N + 255) / 256, nrhs), 256, 0, s>>>(c->N, nrhs, ld, x, c->m32.xf);
-    k32_aggregate<<<leaf.nb * nrhs, 256, 0, s>>>(leaf.K, nrhs, c->N, c->dbox_ptr, c->dperm, c->m32.R, xf,
-                                                 c->m32.lv[nl].C);
+    if (nrhs == 1) {
+        if (!x32) k32_pack_x<<<dim3((c->N + 255) / 256, nrhs), 256, 0, s>>>(c->N, nrhs, ld, x, c->m32.xf);
+        k32_aggregate<<<leaf.nb * nrhs, 256, 0, s>>>(leaf.K, nrhs, c->N, c->dbox_ptr, c->dperm, c->m32.R, xf,
+                                                     c->m32.lv[nl].C);
+    } else {
+        // blocks of columns: box-sorted row-major copy, then per-box GEMMs
+        if ((st = device_blk_pack(c, x, x32, ld, nrhs, c->m32.xT, s))) return st;
+        if ((st = device_agg_blocks32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s))) return st;
+    }
     if (prof) cudaEventRecord(c->ev[1], s);
     for (int n = nl; n >= 4; --n) {
         Level& Lc = c->lv[n];
@@ -338,12 +319,11 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
         const float facy = (float)(c->ph.w * MU / (4. * PI));
         if (nrhs == 1) {
             k32_receive_near<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-                leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, c->m32.lv[nl].A, c->dia, c->dja,
+                leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, (nl == 3 ? c->m32.lv[nl].B : c->m32.lv[nl].A), c->dia, c->dja,
                 c->dZ, xf, facy, y);
         } else {
-            k32_receive<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-                leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, c->m32.lv[nl].A, facy, y);
-            if ((st = device_near_blocks32(c, x, x32, ld, nrhs, c->m32.xT, y, s))) return st;
+            if ((st = device_recv_blocks32(c, c->m32.R, leaf.K, (nl == 3 ? c->m32.lv[nl].B : c->m32.lv[nl].A), facy, nrhs, ld, y, s))) return st;
+            if ((st = device_near_blocks32(c, c->m32.xT, ld, nrhs, y, s))) return st;
         }
     }
     if (prof) cudaEventRecord(c->ev[5], s);

@@ -1,4 +1,5 @@
-// Near field of the FP32 operator for blocks of right-hand sides.
+// Near field, leaf aggregation / receive and the own-box preconditioner of the
+// FP32 operator for blocks of right-hand sides, as dense per-box complex GEMMs.
 //
 // The near matrix (llenarZesparcida, modMLFMA.f90:1594-1634) couples every
 // basis of a leaf box with every basis of each near leaf box, so its CSR rows
@@ -71,9 +72,76 @@ __global__ void k_blk_pack64(int N, int nrhs, int ld, const int* __restrict__ pe
     xs[e] = make_float2((float)v.x, (float)v.y);
 }
 
-// y(:, c0 : c0 + 8 TC) += Z_near x for one 64-row tile of one leaf box.
-// 256 threads: thread (ty = tid / 8, tx = tid % 8) owns rows r0 + 2 ty, +1 and
-// columns c0 + TC tx .. + TC - 1 (2 x TC complex accumulators).
+// ---------------------------------------------------------------------------
+// Box-block complex GEMM engine.  One CTA computes a 64-row x (8 TC)-column
+// tile of Y = A X for one leaf box, streaming the contraction dimension in
+// chunks of 32 through shared memory.  256 threads: thread (ty = tid / 8,
+// tx = tid % 8) owns rows 2 ty, 2 ty + 1 and columns TC tx .. TC tx + TC - 1
+// of the tile (2 x TC complex accumulators in registers).
+//   A element (row, t): AROW ? A[row * lda + t] : A[t * lda + row] (conj if ACONJ)
+//   X element (t, col): XCOL ? X[col * ldx + t] : X[t * ldx + col]
+template <int TC>
+struct BlkTile {
+    float2 Zs[NBK_KC][NBK_ROWS + 2];
+    float2 Xs[NBK_KC][8 * TC];
+};
+
+template <int TC, bool AROW, bool ACONJ, bool XCOL>
+__device__ __forceinline__ void blk_mac(float2 (&acc)[2][TC], BlkTile<TC>& sm, const float2* __restrict__ A,
+                                        long long lda, int r0, int mrows, int kdim, const float2* __restrict__ X,
+                                        long long ldx, int c0, int ncols) {
+    constexpr int NC = 8 * TC;
+    const int tid = threadIdx.x, ty = tid >> 3, tx = tid & 7;
+    for (int t0 = 0; t0 < kdim; t0 += NBK_KC) {
+        for (int q = tid; q < NBK_KC * NBK_ROWS; q += 256) {
+            int k, p;
+            if (AROW) { p = q / NBK_KC; k = q - p * NBK_KC; }
+            else { k = q / NBK_ROWS; p = q - k * NBK_ROWS; }
+            const int t = t0 + k, row = r0 + p;
+            float2 v = make_float2(0.f, 0.f);
+            if (t < kdim && row < mrows) v = AROW ? A[(size_t)row * lda + t] : A[(size_t)t * lda + row];
+            if (ACONJ) v.y = -v.y;
+            sm.Zs[k][p] = v;
+        }
+        for (int q = tid; q < NBK_KC * NC; q += 256) {
+            int k, cc;
+            if (XCOL) { cc = q / NBK_KC; k = q - cc * NBK_KC; }
+            else { k = q / NC; cc = q - k * NC; }
+            const int t = t0 + k, col = c0 + cc;
+            float2 v = make_float2(0.f, 0.f);
+            if (t < kdim && col < ncols) v = XCOL ? X[(size_t)col * ldx + t] : X[(size_t)t * ldx + col];
+            sm.Xs[k][cc] = v;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int k = 0; k < NBK_KC; ++k) {
+            const float4 zz = *reinterpret_cast<const float4*>(&sm.Zs[k][2 * ty]);
+#pragma unroll
+            for (int u = 0; u < TC; ++u) {
+                const float2 xv = sm.Xs[k][tx * TC + u];
+                acc[0][u].x = fmaf(zz.x, xv.x, acc[0][u].x);
+                acc[0][u].x = fmaf(-zz.y, xv.y, acc[0][u].x);
+                acc[0][u].y = fmaf(zz.x, xv.y, acc[0][u].y);
+                acc[0][u].y = fmaf(zz.y, xv.x, acc[0][u].y);
+                acc[1][u].x = fmaf(zz.z, xv.x, acc[1][u].x);
+                acc[1][u].x = fmaf(-zz.w, xv.y, acc[1][u].x);
+                acc[1][u].y = fmaf(zz.z, xv.y, acc[1][u].y);
+                acc[1][u].y = fmaf(zz.w, xv.x, acc[1][u].y);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int TC>
+__device__ __forceinline__ void acc_zero(float2 (&acc)[2][TC]) {
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int u = 0; u < TC; ++u) acc[a][u] = make_float2(0.f, 0.f);
+}
+
+// y(:, c0 : c0 + 8 TC) += Z_near x for one 64-row tile of one leaf box
 template <int TC>
 __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2* __restrict__ tiles,
                                                     const int* __restrict__ box_ptr, const int* __restrict__ nbox_ptr,
@@ -81,54 +149,19 @@ __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2
                                                     const long long* __restrict__ blk_off,
                                                     const float2* __restrict__ Zblk, const float2* __restrict__ xs,
                                                     const int* __restrict__ perm, double2* __restrict__ y) {
-    constexpr int NC = 8 * TC;
-    __shared__ __align__(16) float2 Zs[NBK_KC][NBK_ROWS];
-    __shared__ __align__(16) float2 Xs[NBK_KC][NC];
+    __shared__ __align__(16) BlkTile<TC> sm;
     const int2 tl = tiles[blockIdx.x];
-    const int i = tl.x, r0 = tl.y;
-    const int c0 = blockIdx.y * NC;
+    const int i = tl.x, r0 = tl.y, c0 = blockIdx.y * 8 * TC;
     const int ni = box_ptr[i + 1] - box_ptr[i];
-    const int tid = threadIdx.x, ty = tid >> 3, tx = tid & 7;
     float2 acc[2][TC];
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-        for (int u = 0; u < TC; ++u) acc[a][u] = make_float2(0.f, 0.f);
+    acc_zero<TC>(acc);
     for (int e = nbox_ptr[i]; e < nbox_ptr[i + 1]; ++e) {
         const int j = nbox_list[e];
         const int j0 = box_ptr[j], nj = box_ptr[j + 1] - j0;
-        const float2* zb = Zblk + blk_off[e];
-        for (int t0 = 0; t0 < nj; t0 += NBK_KC) {
-            for (int q = tid; q < NBK_KC * NBK_ROWS; q += 256) {
-                const int k = q / NBK_ROWS, p = q - k * NBK_ROWS;
-                const int t = t0 + k, row = r0 + p;
-                Zs[k][p] = (t < nj && row < ni) ? zb[(size_t)t * ni + row] : make_float2(0.f, 0.f);
-            }
-            for (int q = tid; q < NBK_KC * NC; q += 256) {
-                const int k = q / NC, cc = q - k * NC;
-                const int t = t0 + k, col = c0 + cc;
-                Xs[k][cc] = (t < nj && col < nrhs) ? xs[(size_t)(j0 + t) * nrhs + col] : make_float2(0.f, 0.f);
-            }
-            __syncthreads();
-#pragma unroll 8
-            for (int k = 0; k < NBK_KC; ++k) {
-                const float4 zz = *reinterpret_cast<const float4*>(&Zs[k][2 * ty]);
-#pragma unroll
-                for (int u = 0; u < TC; ++u) {
-                    const float2 xv = Xs[k][tx * TC + u];
-                    acc[0][u].x = fmaf(zz.x, xv.x, acc[0][u].x);
-                    acc[0][u].x = fmaf(-zz.y, xv.y, acc[0][u].x);
-                    acc[0][u].y = fmaf(zz.x, xv.y, acc[0][u].y);
-                    acc[0][u].y = fmaf(zz.y, xv.x, acc[0][u].y);
-                    acc[1][u].x = fmaf(zz.z, xv.x, acc[1][u].x);
-                    acc[1][u].x = fmaf(-zz.w, xv.y, acc[1][u].x);
-                    acc[1][u].y = fmaf(zz.z, xv.y, acc[1][u].y);
-                    acc[1][u].y = fmaf(zz.w, xv.x, acc[1][u].y);
-                }
-            }
-            __syncthreads();
-        }
+        blk_mac<TC, false, false, false>(acc, sm, Zblk + blk_off[e], ni, r0, ni, nj, xs + (size_t)j0 * nrhs, nrhs, c0,
+                                         nrhs);
     }
+    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
         const int row = r0 + 2 * ty + a;
@@ -146,8 +179,94 @@ __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2
     }
 }
 
+// Leaf aggregation (llenar_campoCyB step 2, modMLFMA.f90:1805-1811) for a block
+// of columns: C(:, col, box) = R_box^T x_box, R_box = the box's 2K x n_b
+// patterns.  Grid: (boxes x ceil(2K / 64) row tiles, column tiles).
+template <int TC>
+__global__ void __launch_bounds__(256) k32_agg_blk(int K2, int nrhs, int ntr, const int* __restrict__ box_ptr,
+                                                   const float2* __restrict__ R, const float2* __restrict__ xs,
+                                                   float2* __restrict__ C) {
+    __shared__ __align__(16) BlkTile<TC> sm;
+    const int b = blockIdx.x / ntr, r0 = (blockIdx.x - b * ntr) * NBK_ROWS, c0 = blockIdx.y * 8 * TC;
+    const int j0 = box_ptr[b], nb = box_ptr[b + 1] - j0;
+    float2 acc[2][TC];
+    acc_zero<TC>(acc);
+    blk_mac<TC, false, false, false>(acc, sm, R + (size_t)j0 * K2, K2, r0, K2, nb, xs + (size_t)j0 * nrhs, nrhs, c0,
+                                     nrhs);
+    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        const int row = r0 + 2 * ty + a;
+        if (row >= K2) continue;
+#pragma unroll
+        for (int u = 0; u < TC; ++u) {
+            const int col = c0 + tx * TC + u;
+            if (col < nrhs) C[((size_t)b * nrhs + col) * K2 + row] = acc[a][u];
+        }
+    }
+}
+
+// Leaf receive (MatxVec_MLFMA, modMLFMA.f90:1915-1924) for a block of
+// columns: y(basis, col) = j facy sum_q conj(R[basis][q]) A(q, col, box).
+template <int TC>
+__global__ void __launch_bounds__(256) k32_recv_blk(int K2, int nrhs, int ld, float facy,
+                                                    const int2* __restrict__ tiles, const int* __restrict__ box_ptr,
+                                                    const int* __restrict__ perm, const float2* __restrict__ R,
+                                                    const float2* __restrict__ Af, double2* __restrict__ y) {
+    __shared__ __align__(16) BlkTile<TC> sm;
+    const int2 tl = tiles[blockIdx.x];
+    const int b = tl.x, r0 = tl.y, c0 = blockIdx.y * 8 * TC;
+    const int j0 = box_ptr[b], nb = box_ptr[b + 1] - j0;
+    float2 acc[2][TC];
+    acc_zero<TC>(acc);
+    blk_mac<TC, true, true, true>(acc, sm, R + (size_t)j0 * K2, K2, r0, nb, K2, Af + (size_t)b * nrhs * K2, K2, c0,
+                                  nrhs);
+    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        const int row = r0 + 2 * ty + a;
+        if (row >= nb) continue;
+        const int n = perm[j0 + row];
+#pragma unroll
+        for (int u = 0; u < TC; ++u) {
+            const int col = c0 + tx * TC + u;
+            if (col < nrhs)
+                y[(size_t)col * ld + n] = make_double2(-(double)(facy * acc[a][u].y), (double)(facy * acc[a][u].x));
+        }
+    }
+}
+
+// Own-box block preconditioner for a block of FP32 columns:
+// out(basis, col) = sum_t M_box[row][t] xs(box basis t, col), M row-major n_b x n_b at boff[box].
+template <int TC>
+__global__ void __launch_bounds__(256) k32_own_blk(int N, int nrhs, const int2* __restrict__ tiles,
+                                                   const int* __restrict__ box_ptr, const int* __restrict__ perm,
+                                                   const long long* __restrict__ boff, const float2* __restrict__ M,
+                                                   const float2* __restrict__ xs, float2* __restrict__ out) {
+    __shared__ __align__(16) BlkTile<TC> sm;
+    const int2 tl = tiles[blockIdx.x];
+    const int b = tl.x, r0 = tl.y, c0 = blockIdx.y * 8 * TC;
+    const int j0 = box_ptr[b], nb = box_ptr[b + 1] - j0;
+    float2 acc[2][TC];
+    acc_zero<TC>(acc);
+    blk_mac<TC, true, false, false>(acc, sm, M + boff[b], nb, r0, nb, nb, xs + (size_t)j0 * nrhs, nrhs, c0, nrhs);
+    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        const int row = r0 + 2 * ty + a;
+        if (row >= nb) continue;
+        const int n = perm[j0 + row];
+#pragma unroll
+        for (int u = 0; u < TC; ++u) {
+            const int col = c0 + tx * TC + u;
+            if (col < nrhs) out[(size_t)col * N + n] = acc[a][u];
+        }
+    }
+}
+
 static int near_blocks_setup(Ctx* c) {
     if (c->blk_ok) return MLF_OK;
+    if (need_tree(c)) return MLF_E_STATE;
     const int nb = (int)c->box_ptr.size() - 1;
     if ((int)c->nbox_ptr.size() != nb + 1) {
         c->err = "near box lists missing";
@@ -192,25 +311,69 @@ static int near_blocks_setup(Ctx* c) {
     return MLF_OK;
 }
 
-// y(:, 0:nrhs) += Z_near x with x given as FP32 columns (x32, ld N) or FP64
-// columns (x, ld); xs is an N x nrhs FP32 scratch.
-int device_near_blocks32(Ctx* c, const double2* x, const float2* x32, int ld, int nrhs, float2* xs, double2* y,
-                         cudaStream_t s) {
-    int st;
-    if ((st = near_blocks_setup(c))) return st;
+static bool blk_narrow(const Ctx* c, int nrhs) { return c->blk_cols ? c->blk_cols == 8 : nrhs <= 8; }
+
+// xs (N x nrhs FP32, box-sorted rows) from FP32 columns (x32, ld N) or FP64 columns (x, ld)
+int device_blk_pack(Ctx* c, const double2* x, const float2* x32, int ld, int nrhs, float2* xs, cudaStream_t s) {
     const size_t ne = (size_t)c->N * nrhs;
     if (x32) k_blk_pack32<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(c->N, nrhs, c->dperm, x32, xs);
     else k_blk_pack64<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(c->N, nrhs, ld, c->dperm, x, xs);
-    const bool narrow = c->blk_cols ? c->blk_cols == 8 : nrhs <= 8;
-    if (narrow) {
+    return cuda_ok(c, cudaGetLastError(), "pack") ? MLF_OK : MLF_E_CUDA;
+}
+
+// y(:, 0:nrhs) += Z_near xs
+int device_near_blocks32(Ctx* c, const float2* xs, int ld, int nrhs, double2* y, cudaStream_t s) {
+    int st;
+    if ((st = near_blocks_setup(c))) return st;
+    if (blk_narrow(c, nrhs))
         k32_near_blk<1><<<dim3(c->nblk_tiles, (nrhs + 7) / 8), 256, 0, s>>>(
             nrhs, ld, c->dblk_tiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, c->dblk_off, c->dZblk, xs, c->dperm, y);
-    } else {
+    else
         k32_near_blk<4><<<dim3(c->nblk_tiles, (nrhs + 31) / 32), 256, 0, s>>>(
             nrhs, ld, c->dblk_tiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, c->dblk_off, c->dZblk, xs, c->dperm, y);
-    }
     return cuda_ok(c, cudaGetLastError(), "near blocks") ? MLF_OK : MLF_E_CUDA;
 }
+
+// C (leaf fields, FP32) = R^T x for every leaf box
+int device_agg_blocks32(Ctx* c, const float2* R, int K, const float2* xs, int nrhs, float2* C, cudaStream_t s) {
+    const int nb = (int)c->box_ptr.size() - 1, K2 = 2 * K, ntr = (K2 + NBK_ROWS - 1) / NBK_ROWS;
+    if (blk_narrow(c, nrhs))
+        k32_agg_blk<1><<<dim3(nb * ntr, (nrhs + 7) / 8), 256, 0, s>>>(K2, nrhs, ntr, c->dbox_ptr, R, xs, C);
+    else
+        k32_agg_blk<4><<<dim3(nb * ntr, (nrhs + 31) / 32), 256, 0, s>>>(K2, nrhs, ntr, c->dbox_ptr, R, xs, C);
+    return cuda_ok(c, cudaGetLastError(), "aggregation blocks") ? MLF_OK : MLF_E_CUDA;
+}
+
+// y = j facy conj(R) A (leaf receive), written (not added)
+int device_recv_blocks32(Ctx* c, const float2* R, int K, const float2* A, float facy, int nrhs, int ld, double2* y,
+                         cudaStream_t s) {
+    int st;
+    if ((st = near_blocks_setup(c))) return st;
+    const int K2 = 2 * K;
+    if (blk_narrow(c, nrhs))
+        k32_recv_blk<1><<<dim3(c->nblk_tiles, (nrhs + 7) / 8), 256, 0, s>>>(K2, nrhs, ld, facy, c->dblk_tiles,
+                                                                             c->dbox_ptr, c->dperm, R, A, y);
+    else
+        k32_recv_blk<4><<<dim3(c->nblk_tiles, (nrhs + 31) / 32), 256, 0, s>>>(K2, nrhs, ld, facy, c->dblk_tiles,
+                                                                              c->dbox_ptr, c->dperm, R, A, y);
+    return cuda_ok(c, cudaGetLastError(), "receive blocks") ? MLF_OK : MLF_E_CUDA;
+}
+
+// out (FP32 columns, ld N) = own-box blocks M applied to xs
+int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const float2* xs, int nrhs, float2* out,
+                        cudaStream_t s) {
+    int st;
+    if ((st = near_blocks_setup(c))) return st;
+    if (blk_narrow(c, nrhs))
+        k32_own_blk<1><<<dim3(c->nblk_tiles, (nrhs + 7) / 8), 256, 0, s>>>(c->N, nrhs, c->dblk_tiles, c->dbox_ptr,
+                                                                            c->dperm, boff, M, xs, out);
+    else
+        k32_own_blk<4><<<dim3(c->nblk_tiles, (nrhs + 31) / 32), 256, 0, s>>>(c->N, nrhs, c->dblk_tiles, c->dbox_ptr,
+                                                                             c->dperm, boff, M, xs, out);
+    return cuda_ok(c, cudaGetLastError(), "own-box blocks") ? MLF_OK : MLF_E_CUDA;
+}
+
+int near_blocks_ensure(Ctx* c) { return near_blocks_setup(c); }
 
 void near_blocks_free(Ctx* c) {
     auto F = [](void* p) { if (p) cudaFree(p); };

@@ -71,6 +71,11 @@ using namespace mlf;
 extern "C" int mlf_matvec_device_noalloc(mlf_ctx* h, const void* x_dev, void* y_dev, void* stream) {
     if (!h || !x_dev || !y_dev) return MLF_E_ARG;
     Ctx* c = &h->c;
+    if (need_tree(c)) return MLF_E_STATE;
+    if (c->nlev == 3) {
+        c->err = "mlf_matvec_device_noalloc: single-level FMM contexts are not supported";
+        return MLF_E_STATE;
+    }
     if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
     const int nl = c->nlev;
     size_t need = 0;

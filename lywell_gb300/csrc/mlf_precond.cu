@@ -282,6 +282,19 @@ int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStr
         k_d2f<<<4096, 256, 0, s>>>((size_t)c->minv_len, c->dMinv, c->dMinv32);
     }
     const long long warps = (long long)c->N * nrhs;
+    if (c->nearinv_own && nrhs > 1) {
+        // blocks of columns: per-box GEMMs on a box-sorted copy of y
+        const size_t need = (size_t)c->N * nrhs;
+        if (c->pre_xs_cap < need) {
+            if (c->dpre_xs) cudaFree(c->dpre_xs);
+            c->dpre_xs = nullptr;
+            CK(cudaMalloc(&c->dpre_xs, need * sizeof(float2)));
+            c->pre_xs_cap = need;
+        }
+        int st;
+        if ((st = device_blk_pack(c, nullptr, y, c->N, nrhs, c->dpre_xs, s))) return st;
+        return device_own_blocks32(c, c->dboff, c->dMinv32, c->dpre_xs, nrhs, x, s);
+    }
     if (c->nearinv_own)
         k32_blockdiag_apply<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
             c->N, nrhs, c->dbox_ptr, c->dbox_of_sorted, c->dperm, c->dboff, c->dMinv32, y, x);
@@ -291,6 +304,7 @@ int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStr
 }
 
 int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
+    if (need_tree(c)) return MLF_E_STATE;
     const int nl = c->nlev;
     const Level& leaf = c->lv[nl];
     int nmax = 0, nownmax = 0;
@@ -309,6 +323,7 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     c->dboff = nullptr;
     c->dMinv32 = nullptr;
     c->nearinv_ok = 0;
+    c->learned = 0;
     c->nearinv_own = own_only;
     long long total = c->nnz;
     if (own_only) {

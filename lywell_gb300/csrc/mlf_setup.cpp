@@ -633,6 +633,195 @@ int build_octree(Ctx* c) {
     return MLF_OK;
 }
 
+// Single-level FMM (inicializar_FMM, geomFMM, buscarFuncBases,
+// llenar_functransf: modFMM.f90:170-268, 278-469, 650-778) as a one-level
+// tree: level 3 is the FMM grid and nlev = 3, so the patterns, translation
+// tables, near field and matvec stages are the MLFMA ones without
+// interpolation (the receive reads B when nlev = 3).  Box side criterion
+// ladomax * lambda (the reference's criterio_ladoW is lambda / 2); the cube of
+// side max-extent + lambda/1e4 is cut into ceiling(extent / criterion) boxes
+// per axis.  Boxes are visited z-major, then y, then x from the corner
+// (max + lambda/2e4) downwards, offsets accumulated by repeated addition, and
+// a basis belongs to the first box whose closed bounds hold its edge centre:
+// only the (up to 27) grid cells around it can, so each basis tests those in
+// visiting order.  Far pairs: |c_i - c_j| >= 2 side - lambda/100, translation
+// vectors numbered in order of first appearance (keyed by their grid
+// offsets).  Near rows are the near boxes' bases sorted ascending.
+int build_fmm(Ctx* c) {
+    const int N = c->N;
+    const double lambda = c->ph.lambda;
+    int lim[6] = {0, 0, 0, 0, 0, 0};
+    const double* ec = c->e_centro.data();
+    for (int i = 1; i < N; ++i) {
+        const double* p = ec + 3 * i;
+        if (p[0] > ec[3 * lim[0]]) lim[0] = i;
+        if (p[0] < ec[3 * lim[1]]) lim[1] = i;
+        if (p[1] > ec[3 * lim[2] + 1]) lim[2] = i;
+        if (p[1] < ec[3 * lim[3] + 1]) lim[3] = i;
+        if (p[2] > ec[3 * lim[4] + 2]) lim[4] = i;
+        if (p[2] < ec[3 * lim[5] + 2]) lim[5] = i;
+    }
+    const double maxX = ec[3 * lim[0]], minX = ec[3 * lim[1]];
+    const double maxY = ec[3 * lim[2] + 1], minY = ec[3 * lim[3] + 1];
+    const double maxZ = ec[3 * lim[4] + 2], minZ = ec[3 * lim[5] + 2];
+    const double dX = maxX - minX, dY = maxY - minY, dZ = maxZ - minZ;
+    double mayor;
+    if (dX >= dY && dX >= dZ) mayor = dX;
+    else if (dY >= dX && dY >= dZ) mayor = dY;
+    else mayor = dZ;
+    double tol = lambda / 10000.;
+    mayor = mayor + tol;
+    tol = tol / 2.;
+    const double corner[3] = {maxX + tol, maxY + tol, maxZ + tol};
+    const int ne = (int)std::ceil(mayor / (c->ladomax * lambda));
+    if (ne < 1 || ne > 400) {
+        c->err = "FMM grid of more than 400 boxes per axis";
+        return MLF_E_ARG;
+    }
+    const double lado = mayor / ne;
+    c->nlev = 3;
+    c->root_side = mayor;
+    for (int d = 0; d < 3; ++d) c->root_centre[d] = corner[d] - mayor / 2.;
+    Level& L = c->lv[3];
+    L.side = lado;
+    const double s3 = (double)std::sqrt(3.0f), third = (double)(1.0f / 3.0f);
+    const double kd = (2. * PI / lambda) * (s3 * lado);
+    L.L = (int)std::floor(kd + 6 * std::pow(kd, third));
+    L.nth = L.L;
+    L.nph = 2 * L.L;
+    L.K = L.nth * L.nph;
+    sampling(L);
+    // offsets by repeated addition, as the reference's loops accumulate them
+    std::vector<double> off(ne);
+    {
+        double acc = 0.;
+        for (int q = 0; q < ne; ++q) { off[q] = acc; acc = acc + lado; }
+    }
+    auto centre_of = [&](int i, int j, int k, double* cen) {
+        cen[0] = (corner[0] - off[k]) - lado / 2.;
+        cen[1] = (corner[1] - off[j]) - lado / 2.;
+        cen[2] = (corner[2] - off[i]) - lado / 2.;
+    };
+    // owner cell (loop index i*ne*ne + j*ne + k) of each basis
+    std::vector<long long> owner(N, -1);
+    for (int n = 0; n < N; ++n) {
+        const double* e = ec + 3 * n;
+        const int k0 = (int)std::floor((corner[0] - e[0]) / lado);
+        const int j0 = (int)std::floor((corner[1] - e[1]) / lado);
+        const int i0 = (int)std::floor((corner[2] - e[2]) / lado);
+        long long best = -1;
+        for (int i = std::max(0, i0 - 1); i <= std::min(ne - 1, i0 + 1); ++i)
+            for (int j = std::max(0, j0 - 1); j <= std::min(ne - 1, j0 + 1); ++j)
+                for (int k = std::max(0, k0 - 1); k <= std::min(ne - 1, k0 + 1); ++k) {
+                    double cen[3];
+                    centre_of(i, j, k, cen);
+                    const double lq = lado / 2.;
+                    if (e[0] <= cen[0] + lq && e[0] >= cen[0] - lq && e[1] <= cen[1] + lq && e[1] >= cen[1] - lq &&
+                        e[2] <= cen[2] + lq && e[2] >= cen[2] - lq) {
+                        const long long idx = ((long long)i * ne + j) * ne + k;
+                        if (best < 0 || idx < best) best = idx;
+                    }
+                }
+        if (best < 0) {
+            c->err = "an edge centre lies in no FMM box";
+            return MLF_E_STATE;
+        }
+        owner[n] = best;
+    }
+    std::vector<int> order(N);
+    for (int n = 0; n < N; ++n) order[n] = n;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return owner[a] < owner[b]; });
+    c->box_bases.clear();
+    c->box_ptr.assign(1, 0);
+    L.centre.clear();
+    std::vector<int> cell(0);
+    for (int t = 0; t < N; ++t) {
+        const int n = order[t];
+        if (t == 0 || owner[n] != owner[order[t - 1]]) {
+            if (t) c->box_ptr.push_back(t);
+            const long long idx = owner[n];
+            const int i = (int)(idx / ((long long)ne * ne)), j = (int)((idx / ne) % ne), k = (int)(idx % ne);
+            double cen[3];
+            centre_of(i, j, k, cen);
+            L.centre.insert(L.centre.end(), cen, cen + 3);
+            cell.push_back(i); cell.push_back(j); cell.push_back(k);
+        }
+        c->box_bases.push_back(n);
+    }
+    c->box_ptr.push_back(N);
+    L.nb = (int)c->box_ptr.size() - 1;
+    L.parent.assign(L.nb, -1);
+    L.octant.assign(L.nb, 0);
+    c->lv[1].nb = 0;
+    c->lv[2].nb = 0;
+    c->box_of.assign(N, -1);
+    for (int b = 0; b < L.nb; ++b)
+        for (int t = c->box_ptr[b]; t < c->box_ptr[b + 1]; ++t) c->box_of[c->box_bases[t]] = b;
+    // far / near lists
+    const double ftol = lambda / 100.;
+    const int span = 2 * ne - 1;
+    std::unordered_map<long long, int> tid_of;
+    L.far_ptr.assign(1, 0);
+    L.far_src.clear();
+    L.far_tid.clear();
+    L.rab.clear();
+    c->near_ptr.assign(1, 0);
+    c->near_bases.clear();
+    c->nbox_ptr.assign(1, 0);
+    c->nbox_list.clear();
+    for (int i = 0; i < L.nb; ++i) {
+        const size_t near_start = c->near_bases.size();
+        for (int j = 0; j < L.nb; ++j) {
+            double rh[3];
+            for (int d = 0; d < 3; ++d) rh[d] = L.centre[3 * i + d] - L.centre[3 * j + d];
+            const double nh = std::sqrt(rh[0] * rh[0] + rh[1] * rh[1] + rh[2] * rh[2]);
+            if (nh >= 2 * lado - ftol) {
+                // grid offsets (the reference's lambda/100 dedup identifies the same vectors)
+                const long long key = ((long long)(cell[3 * j] - cell[3 * i] + ne - 1) * span +
+                                       (cell[3 * j + 1] - cell[3 * i + 1] + ne - 1)) * span +
+                                      (cell[3 * j + 2] - cell[3 * i + 2] + ne - 1);
+                auto it = tid_of.find(key);
+                int tid;
+                if (it == tid_of.end()) {
+                    tid = (int)(L.rab.size() / 3);
+                    tid_of.emplace(key, tid);
+                    L.rab.insert(L.rab.end(), rh, rh + 3);
+                } else {
+                    tid = it->second;
+                }
+                L.far_src.push_back(j);
+                L.far_tid.push_back(tid);
+            } else {
+                c->nbox_list.push_back(j);
+                c->near_bases.insert(c->near_bases.end(), c->box_bases.begin() + c->box_ptr[j],
+                                     c->box_bases.begin() + c->box_ptr[j + 1]);
+            }
+        }
+        L.far_ptr.push_back((int)L.far_src.size());
+        std::sort(c->near_bases.begin() + near_start, c->near_bases.end());
+        c->near_ptr.push_back((int)c->near_bases.size());
+        c->nbox_ptr.push_back((int)c->nbox_list.size());
+    }
+    L.ntrans = (int)(L.rab.size() / 3);
+    c->ia.assign(N + 1, 0);
+    for (int m = 0; m < N; ++m) {
+        const int b = c->box_of[m];
+        c->ia[m + 1] = c->ia[m] + (c->near_ptr[b + 1] - c->near_ptr[b]);
+    }
+    c->nnz = c->ia[N];
+    if (c->nnz > 2000000000LL) {
+        c->err = "near field larger than 2^31 entries";
+        return MLF_E_ARG;
+    }
+    c->ja.resize(c->nnz);
+    for (int m = 0; m < N; ++m) {
+        const int b = c->box_of[m];
+        std::copy(c->near_bases.begin() + c->near_ptr[b], c->near_bases.begin() + c->near_ptr[b + 1],
+                  c->ja.begin() + c->ia[m]);
+    }
+    return MLF_OK;
+}
+
 // ---------------------------------------------------------------------------
 // ILU(0)
 // ---------------------------------------------------------------------------

@@ -27,9 +27,9 @@ import ctypes as C
 
 import numpy as np
 
-from ._capi import CGS_STATUS, FLAG_LEGENDRE_RECURRENCE, PRECOND, MLFError, load
+from ._capi import CGS_STATUS, FLAG_DENSE_MOM, FLAG_FMM, FLAG_LEGENDRE_RECURRENCE, PRECOND, MLFError, load
 
-__all__ = ["RWG", "MLFMA", "MLFError", "FLAG_LEGENDRE_RECURRENCE", "ajustar_polariz", "direction"]
+__all__ = ["RWG", "MLFMA", "MoM", "FMM", "MLFError", "FLAG_LEGENDRE_RECURRENCE", "ajustar_polariz", "direction"]
 
 
 def _p(a):
@@ -303,6 +303,15 @@ class MLFMA:
         return dict(block=best.value, tile_cols=cols.value,
                     per_rhs_ms={int(b): float(t) for b, t in zip(cand, per)})
 
+    def precond_apply32(self, y):
+        """mlf_precond_apply32: the FP32 preconditioner of the mixed inner loop."""
+        y = np.asarray(y, dtype=np.complex128)
+        single = y.ndim == 1
+        Y = np.asfortranarray(y.reshape(self.N, -1))
+        X = np.zeros_like(Y, order="F")
+        _check(load().mlf_precond_apply32(self._h, _p(Y), _p(X), Y.shape[1]), self._h)
+        return X[:, 0] if single else X
+
     def solve_times(self):
         """Phase times (ms) of the last mixed solve run with profiling on:
         preconditioner, FP32 operator, orthogonalisation, total."""
@@ -411,3 +420,24 @@ class MLFMA:
         out = np.zeros((lv["nb"], 2, lv["K"]), dtype=np.complex128)
         _check(load().mlf_debug_field(self._h, int(level), int(which), _p(out)), self._h)
         return out
+
+
+class MoM(MLFMA):
+    """Dense method-of-moments operator on the GPU (MoM + MatxVec_MoM,
+    modMoM.f90:85-128, 273-277): the full impedance matrix in FP64 on the
+    device.  matvec, cgs / CGSold without preconditioner, excitation, rcs and
+    the FP64 monostatic modes work as for MLFMA; octree-based calls raise."""
+
+    def __init__(self, rwg: RWG, lam: float = 1.0):
+        super().__init__(rwg, lam=lam, ladomax=1.0, flags=FLAG_DENSE_MOM)
+
+
+class FMM(MLFMA):
+    """Single-level FMM (inicializar_FMM + MatxVec_FMM, modFMM.f90:170-268,
+    904-963): one grid level of boxes of side <= side * lambda (the
+    reference's is lambda / 2), far pairs translated directly; matvec,
+    ILU0 / ILUT / neighbourhood preconditioners, CGS, mixed solves and RCS as
+    for MLFMA."""
+
+    def __init__(self, rwg: RWG, lam: float = 1.0, side: float = 0.5):
+        super().__init__(rwg, lam=lam, ladomax=side, flags=FLAG_FMM)

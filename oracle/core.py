@@ -42,6 +42,8 @@ def lib():
         vp = C.c_void_p
         L.ora_create.restype = vp
         L.ora_create.argtypes = [C.c_int, C.c_int, C.c_int] + [vp] * 7 + [C.c_double, C.c_double, C.c_int, vp]
+        L.ora_create_fmm.restype = vp
+        L.ora_create_fmm.argtypes = [C.c_int, C.c_int, C.c_int] + [vp] * 7 + [C.c_double, C.c_double, C.c_int, vp]
         L.ora_free.argtypes = [vp]
         L.ora_nlev.argtypes = [vp]
         L.ora_nnz.argtypes = [vp]
@@ -90,7 +92,10 @@ class OracleError(RuntimeError):
 
 
 class OracleMLFMA:
-    def __init__(self, rwg: RWG, lam: float = 1.0, ladomax: float = 0.5, legendre_mode: int = 0):
+    def __init__(self, rwg: RWG, lam: float = 1.0, ladomax: float = 0.5, legendre_mode: int = 0,
+                 fmm: bool = False):
+        """fmm=True builds the single-level FMM of modFMM.f90 instead, with box
+        side ladomax * lambda as the criterion (the reference's is 0.5)."""
         L = lib()
         self.rwg = rwg
         self.lam = float(lam)
@@ -104,7 +109,8 @@ class OracleMLFMA:
         self._et = np.ascontiguousarray(rwg.e_t, dtype=np.int32)
         self._epo = np.ascontiguousarray(rwg.e_po, dtype=np.int32)
         st = C.c_int(0)
-        self._h = L.ora_create(rwg.N, rwg.T, rwg.P, _p(self._pc), _p(self._tb), _p(self._tbs), _p(self._el),
+        create = L.ora_create_fmm if fmm else L.ora_create
+        self._h = create(rwg.N, rwg.T, rwg.P, _p(self._pc), _p(self._tb), _p(self._tbs), _p(self._el),
                                _p(self._ec), _p(self._et), _p(self._epo), self.lam, float(ladomax),
                                int(legendre_mode), C.byref(st))
         self.status = st.value

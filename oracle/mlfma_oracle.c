@@ -730,6 +730,162 @@ Ctx* ora_create(int N, int T, int P, const double* p_coord, const double* t_bari
     return c;
 }
 
+/* inicializar_FMM, geomFMM, buscarFuncBases, hallar_n_multipolos_muestras,
+ * llenar_functransf (modFMM.f90:170-268, 278-469, 479-490, 650-778): the
+ * single-level FMM as a one-level tree (level 3 of this context, nlev = 3),
+ * so calc_rad, fill_trans, fill_near and ora_matvec (which receives from B
+ * when nlev = 3) apply unchanged.  Box side: ladomayor / ceiling(ladomayor /
+ * (side_lambda * lambda)); the reference uses side_lambda = 1/2
+ * (criterio_ladoW = lambda/2).  Boxes are visited z-major, then y, then x,
+ * from the corner (max + tol/2) downwards with offsets accumulated by
+ * repeated addition, and a basis belongs to the first box whose closed
+ * bounds contain its edge centre.  Far: |c_i - c_j| >= 2 side - lambda/100;
+ * displacements are deduplicated in order of first appearance (keyed here by
+ * their integer grid offsets, which the reference's lambda/100 tolerance
+ * identifies the same way).  Near rows: union of the near boxes' bases,
+ * sorted ascending as the MLFMA rows are (the reference keeps box order,
+ * which changes only the near sum's rounding). */
+Ctx* ora_create_fmm(int N, int T, int P, const double* p_coord, const double* t_baric,
+                    const double* t_baric_sub, const double* e_long, const double* e_centro,
+                    const int* e_t, const int* e_po, double lambda, double side_lambda,
+                    int legendre_mode, int* status) {
+    Ctx* c = xcalloc(1, sizeof(Ctx));
+    c->ph = phys_from_lambda(lambda);
+    c->ladomax = side_lambda;
+    c->legendre_mode = legendre_mode;
+    c->N = N; c->T = T; c->P = P;
+    c->p_coord = p_coord; c->t_baric = t_baric; c->t_baric_sub = t_baric_sub;
+    c->e_long = e_long; c->e_centro = e_centro; c->e_t = e_t; c->e_po = e_po;
+    c->ilu_status = -1;
+    int lim[6];
+    limites(e_centro, N, lim);
+    double maxX = e_centro[3 * lim[0]], minX = e_centro[3 * lim[1]];
+    double maxY = e_centro[3 * lim[2] + 1], minY = e_centro[3 * lim[3] + 1];
+    double maxZ = e_centro[3 * lim[4] + 2], minZ = e_centro[3 * lim[5] + 2];
+    double dX = maxX - minX, dY = maxY - minY, dZ = maxZ - minZ;
+    double mayor;
+    if (dX >= dY && dX >= dZ) mayor = dX;
+    else if (dY >= dX && dY >= dZ) mayor = dY;
+    else mayor = dZ;
+    double tol = lambda / 10000.;
+    mayor = mayor + tol;
+    tol = tol / 2.;
+    double corner[3] = {maxX + tol, maxY + tol, maxZ + tol};
+    int ne = (int)ceil(mayor / (side_lambda * lambda));
+    double lado = mayor / ne;
+    c->nlev = 3;
+    c->root_side = mayor;
+    Level* L = &c->lv[3];
+    L->side = lado;
+    double s3 = (double)sqrtf(3.0f), third = (double)(1.0f / 3.0f);
+    double kd = (2. * PI / lambda) * (s3 * lado);
+    L->L = (int)floor(kd + 6 * pow(kd, third));
+    L->nth = L->L; L->nph = 2 * L->L; L->K = L->nth * L->nph;
+    fill_kappas(L);
+    /* geomFMM: boxes in loop order, each takes the remaining bases inside it */
+    int* rem = malloc(sizeof(int) * N);
+    int* rest = malloc(sizeof(int) * N);
+    for (int i = 0; i < N; i++) rem[i] = i;
+    int nrem = N;
+    IVec lb = {0}, lp = {0};
+    iv_push(&lp, 0);
+    double dz = 0.;
+    for (int i = 0; i < ne; i++) {
+        double dy = 0.;
+        for (int j = 0; j < ne; j++) {
+            double dx = 0.;
+            for (int k = 0; k < ne; k++) {
+                double esq[3] = {corner[0] - dx, corner[1] - dy, corner[2] - dz};
+                double cen[3] = {esq[0] - lado / 2., esq[1] - lado / 2., esq[2] - lado / 2.};
+                double lq = lado / 2.;
+                double xmax = cen[0] + lq, xmin = cen[0] - lq, ymax = cen[1] + lq, ymin = cen[1] - lq;
+                double zmax = cen[2] + lq, zmin = cen[2] - lq;
+                int nf = 0, nr = 0;
+                for (int t = 0; t < nrem; t++) {
+                    const double* e = e_centro + 3 * rem[t];
+                    if (e[0] <= xmax && e[0] >= xmin && e[1] <= ymax && e[1] >= ymin && e[2] <= zmax && e[2] >= zmin) {
+                        iv_push(&lb, rem[t]);
+                        nf++;
+                    } else {
+                        rest[nr++] = rem[t];
+                    }
+                }
+                if (nf > 0) {
+                    lv_append(L, cen, -1);
+                    iv_push(&lp, lb.n);
+                    memcpy(rem, rest, sizeof(int) * nr);
+                    nrem = nr;
+                }
+                dx = dx + lado;
+            }
+            dy = dy + lado;
+        }
+        dz = dz + lado;
+    }
+    free(rem); free(rest);
+    c->box_bases = lb.b; c->box_ptr = lp.b;
+    c->box_of = malloc(sizeof(int) * N);
+    for (int b = 0; b < L->nb; b++)
+        for (int t = c->box_ptr[b]; t < c->box_ptr[b + 1]; t++) c->box_of[c->box_bases[t]] = b;
+    size_t sz = (size_t)L->nb * 2 * L->K;
+    L->C = xcalloc(sz, sizeof(cplx)); L->B = xcalloc(sz, sizeof(cplx)); L->A = xcalloc(sz, sizeof(cplx));
+    calc_rad(c);
+    /* llenar_functransf */
+    double ftol = lambda / 100.;
+    int span = 2 * ne - 1;
+    int* tid_of = malloc(sizeof(int) * (size_t)span * span * span);
+    for (size_t q = 0; q < (size_t)span * span * span; q++) tid_of[q] = -1;
+    L->far_ptr = xcalloc(L->nb + 1, sizeof(int));
+    IVec fs = {0}, ft = {0}, nearb = {0}, nearp = {0};
+    iv_push(&nearp, 0);
+    double* rab = NULL;
+    int cont = 0;
+    for (int i = 0; i < L->nb; i++) {
+        int nstart = nearb.n;
+        for (int j = 0; j < L->nb; j++) {
+            double rh[3];
+            for (int d = 0; d < 3; d++) rh[d] = L->centre[3 * i + d] - L->centre[3 * j + d];
+            double nh = sqrt(rh[0] * rh[0] + rh[1] * rh[1] + rh[2] * rh[2]);
+            if (nh >= 2 * lado - ftol) {
+                int o[3];
+                for (int d = 0; d < 3; d++) o[d] = (int)lround(rh[d] / lado) + ne - 1;
+                size_t key = ((size_t)o[0] * span + o[1]) * span + o[2];
+                int k = tid_of[key];
+                if (k < 0) {
+                    k = cont++;
+                    tid_of[key] = k;
+                    rab = realloc(rab, sizeof(double) * 3 * cont);
+                    memcpy(rab + 3 * k, rh, sizeof(rh));
+                }
+                iv_push(&fs, j);
+                iv_push(&ft, k);
+            } else {
+                for (int t = c->box_ptr[j]; t < c->box_ptr[j + 1]; t++) iv_push(&nearb, c->box_bases[t]);
+            }
+        }
+        L->far_ptr[i + 1] = fs.n;
+        int cnt = nearb.n - nstart;
+        int* a = nearb.b + nstart;
+        for (int t = 1; t < cnt; t++) {
+            int v = a[t], q = t - 1;
+            while (q >= 0 && a[q] > v) { a[q + 1] = a[q]; q--; }
+            a[q + 1] = v;
+        }
+        iv_push(&nearp, nearb.n);
+    }
+    free(tid_of);
+    L->far_src = fs.b ? fs.b : xcalloc(1, sizeof(int));
+    L->far_tid = ft.b ? ft.b : xcalloc(1, sizeof(int));
+    L->ntrans = cont;
+    L->rab = rab ? rab : xcalloc(3, sizeof(double));
+    c->near_ptr = nearp.b;
+    c->near_bases = nearb.b;
+    fill_trans(c);
+    fill_near(c);
+    *status = 0;
+    return c;
+}
+
 /* ------------------------------------------------------------------ */
 /* matvec                                                               */
 /* ------------------------------------------------------------------ */

@@ -142,3 +142,28 @@ def test_own_box_inverse_apply(ico4):
         ref[own] = np.linalg.solve(Z[own][:, own].toarray(), y[own])
     assert _rel(x, ref) < 1e-10
     assert m.nearinv() == 0   # back to the full neighbourhood for the other tests
+
+
+@pytest.mark.parametrize("ncols", [1, 6, 12, 40])
+def test_own_box_fp32_block_apply(ico4, ncols):
+    """The FP32 own-box preconditioner of the mixed inner loop (per-box GEMMs
+    for blocks of columns, 8- and 32-column tiles) against numpy block
+    solves on the same near field; FP32 values and sums, so 1e-4 relative."""
+    _, m, o = ico4
+    assert m.nearinv(own_only=True) == 0
+    try:
+        ia, ja, z = m.near_csr()
+        import scipy.sparse as sps
+        Z = sps.csr_matrix((z.astype(np.complex128), ja - 1, ia - 1), shape=(m.N, m.N))
+        ptr, bases = o.leaf_boxes()
+        rng = np.random.default_rng(ncols)
+        Y = rng.standard_normal((m.N, ncols)) + 1j * rng.standard_normal((m.N, ncols))
+        X = m.precond_apply32(Y).reshape(m.N, ncols)
+        ref = np.zeros_like(Y)
+        for b in range(len(ptr) - 1):
+            own = bases[ptr[b]:ptr[b + 1]]
+            ref[own] = np.linalg.solve(Z[own][:, own].toarray(), Y[own])
+        for k in range(ncols):
+            assert _rel(X[:, k], ref[:, k]) < 1e-4
+    finally:
+        assert m.nearinv() == 0
