@@ -256,6 +256,39 @@ def batched_rcs_sample(seq_angles=3, block=0, maxit=4000):
     return out
 
 
+def profile_fp32_block(nrhs, steps):
+    """Profiling aid (not the bench line): the FP32 operator on `nrhs` random
+    columns of a 30720-RWG spheroid with the 122880-RWG spheroid's mesh density
+    (icosphere-5, semi-axes 1.5 x 0.375 x 0.375 lambda, so ~145 bases per leaf
+    box as in the 722-RHS workload) -- small enough for multi-pass ncu."""
+    import ctypes
+    import torch
+    from lywell_gb300 import MLFMA, RWG, _capi, meshes
+
+    tris = meshes.spheroid(5, (1.5, 0.375, 0.375), noise=0.005, seed=1234)
+    m = MLFMA(RWG(tris), lam=1.0, ladomax=0.25)
+    lib = _capi.load()
+    X = torch.randn(nrhs, m.N, dtype=torch.complex128, device="cuda")
+    Y = torch.empty_like(X)
+    stream = torch.cuda.Stream()            # a real stream handle (the default stream's is 0)
+    torch.cuda.set_stream(stream)
+    s = stream.cuda_stream
+    call = lambda: lib.mlf_matvec32_device(m.handle, ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(Y.data_ptr()),
+                                           nrhs, m.N, ctypes.c_void_p(s))
+    for _ in range(2):
+        assert call() == 0
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        call()
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "fp32 operator", "N": m.N, "nrhs": nrhs, "near_nnz": m.nnz,
+                      "ms_per_call": e0.elapsed_time(e1) / steps}), flush=True)
+    m.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -267,9 +300,14 @@ def main():
     ap.add_argument("--no-time-to-rcs", action="store_true")
     ap.add_argument("--rcs-maxit", type=int, default=4000)
     ap.add_argument("--no-batched", action="store_true", help="skip the 722-RHS spheroid sweep sample")
+    ap.add_argument("--profile-fp32-block", type=int, default=0,
+                    help="profiling aid: time the FP32 operator on this many columns of a small spheroid and exit")
     ap.add_argument("--seq-angles", type=int, default=3)
     ap.add_argument("--block", type=int, default=0, help="RHS per block of the batched sweep (0: autotuned)")
     args = ap.parse_args()
+    if args.profile_fp32_block > 0:
+        profile_fp32_block(args.profile_fp32_block, args.steps)
+        return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, wl)

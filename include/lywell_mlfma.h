@@ -174,7 +174,7 @@ int mlf_cgs(mlf_ctx* ctx, const double* b, const double* x0, double tol, int max
 /* Solve Z_MLFMA x = b for nrhs columns.  mode 0: CGS on the FP64 operator
  * (exactly mlf_cgs).  mode 1: mixed precision — iterative refinement whose
  * residual r = b - Z x is formed with the FP64 operator and whose
- * corrections come from one right-preconditioned GMRES(m) cycle (m = 400 by
+ * corrections come from one right-preconditioned GMRES(m) cycle (m = 800 by
  * default, mlf_set_gmres_restart) on the FP32
  * operator (patterns, translations, interpolation and fields in float;
  * complex(4) near field), stopped when its residual estimate drops below
@@ -189,6 +189,11 @@ int mlf_solve(mlf_ctx* ctx, const double* b, const double* x0, double tol, int m
 /* Restart length m of mode 1's GMRES cycles (4..2000; memory (m+1) N nrhs
  * complex(8) values). */
 int mlf_set_gmres_restart(mlf_ctx* ctx, int m);
+
+/* Classical Gram-Schmidt passes per Arnoldi step of mode 1 (1, the default:
+ * one pass, FP32 orthogonality losses left to the FP64 refinement; 2 = CGS2,
+ * twice the basis traffic). */
+int mlf_set_gs_passes(mlf_ctx* ctx, int passes);
 
 /* Phase times (ms) of the last mixed-precision solve run while profiling was
  * on (mlf_set_profiling): out4 = {preconditioner, FP32 operator,

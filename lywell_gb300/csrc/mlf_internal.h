@@ -91,7 +91,8 @@ struct Ctx {
     int dense = 0;                    // dense MoM operator instead of the octree (MLF_FLAG_DENSE_MOM)
     double2* dZdense = nullptr;       // N x N row-major, FP64
     int mv_prec = 0;                  // operator precision used by device_matvec: 0 FP64, 1 FP32
-    int gmres_m = 400;                // restart length of the mixed-precision GMRES cycles
+    int gmres_m = 800;                // restart length of the mixed-precision GMRES cycles
+    int gs_passes = 1;                // classical Gram-Schmidt passes per Arnoldi step (1 or 2)
     Mixed32 m32;
     cudaStream_t stream = nullptr;
     std::string err;

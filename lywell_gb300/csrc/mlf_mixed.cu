@@ -775,7 +775,7 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
             }
             if (prof) cudaEventRecord(c->sev[2], s);
             std::vector<double2> hsum((size_t)(j + 1) * nrhs, make_double2(0, 0));
-            for (int pass = 0; pass < 2; ++pass) {
+            for (int pass = 0; pass < c->gs_passes; ++pass) {
                 k_mdot32b<<<dim3(md_chunks, nrhs), 256, 0, s>>>(N, nrhs, j + 1, V, V1, w32, partial);
                 k_reduce_partials_n<<<((j + 1) * nrhs + 127) / 128, 128, 0, s>>>((j + 1) * nrhs, md_chunks, partial,
                                                                                   dred);
@@ -873,6 +873,12 @@ extern "C" int mlf_solve_times(mlf_ctx* h, double* out4) {
 int mlf_set_gmres_restart(mlf_ctx* h, int m) {
     if (!h || m < 4 || m > 2000) return MLF_E_ARG;
     h->c.gmres_m = m;
+    return MLF_OK;
+}
+
+int mlf_set_gs_passes(mlf_ctx* h, int passes) {
+    if (!h || passes < 1 || passes > 2) return MLF_E_ARG;
+    h->c.gs_passes = passes;
     return MLF_OK;
 }
 

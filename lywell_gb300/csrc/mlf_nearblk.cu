@@ -141,7 +141,11 @@ __device__ __forceinline__ void acc_zero(float2 (&acc)[2][TC]) {
         for (int u = 0; u < TC; ++u) acc[a][u] = make_float2(0.f, 0.f);
 }
 
-// y(:, c0 : c0 + 8 TC) += Z_near x for one 64-row tile of one leaf box
+// y(:, c0 : c0 + 8 TC) += Z_near x for one 64-row tile of one leaf box.
+// The chunks of all near boxes form one sequence; the next chunk's Z and x
+// values are loaded into registers while the current one is multiplied out
+// of shared memory (software double buffering), so the global loads overlap
+// the FMAs instead of stalling between barriers.
 template <int TC>
 __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2* __restrict__ tiles,
                                                     const int* __restrict__ box_ptr, const int* __restrict__ nbox_ptr,
@@ -149,19 +153,78 @@ __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2
                                                     const long long* __restrict__ blk_off,
                                                     const float2* __restrict__ Zblk, const float2* __restrict__ xs,
                                                     const int* __restrict__ perm, double2* __restrict__ y) {
+    constexpr int NC = 8 * TC;
+    constexpr int ZPT = NBK_KC * NBK_ROWS / 256;   // Z values per thread per chunk
+    constexpr int XPT = NBK_KC * NC / 256;         // x values per thread per chunk
     __shared__ __align__(16) BlkTile<TC> sm;
     const int2 tl = tiles[blockIdx.x];
     const int i = tl.x, r0 = tl.y, c0 = blockIdx.y * 8 * TC;
     const int ni = box_ptr[i + 1] - box_ptr[i];
+    const int tid = threadIdx.x, ty = tid >> 3, tx = tid & 7;
     float2 acc[2][TC];
     acc_zero<TC>(acc);
-    for (int e = nbox_ptr[i]; e < nbox_ptr[i + 1]; ++e) {
-        const int j = nbox_list[e];
+    const int e_end = nbox_ptr[i + 1];
+    // chunk cursor
+    int e = nbox_ptr[i], t0 = 0;
+    float2 zr[ZPT], xr[XPT];
+    auto load = [&](int ec, int tc) {
+        const int j = nbox_list[ec];
         const int j0 = box_ptr[j], nj = box_ptr[j + 1] - j0;
-        blk_mac<TC, false, false, false>(acc, sm, Zblk + blk_off[e], ni, r0, ni, nj, xs + (size_t)j0 * nrhs, nrhs, c0,
-                                         nrhs);
+        const float2* zb = Zblk + blk_off[ec];
+#pragma unroll
+        for (int u = 0; u < ZPT; ++u) {
+            const int q = tid + 256 * u;
+            const int k = q / NBK_ROWS, p = q - k * NBK_ROWS;
+            const int t = tc + k, row = r0 + p;
+            zr[u] = (t < nj && row < ni) ? zb[(size_t)t * ni + row] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < XPT; ++u) {
+            const int q = tid + 256 * u;
+            const int k = q / NC, cc = q - k * NC;
+            const int t = tc + k, col = c0 + cc;
+            xr[u] = (t < nj && col < nrhs) ? xs[(size_t)(j0 + t) * nrhs + col] : make_float2(0.f, 0.f);
+        }
+    };
+    auto next = [&](int& ec, int& tc) {
+        const int j = nbox_list[ec];
+        const int nj = box_ptr[j + 1] - box_ptr[j];
+        tc += NBK_KC;
+        if (tc >= nj) { ++ec; tc = 0; }
+    };
+    if (e < e_end) load(e, t0);
+    while (e < e_end) {
+#pragma unroll
+        for (int u = 0; u < ZPT; ++u) {
+            const int q = tid + 256 * u;
+            sm.Zs[q / NBK_ROWS][q % NBK_ROWS] = zr[u];
+        }
+#pragma unroll
+        for (int u = 0; u < XPT; ++u) {
+            const int q = tid + 256 * u;
+            sm.Xs[q / NC][q % NC] = xr[u];
+        }
+        __syncthreads();
+        next(e, t0);
+        if (e < e_end) load(e, t0);
+#pragma unroll 8
+        for (int k = 0; k < NBK_KC; ++k) {
+            const float4 zz = *reinterpret_cast<const float4*>(&sm.Zs[k][2 * ty]);
+#pragma unroll
+            for (int u = 0; u < TC; ++u) {
+                const float2 xv = sm.Xs[k][tx * TC + u];
+                acc[0][u].x = fmaf(zz.x, xv.x, acc[0][u].x);
+                acc[0][u].x = fmaf(-zz.y, xv.y, acc[0][u].x);
+                acc[0][u].y = fmaf(zz.x, xv.y, acc[0][u].y);
+                acc[0][u].y = fmaf(zz.y, xv.x, acc[0][u].y);
+                acc[1][u].x = fmaf(zz.z, xv.x, acc[1][u].x);
+                acc[1][u].x = fmaf(-zz.w, xv.y, acc[1][u].x);
+                acc[1][u].y = fmaf(zz.z, xv.y, acc[1][u].y);
+                acc[1][u].y = fmaf(zz.w, xv.x, acc[1][u].y);
+            }
+        }
+        __syncthreads();
     }
-    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
         const int row = r0 + 2 * ty + a;

@@ -19,7 +19,8 @@ module lywell_mlfma_cabi
     implicit none
 
     integer(c_int), parameter :: MLF_OK = 0, MLF_E_ARG = -1, MLF_E_TOO_SMALL = -2, MLF_E_CUDA = -3
-    integer(c_int), parameter :: MLF_FLAG_LEGENDRE_RECURRENCE = 1
+    integer(c_int), parameter :: MLF_FLAG_LEGENDRE_RECURRENCE = 1, MLF_FLAG_DENSE_MOM = 2, MLF_FLAG_FMM = 4
+    integer(c_int), parameter :: MLF_PRECOND_NONE = 0, MLF_PRECOND_ILU0 = 1, MLF_PRECOND_NEARINV = 2
 
     ! context used by matxvec_gpu (the reference's module state is single-instance too)
     type(c_ptr) :: mlf_current = c_null_ptr
@@ -95,6 +96,42 @@ module lywell_mlfma_cabi
             complex(c_double_complex), intent(out) :: x(*)
             integer(c_int), intent(out) :: iters(*), status_out(*)
             real(c_double), intent(out) :: relres(*)
+        end function
+
+        integer(c_int) function mlf_ilut(ctx, fill_in_prc, droptol, ierr) bind(C)
+            import :: c_int, c_double, c_ptr
+            type(c_ptr), value :: ctx
+            real(c_double), value :: fill_in_prc, droptol
+            integer(c_int), intent(out) :: ierr
+        end function
+
+        integer(c_int) function mlf_nearinv(ctx, bad_box) bind(C)
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), intent(out) :: bad_box
+        end function
+
+        integer(c_int) function mlf_solve(ctx, b, x0, tol, maxit, nrhs, precond_kind, mode, inner_tol, &
+                                          x, iters, relres, status_out, outer) bind(C)
+            import :: c_int, c_double, c_double_complex, c_ptr
+            type(c_ptr), value :: ctx
+            complex(c_double_complex), intent(in) :: b(*)
+            type(c_ptr), value :: x0
+            real(c_double), value :: tol, inner_tol
+            integer(c_int), value :: maxit, nrhs, precond_kind, mode
+            complex(c_double_complex), intent(out) :: x(*)
+            integer(c_int), intent(out) :: iters(*), status_out(*), outer
+            real(c_double), intent(out) :: relres(*)
+        end function
+
+        integer(c_int) function mlf_monostatic(ctx, nang, phis, hh, ctte_re, ctte_im, tol, maxit, &
+                                               precond_kind, mode, block, sigma, iters, status_out) bind(C)
+            import :: c_int, c_double, c_ptr
+            type(c_ptr), value :: ctx, phis
+            integer(c_int), value :: nang, hh, maxit, precond_kind, mode, block
+            real(c_double), value :: ctte_re, ctte_im, tol
+            real(c_double), intent(out) :: sigma(*)
+            integer(c_int), intent(out) :: iters(*), status_out(*)
         end function
 
         integer(c_int) function mlf_excitation(ctx, dirs, pols, ctte_re, ctte_im, nrhs, b) bind(C)

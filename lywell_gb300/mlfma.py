@@ -322,6 +322,9 @@ class MLFMA:
     def set_gmres_restart(self, m: int):
         _check(load().mlf_set_gmres_restart(self._h, int(m)), self._h)
 
+    def set_gs_passes(self, passes: int):
+        _check(load().mlf_set_gs_passes(self._h, int(passes)), self._h)
+
     def matvec32(self, x):
         x = np.asarray(x, dtype=np.complex128)
         single = x.ndim == 1
