@@ -315,23 +315,27 @@ int mlf_mlp_train(mlf_mlp* net, const float* X, const float* T, long long ntok, 
                   unsigned long long seed, float* loss_hist);
 
 /* ---- Learned near-field preconditioner: tokens and installation -----------
- * A token is one entry (p, q) of a leaf box's own near-field block, in
- * box-major, row-major block order.  With s_p = 1 / sqrt(Z_pp) and
- * Zh = S Z S, its 16 features are: Re, Im, |.| of Zh_pq, [p == q], the edge
- * centre offset r_q - r_p (3) and its length in wavelengths, l_p, l_q in
- * wavelengths, n_b / 100, the mean |Zh| of row p and of column q, the phase
- * (Re, Im) of Z_pp, 1.  Targets (2) are Re, Im of M_pq / (s_p s_q) for an
- * exact preconditioner M: target 1 = the own-box inverse (after
- * mlf_nearinv_own), 2 = the rows of the neighbourhood inverse restricted to
- * the box's own columns (after mlf_nearinv); target 0 = features only.
- * X (16 floats per token), T (2 per token): device arrays of capacity cap
- * tokens; X = NULL returns the token count only.
- * mlf_lp_install replaces the context's preconditioner by the network's
- * prediction, M_pq = s_p net(features)_pq s_q, applied like the own-box
- * inverse (precond_kind MLF_PRECOND_NEARINV); *nonfinite counts outputs
- * that were not finite (set to zero).  No counterpart in the reference. */
-int mlf_lp_tokens(mlf_ctx* ctx, int target, float* X, float* T, long long cap, long long* ntok);
-int mlf_lp_install(mlf_ctx* ctx, mlf_mlp* net, int* nonfinite);
+ * Base: the exact neighbourhood inverse M1 (mlf_nearinv, 27-box
+ * neighbourhoods).  The network predicts, per near-field entry (row m,
+ * column j), the correction D = M2 - M1 towards the inverse over the 2-ring
+ * (125-box) neighbourhood restricted to the same pattern, in units of
+ * s_m s_j, s_m = 1/sqrt(Z_mm).  Token features (16 floats, in the near CSR's
+ * entry order): Re, Im of s_m Z_mj s_j; Re, Im, |.| of M1_mj / (s_m s_j);
+ * [same leaf box]; [m == j]; (r_j - r_m) / lambda (3) and its length; the
+ * leaf-cell distance of the two boxes (max norm, Euclidean); n_own / 100 and
+ * near boxes / 27 of m's box; 1.  Target (2 floats): Re, Im of
+ * D_mj / (s_m s_j), the 2-ring inverses computed on the device (FP32
+ * elimination; bodies up to 55 000 unknowns).
+ * mlf_lp_tokens needs mlf_nearinv first; X (16 per token) and T (2 per
+ * token, with_target only) are device arrays of capacity cap; X = NULL
+ * returns the token count (the near nnz) only; *bad_box: first 2-ring block
+ * that was singular, 0 if none.
+ * mlf_lp_install: M = M1 + scale * s_m s_j net(tokens), on M1's pattern,
+ * applied as MLF_PRECOND_NEARINV; repeated installs start from the exact M1;
+ * mlf_nearinv restores it.  *nonfinite counts non-finite network outputs
+ * (set to zero).  No counterpart in the reference. */
+int mlf_lp_tokens(mlf_ctx* ctx, int with_target, float* X, float* T, long long cap, long long* ntok, int* bad_box);
+int mlf_lp_install(mlf_ctx* ctx, mlf_mlp* net, float scale, int* nonfinite);
 
 #ifdef __cplusplus
 }

@@ -49,8 +49,8 @@ SIGNATURES = {
     "mlf_mlp_get_params": (C.c_int, [vp, vp, vp]),
     "mlf_mlp_forward": (C.c_int, [vp, vp, C.c_longlong, vp, vp]),
     "mlf_mlp_grad": (C.c_int, [vp, vp, vp, C.c_longlong, vp, vp]),
-    "mlf_lp_tokens": (C.c_int, [vp, C.c_int, vp, vp, C.c_longlong, vp]),
-    "mlf_lp_install": (C.c_int, [vp, vp, vp]),
+    "mlf_lp_tokens": (C.c_int, [vp, C.c_int, vp, vp, C.c_longlong, vp, vp]),
+    "mlf_lp_install": (C.c_int, [vp, vp, C.c_float, vp]),
     "mlf_mlp_train": (C.c_int, [vp, vp, vp, C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_ulonglong, vp]),
     "mlf_matvec32_device": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, vp]),
     "mlf_nearinv_values": (C.c_int, [vp, vp]),

@@ -649,7 +649,7 @@ void device_free(Ctx* c) {
     F(c->dR); F(c->dperm); F(c->dbox_ptr); F(c->dbox_of_sorted); F(c->dia); F(c->dja); F(c->dZ);
     F(c->dp_coord); F(c->dt_baric); F(c->dt_baric_sub); F(c->de_long); F(c->de_centro); F(c->de_t);
     F(c->de_po); F(c->dalu); F(c->djlu); F(c->dju); F(c->dlvl_rows_f); F(c->dlvl_rows_b);
-    F(c->dwork); F(c->dscal); F(c->dflags); F(c->dx_io); F(c->dy_io); F(c->dMinv); F(c->dZd); F(c->dboff); F(c->dMinv32); F(c->dpre_xs); F(c->dZdense);
+    F(c->dwork); F(c->dscal); F(c->dflags); F(c->dx_io); F(c->dy_io); F(c->dMinv); F(c->dZd); F(c->dboff); F(c->dMinv32); F(c->dpre_xs); F(c->dZdense); F(c->dMinv_base);
     mixed_free(c);
     near_blocks_free(c);
     for (int i = 0; i < 8; ++i)

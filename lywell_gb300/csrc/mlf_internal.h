@@ -142,6 +142,7 @@ struct Ctx {
     double2* dMinv = nullptr;         // CSR values, or compact own-box blocks when nearinv_own
     long long* dboff = nullptr;       // own-box block offsets
     float2* dMinv32 = nullptr;        // FP32 copy for the FP32 inner solves
+    double2* dMinv_base = nullptr;    // the exact neighbourhood inverse kept under a learned correction
     long long minv_len = 0;
     float2* dpre_xs = nullptr;        // box-sorted copy of the preconditioner input (blocks of columns)
     size_t pre_xs_cap = 0;
@@ -210,7 +211,7 @@ int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const fl
                         cudaStream_t s);
 void near_blocks_free(Ctx* c);
 int near_blocks_ensure(Ctx* c);
-int lp_tokens(Ctx* c, int target, float* X, float* T, long long cap, long long* ntok);
+int lp_tokens(Ctx* c, int with_target, float* X, float* T, long long cap, long long* ntok, int* bad_box);
 int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* best_cols, float* per_rhs_ms);
 int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
                        int* iters, double* relres, int precond, int* status, double inner_tol, int* outer);

@@ -1,28 +1,32 @@
-// Learned near-field preconditioner: tokens, targets and installation.
+// Learned near-field preconditioner: targets, tokens and installation.
 //
-// A token is one entry (p, q) of a leaf box's own near-field block Z_bb
-// (llenarZesparcida's values, complex(4)), in the own-box compact order
-// (box-major, row-major n_b x n_b blocks, offsets boff).  With the symmetric
-// diagonal scaling s_p = 1 / sqrt(Z_pp) (principal root) and Zh = S Z S:
-//   features (16): Re Zh_pq, Im Zh_pq, |Zh_pq|, [p == q],
-//                  (r_q - r_p) / lambda (3), |r_q - r_p| / lambda,
-//                  l_p / lambda, l_q / lambda, n_b / 100,
-//                  sum_q' |Zh_pq'| / n_b, sum_p' |Zh_p'q| / n_b,
-//                  Re, Im of Z_pp / |Z_pp|, 1
-//   target  (2):   Re, Im of Mh_pq = M_pq / (s_p s_q) for an exact
-//                  preconditioner M: the own-box inverse, or the rows of the
-//                  leaf box's neighbourhood inverse restricted to its own
-//                  columns.
-// Installed, the network's outputs Mh give M_pq = s_p Mh_pq s_q in the
-// own-box block storage, so the preconditioner is the same linear,
-// block-diagonal apply as the own-box inverse.  No counterpart in the
-// reference.
+// Base: the exact neighbourhood inverse M1 (mlf_nearinv): for each leaf box,
+// the rows of inv(Z[S1, S1]) of its own bases, S1 = the bases of the 27-box
+// neighbourhood (the near list), on the near CSR pattern.  The rows of the
+// inverse over the larger 2-ring neighbourhood S2 (boxes within two leaf
+// cells in every axis, 125 boxes) restricted to the same pattern, M2, make a
+// better preconditioner but cost (125/27)^3 ~ 100 times more to build.  The
+// network learns the correction D = M2 - M1 from local quantities, so the
+// installed preconditioner M = M1 + scale * net(tokens) keeps M1's pattern,
+// apply cost and linearity.
+//
+// A token is one near-field entry (row m, column j).  With s_m = 1/sqrt(Z_mm)
+// (principal root) the scaled quantities are Zh = s_m Z_mj s_j,
+// M1h = M1_mj / (s_m s_j), Dh = D_mj / (s_m s_j); features (16):
+//   Re Zh, Im Zh, Re M1h, Im M1h, |M1h|, [same leaf box], [m == j],
+//   (r_j - r_m) / lambda (3), |r_j - r_m| / lambda,
+//   leaf-cell distance of the two boxes (max norm, Euclidean),
+//   n_own(box of m) / 100, near boxes of that box / 27, 1;
+// target (2): Re, Im of Dh.  No counterpart in the reference.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
+#include <unordered_map>
 #include <vector>
 
 #include "mlf_internal.h"
+#include "mlf_zmn.cuh"
 
 namespace mlf {
 
@@ -31,295 +35,477 @@ namespace mlf {
         if (!cuda_ok(c, (call), #call)) return MLF_E_CUDA;   \
     } while (0)
 
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 cdivf(float2 a, float2 b) {
+    const float d = b.x * b.x + b.y * b.y;
+    return make_float2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
 __device__ __forceinline__ float2 csqrt_inv(float2 z) {
-    // 1 / sqrt(z), principal branch
     const float r = sqrtf(sqrtf(z.x * z.x + z.y * z.y));
     const float th = 0.5f * atan2f(z.y, z.x);
     float sn, cs;
     sincosf(th, &sn, &cs);
     return make_float2(cs / r, -sn / r);
 }
-
-__device__ __forceinline__ float2 cmulf(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-
-// own block of box b: column-major n_b x n_b at Zblk + self_off[b]
-// s (per box-sorted position) = 1 / sqrt(Z_pp)
-__global__ void k_lp_scale(int nb, const int* __restrict__ box_ptr, const long long* __restrict__ self_off,
-                           const float2* __restrict__ Zblk, float2* __restrict__ s) {
-    const int b = blockIdx.x;
-    const int j0 = box_ptr[b], n = box_ptr[b + 1] - j0;
-    const float2* Zs = Zblk + self_off[b];
-    for (int p = threadIdx.x; p < n; p += blockDim.x) s[j0 + p] = csqrt_inv(Zs[(size_t)p * n + p]);
+__device__ __forceinline__ int find_sorted(const int* S, int n, int v) {
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        if (S[mid] == v) return mid;
+        if (S[mid] < v) lo = mid + 1; else hi = mid - 1;
+    }
+    return -1;
 }
 
-// features of every own-block entry of box b (one CTA per box)
-__global__ void k_lp_features(const int* __restrict__ box_ptr, const long long* __restrict__ self_off,
-                              const long long* __restrict__ tok_off, const float2* __restrict__ Zblk,
-                              const float2* __restrict__ s, const int* __restrict__ perm,
-                              const double* __restrict__ e_centro, const double* __restrict__ e_long, float inv_lambda,
-                              float* __restrict__ X) {
-    extern __shared__ float lp_sm[];
-    const int b = blockIdx.x;
-    const int j0 = box_ptr[b], n = box_ptr[b + 1] - j0;
-    const float2* Zs = Zblk + self_off[b];
-    float* rsum = lp_sm;
-    float* csum = lp_sm + n;
-    for (int p = threadIdx.x; p < n; p += blockDim.x) { rsum[p] = 0.f; csum[p] = 0.f; }
-    __syncthreads();
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        const int p = e / n, q = e - p * n;
-        const float2 zh = cmulf(cmulf(s[j0 + p], Zs[(size_t)q * n + p]), s[j0 + q]);
-        const float a = sqrtf(zh.x * zh.x + zh.y * zh.y);
-        atomicAdd(&rsum[p], a);
-        atomicAdd(&csum[q], a);
+// dense Z (complex(4), row-major N x N) for the 2-ring blocks
+__global__ void k_lp_dense(int N, const double* __restrict__ t_baric, const double* __restrict__ t_baric_sub,
+                           const double* __restrict__ p_coord, const int* __restrict__ e_t, const int* __restrict__ e_po,
+                           const double* __restrict__ e_long, double w, double w_smue, double c72,
+                           float2* __restrict__ Zd) {
+    const int m = blockIdx.x;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) {
+        const double2 v = zmn_mom(m, n, t_baric, t_baric_sub, p_coord, e_t, e_po, e_long, w, w_smue, c72);
+        Zd[(size_t)m * N + n] = make_float2((float)v.x, (float)v.y);
     }
+}
+
+// Rows of inv(Z[S2, S2]) for the own bases of box b, on the near pattern
+// (FP32 Gaussian elimination with partial pivoting on A^T, one CTA per box).
+__global__ void __launch_bounds__(256) k_ring_inverse32(int b0, int nb, const long long* __restrict__ ring_off,
+                                                        const int* __restrict__ ring_len,
+                                                        const int* __restrict__ ring_bases,
+                                                        const int* __restrict__ box_ptr, const int* __restrict__ perm,
+                                                        const float2* __restrict__ Zd, int N,
+                                                        const int* __restrict__ ia, const int* __restrict__ ja,
+                                                        size_t slab, float2* __restrict__ work,
+                                                        float2* __restrict__ M2, int* __restrict__ bad) {
+    const int b = b0 + blockIdx.x;
+    if (b >= nb) return;
+    const int tid = threadIdx.x, bd = blockDim.x;
+    const int n = ring_len[b];
+    const int* S = ring_bases + ring_off[b];
+    const int nown = box_ptr[b + 1] - box_ptr[b];
+    float2* At = work + (size_t)blockIdx.x * slab;
+    float2* X = At + (size_t)n * n;
+    for (size_t e = tid; e < (size_t)n * n; e += bd) {
+        const int pos = (int)(e / n), r = (int)(e - (size_t)pos * n);
+        At[e] = Zd[(size_t)S[r] * N + S[pos]];
+    }
+    for (int e = tid; e < n * nown; e += bd) X[e] = make_float2(0.f, 0.f);
     __syncthreads();
-    float* Xb = X + tok_off[b] * 16;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        const int p = e / n, q = e - p * n;
-        const float2 zpq = Zs[(size_t)q * n + p];
-        const float2 zh = cmulf(cmulf(s[j0 + p], zpq), s[j0 + q]);
-        const int gp = perm[j0 + p], gq = perm[j0 + q];
-        const float dx = (float)(e_centro[3 * gq] - e_centro[3 * gp]) * inv_lambda;
-        const float dy = (float)(e_centro[3 * gq + 1] - e_centro[3 * gp + 1]) * inv_lambda;
-        const float dz = (float)(e_centro[3 * gq + 2] - e_centro[3 * gp + 2]) * inv_lambda;
-        const float2 zd = Zs[(size_t)p * n + p];
-        const float zdn = sqrtf(zd.x * zd.x + zd.y * zd.y);
-        float* f = Xb + (size_t)e * 16;
+    for (int i = tid; i < nown; i += bd) {
+        const int pos = find_sorted(S, n, perm[box_ptr[b] + i]);
+        X[(size_t)pos * nown + i] = make_float2(1.f, 0.f);
+    }
+    __shared__ float s_val[8];
+    __shared__ int s_idx[8];
+    __shared__ int s_piv, s_sing;
+    if (tid == 0) s_sing = 0;
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        float best = -1.f;
+        int bi = n;
+        for (int i = k + tid; i < n; i += bd) {
+            const float2 a = At[(size_t)i * n + k];
+            const float v = a.x * a.x + a.y * a.y;
+            if (v > best) { best = v; bi = i; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffff, best, o);
+            const int oi = __shfl_xor_sync(0xffffffff, bi, o);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if ((tid & 31) == 0) { s_val[tid >> 5] = best; s_idx[tid >> 5] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+            float bv = s_val[0];
+            int bx = s_idx[0];
+            for (int w = 1; w < bd / 32; ++w)
+                if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bx)) { bv = s_val[w]; bx = s_idx[w]; }
+            s_piv = bx;
+            if (!(bv > 0.f)) s_sing = 1;
+        }
+        __syncthreads();
+        if (s_sing) break;
+        const int piv = s_piv;
+        if (piv != k) {
+            for (int j = tid; j < n; j += bd) {
+                const float2 t = At[(size_t)k * n + j];
+                At[(size_t)k * n + j] = At[(size_t)piv * n + j];
+                At[(size_t)piv * n + j] = t;
+            }
+            for (int j = tid; j < nown; j += bd) {
+                const float2 t = X[(size_t)k * nown + j];
+                X[(size_t)k * nown + j] = X[(size_t)piv * nown + j];
+                X[(size_t)piv * nown + j] = t;
+            }
+        }
+        __syncthreads();
+        const float2 d = At[(size_t)k * n + k];
+        for (int i = k + 1 + tid; i < n; i += bd) At[(size_t)i * n + k] = cdivf(At[(size_t)i * n + k], d);
+        __syncthreads();
+        const int rows = n - k - 1, wcols = (n - k - 1) + nown;
+        for (long long e = tid; e < (long long)rows * wcols; e += bd) {
+            const int i = k + 1 + (int)(e / wcols), jj = (int)(e % wcols);
+            const float2 f = At[(size_t)i * n + k];
+            float2* dst;
+            float2 src;
+            if (jj < n - k - 1) {
+                dst = &At[(size_t)i * n + k + 1 + jj];
+                src = At[(size_t)k * n + k + 1 + jj];
+            } else {
+                dst = &X[(size_t)i * nown + (jj - (n - k - 1))];
+                src = X[(size_t)k * nown + (jj - (n - k - 1))];
+            }
+            float2 v = *dst;
+            v.x -= f.x * src.x - f.y * src.y;
+            v.y -= f.x * src.y + f.y * src.x;
+            *dst = v;
+        }
+        __syncthreads();
+    }
+    if (s_sing) {
+        if (tid == 0) atomicMin(bad, b + 1);
+        return;
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        const float2 d = At[(size_t)k * n + k];
+        for (int j = tid; j < nown; j += bd) X[(size_t)k * nown + j] = cdivf(X[(size_t)k * nown + j], d);
+        __syncthreads();
+        for (int e = tid; e < k * nown; e += bd) {
+            const int i = e / nown, j = e % nown;
+            const float2 f = At[(size_t)i * n + k];
+            const float2 s = X[(size_t)k * nown + j];
+            float2 v = X[(size_t)i * nown + j];
+            v.x -= f.x * s.x - f.y * s.y;
+            v.y -= f.x * s.y + f.y * s.x;
+            X[(size_t)i * nown + j] = v;
+        }
+        __syncthreads();
+    }
+    // own row i, near column ja[q]: X[pos(ja[q]) * nown + i]
+    for (int i = 0; i < nown; ++i) {
+        const int g = perm[box_ptr[b] + i];
+        for (int q = ia[g] + tid; q < ia[g + 1]; q += bd) {
+            const int pos = find_sorted(S, n, ja[q]);
+            M2[q] = pos >= 0 ? X[(size_t)pos * nown + i] : make_float2(0.f, 0.f);
+        }
+    }
+}
+
+// s_m = 1/sqrt(Z_mm) from the near CSR diagonal
+__global__ void k_lp_scale(int N, const int* __restrict__ ia, const int* __restrict__ ja, const float2* __restrict__ Z,
+                           float2* __restrict__ s) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= N) return;
+    const int q = ia[m] + find_sorted(ja + ia[m], ia[m + 1] - ia[m], m);
+    s[m] = csqrt_inv(Z[q]);
+}
+
+// one warp per row m
+__global__ void k_lp_tokens(int N, const int* __restrict__ ia, const int* __restrict__ ja,
+                            const float2* __restrict__ Z, const double2* __restrict__ M1,
+                            const float2* __restrict__ M2, const float2* __restrict__ s,
+                            const int* __restrict__ box_of, const int* __restrict__ cell,
+                            const int* __restrict__ nown, const int* __restrict__ nnear,
+                            const double* __restrict__ e_centro, float inv_lambda, float* __restrict__ X,
+                            float* __restrict__ T) {
+    const int m = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (m >= N) return;
+    const int bm = box_of[m];
+    const float2 sm = s[m];
+    for (int q = ia[m] + lane; q < ia[m + 1]; q += 32) {
+        const int j = ja[q], bj = box_of[j];
+        const float2 ss = cmulf(sm, s[j]);
+        const float2 zh = cmulf(ss, Z[q]);
+        const float2 m1 = make_float2((float)M1[q].x, (float)M1[q].y);
+        const float2 m1h = cdivf(m1, ss);
+        const float dx = (float)(e_centro[3 * j] - e_centro[3 * m]) * inv_lambda;
+        const float dy = (float)(e_centro[3 * j + 1] - e_centro[3 * m + 1]) * inv_lambda;
+        const float dz = (float)(e_centro[3 * j + 2] - e_centro[3 * m + 2]) * inv_lambda;
+        const int cx = cell[3 * bj] - cell[3 * bm], cy = cell[3 * bj + 1] - cell[3 * bm + 1],
+                  cz = cell[3 * bj + 2] - cell[3 * bm + 2];
+        float* f = X + (size_t)q * 16;
         f[0] = zh.x;
         f[1] = zh.y;
-        f[2] = sqrtf(zh.x * zh.x + zh.y * zh.y);
-        f[3] = p == q ? 1.f : 0.f;
-        f[4] = dx;
-        f[5] = dy;
-        f[6] = dz;
-        f[7] = sqrtf(dx * dx + dy * dy + dz * dz);
-        f[8] = (float)e_long[gp] * inv_lambda;
-        f[9] = (float)e_long[gq] * inv_lambda;
-        f[10] = n * 0.01f;
-        f[11] = rsum[p] / n;
-        f[12] = csum[q] / n;
-        f[13] = zd.x / zdn;
-        f[14] = zd.y / zdn;
+        f[2] = m1h.x;
+        f[3] = m1h.y;
+        f[4] = sqrtf(m1h.x * m1h.x + m1h.y * m1h.y);
+        f[5] = bm == bj ? 1.f : 0.f;
+        f[6] = m == j ? 1.f : 0.f;
+        f[7] = dx;
+        f[8] = dy;
+        f[9] = dz;
+        f[10] = sqrtf(dx * dx + dy * dy + dz * dz);
+        f[11] = (float)max(abs(cx), max(abs(cy), abs(cz)));
+        f[12] = sqrtf((float)(cx * cx + cy * cy + cz * cz));
+        f[13] = nown[bm] * 0.01f;
+        f[14] = nnear[bm] * (1.f / 27.f);
         f[15] = 1.f;
-    }
-}
-
-// targets from the own-box inverse (compact row-major blocks at boff, FP64)
-__global__ void k_lp_target_own(const int* __restrict__ box_ptr, const long long* __restrict__ boff,
-                                const double2* __restrict__ M, const float2* __restrict__ s, float* __restrict__ T) {
-    const int b = blockIdx.x;
-    const int j0 = box_ptr[b], n = box_ptr[b + 1] - j0;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        const int p = e / n, q = e - p * n;
-        const double2 m = M[boff[b] + e];
-        const float2 sp = s[j0 + p], sq = s[j0 + q];
-        const float2 ss = cmulf(sp, sq);
-        const float den = ss.x * ss.x + ss.y * ss.y;
-        // m / (s_p s_q)
-        const float mx = (float)m.x, my = (float)m.y;
-        T[(boff[b] + e) * 2] = (mx * ss.x + my * ss.y) / den;
-        T[(boff[b] + e) * 2 + 1] = (my * ss.x - mx * ss.y) / den;
-    }
-}
-
-// targets from the neighbourhood inverse (full CSR values in near order),
-// restricted to the box's own columns
-__global__ void k_lp_target_nbhd(const int* __restrict__ box_ptr, const long long* __restrict__ boff,
-                                 const int* __restrict__ perm, const int* __restrict__ ia, const int* __restrict__ ja,
-                                 const double2* __restrict__ M, const float2* __restrict__ s, float* __restrict__ T) {
-    const int b = blockIdx.x;
-    const int j0 = box_ptr[b], n = box_ptr[b + 1] - j0;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        const int p = e / n, q = e - p * n;
-        const int m = perm[j0 + p], col = perm[j0 + q];
-        int lo = ia[m], hi = ia[m + 1] - 1;
-        double2 v = make_double2(0, 0);
-        while (lo <= hi) {
-            const int mid = (lo + hi) >> 1;
-            if (ja[mid] == col) { v = M[mid]; break; }
-            if (ja[mid] < col) lo = mid + 1; else hi = mid - 1;
+        if (T) {
+            const float2 d = make_float2(M2[q].x - m1.x, M2[q].y - m1.y);
+            const float2 dh = cdivf(d, ss);
+            T[2 * (size_t)q] = dh.x;
+            T[2 * (size_t)q + 1] = dh.y;
         }
-        const float2 ss = cmulf(s[j0 + p], s[j0 + q]);
-        const float den = ss.x * ss.x + ss.y * ss.y;
-        const float mx = (float)v.x, my = (float)v.y;
-        T[(boff[b] + e) * 2] = (mx * ss.x + my * ss.y) / den;
-        T[(boff[b] + e) * 2 + 1] = (my * ss.x - mx * ss.y) / den;
     }
 }
 
-// M_pq = s_p Mh_pq s_q into the own-box storage; counts non-finite outputs
-__global__ void k_lp_install(const int* __restrict__ box_ptr, const long long* __restrict__ boff,
-                             const float2* __restrict__ s, const float* __restrict__ Y, double2* __restrict__ M,
+// M = M1 + scale * s_m s_j (Y.x + j Y.y); counts non-finite outputs (set to zero)
+__global__ void k_lp_install(int N, const int* __restrict__ ia, const int* __restrict__ ja,
+                             const float2* __restrict__ s, const double2* __restrict__ M1,
+                             const float* __restrict__ Y, float scale, double2* __restrict__ M,
                              int* __restrict__ nonfinite) {
-    const int b = blockIdx.x;
-    const int j0 = box_ptr[b], n = box_ptr[b + 1] - j0;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        const int p = e / n, q = e - p * n;
-        const long long t = boff[b] + e;
-        float2 mh = make_float2(Y[2 * t], Y[2 * t + 1]);
-        if (!isfinite(mh.x) || !isfinite(mh.y)) {
+    const int m = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (m >= N) return;
+    const float2 sm = s[m];
+    for (int q = ia[m] + lane; q < ia[m + 1]; q += 32) {
+        float2 y = make_float2(Y[2 * (size_t)q], Y[2 * (size_t)q + 1]);
+        if (!isfinite(y.x) || !isfinite(y.y)) {
             atomicAdd(nonfinite, 1);
-            mh = make_float2(0.f, 0.f);
+            y = make_float2(0.f, 0.f);
         }
-        const float2 v = cmulf(cmulf(s[j0 + p], mh), s[j0 + q]);
-        M[t] = make_double2(v.x, v.y);
+        const float2 d = cmulf(cmulf(sm, s[ja[q]]), y);
+        M[q] = make_double2(M1[q].x + (double)(scale * d.x), M1[q].y + (double)(scale * d.y));
     }
 }
 
-struct LpLayout {
-    std::vector<long long> boff, self_off;
-    long long ntok = 0;
-    int nmax = 0;
+// ---------------------------------------------------------------------------
+
+struct LpHost {
+    std::vector<int> cell, nown, nnear, box_of;
 };
 
-static int lp_layout(Ctx* c, LpLayout& L) {
-    const int nb = (int)c->box_ptr.size() - 1;
-    L.boff.assign(nb + 1, 0);
-    L.self_off.assign(nb, -1);
-    long long off = 0;
+static int lp_host(Ctx* c, LpHost& H) {
+    const int nl = c->nlev;
+    const Level& leaf = c->lv[nl];
+    const int nb = leaf.nb;
+    double mn[3] = {1e300, 1e300, 1e300};
+    for (int b = 0; b < nb; ++b)
+        for (int d = 0; d < 3; ++d) mn[d] = std::min(mn[d], leaf.centre[3 * b + d]);
+    H.cell.resize(3 * (size_t)nb);
+    for (int b = 0; b < nb; ++b)
+        for (int d = 0; d < 3; ++d) H.cell[3 * b + d] = (int)std::lround((leaf.centre[3 * b + d] - mn[d]) / leaf.side);
+    H.nown.resize(nb);
+    H.nnear.resize(nb);
     for (int b = 0; b < nb; ++b) {
-        const long long n = c->box_ptr[b + 1] - c->box_ptr[b];
-        L.boff[b + 1] = L.boff[b] + n * n;
-        L.nmax = std::max<int>(L.nmax, (int)n);
-        for (int e = c->nbox_ptr[b]; e < c->nbox_ptr[b + 1]; ++e) {
-            const int j = c->nbox_list[e];
-            if (j == b) L.self_off[b] = off;
-            off += n * (c->box_ptr[j + 1] - c->box_ptr[j]);
-        }
-        if (L.self_off[b] < 0) {
-            c->err = "a leaf box is missing from its own near list";
-            return MLF_E_STATE;
-        }
+        H.nown[b] = c->box_ptr[b + 1] - c->box_ptr[b];
+        H.nnear[b] = c->nbox_ptr[b + 1] - c->nbox_ptr[b];
     }
-    L.ntok = L.boff[nb];
+    H.box_of = c->box_of;
     return MLF_OK;
 }
 
 struct LpDev {
-    long long* boff = nullptr;
-    long long* self_off = nullptr;
+    int *cell = nullptr, *nown = nullptr, *nnear = nullptr, *box_of = nullptr;
     float2* s = nullptr;
+    void release() {
+        for (void* p : {(void*)cell, (void*)nown, (void*)nnear, (void*)box_of, (void*)s})
+            if (p) cudaFree(p);
+        cell = nown = nnear = box_of = nullptr;
+        s = nullptr;
+    }
 };
 
-static int lp_upload(Ctx* c, const LpLayout& L, LpDev& D) {
-    const int nb = (int)c->box_ptr.size() - 1;
-    CK(cudaMalloc(&D.boff, (nb + 1) * sizeof(long long)));
-    CK(cudaMalloc(&D.self_off, nb * sizeof(long long)));
+static int lp_upload(Ctx* c, const LpHost& H, LpDev& D) {
+    auto up = [&](int** d, const std::vector<int>& v) -> bool {
+        if (!cuda_ok(c, cudaMalloc(d, std::max<size_t>(v.size(), 1) * sizeof(int)), "alloc")) return false;
+        return v.empty() || cuda_ok(c, cudaMemcpy(*d, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice), "copy");
+    };
+    if (!up(&D.cell, H.cell) || !up(&D.nown, H.nown) || !up(&D.nnear, H.nnear) || !up(&D.box_of, H.box_of))
+        return MLF_E_CUDA;
     CK(cudaMalloc(&D.s, (size_t)c->N * sizeof(float2)));
-    CK(cudaMemcpy(D.boff, L.boff.data(), (nb + 1) * sizeof(long long), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(D.self_off, L.self_off.data(), nb * sizeof(long long), cudaMemcpyHostToDevice));
-    k_lp_scale<<<nb, 128, 0, c->stream>>>(nb, c->dbox_ptr, D.self_off, c->dZblk, D.s);
+    k_lp_scale<<<(c->N + 255) / 256, 256, 0, c->stream>>>(c->N, c->dia, c->dja, c->dZ, D.s);
     CK(cudaGetLastError());
     return MLF_OK;
 }
 
-static void lp_free(LpDev& D) {
-    if (D.boff) cudaFree(D.boff);
-    if (D.self_off) cudaFree(D.self_off);
-    if (D.s) cudaFree(D.s);
+// M2 (near pattern, FP32) from the 2-ring inverses; bad: first singular box + 1
+static int lp_ring_targets(Ctx* c, const LpHost& H, float2* M2, int* bad_box) {
+    const int nl = c->nlev;
+    const int nb = c->lv[nl].nb;
+    const int N = c->N;
+    if ((size_t)N * N * sizeof(float2) > ((size_t)24 << 30)) {
+        c->err = "2-ring targets are generated on bodies up to 55 000 unknowns";
+        return MLF_E_ARG;
+    }
+    // 2-ring lists: boxes within two cells (max norm), their bases sorted
+    std::unordered_map<long long, int> at;
+    auto key = [](int x, int y, int z) { return ((long long)(x + 4096) << 26) | ((long long)(y + 4096) << 13) | (z + 4096); };
+    for (int b = 0; b < nb; ++b) at.emplace(key(H.cell[3 * b], H.cell[3 * b + 1], H.cell[3 * b + 2]), b);
+    std::vector<long long> off(nb + 1, 0);
+    std::vector<int> len(nb), bases;
+    size_t nmax = 0, ownmax = 0;
+    for (int b = 0; b < nb; ++b) {
+        const size_t start = bases.size();
+        for (int dx = -2; dx <= 2; ++dx)
+            for (int dy = -2; dy <= 2; ++dy)
+                for (int dz = -2; dz <= 2; ++dz) {
+                    auto it = at.find(key(H.cell[3 * b] + dx, H.cell[3 * b + 1] + dy, H.cell[3 * b + 2] + dz));
+                    if (it == at.end()) continue;
+                    const int j = it->second;
+                    bases.insert(bases.end(), c->box_bases.begin() + c->box_ptr[j],
+                                 c->box_bases.begin() + c->box_ptr[j + 1]);
+                }
+        std::sort(bases.begin() + start, bases.end());
+        len[b] = (int)(bases.size() - start);
+        off[b + 1] = (long long)bases.size();
+        nmax = std::max(nmax, (size_t)len[b]);
+        ownmax = std::max(ownmax, (size_t)(c->box_ptr[b + 1] - c->box_ptr[b]));
+    }
+    const size_t slab = nmax * nmax + nmax * ownmax;
+    size_t fre = 0, tot = 0;
+    CK(cudaMemGetInfo(&fre, &tot));
+    const size_t zbytes = (size_t)N * N * sizeof(float2);
+    if (zbytes + ((size_t)2 << 30) > fre) {
+        c->err = "not enough device memory for the 2-ring targets";
+        return MLF_E_NOMEM;
+    }
+    const size_t budget = std::min<size_t>((fre - zbytes - ((size_t)1 << 30)) / 2, (size_t)16 << 30);
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>(nb, budget / (slab * sizeof(float2))));
+    float2 *Zd = nullptr, *work = nullptr;
+    long long* doff = nullptr;
+    int *dlen = nullptr, *dbases = nullptr, *dbad = nullptr;
+    int st = MLF_OK;
+    auto fail = [&](int code) { st = code; };
+    if (!cuda_ok(c, cudaMalloc(&Zd, zbytes), "alloc") ||
+        !cuda_ok(c, cudaMalloc(&work, slab * batch * sizeof(float2)), "alloc") ||
+        !cuda_ok(c, cudaMalloc(&doff, off.size() * sizeof(long long)), "alloc") ||
+        !cuda_ok(c, cudaMalloc(&dlen, len.size() * sizeof(int)), "alloc") ||
+        !cuda_ok(c, cudaMalloc(&dbases, std::max<size_t>(bases.size(), 1) * sizeof(int)), "alloc") ||
+        !cuda_ok(c, cudaMalloc(&dbad, sizeof(int)), "alloc"))
+        fail(MLF_E_CUDA);
+    if (!st) {
+        const int big = 0x7fffffff;
+        if (!cuda_ok(c, cudaMemcpy(doff, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice), "copy") ||
+            !cuda_ok(c, cudaMemcpy(dlen, len.data(), len.size() * sizeof(int), cudaMemcpyHostToDevice), "copy") ||
+            !cuda_ok(c, cudaMemcpy(dbases, bases.data(), bases.size() * sizeof(int), cudaMemcpyHostToDevice), "copy") ||
+            !cuda_ok(c, cudaMemcpy(dbad, &big, sizeof(int), cudaMemcpyHostToDevice), "copy"))
+            fail(MLF_E_CUDA);
+    }
+    if (!st) {
+        const double c72 = (double)(1.0f / 72.0f);
+        k_lp_dense<<<N, 256, 0, c->stream>>>(N, c->dt_baric, c->dt_baric_sub, c->dp_coord, c->de_t, c->de_po,
+                                             c->de_long, c->ph.w, c->ph.w * c->ph.smue, c72, Zd);
+        for (int b0 = 0; b0 < nb && !st; b0 += batch) {
+            k_ring_inverse32<<<std::min(batch, nb - b0), 256, 0, c->stream>>>(
+                b0, nb, doff, dlen, dbases, c->dbox_ptr, c->dperm, Zd, N, c->dia, c->dja, slab, work, M2, dbad);
+            if (!cuda_ok(c, cudaGetLastError(), "ring inverse")) fail(MLF_E_CUDA);
+        }
+        int hbad = 0;
+        if (!st && (!cuda_ok(c, cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "copy") ||
+                    !cuda_ok(c, cudaStreamSynchronize(c->stream), "ring inverse")))
+            fail(MLF_E_CUDA);
+        *bad_box = hbad == 0x7fffffff ? 0 : hbad;
+    }
+    for (void* p : {(void*)Zd, (void*)work, (void*)doff, (void*)dlen, (void*)dbases, (void*)dbad})
+        if (p) cudaFree(p);
+    return st;
 }
 
-int lp_tokens(Ctx* c, int target, float* X, float* T, long long cap, long long* ntok) {
-    int st = near_blocks_ensure(c);
-    if (st) return st;
-    LpLayout L;
-    if ((st = lp_layout(c, L))) return st;
-    *ntok = L.ntok;
+int lp_tokens(Ctx* c, int with_target, float* X, float* T, long long cap, long long* ntok, int* bad_box) {
+    if (need_tree(c)) return MLF_E_STATE;
+    *ntok = c->nnz;
+    if (bad_box) *bad_box = 0;
     if (!X) return MLF_OK;
-    if (cap < L.ntok) {
+    if (cap < c->nnz) {
         c->err = "token buffers too small";
         return MLF_E_ARG;
     }
-    if (target == 1 && !(c->nearinv_ok && c->nearinv_own)) {
-        c->err = "own-box targets need mlf_nearinv_own first";
+    if (!(c->nearinv_ok && !c->nearinv_own)) {
+        c->err = "tokens need the exact neighbourhood inverse (mlf_nearinv) first";
         return MLF_E_STATE;
     }
-    if (target == 2 && !(c->nearinv_ok && !c->nearinv_own)) {
-        c->err = "neighbourhood targets need mlf_nearinv first";
-        return MLF_E_STATE;
-    }
-    if (target && !T) return MLF_E_ARG;
-    const int nb = (int)c->box_ptr.size() - 1;
+    const double2* M1 = c->dMinv_base ? c->dMinv_base : c->dMinv;
+    LpHost H;
+    int st;
+    if ((st = lp_host(c, H))) return st;
     LpDev D;
-    if ((st = lp_upload(c, L, D))) { lp_free(D); return st; }
-    const size_t smem = 2 * (size_t)L.nmax * sizeof(float);
-    if (smem > 48 * 1024) {
-        lp_free(D);
-        c->err = "leaf box too large for the feature kernel";
-        return MLF_E_ARG;
+    if ((st = lp_upload(c, H, D))) { D.release(); return st; }
+    float2* M2 = nullptr;
+    if (with_target) {
+        if (!T) { D.release(); return MLF_E_ARG; }
+        if (!cuda_ok(c, cudaMalloc(&M2, std::max<long long>(c->nnz, 1) * sizeof(float2)), "alloc")) {
+            D.release();
+            return MLF_E_CUDA;
+        }
+        int bad = 0;
+        if ((st = lp_ring_targets(c, H, M2, &bad))) { cudaFree(M2); D.release(); return st; }
+        if (bad_box) *bad_box = bad;
     }
-    k_lp_features<<<nb, 256, smem, c->stream>>>(c->dbox_ptr, D.self_off, D.boff, c->dZblk, D.s, c->dperm,
-                                                c->de_centro, c->de_long, (float)(1.0 / c->ph.lambda), X);
-    if (target == 1) k_lp_target_own<<<nb, 256, 0, c->stream>>>(c->dbox_ptr, c->dboff, c->dMinv, D.s, T);
-    if (target == 2)
-        k_lp_target_nbhd<<<nb, 256, 0, c->stream>>>(c->dbox_ptr, D.boff, c->dperm, c->dia, c->dja, c->dMinv, D.s, T);
-    if (!cuda_ok(c, cudaGetLastError(), "tokens") || !cuda_ok(c, cudaStreamSynchronize(c->stream), "tokens")) {
-        lp_free(D);
-        return MLF_E_CUDA;
-    }
-    lp_free(D);
-    return MLF_OK;
+    const long long threads = (long long)c->N * 32;
+    k_lp_tokens<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+        c->N, c->dia, c->dja, c->dZ, M1, M2, D.s, D.box_of, D.cell, D.nown, D.nnear, c->de_centro,
+        (float)(1.0 / c->ph.lambda), X, with_target ? T : nullptr);
+    const bool okc = cuda_ok(c, cudaGetLastError(), "tokens") && cuda_ok(c, cudaStreamSynchronize(c->stream), "tokens");
+    if (M2) cudaFree(M2);
+    D.release();
+    return okc ? MLF_OK : MLF_E_CUDA;
 }
 
 }  // namespace mlf
 
 using namespace mlf;
 
-extern "C" int mlf_lp_tokens(mlf_ctx* h, int target, float* X, float* T, long long cap, long long* ntok) {
-    if (!h || !ntok || target < 0 || target > 2) return MLF_E_ARG;
+extern "C" int mlf_lp_tokens(mlf_ctx* h, int with_target, float* X, float* T, long long cap, long long* ntok,
+                             int* bad_box) {
+    if (!h || !ntok) return MLF_E_ARG;
     Ctx* c = &h->c;
     if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
-    return lp_tokens(c, target, X, T, cap, ntok);
+    return lp_tokens(c, with_target, X, T, cap, ntok, bad_box);
 }
 
 extern "C" int mlf_mlp_forward(mlf_mlp* net, const float* X, long long ntok, float* Y, void* stream);
 
-extern "C" int mlf_lp_install(mlf_ctx* h, mlf_mlp* net, int* nonfinite) {
+extern "C" int mlf_lp_install(mlf_ctx* h, mlf_mlp* net, float scale, int* nonfinite) {
     if (!h || !net || !nonfinite) return MLF_E_ARG;
     Ctx* c = &h->c;
     if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
-    long long ntok = 0;
-    int st = lp_tokens(c, 0, nullptr, nullptr, 0, &ntok);
-    if (st) return st;
-    LpLayout L;
-    if ((st = lp_layout(c, L))) return st;
+    if (need_tree(c)) return MLF_E_STATE;
+    if (!(c->nearinv_ok && !c->nearinv_own)) {
+        c->err = "mlf_lp_install needs the exact neighbourhood inverse (mlf_nearinv) first";
+        return MLF_E_STATE;
+    }
+    const long long nnz = c->nnz;
+    // keep the exact M1 so that installs can be repeated with other scales
+    if (!c->dMinv_base) {
+        CK(cudaMalloc(&c->dMinv_base, std::max<long long>(nnz, 1) * sizeof(double2)));
+        CK(cudaMemcpy(c->dMinv_base, c->dMinv, nnz * sizeof(double2), cudaMemcpyDeviceToDevice));
+    }
     float *X = nullptr, *Y = nullptr;
     int* dbad = nullptr;
-    CK(cudaMalloc(&X, std::max<long long>(ntok, 1) * 16 * sizeof(float)));
-    CK(cudaMalloc(&Y, std::max<long long>(ntok, 1) * 2 * sizeof(float)));
-    CK(cudaMalloc(&dbad, sizeof(int)));
-    CK(cudaMemset(dbad, 0, sizeof(int)));
-    if ((st = lp_tokens(c, 0, X, nullptr, ntok, &ntok))) { cudaFree(X); cudaFree(Y); cudaFree(dbad); return st; }
-    if ((st = mlf_mlp_forward(net, X, ntok, Y, nullptr))) {
+    long long ntok = 0;
+    int st = MLF_OK;
+    if (!cuda_ok(c, cudaMalloc(&X, std::max<long long>(nnz, 1) * 16 * sizeof(float)), "alloc") ||
+        !cuda_ok(c, cudaMalloc(&Y, std::max<long long>(nnz, 1) * 2 * sizeof(float)), "alloc") ||
+        !cuda_ok(c, cudaMalloc(&dbad, sizeof(int)), "alloc") || !cuda_ok(c, cudaMemset(dbad, 0, sizeof(int)), "memset"))
+        st = MLF_E_CUDA;
+    if (!st) st = lp_tokens(c, 0, X, nullptr, nnz, &ntok, nullptr);
+    if (!st && mlf_mlp_forward(net, X, ntok, Y, nullptr) != MLF_OK) {
         c->err = "network forward failed";
-        cudaFree(X); cudaFree(Y); cudaFree(dbad);
-        return st;
+        st = MLF_E_CUDA;
     }
-    // own-box storage, replacing any exact preconditioner
-    if (c->dMinv) cudaFree(c->dMinv);
-    if (c->dboff) cudaFree(c->dboff);
-    if (c->dMinv32) cudaFree(c->dMinv32);
-    c->dMinv = nullptr; c->dboff = nullptr; c->dMinv32 = nullptr;
-    c->nearinv_ok = 0;
-    const int nb = (int)c->box_ptr.size() - 1;
+    LpHost H;
     LpDev D;
-    if ((st = lp_upload(c, L, D))) { lp_free(D); cudaFree(X); cudaFree(Y); cudaFree(dbad); return st; }
-    CK(cudaMalloc(&c->dMinv, std::max<long long>(ntok, 1) * sizeof(double2)));
-    c->dboff = D.boff;
-    D.boff = nullptr;
-    c->minv_len = ntok;
-    k_lp_install<<<nb, 256, 0, c->stream>>>(c->dbox_ptr, c->dboff, D.s, Y, c->dMinv, dbad);
+    if (!st) st = lp_host(c, H);
+    if (!st) st = lp_upload(c, H, D);
     int hbad = 0;
-    const bool okc = cuda_ok(c, cudaGetLastError(), "install") &&
-                     cuda_ok(c, cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "install") &&
-                     cuda_ok(c, cudaStreamSynchronize(c->stream), "install");
-    lp_free(D);
-    cudaFree(X); cudaFree(Y); cudaFree(dbad);
-    if (!okc) return MLF_E_CUDA;
+    if (!st) {
+        const long long threads = (long long)c->N * 32;
+        k_lp_install<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(c->N, c->dia, c->dja, D.s,
+                                                                              c->dMinv_base, Y, scale, c->dMinv, dbad);
+        if (!cuda_ok(c, cudaGetLastError(), "install") ||
+            !cuda_ok(c, cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "install") ||
+            !cuda_ok(c, cudaStreamSynchronize(c->stream), "install"))
+            st = MLF_E_CUDA;
+    }
+    D.release();
+    if (X) cudaFree(X);
+    if (Y) cudaFree(Y);
+    if (dbad) cudaFree(dbad);
+    if (st) return st;
+    if (c->dMinv32) { cudaFree(c->dMinv32); c->dMinv32 = nullptr; }   // FP32 copy rebuilt on next use
     *nonfinite = hbad;
-    c->nearinv_own = 1;
-    c->nearinv_ok = 1;
     c->learned = 1;
     return MLF_OK;
 }

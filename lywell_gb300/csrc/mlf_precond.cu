@@ -319,6 +319,8 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     if (c->dMinv) cudaFree(c->dMinv);
     if (c->dboff) cudaFree(c->dboff);
     if (c->dMinv32) cudaFree(c->dMinv32);
+    if (c->dMinv_base) cudaFree(c->dMinv_base);
+    c->dMinv_base = nullptr;
     c->dMinv = nullptr;
     c->dboff = nullptr;
     c->dMinv32 = nullptr;

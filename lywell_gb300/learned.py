@@ -1,12 +1,17 @@
-"""Learned near-field preconditioner: host side of the network and tokens.
+"""Learned near-field preconditioner: host side.
 
-The network (16 -> 128 -> 128 -> 2, ReLU; BF16 parameters and activations,
-FP32 accumulation) is trained and evaluated by the library's own CUDA kernels
-(mlf_mlp_*); the tokens and targets come from a context's near field and an
-exact preconditioner (mlf_lp_tokens), and mlf_lp_install writes the
-prediction into the context's preconditioner slot.  Device buffers are torch
-CUDA tensors (memory only: all arithmetic runs in the library).  No
-counterpart in the reference.
+The exact neighbourhood inverse M1 (27-box neighbourhoods, mlf_nearinv) is
+the base; a network (16 -> 128 -> 128 -> 2, ReLU; BF16 parameters and
+activations, FP32 accumulation) predicts, per near-field entry, the
+correction towards the inverse over the 125-box 2-ring neighbourhood, and the
+installed preconditioner is M = M1 + gamma * tscale * net(tokens): the same
+pattern and apply cost as M1, still linear.  Training, inference and
+gradients run in the library's own CUDA kernels (mlf_mlp_*); tokens and the
+2-ring targets come from mlf_lp_tokens; gamma is chosen from CGS traces on
+the training bodies; solve_with_fallback switches to ILU0 when the learned
+solve has not converged within the unpreconditioned iteration count, judged
+by the true FP64 MLFMA residual.  Device buffers are torch CUDA tensors
+(memory only).  No counterpart in the reference.
 """
 from __future__ import annotations
 
@@ -16,7 +21,6 @@ import numpy as np
 
 from ._capi import MLFError, load
 
-TARGETS = {"none": 0, "own": 1, "nbhd": 2}
 
 
 def _p(t):
@@ -64,7 +68,7 @@ class MLP:
         import torch
         mu = X.mean(0).double().cpu().numpy()
         sd = X.double().std(0).cpu().numpy() + 1e-6
-        for q in (3, 15):
+        for q in (5, 6, 15):
             mu[q], sd[q] = 0.0, 1.0
         self.set_params(None, np.concatenate([mu, sd]).astype(np.float32))
         return mu, sd
@@ -88,30 +92,107 @@ class MLP:
         return hist
 
 
-def tokens(m, target="nbhd"):
-    """(X [ntok, 16], T [ntok, 2]) CUDA tensors for the context `m`; target
-    'own' needs m.nearinv(own_only=True) first, 'nbhd' m.nearinv()."""
+def tokens(m, with_target=True):
+    """(X [nnz, 16], T [nnz, 2] or None, bad_box) CUDA tensors for the
+    context `m` (m.nearinv() first); T is the 2-ring correction target."""
     import torch
-    tk = TARGETS[target] if isinstance(target, str) else int(target)
     n = C.c_longlong()
+    bad = C.c_int()
     L = load()
-    code = L.mlf_lp_tokens(m.handle, tk, None, None, 0, C.byref(n))
+    code = L.mlf_lp_tokens(m.handle, int(bool(with_target)), None, None, 0, C.byref(n), C.byref(bad))
     if code:
         raise MLFError(code, L.mlf_last_error(m.handle).decode())
     X = torch.empty((n.value, 16), dtype=torch.float32, device="cuda")
-    T = torch.empty((n.value, 2), dtype=torch.float32, device="cuda") if tk else None
-    code = L.mlf_lp_tokens(m.handle, tk, _p(X), None if T is None else _p(T), n.value, C.byref(n))
+    T = torch.empty((n.value, 2), dtype=torch.float32, device="cuda") if with_target else None
+    code = L.mlf_lp_tokens(m.handle, int(bool(with_target)), _p(X), None if T is None else _p(T), n.value,
+                           C.byref(n), C.byref(bad))
     if code:
         raise MLFError(code, L.mlf_last_error(m.handle).decode())
-    return X, T
+    return X, T, bad.value
 
 
-def install(m, net: MLP) -> int:
-    """Replace m's preconditioner by the network's prediction; returns the
+def install(m, net: MLP, scale: float) -> int:
+    """M = M1 + scale * net(tokens) in m's preconditioner slot; returns the
     number of non-finite outputs (zeroed)."""
     bad = C.c_int()
     L = load()
-    code = L.mlf_lp_install(m.handle, net.handle, C.byref(bad))
+    code = L.mlf_lp_install(m.handle, net.handle, C.c_float(scale), C.byref(bad))
     if code:
         raise MLFError(code, L.mlf_last_error(m.handle).decode())
     return bad.value
+
+
+class LearnedPreconditioner:
+    """A trained network with its target scale and the damping chosen from
+    solve traces; `apply_to(m)` installs it on a context that has its exact
+    neighbourhood inverse (m.nearinv())."""
+
+    def __init__(self, net: MLP, tscale: float, gamma: float, trace=None):
+        self.net, self.tscale, self.gamma, self.trace = net, float(tscale), float(gamma), trace or {}
+
+    def apply_to(self, m) -> int:
+        return install(m, self.net, self.gamma * self.tscale)
+
+
+def _cgs_iters(m, b, errmax, maxit):
+    out = m.cgs(b, errmax=errmax, maxit=maxit, precond="nearinv")
+    return int(out["iters"]) if out["status"] == "converged" else maxit + 1
+
+
+def train(contexts, excitations, steps=4000, batch=8192, lr=1e-3, seed=0, gammas=(0.25, 0.5, 0.75, 1.0),
+          errmax=1e-4, maxit=3000):
+    """Train on the 2-ring targets of `contexts` (MLFMA objects whose exact
+    neighbourhood inverse is built) with the library's kernels, then pick the
+    damping gamma from CGS traces on the same bodies: the gamma whose
+    iteration count, relative to the exact neighbourhood inverse's, is lowest
+    on average (0 = no correction if none helps)."""
+    import torch
+    Xs, Ts = [], []
+    for m in contexts:
+        X, T, bad = tokens(m, True)
+        if bad:
+            raise MLFError(-6, f"2-ring block of leaf box {bad - 1} is singular")
+        Xs.append(X)
+        Ts.append(T)
+    X = torch.cat(Xs)
+    T = torch.cat(Ts)
+    tscale = float(torch.sqrt((T.double() ** 2).mean()).item())
+    net = MLP(seed=seed)
+    net.fit_norm(X)
+    hist = net.train(X, (T / tscale).contiguous(), steps=steps, batch=batch, lr=lr, seed=seed + 1)
+    del X, T, Xs, Ts
+    base = [_cgs_iters(m, b, errmax, maxit) for m, b in zip(contexts, excitations)]
+    trace = {"exact": base}
+    best_g, best_r = 0.0, 1.0
+    for g in gammas:
+        its = []
+        for m, b in zip(contexts, excitations):
+            install(m, net, g * tscale)
+            its.append(_cgs_iters(m, b, errmax, maxit))
+            install(m, net, 0.0)              # back to the exact M1 (kept under the correction)
+        trace[g] = its
+        r = float(np.mean([i / b0 for i, b0 in zip(its, base)]))
+        if r < best_r:
+            best_g, best_r = g, r
+    lp = LearnedPreconditioner(net, tscale, best_g, trace)
+    lp.loss_history = hist
+    return lp
+
+
+def solve_with_fallback(m, b, lp: LearnedPreconditioner, plain_iters: int, errmax=1e-4, maxit=5000):
+    """CGS with the learned preconditioner, judged by the true FP64 MLFMA
+    residual; if it has not converged within `plain_iters` iterations (the
+    count of the solve without a preconditioner), solve again with ILU0, the
+    reference's preconditioner.  Returns the result dict with 'used'."""
+    lp.apply_to(m)
+    out = m.cgs(b, errmax=errmax, maxit=plain_iters, precond="nearinv")
+    rel = float(np.linalg.norm(m.matvec(out["x"]) - b) / np.linalg.norm(b))
+    if out["status"] == "converged" and rel < errmax * 1.01:
+        out["used"] = "learned"
+        out["true_relres"] = rel
+        return out
+    ierr = m.ilu0()
+    out = m.cgs(b, errmax=errmax, maxit=maxit, precond="ilu0" if ierr == 0 else "none")
+    out["used"] = "ilu0" if ierr == 0 else "none"
+    out["true_relres"] = float(np.linalg.norm(m.matvec(out["x"]) - b) / np.linalg.norm(b))
+    return out
