@@ -626,13 +626,19 @@ int configure_kernels(Ctx* c) {
         mx2 = std::max(mx2, ((size_t)c->lv[n].K + (size_t)c->lv[n].L * 2 * c->lv[n + 1].L) * sizeof(double2));
         mx3 = std::max(mx3, (size_t)SEP_SLAB * 2 * c->lv[n + 1].L * sizeof(double2));
     }
-    if (mx > 227 * 1024 || mx2 > 227 * 1024) {
-        c->err = "parent sampling grid too large for the shared-memory anterpolation stage";
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->dev));
+    if (mx > (size_t)optin || mx2 > (size_t)optin || mx3 > (size_t)optin) {
+        c->err = "parent sampling grid too large for the shared-memory interpolation stages";
         return MLF_E_ARG;
     }
-    CK(cudaFuncSetAttribute(k_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-    CK(cudaFuncSetAttribute(k_anterp_sep<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx2));
-    CK(cudaFuncSetAttribute(k_interp_sep<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx3));
+    // The limit is a property of the kernel, shared by every context in the
+    // process: raise it to the device maximum (what a launch actually uses is
+    // its own dynamic size), never to one context's need, which would break
+    // the launches of an earlier context with larger grids.
+    CK(cudaFuncSetAttribute(k_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    CK(cudaFuncSetAttribute(k_anterp_sep<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    CK(cudaFuncSetAttribute(k_interp_sep<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     return MLF_OK;
 }
 

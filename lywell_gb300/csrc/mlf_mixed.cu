@@ -227,9 +227,16 @@ int mixed_setup(Ctx* c) {
         mx2 = std::max(mx2, ((size_t)c->lv[n].K + (size_t)c->lv[n].L * 2 * c->lv[n + 1].L) * sizeof(float2));
         mx3 = std::max(mx3, (size_t)SEP_SLAB * 2 * c->lv[n + 1].L * sizeof(float2));
     }
-    CK(cudaFuncSetAttribute(k32_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-    CK(cudaFuncSetAttribute(k_anterp_sep<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx2));
-    CK(cudaFuncSetAttribute(k_interp_sep<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx3));
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->dev));
+    if (mx > (size_t)optin || mx2 > (size_t)optin || mx3 > (size_t)optin) {
+        c->err = "parent sampling grid too large for the shared-memory interpolation stages";
+        return MLF_E_ARG;
+    }
+    // kernel-wide limit shared by all contexts: the device maximum (see configure_kernels)
+    CK(cudaFuncSetAttribute(k32_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    CK(cudaFuncSetAttribute(k_anterp_sep<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    CK(cudaFuncSetAttribute(k_interp_sep<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     CK(cudaStreamSynchronize(c->stream));
     c->m32.ready = 1;
     return MLF_OK;

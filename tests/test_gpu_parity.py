@@ -299,3 +299,20 @@ def test_ilut_against_binary_run(gpu_lib):
     assert abs(out["iters"] - int(g["iterations"])) <= 2
     assert _rel(out["x"], g["I"]) < 1e-5
     m.close()
+
+
+def test_contexts_with_different_grids_coexist(gpu_lib):
+    """A context with larger sampling grids stays usable after a context with
+    smaller ones is created (the kernels' dynamic shared-memory limit is
+    process-wide and must not shrink to the newer context's need)."""
+    big = MLFMA(RWG(meshes.icosphere(4, 1.0, quantum=2.0 ** -12)), lam=0.5, ladomax=0.3)
+    x = _vectors(big.N, [3])[0]
+    y0 = big.matvec(x)
+    small = MLFMA(RWG(meshes.icosphere(3, 1.0, quantum=2.0 ** -12)), lam=1.0, ladomax=0.3)
+    small.matvec(_vectors(small.N, [4])[0])
+    y1 = big.matvec(x)
+    assert np.array_equal(y0, y1)
+    y32 = big.matvec32(x)
+    assert _rel(y32, y0) < 2e-5
+    small.close()
+    big.close()
