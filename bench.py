@@ -32,6 +32,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "time-to-RCS & MLFMA matvec/s at 123k RWG, rel.res 1e-4, ≤0.1 dB vs FP64 plain"
+TRANSLATE6_DRAM_BYTES = 246.6e6 + 71.2e6
 WORKLOADS = {
     "sphere6": dict(level=6, radius=6.0, lam=1.0, ladomax=0.25,
                     name="PEC sphere r=6 lambda, icosphere-6 (81920 tri, 122880 RWG), leaf 0.25 lambda, FP64"),
@@ -289,6 +290,77 @@ def profile_fp32_block(nrhs, steps):
     m.close()
 
 
+def learned_sample(steps=3000, seed=0):
+    """Learned preconditioner: trained on three seeded superellipsoids
+    (exponent U[2, 6], semi-axes (2, 1, 1) lambda x U[0.85, 1.15], 7680 RWG)
+    with the library's MLP kernels, evaluated on the held-out superellipsoid
+    (exponent 4, 2 x 1 x 1 lambda): CGS to 1e-4, x-polarised wave from -z,
+    against no preconditioner, ILU0 and the exact neighbourhood inverse it
+    corrects; time to RCS = preconditioner set-up + solve + two bistatic cuts."""
+    import torch
+    from lywell_gb300 import MLFMA, RWG, meshes
+    from lywell_gb300.learned import solve_with_fallback, train
+
+    rng = np.random.default_rng(7)
+    d = np.array([0.0, 0.0, 1.0])
+    p = np.array([1.0, 0.0, 0.0], dtype=complex)
+    th = np.deg2rad(np.arange(0, 181, 1.0))
+    t0 = time.time()
+    ctxs, bs = [], []
+    for _ in range(3):
+        e = rng.uniform(2, 6)
+        ax = np.array([2.0, 1.0, 1.0]) * rng.uniform(0.85, 1.15, 3)
+        mt = MLFMA(RWG(meshes.superellipsoid(4, tuple(ax), e)), lam=1.0, ladomax=0.25)
+        mt.nearinv()
+        ctxs.append(mt)
+        bs.append(mt.excitation(d, p))
+    lp = train(ctxs, bs, steps=steps, batch=8192, lr=1e-3, seed=seed)
+    t_train = time.time() - t0
+    for mt in ctxs:
+        mt.close()
+    m = MLFMA(RWG(meshes.superellipsoid(4, (2.0, 1.0, 1.0), 4.0)), lam=1.0, ladomax=0.25)
+    b = m.excitation(d, p)
+    res = {}
+    ref_db = None
+
+    def finish(label, t_setup, out):
+        torch.cuda.synchronize()
+        t1 = time.time()
+        s0 = m.rcs(out["x"], p, th, 0 * th)
+        s9 = m.rcs(out["x"], p, th, 0 * th + np.pi / 2)
+        t_rcs = time.time() - t1
+        db = 10 * np.log10(np.concatenate([s0, s9]))
+        rel = float(np.linalg.norm(m.matvec(out["x"]) - b) / np.linalg.norm(b))
+        res[label] = {"iters": int(out["iters"]), "status": out["status"], "setup_s": t_setup,
+                      "solve_s": out["_t"], "time_to_rcs_s": t_setup + out["_t"] + t_rcs, "true_relres": rel,
+                      "_db": db}
+
+    def timed(fn):
+        t1 = time.time()
+        out = fn()
+        out["_t"] = time.time() - t1
+        return out
+
+    finish("none", 0.0, timed(lambda: m.cgs(b, errmax=1e-4, maxit=3000)))
+    plain = res["none"]["iters"] if res["none"]["status"] == "converged" else 3000
+    t1 = time.time(); ierr = m.ilu0(); t_ilu = time.time() - t1
+    finish("ilu0", t_ilu, timed(lambda: m.cgs(b, errmax=1e-4, maxit=3000, precond="ilu0")))
+    t1 = time.time(); m.nearinv(); t_nb = time.time() - t1
+    finish("exact_neighbourhood_inverse", t_nb, timed(lambda: m.cgs(b, errmax=1e-4, maxit=3000, precond="nearinv")))
+    t1 = time.time(); lp.apply_to(m); t_inst = time.time() - t1
+    out = timed(lambda: solve_with_fallback(m, b, lp, plain_iters=plain, install_first=False))
+    finish("learned", t_nb + t_inst, out)
+    res["learned"]["used"] = out["used"]
+    ref = res["exact_neighbourhood_inverse"]["_db"]
+    for k in res:
+        res[k]["rcs_db_maxdiff_vs_exact"] = float(np.abs(res[k].pop("_db") - ref).max()) \
+            if res[k]["status"] == "converged" else None
+    m.close()
+    return {"workload": "superellipsoid exponent 4, 2 x 1 x 1 lambda, icosphere-4 (7680 RWG); trained on 3 seeded "
+                        "superellipsoids of the same mesh density", "train_s": t_train, "gamma": lp.gamma,
+            "trace": {str(k): v for k, v in lp.trace.items()}, "ilu0_ierr": ierr, "results": res}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -300,6 +372,7 @@ def main():
     ap.add_argument("--no-time-to-rcs", action="store_true")
     ap.add_argument("--rcs-maxit", type=int, default=4000)
     ap.add_argument("--no-batched", action="store_true", help="skip the 722-RHS spheroid sweep sample")
+    ap.add_argument("--learned", action="store_true", help="add the learned-preconditioner sample (about 3 min)")
     ap.add_argument("--profile-fp32-block", type=int, default=0,
                     help="profiling aid: time the FP32 operator on this many columns of a small spheroid and exit")
     ap.add_argument("--seq-angles", type=int, default=3)
@@ -388,7 +461,11 @@ def main():
     achieved = tr_flops / tr_s / 1e12
     total_tflops = cnt["flops_total"] / (t / args.steps * ws) / 1e12
     roof = {"bound": "fp64", "kernel": "k_translate (5 launches/matvec)", "achieved": achieved, "peak": fp64,
-            "unit": "TFLOP/s", "frac": achieved / fp64, "traffic": None,
+            "unit": "TFLOP/s", "frac": achieved / fp64,
+            # DRAM bytes of the stage's 5 launches in one matvec (ncu dram__bytes_read.sum +
+            # dram__bytes_write.sum on this workload, profiles/matvec_launches_sphere6_fp64.md)
+            "traffic": (TRANSLATE6_DRAM_BYTES if wl is WORKLOADS["sphere6"] else None),
+            "traffic_unit": "bytes per matvec (5 launches)",
             "peak_source": "measured here: cuBLAS DGEMM 4096^3 (GB300 FP64 pipe)",
             "algorithmic_flops_per_matvec": tr_flops,
             "hbm": {"achieved_gbs": cnt["translation_bytes"] / tr_s / 1e9, "peak_gbs": hbm,
@@ -441,6 +518,8 @@ def main():
     if not args.no_batched and rank == 0:
         batched = batched_rcs_sample(args.seq_angles, args.block, args.rcs_maxit)
 
+    learned = learned_sample() if (args.learned and rank == 0) else None
+
     launches_per_matvec = 1 + (m.nlev - 3) + (m.nlev - 2) + (m.nlev - 3) + 1
     line = {"metric": METRIC, "value": value, "unit": "matvec/s", "n_gpus": ws, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
@@ -452,6 +531,8 @@ def main():
             "e2e": {"value": e2e, "unit": "matvec/s", "h2d_bytes_per_step": N * 16, "d2h_bytes_per_step": N * 16},
             "roofline": roof, "clocks": clk, "gpu_launches": launches_per_matvec * args.steps,
             "setup_s": setup_s, "time_to_rcs": ttr, "batched_rcs": batched}
+    if learned is not None:
+        line["learned_preconditioner"] = learned
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(wl)
     if rank == 0:

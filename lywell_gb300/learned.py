@@ -179,12 +179,15 @@ def train(contexts, excitations, steps=4000, batch=8192, lr=1e-3, seed=0, gammas
     return lp
 
 
-def solve_with_fallback(m, b, lp: LearnedPreconditioner, plain_iters: int, errmax=1e-4, maxit=5000):
+def solve_with_fallback(m, b, lp: LearnedPreconditioner, plain_iters: int, errmax=1e-4, maxit=5000,
+                        install_first=True):
     """CGS with the learned preconditioner, judged by the true FP64 MLFMA
     residual; if it has not converged within `plain_iters` iterations (the
     count of the solve without a preconditioner), solve again with ILU0, the
-    reference's preconditioner.  Returns the result dict with 'used'."""
-    lp.apply_to(m)
+    reference's preconditioner.  install_first=False when lp is already
+    installed on m.  Returns the result dict with 'used'."""
+    if install_first:
+        lp.apply_to(m)
     out = m.cgs(b, errmax=errmax, maxit=plain_iters, precond="nearinv")
     rel = float(np.linalg.norm(m.matvec(out["x"]) - b) / np.linalg.norm(b))
     if out["status"] == "converged" and rel < errmax * 1.01:
