@@ -81,7 +81,7 @@ struct Mixed32 {
     float2* xT = nullptr;             // box-sorted row-major copy of the input block (near blocks)
     struct Lv {
         float2 *T = nullptr, *shift = nullptr, *C = nullptr, *B = nullptr, *A = nullptr;
-        float *wq = nullptr, *iw = nullptr, *ant_w = nullptr;
+        float* wq = nullptr;
         float *wth = nullptr, *wph = nullptr, *thT_w = nullptr, *phT_w = nullptr;
     } lv[32];
 };

@@ -65,35 +65,6 @@ __global__ void k32_aggregate(int K, int nrhs, int N, const int* __restrict__ bo
     }
 }
 
-__global__ void k32_interp_up(int Kp, int Kc, int nrhs, int nchunk, const int* __restrict__ child_ptr,
-                              const int* __restrict__ octant, const float* __restrict__ iw,
-                              const int* __restrict__ iidx, const float2* __restrict__ shift,
-                              const float2* __restrict__ Cc, float2* __restrict__ Cp) {
-    const int chunk = blockIdx.x % nchunk;
-    const int pr = blockIdx.x / nchunk;
-    const int P = pr / nrhs, r = pr % nrhs;
-    const int q = chunk * blockDim.x + threadIdx.x;
-    if (q >= 2 * Kp) return;
-    const int pol = q >= Kp, m = q - pol * Kp;
-    float w9[9];
-    int i9[9];
-#pragma unroll
-    for (int t = 0; t < 9; ++t) { w9[t] = iw[9 * m + t]; i9[t] = iidx[9 * m + t] + pol * Kc; }
-    float2 acc = make_float2(0.f, 0.f);
-    for (int cb = child_ptr[P]; cb < child_ptr[P + 1]; ++cb) {
-        const float2* src = Cc + ((size_t)cb * nrhs + r) * 2 * Kc;
-        float2 v = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const float2 s = src[i9[t]];
-            v.x = fmaf(w9[t], s.x, v.x);
-            v.y = fmaf(w9[t], s.y, v.y);
-        }
-        fmac(acc, v, shift[octant[cb] * Kp + m]);
-    }
-    Cp[((size_t)P * nrhs + r) * 2 * Kp + q] = acc;
-}
-
 __global__ void k32_translate(int K, int nrhs, int nchunk, const int* __restrict__ far_ptr,
                               const int* __restrict__ far_src, const int* __restrict__ far_tid,
                               const float2* __restrict__ T, const float* __restrict__ wq,
@@ -110,39 +81,6 @@ __global__ void k32_translate(int K, int nrhs, int nchunk, const int* __restrict
         fmac(acc, C[((size_t)far_src[f] * nrhs + r) * 2 * K + q], T[(size_t)far_tid[f] * K + k]);
     const float wk = wq[k];
     B[((size_t)b * nrhs + r) * 2 * K + q] = make_float2(acc.x * wk, acc.y * wk);
-}
-
-__global__ void k32_anterp_down(int Kp, int Kc, int nrhs, const int* __restrict__ parent,
-                                const int* __restrict__ octant, const int* __restrict__ ant_ptr,
-                                const int* __restrict__ ant_row, const float* __restrict__ ant_w,
-                                const float2* __restrict__ shift, const float2* __restrict__ Psrc,
-                                const float2* __restrict__ Bc, float2* __restrict__ Ac) {
-    extern __shared__ float2 D32[];
-    const int cb = blockIdx.x / nrhs, r = blockIdx.x % nrhs;
-    const int P = parent[cb];
-    const float2* sh = shift + (size_t)octant[cb] * Kp;
-    const float2* src = Psrc + ((size_t)P * nrhs + r) * 2 * Kp;
-    for (int q = threadIdx.x; q < 2 * Kp; q += blockDim.x) {
-        const int m = q >= Kp ? q - Kp : q;
-        const float2 s = sh[m];
-        const float2 v = src[q];
-        D32[q] = make_float2(v.x * s.x + v.y * s.y, v.y * s.x - v.x * s.y);
-    }
-    __syncthreads();
-    const size_t off = ((size_t)cb * nrhs + r) * 2 * Kc;
-    for (int q = threadIdx.x; q < 2 * Kc; q += blockDim.x) {
-        const int pol = q >= Kc, k = q - pol * Kc;
-        float2 acc = make_float2(0.f, 0.f);
-        const int e1 = ant_ptr[k + 1];
-        for (int e = ant_ptr[k]; e < e1; ++e) {
-            const float w = ant_w[e];
-            const float2 d = D32[ant_row[e] + pol * Kp];
-            acc.x = fmaf(w, d.x, acc.x);
-            acc.y = fmaf(w, d.y, acc.y);
-        }
-        const float2 bv = Bc[off + q];
-        Ac[off + q] = make_float2(bv.x + acc.x, bv.y + acc.y);
-    }
 }
 
 __global__ void k32_receive_near(int K, int N, int nrhs, int ld, const int* __restrict__ perm,
@@ -207,8 +145,6 @@ int mixed_setup(Ctx* c) {
         if ((st = conv32(c, &M.T, L.dT, (size_t)L.ntrans * L.K))) return st;
         if ((st = up32(c, &M.wq, L.wq))) return st;
         if (n < nl) {
-            if ((st = up32(c, &M.iw, L.iw))) return st;
-            if ((st = up32(c, &M.ant_w, L.ant_w))) return st;
             if ((st = up32(c, &M.wth, L.wth))) return st;
             if ((st = up32(c, &M.wph, L.wph))) return st;
             if ((st = up32(c, &M.thT_w, L.thT_w))) return st;
@@ -221,20 +157,18 @@ int mixed_setup(Ctx* c) {
             CK(cudaMemcpy(M.shift, s32.data(), s32.size() * sizeof(float2), cudaMemcpyHostToDevice));
         }
     }
-    size_t mx = 0, mx2 = 0, mx3 = 0;
+    size_t mx2 = 0, mx3 = 0;
     for (int n = 3; n < nl; ++n) {
-        mx = std::max(mx, 2 * (size_t)c->lv[n].K * sizeof(float2));
         mx2 = std::max(mx2, ((size_t)c->lv[n].K + (size_t)c->lv[n].L * 2 * c->lv[n + 1].L) * sizeof(float2));
         mx3 = std::max(mx3, (size_t)SEP_SLAB * 2 * c->lv[n + 1].L * sizeof(float2));
     }
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->dev));
-    if (mx > (size_t)optin || mx2 > (size_t)optin || mx3 > (size_t)optin) {
+    if (mx2 > (size_t)optin || mx3 > (size_t)optin) {
         c->err = "parent sampling grid too large for the shared-memory interpolation stages";
         return MLF_E_ARG;
     }
     // kernel-wide limit shared by all contexts: the device maximum (see configure_kernels)
-    CK(cudaFuncSetAttribute(k32_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     CK(cudaFuncSetAttribute(k_anterp_sep<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     CK(cudaFuncSetAttribute(k_interp_sep<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     CK(cudaStreamSynchronize(c->stream));
@@ -347,7 +281,7 @@ void mixed_free(Ctx* c) {
     F(c->m32.R); F(c->m32.xf); F(c->m32.xT);
     for (int n = 0; n < 32; ++n) {
         Mixed32::Lv& M = c->m32.lv[n];
-        F(M.T); F(M.wq); F(M.iw); F(M.ant_w); F(M.shift); F(M.C); F(M.B); F(M.A);
+        F(M.T); F(M.wq); F(M.shift); F(M.C); F(M.B); F(M.A);
         F(M.wth); F(M.wph); F(M.thT_w); F(M.phT_w);
     }
 }
@@ -413,48 +347,6 @@ __global__ void k_reduce_partials(int nk, const double2* __restrict__ partial, d
         s.y += partial[(size_t)k * GM_BLOCKS + b].y;
     }
     out[k] = s;
-}
-
-// w -= sum_{i<nvec} h[i*nrhs+col] V_i
-__global__ void k_gs_update(int N, int nrhs, int nvec, const double2* __restrict__ V, size_t vstride,
-                            const double2* __restrict__ h, double2* __restrict__ w) {
-    const int col = blockIdx.y;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
-        double2 acc = w[(size_t)col * N + e];
-        for (int i = 0; i < nvec; ++i) {
-            const double2 hv = h[i * nrhs + col];
-            const double2 v = V[i * vstride + (size_t)col * N + e];
-            acc.x -= hv.x * v.x - hv.y * v.y;
-            acc.y -= hv.x * v.y + hv.y * v.x;
-        }
-        w[(size_t)col * N + e] = acc;
-    }
-}
-
-// dst[col] = src[col] * s[col] (real scale per column)
-__global__ void k_colscale(int N, const double2* __restrict__ src, const double* __restrict__ s, double2* __restrict__ dst) {
-    const int col = blockIdx.y;
-    const double f = s[col];
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
-        const double2 v = src[(size_t)col * N + e];
-        dst[(size_t)col * N + e] = make_double2(v.x * f, v.y * f);
-    }
-}
-
-// d[col] = sum_{i<nvec} y[i*nrhs+col] V_i[col]
-__global__ void k_combine(int N, int nrhs, int nvec, const double2* __restrict__ V, size_t vstride,
-                          const double2* __restrict__ y, double2* __restrict__ d) {
-    const int col = blockIdx.y;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
-        double2 acc = make_double2(0, 0);
-        for (int i = 0; i < nvec; ++i) {
-            const double2 yv = y[i * nrhs + col];
-            const double2 v = V[i * vstride + (size_t)col * N + e];
-            acc.x += yv.x * v.x - yv.y * v.y;
-            acc.y += yv.x * v.y + yv.y * v.x;
-        }
-        d[(size_t)col * N + e] = acc;
-    }
 }
 
 // FP32 Arnoldi kernels: basis V32 and work vector w32 in float, per-thread
