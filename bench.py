@@ -41,6 +41,13 @@ WORKLOADS = {
 }
 
 
+def _jsonable(o):
+    """numpy scalars and arrays in the JSON line"""
+    if hasattr(o, "tolist"):
+        return o.tolist()
+    return str(o)
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -178,7 +185,7 @@ def run_reference(args, wl):
             "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": core.get_threads(), "kind": "port",
                              "sample": f"{steps} FP64 MLFMA matvecs after {setup:.1f}s set-up"},
             "e2e": {"value": v, "unit": "matvec/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_jsonable), flush=True)
 
 
 def cpu_baseline_sample(wl, budget_steps=2):
@@ -257,7 +264,7 @@ def batched_rcs_sample(seq_angles=3, block=0, maxit=4000):
     return out
 
 
-def profile_fp32_block(nrhs, steps):
+def profile_fp32_block(nrhs, steps, engine=-1, cols=0):
     """Profiling aid (not the bench line): the FP32 operator on `nrhs` random
     columns of a 30720-RWG spheroid with the 122880-RWG spheroid's mesh density
     (icosphere-5, semi-axes 1.5 x 0.375 x 0.375 lambda, so ~145 bases per leaf
@@ -268,6 +275,8 @@ def profile_fp32_block(nrhs, steps):
 
     tris = meshes.spheroid(5, (1.5, 0.375, 0.375), noise=0.005, seed=1234)
     m = MLFMA(RWG(tris), lam=1.0, ladomax=0.25)
+    if engine >= 0:
+        m.set_block_engine(engine, cols)
     lib = _capi.load()
     X = torch.randn(nrhs, m.N, dtype=torch.complex128, device="cuda")
     Y = torch.empty_like(X)
@@ -285,7 +294,7 @@ def profile_fp32_block(nrhs, steps):
         call()
     e1.record()
     torch.cuda.synchronize()
-    print(json.dumps({"profile": "fp32 operator", "N": m.N, "nrhs": nrhs, "near_nnz": m.nnz,
+    print(json.dumps({"profile": "fp32 operator", "N": m.N, "nrhs": nrhs, "near_nnz": m.nnz, "engine": engine, "cols": cols,
                       "ms_per_call": e0.elapsed_time(e1) / steps}), flush=True)
     m.close()
 
@@ -373,13 +382,15 @@ def main():
     ap.add_argument("--rcs-maxit", type=int, default=4000)
     ap.add_argument("--no-batched", action="store_true", help="skip the 722-RHS spheroid sweep sample")
     ap.add_argument("--learned", action="store_true", help="add the learned-preconditioner sample (about 3 min)")
+    ap.add_argument("--block-engine", type=int, default=-1, help="profiling aid: 1 tensor cores, 0 FP32 FMA")
+    ap.add_argument("--block-cols", type=int, default=0, help="profiling aid: box-block tile width 8/32/64")
     ap.add_argument("--profile-fp32-block", type=int, default=0,
                     help="profiling aid: time the FP32 operator on this many columns of a small spheroid and exit")
     ap.add_argument("--seq-angles", type=int, default=3)
     ap.add_argument("--block", type=int, default=0, help="RHS per block of the batched sweep (0: autotuned)")
     args = ap.parse_args()
     if args.profile_fp32_block > 0:
-        profile_fp32_block(args.profile_fp32_block, args.steps)
+        profile_fp32_block(args.profile_fp32_block, args.steps, args.block_engine, args.block_cols)
         return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -536,7 +547,7 @@ def main():
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(wl)
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        print(json.dumps(line, default=_jsonable), flush=True)
     m.close()
     if ws > 1:
         torch.distributed.destroy_process_group()

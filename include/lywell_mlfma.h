@@ -210,6 +210,13 @@ int mlf_solve_times(mlf_ctx* ctx, double* out4);
 int mlf_autotune_block(mlf_ctx* ctx, const int* candidates, int ncand, int* best_block, int* best_cols,
                        float* per_rhs_ms);
 
+/* Box-block GEMM engine of the FP32 operator on blocks of columns: 1 = tensor
+ * cores (mma.sync m16n8k8 TF32 with the 3xTF32 split, within a few 1e-6 of
+ * FP32; the default), 0 = FP32 FMA; cols = tile width 8, 32 or 64 (0: by the
+ * block's width).  mlf_autotune_block sets both.  No counterpart in the
+ * reference. */
+int mlf_set_block_engine(mlf_ctx* ctx, int engine, int cols);
+
 /* y = Z_MLFMA x with the FP32 operator of mode 1 (host or device arrays);
  * inputs and outputs complex(8). */
 int mlf_matvec32(mlf_ctx* ctx, const double* x, double* y, int nrhs, int ld);

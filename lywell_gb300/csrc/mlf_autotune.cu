@@ -1,8 +1,9 @@
 // Block-size and tile autotuner for batched solves.
 //
-// For each candidate number of right-hand sides per block B and each
-// near-field tile width (8 or 32 columns), one FP32 operator application on
-// B random columns is timed with CUDA events (two warm-up calls, three timed).
+// For each candidate number of right-hand sides per block B, each box-block
+// GEMM engine (tensor-core mma.sync 3xTF32 or FP32 FMA) and each tile width
+// (8, 32 or 64 columns), one FP32 operator application on B random columns is
+// timed with CUDA events (two warm-up calls, three timed).
 // The choice minimises operator time per right-hand side; a smaller block is
 // kept when it is within 5 % of the best (it retires columns sooner and holds
 // a smaller Krylov basis).  No counterpart in the reference, whose monostatic
@@ -42,21 +43,24 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    const int saved_cols = c->blk_cols, saved_prof = c->profiling;
+    const int saved_cols = c->blk_cols, saved_eng = c->blk_engine, saved_prof = c->profiling;
     c->profiling = 0;
     int st = MLF_OK;
     double best = 1e300;
     *best_block = cand[0];
     *best_cols = 0;
     std::vector<std::pair<double, int>> per(ncand);
-    std::vector<int> colsel(ncand, 0);
+    std::vector<int> colsel(ncand, 0), engsel(ncand, 1);
     for (int q = 0; q < ncand && !st; ++q) {
         const int B = cand[q];
         double tq = 1e300;
-        const int widths[2] = {8, 32};
-        for (int wv = 0; wv < 2 && !st; ++wv) {
-            if (B == 1 && wv) break;   // one column uses the CSR kernel
+        const int widths[3] = {8, 32, 64};
+        for (int var = 0; var < 6 && !st; ++var) {
+            const int wv = var % 3, eng = 1 - var / 3;   // tensor-core engine first, then FP32 FMA
+            if (B == 1 && var) break;   // one column uses the CSR kernels
+            if (wv > 0 && widths[wv - 1] >= B) continue;   // a narrower tile already covers the block
             c->blk_cols = widths[wv];
+            c->blk_engine = eng;
             for (int w = 0; w < 2 && !st; ++w) st = device_matvec32(c, x, y, B, c->N, s);
             if (st) break;
             cudaEventRecord(e0, s);
@@ -67,7 +71,7 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             const double t = ms / 3.0 / B;
-            if (t < tq) { tq = t; colsel[q] = widths[wv]; }
+            if (t < tq) { tq = t; colsel[q] = widths[wv]; engsel[q] = eng; }
         }
         per[q] = {tq, B};
         if (per_rhs_ms) per_rhs_ms[q] = (float)tq;
@@ -80,6 +84,9 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
             if (per[q].first <= 1.05 * best && (pick < 0 || cand[q] < cand[pick])) pick = q;
         *best_block = cand[pick];
         *best_cols = cand[pick] == 1 ? 0 : colsel[pick];
+        c->blk_engine = engsel[pick];
+    } else {
+        c->blk_engine = saved_eng;
     }
     c->blk_cols = st ? saved_cols : *best_cols;
     c->profiling = saved_prof;
@@ -93,6 +100,13 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
 }  // namespace mlf
 
 using namespace mlf;
+
+extern "C" int mlf_set_block_engine(mlf_ctx* h, int engine, int cols) {
+    if (!h || engine < 0 || engine > 1 || (cols != 0 && cols != 8 && cols != 32 && cols != 64)) return MLF_E_ARG;
+    h->c.blk_engine = engine;
+    h->c.blk_cols = cols;
+    return MLF_OK;
+}
 
 extern "C" int mlf_autotune_block(mlf_ctx* h, const int* candidates, int ncand, int* best_block, int* best_cols,
                                   float* per_rhs_ms) {

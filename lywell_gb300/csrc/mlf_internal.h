@@ -115,7 +115,8 @@ struct Ctx {
     // column-major at Zblk + blk_off[e]; tiles = (box, first row) of each
     // 64-row tile of the leaf boxes
     int blk_ok = 0, nblk_tiles = 0;
-    int blk_cols = 0;                 // near-block tile width: 0 = by nrhs, else 8 or 32 (autotuner)
+    int blk_cols = 0;                 // box-block tile width: 0 = by nrhs, else 8, 32 or 64 (autotuner)
+    int blk_engine = 1;               // box-block multiply: 0 FP32 FMA, 1 mma.sync 3xTF32 (autotuner)
     float2* dZblk = nullptr;
     long long* dblk_off = nullptr;
     int *dnbox_ptr = nullptr, *dnbox_list = nullptr;

@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
+#include <type_traits>
 #include <vector>
 
 #include "mlf_internal.h"
@@ -73,80 +75,198 @@ __global__ void k_blk_pack64(int N, int nrhs, int ld, const int* __restrict__ pe
 }
 
 // ---------------------------------------------------------------------------
-// Box-block complex GEMM engine.  One CTA computes a 64-row x (8 TC)-column
-// tile of Y = A X for one leaf box, streaming the contraction dimension in
-// chunks of 32 through shared memory.  256 threads: thread (ty = tid / 8,
-// tx = tid % 8) owns rows 2 ty, 2 ty + 1 and columns TC tx .. TC tx + TC - 1
-// of the tile (2 x TC complex accumulators in registers).
+// Box-block complex GEMM engine.  One CTA (256 threads) computes a 64-row x
+// NC = 8 TC column tile of Y = A X for one leaf box, streaming the
+// contraction dimension in chunks of 32 through shared memory:
 //   A element (row, t): AROW ? A[row * lda + t] : A[t * lda + row] (conj if ACONJ)
 //   X element (t, col): XCOL ? X[col * ldx + t] : X[t * ldx + col]
+// Two interchangeable multiply engines (the autotuner picks per block size):
+//   FmaAcc  FP32 FMAs, thread (ty = tid / 8, tx = tid % 8) owns rows 2 ty,
+//           2 ty + 1 and columns TC tx .. TC tx + TC - 1;
+//   MmaAcc  tensor-core mma.sync m16n8k8 TF32 with the 3xTF32 split
+//           (a_hi b_hi + a_hi b_lo + a_lo b_hi, FP32 accuracy) on the real
+//           embedding [Ar Ai] (64 x 64) x [[Br, Bi], [-Bi, Br]] (64 x 2 NC);
+//           warp w owns rows 16 (w % 4) .. + 15 and real columns
+//           NC (w / 4) .. + NC - 1; the tile is staged through shared memory
+//           so the real and imaginary halves meet in one thread.
 template <int TC>
 struct BlkTile {
     float2 Zs[NBK_KC][NBK_ROWS + 2];
     float2 Xs[NBK_KC][8 * TC];
 };
 
-template <int TC, bool AROW, bool ACONJ, bool XCOL>
-__device__ __forceinline__ void blk_mac(float2 (&acc)[2][TC], BlkTile<TC>& sm, const float2* __restrict__ A,
-                                        long long lda, int r0, int mrows, int kdim, const float2* __restrict__ X,
-                                        long long ldx, int c0, int ncols) {
-    constexpr int NC = 8 * TC;
-    const int tid = threadIdx.x, ty = tid >> 3, tx = tid & 7;
-    for (int t0 = 0; t0 < kdim; t0 += NBK_KC) {
-        for (int q = tid; q < NBK_KC * NBK_ROWS; q += 256) {
-            int k, p;
-            if (AROW) { p = q / NBK_KC; k = q - p * NBK_KC; }
-            else { k = q / NBK_ROWS; p = q - k * NBK_ROWS; }
-            const int t = t0 + k, row = r0 + p;
-            float2 v = make_float2(0.f, 0.f);
-            if (t < kdim && row < mrows) v = AROW ? A[(size_t)row * lda + t] : A[(size_t)t * lda + row];
-            if (ACONJ) v.y = -v.y;
-            sm.Zs[k][p] = v;
-        }
-        for (int q = tid; q < NBK_KC * NC; q += 256) {
-            int k, cc;
-            if (XCOL) { cc = q / NBK_KC; k = q - cc * NBK_KC; }
-            else { k = q / NC; cc = q - k * NC; }
-            const int t = t0 + k, col = c0 + cc;
-            float2 v = make_float2(0.f, 0.f);
-            if (t < kdim && col < ncols) v = XCOL ? X[(size_t)col * ldx + t] : X[(size_t)t * ldx + col];
-            sm.Xs[k][cc] = v;
-        }
-        __syncthreads();
+template <int TC>
+struct FmaAcc {
+    float2 v[2][TC];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int u = 0; u < TC; ++u) v[a][u] = make_float2(0.f, 0.f);
+    }
+    __device__ __forceinline__ void chunk(const BlkTile<TC>& sm) {
+        const int tid = threadIdx.x, ty = tid >> 3, tx = tid & 7;
 #pragma unroll 8
         for (int k = 0; k < NBK_KC; ++k) {
             const float4 zz = *reinterpret_cast<const float4*>(&sm.Zs[k][2 * ty]);
 #pragma unroll
             for (int u = 0; u < TC; ++u) {
                 const float2 xv = sm.Xs[k][tx * TC + u];
-                acc[0][u].x = fmaf(zz.x, xv.x, acc[0][u].x);
-                acc[0][u].x = fmaf(-zz.y, xv.y, acc[0][u].x);
-                acc[0][u].y = fmaf(zz.x, xv.y, acc[0][u].y);
-                acc[0][u].y = fmaf(zz.y, xv.x, acc[0][u].y);
-                acc[1][u].x = fmaf(zz.z, xv.x, acc[1][u].x);
-                acc[1][u].x = fmaf(-zz.w, xv.y, acc[1][u].x);
-                acc[1][u].y = fmaf(zz.z, xv.y, acc[1][u].y);
-                acc[1][u].y = fmaf(zz.w, xv.x, acc[1][u].y);
+                v[0][u].x = fmaf(zz.x, xv.x, v[0][u].x);
+                v[0][u].x = fmaf(-zz.y, xv.y, v[0][u].x);
+                v[0][u].y = fmaf(zz.x, xv.y, v[0][u].y);
+                v[0][u].y = fmaf(zz.y, xv.x, v[0][u].y);
+                v[1][u].x = fmaf(zz.z, xv.x, v[1][u].x);
+                v[1][u].x = fmaf(-zz.w, xv.y, v[1][u].x);
+                v[1][u].y = fmaf(zz.z, xv.y, v[1][u].y);
+                v[1][u].y = fmaf(zz.w, xv.x, v[1][u].y);
             }
         }
-        __syncthreads();
     }
+    // out(row in tile, column in tile, value) for every owned element
+    template <class Out>
+    __device__ __forceinline__ void store(BlkTile<TC>&, Out out) {
+        const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int u = 0; u < TC; ++u) out(2 * ty + a, tx * TC + u, v[a][u]);
+    }
+};
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
 template <int TC>
-__device__ __forceinline__ void acc_zero(float2 (&acc)[2][TC]) {
+struct MmaAcc {
+    float c[TC][4];
+    __device__ __forceinline__ void zero() {
 #pragma unroll
-    for (int a = 0; a < 2; ++a)
+        for (int n = 0; n < TC; ++n)
 #pragma unroll
-        for (int u = 0; u < TC; ++u) acc[a][u] = make_float2(0.f, 0.f);
+            for (int q = 0; q < 4; ++q) c[n][q] = 0.f;
+    }
+    __device__ __forceinline__ void chunk(const BlkTile<TC>& sm) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const int wm = warp & 3, wn = warp >> 2;
+        const int g = lane >> 2, t = lane & 3;
+        const int r = 16 * wm + g;
+#pragma unroll
+        for (int ks = 0; ks < 8; ++ks) {
+            const bool kim = ks >= 4;              // real k in [32, 64): the imaginary parts of A
+            const int kc = (ks & 3) * 8;           // complex k of this step
+            const float2 z0 = sm.Zs[kc + t][r], z1 = sm.Zs[kc + t][r + 8];
+            const float2 z2 = sm.Zs[kc + t + 4][r], z3 = sm.Zs[kc + t + 4][r + 8];
+            const float av[4] = {kim ? z0.y : z0.x, kim ? z1.y : z1.x, kim ? z2.y : z2.x, kim ? z3.y : z3.x};
+            uint32_t ah[4], al[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                ah[q] = to_tf32(av[q]);
+                al[q] = to_tf32(av[q] - __uint_as_float(ah[q]));
+            }
+            // B' block: (real rows, real cols) Br, (real rows, imag cols) Bi,
+            // (imag rows, real cols) -Bi, (imag rows, imag cols) Br
+            const bool use_im = (wn == 0) ? kim : !kim;
+            const float sgn = (wn == 0 && kim) ? -1.f : 1.f;
+#pragma unroll
+            for (int n = 0; n < TC; ++n) {
+                const int col = n * 8 + g;
+                const float2 x0 = sm.Xs[kc + t][col], x1 = sm.Xs[kc + t + 4][col];
+                const float bv[2] = {sgn * (use_im ? x0.y : x0.x), sgn * (use_im ? x1.y : x1.x)};
+                uint32_t bh[2], bl[2];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    bh[q] = to_tf32(bv[q]);
+                    bl[q] = to_tf32(bv[q] - __uint_as_float(bh[q]));
+                }
+                mma_tf32(c[n], al, bh);
+                mma_tf32(c[n], ah, bl);
+                mma_tf32(c[n], ah, bh);
+            }
+        }
+    }
+    template <class Out>
+    __device__ __forceinline__ void store(BlkTile<TC>& sm, Out out) {
+        constexpr int NC = 8 * TC, LDC = 2 * NC + 1;
+        static_assert(sizeof(float) * NBK_ROWS * LDC <= sizeof(BlkTile<TC>), "staging tile");
+        float* Cs = reinterpret_cast<float*>(&sm);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const int wm = warp & 3, wn = warp >> 2;
+        const int g = lane >> 2, t = lane & 3;
+        __syncthreads();
+#pragma unroll
+        for (int n = 0; n < TC; ++n) {
+            const int col = wn * NC + n * 8 + 2 * t;
+            const int row = 16 * wm + g;
+            Cs[row * LDC + col] = c[n][0];
+            Cs[row * LDC + col + 1] = c[n][1];
+            Cs[(row + 8) * LDC + col] = c[n][2];
+            Cs[(row + 8) * LDC + col + 1] = c[n][3];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < NBK_ROWS * NC; e += 256) {
+            const int row = e / NC, col = e - row * NC;
+            out(row, col, make_float2(Cs[row * LDC + col], Cs[row * LDC + NC + col]));
+        }
+    }
+};
+
+template <int TC, bool AROW, bool ACONJ, bool XCOL>
+__device__ __forceinline__ void blk_load(BlkTile<TC>& sm, const float2* __restrict__ A, long long lda, int r0,
+                                         int mrows, int kdim, int t0, const float2* __restrict__ X, long long ldx,
+                                         int c0, int ncols) {
+    constexpr int NC = 8 * TC;
+    const int tid = threadIdx.x;
+    for (int q = tid; q < NBK_KC * NBK_ROWS; q += 256) {
+        int k, p;
+        if (AROW) { p = q / NBK_KC; k = q - p * NBK_KC; }
+        else { k = q / NBK_ROWS; p = q - k * NBK_ROWS; }
+        const int t = t0 + k, row = r0 + p;
+        float2 v = make_float2(0.f, 0.f);
+        if (t < kdim && row < mrows) v = AROW ? A[(size_t)row * lda + t] : A[(size_t)t * lda + row];
+        if (ACONJ) v.y = -v.y;
+        sm.Zs[k][p] = v;
+    }
+    for (int q = tid; q < NBK_KC * NC; q += 256) {
+        int k, cc;
+        if (XCOL) { cc = q / NBK_KC; k = q - cc * NBK_KC; }
+        else { k = q / NC; cc = q - k * NC; }
+        const int t = t0 + k, col = c0 + cc;
+        float2 v = make_float2(0.f, 0.f);
+        if (t < kdim && col < ncols) v = XCOL ? X[(size_t)col * ldx + t] : X[(size_t)t * ldx + col];
+        sm.Xs[k][cc] = v;
+    }
+}
+
+template <int TC, bool AROW, bool ACONJ, bool XCOL, class Acc>
+__device__ __forceinline__ void blk_mac(Acc& acc, BlkTile<TC>& sm, const float2* __restrict__ A, long long lda,
+                                        int r0, int mrows, int kdim, const float2* __restrict__ X, long long ldx,
+                                        int c0, int ncols) {
+    for (int t0 = 0; t0 < kdim; t0 += NBK_KC) {
+        blk_load<TC, AROW, ACONJ, XCOL>(sm, A, lda, r0, mrows, kdim, t0, X, ldx, c0, ncols);
+        __syncthreads();
+        acc.chunk(sm);
+        __syncthreads();
+    }
 }
 
 // y(:, c0 : c0 + 8 TC) += Z_near x for one 64-row tile of one leaf box.
 // The chunks of all near boxes form one sequence; the next chunk's Z and x
 // values are loaded into registers while the current one is multiplied out
 // of shared memory (software double buffering), so the global loads overlap
-// the FMAs instead of stalling between barriers.
-template <int TC>
+// the arithmetic instead of stalling between barriers.
+template <int TC, class Acc>
 __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2* __restrict__ tiles,
                                                     const int* __restrict__ box_ptr, const int* __restrict__ nbox_ptr,
                                                     const int* __restrict__ nbox_list,
@@ -158,13 +278,12 @@ __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2
     constexpr int XPT = NBK_KC * NC / 256;         // x values per thread per chunk
     __shared__ __align__(16) BlkTile<TC> sm;
     const int2 tl = tiles[blockIdx.x];
-    const int i = tl.x, r0 = tl.y, c0 = blockIdx.y * 8 * TC;
+    const int i = tl.x, r0 = tl.y, c0 = blockIdx.y * NC;
     const int ni = box_ptr[i + 1] - box_ptr[i];
-    const int tid = threadIdx.x, ty = tid >> 3, tx = tid & 7;
-    float2 acc[2][TC];
-    acc_zero<TC>(acc);
+    const int tid = threadIdx.x;
+    Acc acc;
+    acc.zero();
     const int e_end = nbox_ptr[i + 1];
-    // chunk cursor
     int e = nbox_ptr[i], t0 = 0;
     float2 zr[ZPT], xr[XPT];
     auto load = [&](int ec, int tc) {
@@ -207,71 +326,43 @@ __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2
         __syncthreads();
         next(e, t0);
         if (e < e_end) load(e, t0);
-#pragma unroll 8
-        for (int k = 0; k < NBK_KC; ++k) {
-            const float4 zz = *reinterpret_cast<const float4*>(&sm.Zs[k][2 * ty]);
-#pragma unroll
-            for (int u = 0; u < TC; ++u) {
-                const float2 xv = sm.Xs[k][tx * TC + u];
-                acc[0][u].x = fmaf(zz.x, xv.x, acc[0][u].x);
-                acc[0][u].x = fmaf(-zz.y, xv.y, acc[0][u].x);
-                acc[0][u].y = fmaf(zz.x, xv.y, acc[0][u].y);
-                acc[0][u].y = fmaf(zz.y, xv.x, acc[0][u].y);
-                acc[1][u].x = fmaf(zz.z, xv.x, acc[1][u].x);
-                acc[1][u].x = fmaf(-zz.w, xv.y, acc[1][u].x);
-                acc[1][u].y = fmaf(zz.z, xv.y, acc[1][u].y);
-                acc[1][u].y = fmaf(zz.w, xv.x, acc[1][u].y);
-            }
-        }
+        acc.chunk(sm);
         __syncthreads();
     }
-#pragma unroll
-    for (int a = 0; a < 2; ++a) {
-        const int row = r0 + 2 * ty + a;
-        if (row >= ni) continue;
-        const int n = perm[box_ptr[i] + row];
-#pragma unroll
-        for (int u = 0; u < TC; ++u) {
-            const int col = c0 + tx * TC + u;
-            if (col < nrhs) {
-                double2* yp = y + (size_t)col * ld + n;
-                const double2 v = *yp;
-                *yp = make_double2(v.x + (double)acc[a][u].x, v.y + (double)acc[a][u].y);
-            }
+    const int i0 = box_ptr[i];
+    acc.store(sm, [&](int rt, int ct, float2 v) {
+        const int row = r0 + rt, col = c0 + ct;
+        if (row < ni && col < nrhs) {
+            double2* yp = y + (size_t)col * ld + perm[i0 + row];
+            const double2 o = *yp;
+            *yp = make_double2(o.x + (double)v.x, o.y + (double)v.y);
         }
-    }
+    });
 }
 
 // Leaf aggregation (llenar_campoCyB step 2, modMLFMA.f90:1805-1811) for a block
 // of columns: C(:, col, box) = R_box^T x_box, R_box = the box's 2K x n_b
 // patterns.  Grid: (boxes x ceil(2K / 64) row tiles, column tiles).
-template <int TC>
+template <int TC, class Acc>
 __global__ void __launch_bounds__(256) k32_agg_blk(int K2, int nrhs, int ntr, const int* __restrict__ box_ptr,
                                                    const float2* __restrict__ R, const float2* __restrict__ xs,
                                                    float2* __restrict__ C) {
     __shared__ __align__(16) BlkTile<TC> sm;
     const int b = blockIdx.x / ntr, r0 = (blockIdx.x - b * ntr) * NBK_ROWS, c0 = blockIdx.y * 8 * TC;
     const int j0 = box_ptr[b], nb = box_ptr[b + 1] - j0;
-    float2 acc[2][TC];
-    acc_zero<TC>(acc);
+    Acc acc;
+    acc.zero();
     blk_mac<TC, false, false, false>(acc, sm, R + (size_t)j0 * K2, K2, r0, K2, nb, xs + (size_t)j0 * nrhs, nrhs, c0,
                                      nrhs);
-    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
-#pragma unroll
-    for (int a = 0; a < 2; ++a) {
-        const int row = r0 + 2 * ty + a;
-        if (row >= K2) continue;
-#pragma unroll
-        for (int u = 0; u < TC; ++u) {
-            const int col = c0 + tx * TC + u;
-            if (col < nrhs) C[((size_t)b * nrhs + col) * K2 + row] = acc[a][u];
-        }
-    }
+    acc.store(sm, [&](int rt, int ct, float2 v) {
+        const int row = r0 + rt, col = c0 + ct;
+        if (row < K2 && col < nrhs) C[((size_t)b * nrhs + col) * K2 + row] = v;
+    });
 }
 
 // Leaf receive (MatxVec_MLFMA, modMLFMA.f90:1915-1924) for a block of
 // columns: y(basis, col) = j facy sum_q conj(R[basis][q]) A(q, col, box).
-template <int TC>
+template <int TC, class Acc>
 __global__ void __launch_bounds__(256) k32_recv_blk(int K2, int nrhs, int ld, float facy,
                                                     const int2* __restrict__ tiles, const int* __restrict__ box_ptr,
                                                     const int* __restrict__ perm, const float2* __restrict__ R,
@@ -280,28 +371,20 @@ __global__ void __launch_bounds__(256) k32_recv_blk(int K2, int nrhs, int ld, fl
     const int2 tl = tiles[blockIdx.x];
     const int b = tl.x, r0 = tl.y, c0 = blockIdx.y * 8 * TC;
     const int j0 = box_ptr[b], nb = box_ptr[b + 1] - j0;
-    float2 acc[2][TC];
-    acc_zero<TC>(acc);
+    Acc acc;
+    acc.zero();
     blk_mac<TC, true, true, true>(acc, sm, R + (size_t)j0 * K2, K2, r0, nb, K2, Af + (size_t)b * nrhs * K2, K2, c0,
                                   nrhs);
-    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
-#pragma unroll
-    for (int a = 0; a < 2; ++a) {
-        const int row = r0 + 2 * ty + a;
-        if (row >= nb) continue;
-        const int n = perm[j0 + row];
-#pragma unroll
-        for (int u = 0; u < TC; ++u) {
-            const int col = c0 + tx * TC + u;
-            if (col < nrhs)
-                y[(size_t)col * ld + n] = make_double2(-(double)(facy * acc[a][u].y), (double)(facy * acc[a][u].x));
-        }
-    }
+    acc.store(sm, [&](int rt, int ct, float2 v) {
+        const int row = r0 + rt, col = c0 + ct;
+        if (row < nb && col < nrhs)
+            y[(size_t)col * ld + perm[j0 + row]] = make_double2(-(double)(facy * v.y), (double)(facy * v.x));
+    });
 }
 
 // Own-box block preconditioner for a block of FP32 columns:
 // out(basis, col) = sum_t M_box[row][t] xs(box basis t, col), M row-major n_b x n_b at boff[box].
-template <int TC>
+template <int TC, class Acc>
 __global__ void __launch_bounds__(256) k32_own_blk(int N, int nrhs, const int2* __restrict__ tiles,
                                                    const int* __restrict__ box_ptr, const int* __restrict__ perm,
                                                    const long long* __restrict__ boff, const float2* __restrict__ M,
@@ -310,21 +393,13 @@ __global__ void __launch_bounds__(256) k32_own_blk(int N, int nrhs, const int2* 
     const int2 tl = tiles[blockIdx.x];
     const int b = tl.x, r0 = tl.y, c0 = blockIdx.y * 8 * TC;
     const int j0 = box_ptr[b], nb = box_ptr[b + 1] - j0;
-    float2 acc[2][TC];
-    acc_zero<TC>(acc);
+    Acc acc;
+    acc.zero();
     blk_mac<TC, true, false, false>(acc, sm, M + boff[b], nb, r0, nb, nb, xs + (size_t)j0 * nrhs, nrhs, c0, nrhs);
-    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
-#pragma unroll
-    for (int a = 0; a < 2; ++a) {
-        const int row = r0 + 2 * ty + a;
-        if (row >= nb) continue;
-        const int n = perm[j0 + row];
-#pragma unroll
-        for (int u = 0; u < TC; ++u) {
-            const int col = c0 + tx * TC + u;
-            if (col < nrhs) out[(size_t)col * N + n] = acc[a][u];
-        }
-    }
+    acc.store(sm, [&](int rt, int ct, float2 v) {
+        const int row = r0 + rt, col = c0 + ct;
+        if (row < nb && col < nrhs) out[(size_t)col * N + perm[j0 + row]] = v;
+    });
 }
 
 static int near_blocks_setup(Ctx* c) {
@@ -374,7 +449,26 @@ static int near_blocks_setup(Ctx* c) {
     return MLF_OK;
 }
 
-static bool blk_narrow(const Ctx* c, int nrhs) { return c->blk_cols ? c->blk_cols == 8 : nrhs <= 8; }
+// tile width in columns: the autotuner's choice, else by the block's width
+static int blk_width(const Ctx* c, int nrhs) {
+    if (c->blk_cols) return c->blk_cols;
+    return nrhs <= 8 ? 8 : (nrhs <= 32 ? 32 : 64);
+}
+
+// engine x tile width dispatch: F(std::integral_constant<int, TC>, Acc tag)
+template <class F>
+static void blk_dispatch(const Ctx* c, int nrhs, F f) {
+    const int w = blk_width(c, nrhs);
+    if (c->blk_engine == 1) {
+        if (w == 8) f(std::integral_constant<int, 1>(), MmaAcc<1>());
+        else if (w == 32) f(std::integral_constant<int, 4>(), MmaAcc<4>());
+        else f(std::integral_constant<int, 8>(), MmaAcc<8>());
+    } else {
+        if (w == 8) f(std::integral_constant<int, 1>(), FmaAcc<1>());
+        else if (w == 32) f(std::integral_constant<int, 4>(), FmaAcc<4>());
+        else f(std::integral_constant<int, 8>(), FmaAcc<8>());
+    }
+}
 
 // xs (N x nrhs FP32, box-sorted rows) from FP32 columns (x32, ld N) or FP64 columns (x, ld)
 int device_blk_pack(Ctx* c, const double2* x, const float2* x32, int ld, int nrhs, float2* xs, cudaStream_t s) {
@@ -388,22 +482,22 @@ int device_blk_pack(Ctx* c, const double2* x, const float2* x32, int ld, int nrh
 int device_near_blocks32(Ctx* c, const float2* xs, int ld, int nrhs, double2* y, cudaStream_t s) {
     int st;
     if ((st = near_blocks_setup(c))) return st;
-    if (blk_narrow(c, nrhs))
-        k32_near_blk<1><<<dim3(c->nblk_tiles, (nrhs + 7) / 8), 256, 0, s>>>(
+    blk_dispatch(c, nrhs, [&](auto tc, auto acc) {
+        constexpr int TC = decltype(tc)::value;
+        k32_near_blk<TC, decltype(acc)><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, 0, s>>>(
             nrhs, ld, c->dblk_tiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, c->dblk_off, c->dZblk, xs, c->dperm, y);
-    else
-        k32_near_blk<4><<<dim3(c->nblk_tiles, (nrhs + 31) / 32), 256, 0, s>>>(
-            nrhs, ld, c->dblk_tiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, c->dblk_off, c->dZblk, xs, c->dperm, y);
+    });
     return cuda_ok(c, cudaGetLastError(), "near blocks") ? MLF_OK : MLF_E_CUDA;
 }
 
 // C (leaf fields, FP32) = R^T x for every leaf box
 int device_agg_blocks32(Ctx* c, const float2* R, int K, const float2* xs, int nrhs, float2* C, cudaStream_t s) {
     const int nb = (int)c->box_ptr.size() - 1, K2 = 2 * K, ntr = (K2 + NBK_ROWS - 1) / NBK_ROWS;
-    if (blk_narrow(c, nrhs))
-        k32_agg_blk<1><<<dim3(nb * ntr, (nrhs + 7) / 8), 256, 0, s>>>(K2, nrhs, ntr, c->dbox_ptr, R, xs, C);
-    else
-        k32_agg_blk<4><<<dim3(nb * ntr, (nrhs + 31) / 32), 256, 0, s>>>(K2, nrhs, ntr, c->dbox_ptr, R, xs, C);
+    blk_dispatch(c, nrhs, [&](auto tc, auto acc) {
+        constexpr int TC = decltype(tc)::value;
+        k32_agg_blk<TC, decltype(acc)><<<dim3(nb * ntr, (nrhs + 8 * TC - 1) / (8 * TC)), 256, 0, s>>>(
+            K2, nrhs, ntr, c->dbox_ptr, R, xs, C);
+    });
     return cuda_ok(c, cudaGetLastError(), "aggregation blocks") ? MLF_OK : MLF_E_CUDA;
 }
 
@@ -413,12 +507,11 @@ int device_recv_blocks32(Ctx* c, const float2* R, int K, const float2* A, float 
     int st;
     if ((st = near_blocks_setup(c))) return st;
     const int K2 = 2 * K;
-    if (blk_narrow(c, nrhs))
-        k32_recv_blk<1><<<dim3(c->nblk_tiles, (nrhs + 7) / 8), 256, 0, s>>>(K2, nrhs, ld, facy, c->dblk_tiles,
-                                                                             c->dbox_ptr, c->dperm, R, A, y);
-    else
-        k32_recv_blk<4><<<dim3(c->nblk_tiles, (nrhs + 31) / 32), 256, 0, s>>>(K2, nrhs, ld, facy, c->dblk_tiles,
-                                                                              c->dbox_ptr, c->dperm, R, A, y);
+    blk_dispatch(c, nrhs, [&](auto tc, auto acc) {
+        constexpr int TC = decltype(tc)::value;
+        k32_recv_blk<TC, decltype(acc)><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, 0, s>>>(
+            K2, nrhs, ld, facy, c->dblk_tiles, c->dbox_ptr, c->dperm, R, A, y);
+    });
     return cuda_ok(c, cudaGetLastError(), "receive blocks") ? MLF_OK : MLF_E_CUDA;
 }
 
@@ -427,12 +520,11 @@ int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const fl
                         cudaStream_t s) {
     int st;
     if ((st = near_blocks_setup(c))) return st;
-    if (blk_narrow(c, nrhs))
-        k32_own_blk<1><<<dim3(c->nblk_tiles, (nrhs + 7) / 8), 256, 0, s>>>(c->N, nrhs, c->dblk_tiles, c->dbox_ptr,
-                                                                            c->dperm, boff, M, xs, out);
-    else
-        k32_own_blk<4><<<dim3(c->nblk_tiles, (nrhs + 31) / 32), 256, 0, s>>>(c->N, nrhs, c->dblk_tiles, c->dbox_ptr,
-                                                                             c->dperm, boff, M, xs, out);
+    blk_dispatch(c, nrhs, [&](auto tc, auto acc) {
+        constexpr int TC = decltype(tc)::value;
+        k32_own_blk<TC, decltype(acc)><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, 0, s>>>(
+            c->N, nrhs, c->dblk_tiles, c->dbox_ptr, c->dperm, boff, M, xs, out);
+    });
     return cuda_ok(c, cudaGetLastError(), "own-box blocks") ? MLF_OK : MLF_E_CUDA;
 }
 

@@ -292,6 +292,11 @@ class MLFMA:
                         outer=outer.value)
         return dict(x=X, iters=it, relres=rr, status=[CGS_STATUS[int(s)] for s in st], outer=outer.value)
 
+    def set_block_engine(self, engine: int, cols: int = 0):
+        """Box-block GEMM engine of the batched FP32 operator: 1 tensor cores
+        (3xTF32), 0 FP32 FMA; tile width cols 8, 32, 64 (0: by block width)."""
+        _check(load().mlf_set_block_engine(self._h, int(engine), int(cols)), self._h)
+
     def autotune_block(self, candidates=(8, 16, 32, 64, 128)):
         """mlf_autotune_block: block size and near-field tile width for batched
         solves, with the measured FP32 operator time per right-hand side."""
