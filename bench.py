@@ -294,7 +294,12 @@ def profile_fp32_block(nrhs, steps, engine=-1, cols=0):
         call()
     e1.record()
     torch.cuda.synchronize()
-    print(json.dumps({"profile": "fp32 operator", "N": m.N, "nrhs": nrhs, "near_nnz": m.nnz, "engine": engine, "cols": cols,
+    m.set_profiling(True)
+    call()
+    torch.cuda.synchronize()
+    stages = [float(v) for v in m.stage_times()]
+    m.set_profiling(False)
+    print(json.dumps({"profile": "fp32 operator", "stage_ms": stages, "N": m.N, "nrhs": nrhs, "near_nnz": m.nnz, "engine": engine, "cols": cols,
                       "ms_per_call": e0.elapsed_time(e1) / steps}), flush=True)
     m.close()
 

@@ -13,7 +13,9 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 #include <type_traits>
+#include <unordered_set>
 #include <vector>
 
 #include "mlf_internal.h"
@@ -222,50 +224,84 @@ struct MmaAcc {
     }
 };
 
-template <int TC, bool AROW, bool ACONJ, bool XCOL>
-__device__ __forceinline__ void blk_load(BlkTile<TC>& sm, const float2* __restrict__ A, long long lda, int r0,
-                                         int mrows, int kdim, int t0, const float2* __restrict__ X, long long ldx,
-                                         int c0, int ncols) {
-    constexpr int NC = 8 * TC;
-    const int tid = threadIdx.x;
-    for (int q = tid; q < NBK_KC * NBK_ROWS; q += 256) {
-        int k, p;
-        if (AROW) { p = q / NBK_KC; k = q - p * NBK_KC; }
-        else { k = q / NBK_ROWS; p = q - k * NBK_ROWS; }
-        const int t = t0 + k, row = r0 + p;
-        float2 v = make_float2(0.f, 0.f);
-        if (t < kdim && row < mrows) v = AROW ? A[(size_t)row * lda + t] : A[(size_t)t * lda + row];
-        if (ACONJ) v.y = -v.y;
-        sm.Zs[k][p] = v;
-    }
-    for (int q = tid; q < NBK_KC * NC; q += 256) {
-        int k, cc;
-        if (XCOL) { cc = q / NBK_KC; k = q - cc * NBK_KC; }
-        else { k = q / NC; cc = q - k * NC; }
-        const int t = t0 + k, col = c0 + cc;
-        float2 v = make_float2(0.f, 0.f);
-        if (t < kdim && col < ncols) v = XCOL ? X[(size_t)col * ldx + t] : X[(size_t)t * ldx + col];
-        sm.Xs[k][cc] = v;
-    }
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, int src_bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes));
 }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
+constexpr int NBK_STAGES = 3;
+
+// Y tile += A X over kdim, A and X streamed in chunks of 32 through
+// NBK_STAGES cp.async stages (zero-filled past the edges; conjugation of A
+// applied by each thread to the values it copied, before the barrier).
 template <int TC, bool AROW, bool ACONJ, bool XCOL, class Acc>
-__device__ __forceinline__ void blk_mac(Acc& acc, BlkTile<TC>& sm, const float2* __restrict__ A, long long lda,
+__device__ __forceinline__ void blk_mac(Acc& acc, BlkTile<TC>* stage, const float2* __restrict__ A, long long lda,
                                         int r0, int mrows, int kdim, const float2* __restrict__ X, long long ldx,
                                         int c0, int ncols) {
-    for (int t0 = 0; t0 < kdim; t0 += NBK_KC) {
-        blk_load<TC, AROW, ACONJ, XCOL>(sm, A, lda, r0, mrows, kdim, t0, X, ldx, c0, ncols);
+    constexpr int NC = 8 * TC;
+    constexpr int ZPT = NBK_KC * NBK_ROWS / 256, XPT = NBK_KC * NC / 256;
+    const int tid = threadIdx.x;
+    const int nch = (kdim + NBK_KC - 1) / NBK_KC;
+    auto zslot = [&](int u, int& k, int& p) {
+        const int q = tid + 256 * u;
+        if (AROW) { p = q / NBK_KC; k = q - p * NBK_KC; }
+        else { k = q / NBK_ROWS; p = q - k * NBK_ROWS; }
+    };
+    auto issue = [&](int ch) {
+        if (ch < nch) {
+            BlkTile<TC>& sm = stage[ch % NBK_STAGES];
+            const int t0 = ch * NBK_KC;
+#pragma unroll
+            for (int u = 0; u < ZPT; ++u) {
+                int k, p;
+                zslot(u, k, p);
+                const int t = t0 + k, row = r0 + p;
+                const bool ok = t < kdim && row < mrows;
+                const float2* src = ok ? (AROW ? A + (size_t)row * lda + t : A + (size_t)t * lda + row) : A;
+                cp_async8(&sm.Zs[k][p], src, ok ? 8 : 0);
+            }
+#pragma unroll
+            for (int u = 0; u < XPT; ++u) {
+                const int q = tid + 256 * u;
+                int k, cc;
+                if (XCOL) { cc = q / NBK_KC; k = q - cc * NBK_KC; }
+                else { k = q / NC; cc = q - k * NC; }
+                const int t = t0 + k, col = c0 + cc;
+                const bool ok = t < kdim && col < ncols;
+                const float2* src = ok ? (XCOL ? X + (size_t)col * ldx + t : X + (size_t)t * ldx + col) : X;
+                cp_async8(&sm.Xs[k][cc], src, ok ? 8 : 0);
+            }
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int s = 0; s < NBK_STAGES - 1; ++s) issue(s);
+    for (int ch = 0; ch < nch; ++ch) {
+        cp_async_wait<NBK_STAGES - 2>();
+        if (ACONJ) {
+            BlkTile<TC>& sm = stage[ch % NBK_STAGES];
+#pragma unroll
+            for (int u = 0; u < ZPT; ++u) {
+                int k, p;
+                zslot(u, k, p);
+                sm.Zs[k][p].y = -sm.Zs[k][p].y;
+            }
+        }
         __syncthreads();
-        acc.chunk(sm);
-        __syncthreads();
+        issue(ch + NBK_STAGES - 1);
+        acc.chunk(stage[ch % NBK_STAGES]);
     }
+    cp_async_wait<0>();
+    __syncthreads();
 }
 
 // y(:, c0 : c0 + 8 TC) += Z_near x for one 64-row tile of one leaf box.
-// The chunks of all near boxes form one sequence; the next chunk's Z and x
-// values are loaded into registers while the current one is multiplied out
-// of shared memory (software double buffering), so the global loads overlap
-// the arithmetic instead of stalling between barriers.
+// The chunks of all near boxes form one sequence, staged through
+// NBK_STAGES shared-memory buffers by cp.async (zero-filled past the block
+// edges): while chunk c is multiplied, chunks c+1 .. c+STAGES-1 are in flight.
 template <int TC, class Acc>
 __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2* __restrict__ tiles,
                                                     const int* __restrict__ box_ptr, const int* __restrict__ nbox_ptr,
@@ -276,61 +312,60 @@ __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2
     constexpr int NC = 8 * TC;
     constexpr int ZPT = NBK_KC * NBK_ROWS / 256;   // Z values per thread per chunk
     constexpr int XPT = NBK_KC * NC / 256;         // x values per thread per chunk
-    __shared__ __align__(16) BlkTile<TC> sm;
+    extern __shared__ __align__(16) unsigned char near_smem[];
+    BlkTile<TC>* stage = reinterpret_cast<BlkTile<TC>*>(near_smem);
     const int2 tl = tiles[blockIdx.x];
     const int i = tl.x, r0 = tl.y, c0 = blockIdx.y * NC;
     const int ni = box_ptr[i + 1] - box_ptr[i];
     const int tid = threadIdx.x;
+    const int e_beg = nbox_ptr[i], e_end = nbox_ptr[i + 1];
+    int nch = 0;
+    for (int e = e_beg; e < e_end; ++e) {
+        const int j = nbox_list[e];
+        nch += (box_ptr[j + 1] - box_ptr[j] + NBK_KC - 1) / NBK_KC;
+    }
     Acc acc;
     acc.zero();
-    const int e_end = nbox_ptr[i + 1];
-    int e = nbox_ptr[i], t0 = 0;
-    float2 zr[ZPT], xr[XPT];
-    auto load = [&](int ec, int tc) {
-        const int j = nbox_list[ec];
-        const int j0 = box_ptr[j], nj = box_ptr[j + 1] - j0;
-        const float2* zb = Zblk + blk_off[ec];
+    int le = e_beg, lt = 0;   // next chunk to issue
+    auto issue = [&](BlkTile<TC>& sm) {
+        if (le < e_end) {
+            const int j = nbox_list[le];
+            const int j0 = box_ptr[j], nj = box_ptr[j + 1] - j0;
+            const float2* zb = Zblk + blk_off[le];
+            const float2* xb = xs + (size_t)j0 * nrhs;
 #pragma unroll
-        for (int u = 0; u < ZPT; ++u) {
-            const int q = tid + 256 * u;
-            const int k = q / NBK_ROWS, p = q - k * NBK_ROWS;
-            const int t = tc + k, row = r0 + p;
-            zr[u] = (t < nj && row < ni) ? zb[(size_t)t * ni + row] : make_float2(0.f, 0.f);
-        }
+            for (int u = 0; u < ZPT; ++u) {
+                const int q = tid + 256 * u;
+                const int k = q / NBK_ROWS, p = q - k * NBK_ROWS;
+                const int t = lt + k, row = r0 + p;
+                const bool ok = t < nj && row < ni;
+                cp_async8(&sm.Zs[k][p], ok ? zb + (size_t)t * ni + row : zb, ok ? 8 : 0);
+            }
 #pragma unroll
-        for (int u = 0; u < XPT; ++u) {
-            const int q = tid + 256 * u;
-            const int k = q / NC, cc = q - k * NC;
-            const int t = tc + k, col = c0 + cc;
-            xr[u] = (t < nj && col < nrhs) ? xs[(size_t)(j0 + t) * nrhs + col] : make_float2(0.f, 0.f);
+            for (int u = 0; u < XPT; ++u) {
+                const int q = tid + 256 * u;
+                const int k = q / NC, cc = q - k * NC;
+                const int t = lt + k, col = c0 + cc;
+                const bool ok = t < nj && col < nrhs;
+                cp_async8(&sm.Xs[k][cc], ok ? xb + (size_t)t * nrhs + col : xb, ok ? 8 : 0);
+            }
+            lt += NBK_KC;
+            if (lt >= nj) { ++le; lt = 0; }
         }
+        cp_async_commit();   // one group per chunk slot, empty past the end
     };
-    auto next = [&](int& ec, int& tc) {
-        const int j = nbox_list[ec];
-        const int nj = box_ptr[j + 1] - box_ptr[j];
-        tc += NBK_KC;
-        if (tc >= nj) { ++ec; tc = 0; }
-    };
-    if (e < e_end) load(e, t0);
-    while (e < e_end) {
 #pragma unroll
-        for (int u = 0; u < ZPT; ++u) {
-            const int q = tid + 256 * u;
-            sm.Zs[q / NBK_ROWS][q % NBK_ROWS] = zr[u];
-        }
-#pragma unroll
-        for (int u = 0; u < XPT; ++u) {
-            const int q = tid + 256 * u;
-            sm.Xs[q / NC][q % NC] = xr[u];
-        }
-        __syncthreads();
-        next(e, t0);
-        if (e < e_end) load(e, t0);
-        acc.chunk(sm);
-        __syncthreads();
+    for (int s = 0; s < NBK_STAGES - 1; ++s) issue(stage[s]);
+    for (int cc = 0; cc < nch; ++cc) {
+        cp_async_wait<NBK_STAGES - 2>();   // this thread's copies of chunk cc have landed
+        __syncthreads();                   // everyone's have; everyone is done with chunk cc-1
+        issue(stage[(cc + NBK_STAGES - 1) % NBK_STAGES]);
+        acc.chunk(stage[cc % NBK_STAGES]);
     }
+    cp_async_wait<0>();
+    __syncthreads();
     const int i0 = box_ptr[i];
-    acc.store(sm, [&](int rt, int ct, float2 v) {
+    acc.store(stage[0], [&](int rt, int ct, float2 v) {
         const int row = r0 + rt, col = c0 + ct;
         if (row < ni && col < nrhs) {
             double2* yp = y + (size_t)col * ld + perm[i0 + row];
@@ -347,14 +382,15 @@ template <int TC, class Acc>
 __global__ void __launch_bounds__(256) k32_agg_blk(int K2, int nrhs, int ntr, const int* __restrict__ box_ptr,
                                                    const float2* __restrict__ R, const float2* __restrict__ xs,
                                                    float2* __restrict__ C) {
-    __shared__ __align__(16) BlkTile<TC> sm;
+    extern __shared__ __align__(16) unsigned char blk_smem[];
+    BlkTile<TC>* stage = reinterpret_cast<BlkTile<TC>*>(blk_smem);
     const int b = blockIdx.x / ntr, r0 = (blockIdx.x - b * ntr) * NBK_ROWS, c0 = blockIdx.y * 8 * TC;
     const int j0 = box_ptr[b], nb = box_ptr[b + 1] - j0;
     Acc acc;
     acc.zero();
-    blk_mac<TC, false, false, false>(acc, sm, R + (size_t)j0 * K2, K2, r0, K2, nb, xs + (size_t)j0 * nrhs, nrhs, c0,
-                                     nrhs);
-    acc.store(sm, [&](int rt, int ct, float2 v) {
+    blk_mac<TC, false, false, false>(acc, stage, R + (size_t)j0 * K2, K2, r0, K2, nb, xs + (size_t)j0 * nrhs, nrhs,
+                                     c0, nrhs);
+    acc.store(stage[0], [&](int rt, int ct, float2 v) {
         const int row = r0 + rt, col = c0 + ct;
         if (row < K2 && col < nrhs) C[((size_t)b * nrhs + col) * K2 + row] = v;
     });
@@ -367,15 +403,16 @@ __global__ void __launch_bounds__(256) k32_recv_blk(int K2, int nrhs, int ld, fl
                                                     const int2* __restrict__ tiles, const int* __restrict__ box_ptr,
                                                     const int* __restrict__ perm, const float2* __restrict__ R,
                                                     const float2* __restrict__ Af, double2* __restrict__ y) {
-    __shared__ __align__(16) BlkTile<TC> sm;
+    extern __shared__ __align__(16) unsigned char blk_smem[];
+    BlkTile<TC>* stage = reinterpret_cast<BlkTile<TC>*>(blk_smem);
     const int2 tl = tiles[blockIdx.x];
     const int b = tl.x, r0 = tl.y, c0 = blockIdx.y * 8 * TC;
     const int j0 = box_ptr[b], nb = box_ptr[b + 1] - j0;
     Acc acc;
     acc.zero();
-    blk_mac<TC, true, true, true>(acc, sm, R + (size_t)j0 * K2, K2, r0, nb, K2, Af + (size_t)b * nrhs * K2, K2, c0,
+    blk_mac<TC, true, true, true>(acc, stage, R + (size_t)j0 * K2, K2, r0, nb, K2, Af + (size_t)b * nrhs * K2, K2, c0,
                                   nrhs);
-    acc.store(sm, [&](int rt, int ct, float2 v) {
+    acc.store(stage[0], [&](int rt, int ct, float2 v) {
         const int row = r0 + rt, col = c0 + ct;
         if (row < nb && col < nrhs)
             y[(size_t)col * ld + perm[j0 + row]] = make_double2(-(double)(facy * v.y), (double)(facy * v.x));
@@ -389,14 +426,15 @@ __global__ void __launch_bounds__(256) k32_own_blk(int N, int nrhs, const int2* 
                                                    const int* __restrict__ box_ptr, const int* __restrict__ perm,
                                                    const long long* __restrict__ boff, const float2* __restrict__ M,
                                                    const float2* __restrict__ xs, float2* __restrict__ out) {
-    __shared__ __align__(16) BlkTile<TC> sm;
+    extern __shared__ __align__(16) unsigned char blk_smem[];
+    BlkTile<TC>* stage = reinterpret_cast<BlkTile<TC>*>(blk_smem);
     const int2 tl = tiles[blockIdx.x];
     const int b = tl.x, r0 = tl.y, c0 = blockIdx.y * 8 * TC;
     const int j0 = box_ptr[b], nb = box_ptr[b + 1] - j0;
     Acc acc;
     acc.zero();
-    blk_mac<TC, true, false, false>(acc, sm, M + boff[b], nb, r0, nb, nb, xs + (size_t)j0 * nrhs, nrhs, c0, nrhs);
-    acc.store(sm, [&](int rt, int ct, float2 v) {
+    blk_mac<TC, true, false, false>(acc, stage, M + boff[b], nb, r0, nb, nb, xs + (size_t)j0 * nrhs, nrhs, c0, nrhs);
+    acc.store(stage[0], [&](int rt, int ct, float2 v) {
         const int row = r0 + rt, col = c0 + ct;
         if (row < nb && col < nrhs) out[(size_t)col * N + perm[j0 + row]] = v;
     });
@@ -449,6 +487,19 @@ static int near_blocks_setup(Ctx* c) {
     return MLF_OK;
 }
 
+// dynamic shared memory of the staged kernels: raise each instantiation's
+// limit once (before any stream capture)
+template <class K>
+static size_t staged_smem(K kernel, size_t tile_bytes) {
+    const size_t smem = NBK_STAGES * tile_bytes;
+    static std::mutex mu;
+    static std::unordered_set<const void*> done;   // keyed by the kernel itself
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.insert((const void*)kernel).second)
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return smem;
+}
+
 // tile width in columns: the autotuner's choice, else by the block's width
 static int blk_width(const Ctx* c, int nrhs) {
     if (c->blk_cols) return c->blk_cols;
@@ -484,7 +535,8 @@ int device_near_blocks32(Ctx* c, const float2* xs, int ld, int nrhs, double2* y,
     if ((st = near_blocks_setup(c))) return st;
     blk_dispatch(c, nrhs, [&](auto tc, auto acc) {
         constexpr int TC = decltype(tc)::value;
-        k32_near_blk<TC, decltype(acc)><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, 0, s>>>(
+        const size_t smem = staged_smem(k32_near_blk<TC, decltype(acc)>, sizeof(BlkTile<TC>));
+        k32_near_blk<TC, decltype(acc)><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, smem, s>>>(
             nrhs, ld, c->dblk_tiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, c->dblk_off, c->dZblk, xs, c->dperm, y);
     });
     return cuda_ok(c, cudaGetLastError(), "near blocks") ? MLF_OK : MLF_E_CUDA;
@@ -495,7 +547,8 @@ int device_agg_blocks32(Ctx* c, const float2* R, int K, const float2* xs, int nr
     const int nb = (int)c->box_ptr.size() - 1, K2 = 2 * K, ntr = (K2 + NBK_ROWS - 1) / NBK_ROWS;
     blk_dispatch(c, nrhs, [&](auto tc, auto acc) {
         constexpr int TC = decltype(tc)::value;
-        k32_agg_blk<TC, decltype(acc)><<<dim3(nb * ntr, (nrhs + 8 * TC - 1) / (8 * TC)), 256, 0, s>>>(
+        const size_t smem = staged_smem(k32_agg_blk<TC, decltype(acc)>, sizeof(BlkTile<TC>));
+        k32_agg_blk<TC, decltype(acc)><<<dim3(nb * ntr, (nrhs + 8 * TC - 1) / (8 * TC)), 256, smem, s>>>(
             K2, nrhs, ntr, c->dbox_ptr, R, xs, C);
     });
     return cuda_ok(c, cudaGetLastError(), "aggregation blocks") ? MLF_OK : MLF_E_CUDA;
@@ -509,7 +562,8 @@ int device_recv_blocks32(Ctx* c, const float2* R, int K, const float2* A, float 
     const int K2 = 2 * K;
     blk_dispatch(c, nrhs, [&](auto tc, auto acc) {
         constexpr int TC = decltype(tc)::value;
-        k32_recv_blk<TC, decltype(acc)><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, 0, s>>>(
+        const size_t smem = staged_smem(k32_recv_blk<TC, decltype(acc)>, sizeof(BlkTile<TC>));
+        k32_recv_blk<TC, decltype(acc)><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, smem, s>>>(
             K2, nrhs, ld, facy, c->dblk_tiles, c->dbox_ptr, c->dperm, R, A, y);
     });
     return cuda_ok(c, cudaGetLastError(), "receive blocks") ? MLF_OK : MLF_E_CUDA;
@@ -522,7 +576,8 @@ int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const fl
     if ((st = near_blocks_setup(c))) return st;
     blk_dispatch(c, nrhs, [&](auto tc, auto acc) {
         constexpr int TC = decltype(tc)::value;
-        k32_own_blk<TC, decltype(acc)><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, 0, s>>>(
+        const size_t smem = staged_smem(k32_own_blk<TC, decltype(acc)>, sizeof(BlkTile<TC>));
+        k32_own_blk<TC, decltype(acc)><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, smem, s>>>(
             c->N, nrhs, c->dblk_tiles, c->dbox_ptr, c->dperm, boff, M, xs, out);
     });
     return cuda_ok(c, cudaGetLastError(), "own-box blocks") ? MLF_OK : MLF_E_CUDA;
