@@ -367,8 +367,8 @@ def learned_sample(steps=3000, seed=0):
     res["learned"]["used"] = out["used"]
     ref = res["exact_neighbourhood_inverse"]["_db"]
     for k in res:
-        res[k]["rcs_db_maxdiff_vs_exact"] = float(np.abs(res[k].pop("_db") - ref).max()) \
-            if res[k]["status"] == "converged" else None
+        db = res[k].pop("_db")
+        res[k]["rcs_db_maxdiff_vs_exact"] = float(np.abs(db - ref).max()) if res[k]["status"] == "converged" else None
     m.close()
     return {"workload": "superellipsoid exponent 4, 2 x 1 x 1 lambda, icosphere-4 (7680 RWG); trained on 3 seeded "
                         "superellipsoids of the same mesh density", "train_s": t_train, "gamma": lp.gamma,

@@ -201,14 +201,16 @@ int mlf_set_gs_passes(mlf_ctx* ctx, int passes);
 int mlf_solve_times(mlf_ctx* ctx, double* out4);
 
 /* Autotuner for batched solves: times the FP32 operator on each candidate
- * block of right-hand sides (candidates[ncand], 1..4096) with both near-field
- * tile widths (8 and 32 columns) and returns the smallest block whose time
+ * block of right-hand sides (candidates[ncand], 1..4096) with both box-block
+ * GEMM engines and the tile widths 8, 32 and 64 columns, and returns the
+ * smallest block whose time
  * per right-hand side is within 5 % of the best, with its tile width (0 for a
- * single column); the tile width is kept for later operator calls.
+ * single column) and engine (best_engine, optional: 1 tensor cores, 0 FP32
+ * FMA); both are kept for later operator calls.
  * per_rhs_ms (optional, ncand) receives the best time per right-hand side of
  * each candidate.  No counterpart in the reference. */
 int mlf_autotune_block(mlf_ctx* ctx, const int* candidates, int ncand, int* best_block, int* best_cols,
-                       float* per_rhs_ms);
+                       int* best_engine, float* per_rhs_ms);
 
 /* Box-block GEMM engine of the FP32 operator on blocks of columns: 1 = tensor
  * cores (mma.sync m16n8k8 TF32 with the 3xTF32 split, within a few 1e-6 of

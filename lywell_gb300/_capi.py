@@ -40,7 +40,7 @@ SIGNATURES = {
     "mlf_set_gs_passes": (C.c_int, [vp, C.c_int]),
     "mlf_solve_times": (C.c_int, [vp, vp]),
     "mlf_precond_apply32": (C.c_int, [vp, vp, vp, C.c_int]),
-    "mlf_autotune_block": (C.c_int, [vp, vp, C.c_int, vp, vp, vp]),
+    "mlf_autotune_block": (C.c_int, [vp, vp, C.c_int, vp, vp, vp, vp]),
     "mlf_set_block_engine": (C.c_int, [vp, C.c_int, C.c_int]),
     "mlf_mlp_create": (C.c_int, [vp, C.c_int, C.c_ulonglong]),
     "mlf_mlp_free": (None, [vp]),

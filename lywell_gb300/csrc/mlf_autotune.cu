@@ -30,7 +30,8 @@ __global__ void k_fill_pattern(size_t n, double2* __restrict__ x) {
     x[i] = make_double2(((h & 0xffff) / 32767.5) - 1.0, (((h >> 16) & 0xffff) / 32767.5) - 1.0);
 }
 
-int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* best_cols, float* per_rhs_ms) {
+int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* best_cols, int* best_engine,
+                   float* per_rhs_ms) {
     int bmax = 0;
     for (int q = 0; q < ncand; ++q) bmax = std::max(bmax, cand[q]);
     if (bmax <= 0) return MLF_E_ARG;
@@ -85,6 +86,7 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
         *best_block = cand[pick];
         *best_cols = cand[pick] == 1 ? 0 : colsel[pick];
         c->blk_engine = engsel[pick];
+        if (best_engine) *best_engine = engsel[pick];
     } else {
         c->blk_engine = saved_eng;
     }
@@ -109,11 +111,11 @@ extern "C" int mlf_set_block_engine(mlf_ctx* h, int engine, int cols) {
 }
 
 extern "C" int mlf_autotune_block(mlf_ctx* h, const int* candidates, int ncand, int* best_block, int* best_cols,
-                                  float* per_rhs_ms) {
+                                  int* best_engine, float* per_rhs_ms) {
     if (!h || !candidates || ncand <= 0 || !best_block || !best_cols) return MLF_E_ARG;
     for (int q = 0; q < ncand; ++q)
         if (candidates[q] <= 0 || candidates[q] > 4096) return MLF_E_ARG;
     Ctx* c = &h->c;
     if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
-    return autotune_block(c, candidates, ncand, best_block, best_cols, per_rhs_ms);
+    return autotune_block(c, candidates, ncand, best_block, best_cols, best_engine, per_rhs_ms);
 }

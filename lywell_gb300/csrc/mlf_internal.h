@@ -213,7 +213,8 @@ int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const fl
 void near_blocks_free(Ctx* c);
 int near_blocks_ensure(Ctx* c);
 int lp_tokens(Ctx* c, int with_target, float* X, float* T, long long cap, long long* ntok, int* bad_box);
-int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* best_cols, float* per_rhs_ms);
+int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* best_cols, int* best_engine,
+                   float* per_rhs_ms);
 int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
                        int* iters, double* relres, int precond, int* status, double inner_tol, int* outer);
 int device_nearinv_apply(Ctx* c, const double2* y, double2* x, int nrhs, cudaStream_t s);

@@ -115,7 +115,7 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
             if (b <= nang) cand.push_back(b);
         if (cand.empty()) cand.push_back(nang);
         int cols = 0;
-        if ((st = autotune_block(c, cand.data(), (int)cand.size(), &bsel, &cols, nullptr))) return st;
+        if ((st = autotune_block(c, cand.data(), (int)cand.size(), &bsel, &cols, nullptr, nullptr))) return st;
     }
     const int bs = std::max(1, std::min(bsel, nang));
     double2 *b = nullptr, *x = nullptr;

@@ -302,10 +302,11 @@ class MLFMA:
         solves, with the measured FP32 operator time per right-hand side."""
         cand = np.ascontiguousarray(candidates, dtype=np.int32)
         per = np.zeros(cand.size, dtype=np.float32)
-        best, cols = C.c_int(), C.c_int()
-        _check(load().mlf_autotune_block(self._h, _p(cand), cand.size, C.byref(best), C.byref(cols), _p(per)),
-               self._h)
+        best, cols, eng = C.c_int(), C.c_int(), C.c_int()
+        _check(load().mlf_autotune_block(self._h, _p(cand), cand.size, C.byref(best), C.byref(cols), C.byref(eng),
+                                         _p(per)), self._h)
         return dict(block=best.value, tile_cols=cols.value,
+                    engine="tensor cores (3xTF32 mma.sync)" if eng.value == 1 else "FP32 FMA",
                     per_rhs_ms={int(b): float(t) for b, t in zip(cand, per)})
 
     def precond_apply32(self, y):
