@@ -382,7 +382,7 @@ __global__ void k_mdot32(int N, int nrhs, const float2* __restrict__ V, size_t v
 // w (MD_E values per thread) in registers and streams the nvec basis vectors
 // past it, MD_G vectors per block reduction.
 // partial[(i * nrhs + col) * gridDim.x + blockIdx.x] = sum conj(V_i) w over the slice.
-constexpr int MD_E = 8, MD_G = 4;
+constexpr int MD_E = 8, MD_G = 8;
 __global__ void __launch_bounds__(256) k_mdot32b(int N, int nrhs, int nvec, const float2* __restrict__ V,
                                                  size_t vstride, const float2* __restrict__ w,
                                                  double2* __restrict__ partial) {
