@@ -32,14 +32,15 @@ __global__ void k_fill_pattern(size_t n, double2* __restrict__ x) {
 
 int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* best_cols, int* best_engine,
                    float* per_rhs_ms) {
+    DevScope ds;
     int bmax = 0;
     for (int q = 0; q < ncand; ++q) bmax = std::max(bmax, cand[q]);
     if (bmax <= 0) return MLF_E_ARG;
     cudaStream_t s = c->stream;
     double2 *x = nullptr, *y = nullptr;
     const size_t n = (size_t)c->N * bmax;
-    CK(cudaMalloc(&x, n * sizeof(double2)));
-    CK(cudaMalloc(&y, n * sizeof(double2)));
+    CK(ds.alloc(&x, n * sizeof(double2)));
+    CK(ds.alloc(&y, n * sizeof(double2)));
     k_fill_pattern<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, x);
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -94,8 +95,6 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
     c->profiling = saved_prof;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    cudaFree(x);
-    cudaFree(y);
     return st;
 }
 

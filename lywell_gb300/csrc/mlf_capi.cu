@@ -241,6 +241,7 @@ int mlf_ilu0_solve(mlf_ctx* h, const double* y, double* x, int nrhs) {
 
 int mlf_cgs(mlf_ctx* h, const double* b, const double* x0, double tol, int maxit, int nrhs, double* x,
             int* iters, double* relres, int precond_kind, int* status_out) {
+    DevScope ds;
     if (!h || !b || !x || !iters || !relres || !status_out || nrhs <= 0 || maxit <= 0 || !(tol > 0))
         return MLF_E_ARG;
     Ctx* c = &h->c;
@@ -253,24 +254,22 @@ int mlf_cgs(mlf_ctx* h, const double* b, const double* x0, double tol, int maxit
     if (!bind_device(c)) return MLF_E_CUDA;
     const size_t n = (size_t)c->N * nrhs;
     double2 *db = nullptr, *dx = nullptr, *dx0 = nullptr;
-    CK(cudaMalloc(&db, n * sizeof(double2)));
-    CK(cudaMalloc(&dx, n * sizeof(double2)));
+    CK(ds.alloc(&db, n * sizeof(double2)));
+    CK(ds.alloc(&dx, n * sizeof(double2)));
     int st = h2d_cols(c, db, b, nrhs, c->N);
     if (!st && x0) {
-        CK(cudaMalloc(&dx0, n * sizeof(double2)));
+        CK(ds.alloc(&dx0, n * sizeof(double2)));
         st = h2d_cols(c, dx0, x0, nrhs, c->N);
     }
     if (!st) st = device_cgs(c, db, dx0, tol, maxit, nrhs, dx, iters, relres, precond_kind, status_out);
     if (!st) st = d2h_cols(c, x, dx, nrhs, c->N);
     if (!st) CK(cudaStreamSynchronize(c->stream));
-    cudaFree(db);
-    cudaFree(dx);
-    if (dx0) cudaFree(dx0);
     return st;
 }
 
 int mlf_solve(mlf_ctx* h, const double* b, const double* x0, double tol, int maxit, int nrhs, int precond_kind,
               int mode, double inner_tol, double* x, int* iters, double* relres, int* status_out, int* outer) {
+    DevScope ds;
     if (!h || !b || !x || !iters || !relres || !status_out || nrhs <= 0 || maxit <= 0 || !(tol > 0)) return MLF_E_ARG;
     if (mode != 0 && mode != 1) return MLF_E_ARG;
     if (mode == 0) {
@@ -286,11 +285,11 @@ int mlf_solve(mlf_ctx* h, const double* b, const double* x0, double tol, int max
     if (!bind_device(c)) return MLF_E_CUDA;
     const size_t n = (size_t)c->N * nrhs;
     double2 *db = nullptr, *dx = nullptr, *dx0 = nullptr;
-    CK(cudaMalloc(&db, n * sizeof(double2)));
-    CK(cudaMalloc(&dx, n * sizeof(double2)));
+    CK(ds.alloc(&db, n * sizeof(double2)));
+    CK(ds.alloc(&dx, n * sizeof(double2)));
     int st = h2d_cols(c, db, b, nrhs, c->N);
     if (!st && x0) {
-        CK(cudaMalloc(&dx0, n * sizeof(double2)));
+        CK(ds.alloc(&dx0, n * sizeof(double2)));
         st = h2d_cols(c, dx0, x0, nrhs, c->N);
     }
     int outer_k = 0;
@@ -300,9 +299,6 @@ int mlf_solve(mlf_ctx* h, const double* b, const double* x0, double tol, int max
     if (outer) *outer = outer_k;
     if (!st) st = d2h_cols(c, x, dx, nrhs, c->N);
     if (!st) CK(cudaStreamSynchronize(c->stream));
-    cudaFree(db);
-    cudaFree(dx);
-    if (dx0) cudaFree(dx0);
     return st;
 }
 
@@ -364,6 +360,7 @@ __global__ void k_cast_fd(size_t n, const float2* __restrict__ a, double2* __res
 }  // namespace
 
 int mlf_precond_apply32(mlf_ctx* h, const double* y, double* x, int nrhs) {
+    DevScope ds;
     if (!h || !y || !x || nrhs <= 0) return MLF_E_ARG;
     Ctx* c = &h->c;
     if (!bind_device(c)) return MLF_E_CUDA;
@@ -372,8 +369,8 @@ int mlf_precond_apply32(mlf_ctx* h, const double* y, double* x, int nrhs) {
     if ((st = ensure_io(c, n))) return st;
     if ((st = h2d_cols(c, c->dx_io, y, nrhs, c->N))) return st;
     float2 *a = nullptr, *b = nullptr;
-    CK(cudaMalloc(&a, n * sizeof(float2)));
-    CK(cudaMalloc(&b, n * sizeof(float2)));
+    CK(ds.alloc(&a, n * sizeof(float2)));
+    CK(ds.alloc(&b, n * sizeof(float2)));
     const unsigned g = (unsigned)((n + 255) / 256);
     k_cast_df<<<g, 256, 0, c->stream>>>(n, c->dx_io, a);
     st = device_nearinv_apply32(c, a, b, nrhs, c->stream);
@@ -382,8 +379,6 @@ int mlf_precond_apply32(mlf_ctx* h, const double* y, double* x, int nrhs) {
         st = d2h_cols(c, x, c->dy_io, nrhs, c->N);
     }
     if (!st && !cuda_ok(c, cudaStreamSynchronize(c->stream), "precond32")) st = MLF_E_CUDA;
-    cudaFree(a);
-    cudaFree(b);
     return st;
 }
 

@@ -14,11 +14,16 @@
 //                   steps in the oracle's order
 //   k_near          complex(4) near-field block (Zmn_MoM, modMoM.f90:85-128)
 // Matvec kernels (MatxVec_MLFMA, modMLFMA.f90:1901-1946):
-//   k_aggregate     leaf C = sum_n R_n x_n                (:1805-1811)
-//   k_interp_up     parent C += shift * Interpolar(child C) (:1818-1831)
-//   k_translate     B = w * sum_far C_src T                (:1838-1853)
-//   k_anterp_down   A = B + Anterpolar(shift* parent A|B)  (:1857-1897)
-//   k_receive_near  y = fac sum conj(R) A + Znear x        (:1915-1942)
+//   k_aggregate       leaf C = sum_n R_n x_n                  (:1805-1811)
+//   k_interp_sep      parent C += shift * Interpolar(child C), as a theta
+//                     pass then a phi pass (mlf_sep.cuh)       (:1818-1831)
+//   k_translate       B = w * sum_far C_src T                  (:1838-1853)
+//   k_anterp_sep      A = B + Anterpolar(shift* parent A|B), transposed
+//                     phi pass then theta pass (mlf_sep.cuh)   (:1857-1897)
+//   k_receive_near_d  y = fac sum conj(R) A + Znear x, near values in
+//                     complex(8)                               (:1915-1942)
+//   k_interp_up, k_anterp_down, k_receive_near: the 9-tap forms, used by the
+//                     allocation-free entry point (mlf_noalloc.cu)
 #include <cuda_runtime.h>
 
 #include <algorithm>

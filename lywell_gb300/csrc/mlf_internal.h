@@ -16,6 +16,26 @@
 
 namespace mlf {
 
+// Device allocations of one call, released when the call returns (error
+// returns included).
+struct DevScope {
+    std::vector<void*> ptrs;
+    DevScope() = default;
+    DevScope(const DevScope&) = delete;
+    DevScope& operator=(const DevScope&) = delete;
+    template <class T>
+    cudaError_t alloc(T** p, size_t bytes) {
+        void* q = nullptr;
+        const cudaError_t e = cudaMalloc(&q, bytes);
+        *p = static_cast<T*>(q);
+        if (e == cudaSuccess) ptrs.push_back(q);
+        return e;
+    }
+    ~DevScope() {
+        for (void* q : ptrs) cudaFree(q);
+    }
+};
+
 constexpr double PI = 3.141592653589793;
 constexpr double MU = 1.2566370614E-6;
 constexpr double EPSI = 8.8541878176E-12;

@@ -382,7 +382,7 @@ __global__ void k_mdot32(int N, int nrhs, const float2* __restrict__ V, size_t v
 // w (MD_E values per thread) in registers and streams the nvec basis vectors
 // past it, MD_G vectors per block reduction.
 // partial[(i * nrhs + col) * gridDim.x + blockIdx.x] = sum conj(V_i) w over the slice.
-constexpr int MD_E = 8, MD_G = 8;
+constexpr int MD_E = 8, MD_G = 4;
 __global__ void __launch_bounds__(256) k_mdot32b(int N, int nrhs, int nvec, const float2* __restrict__ V,
                                                  size_t vstride, const float2* __restrict__ w,
                                                  double2* __restrict__ partial) {
@@ -574,6 +574,7 @@ static int apply_precond64(Ctx* c, int precond, int nrhs, const double2* in, dou
 // x += M^-1 d with the FP64 preconditioner.
 int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
                        int* iters, double* relres, int precond, int* status, double inner_tol, int* outer) {
+    DevScope ds;
     const int N = c->N;
     const int m = std::max(4, std::min(c->gmres_m, 2000));
     const size_t V1 = (size_t)N * nrhs;
@@ -581,16 +582,16 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
     float2 *V = nullptr, *w32 = nullptr, *t32 = nullptr;
     double2 *w = nullptr, *r = nullptr, *t64 = nullptr, *partial = nullptr, *dred = nullptr;
     double* dscale = nullptr;
-    CK(cudaMalloc(&V, (size_t)(m + 1) * V1 * sizeof(float2)));
-    CK(cudaMalloc(&w32, V1 * sizeof(float2)));
-    CK(cudaMalloc(&t32, V1 * sizeof(float2)));
-    CK(cudaMalloc(&w, V1 * sizeof(double2)));
-    CK(cudaMalloc(&r, V1 * sizeof(double2)));
-    CK(cudaMalloc(&t64, V1 * sizeof(double2)));
+    CK(ds.alloc(&V, (size_t)(m + 1) * V1 * sizeof(float2)));
+    CK(ds.alloc(&w32, V1 * sizeof(float2)));
+    CK(ds.alloc(&t32, V1 * sizeof(float2)));
+    CK(ds.alloc(&w, V1 * sizeof(double2)));
+    CK(ds.alloc(&r, V1 * sizeof(double2)));
+    CK(ds.alloc(&t64, V1 * sizeof(double2)));
     const int md_chunks = (N + 256 * MD_E - 1) / (256 * MD_E);
-    CK(cudaMalloc(&partial, (size_t)(m + 1) * nrhs * std::max(GM_BLOCKS, md_chunks) * sizeof(double2)));
-    CK(cudaMalloc(&dred, (size_t)(m + 1) * nrhs * sizeof(double2)));
-    CK(cudaMalloc(&dscale, nrhs * sizeof(double)));
+    CK(ds.alloc(&partial, (size_t)(m + 1) * nrhs * std::max(GM_BLOCKS, md_chunks) * sizeof(double2)));
+    CK(ds.alloc(&dred, (size_t)(m + 1) * nrhs * sizeof(double2)));
+    CK(ds.alloc(&dscale, nrhs * sizeof(double)));
     if (x0) CK(cudaMemcpyAsync(x, x0, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     else CK(cudaMemsetAsync(x, 0, V1 * sizeof(double2), s));
     const unsigned g = (unsigned)std::min<size_t>((N + 255) / 256, 2048);
@@ -754,8 +755,6 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
         cudaStreamSynchronize(s);
         c->solve_ms[3] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
     }
-    cudaFree(V); cudaFree(w32); cudaFree(t32); cudaFree(w); cudaFree(r); cudaFree(t64); cudaFree(partial);
-    cudaFree(dred); cudaFree(dscale);
     return st;
 }
 

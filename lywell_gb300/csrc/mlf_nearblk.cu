@@ -441,6 +441,7 @@ __global__ void __launch_bounds__(256) k32_own_blk(int N, int nrhs, const int2* 
 }
 
 static int near_blocks_setup(Ctx* c) {
+    DevScope ds;
     if (c->blk_ok) return MLF_OK;
     if (need_tree(c)) return MLF_E_STATE;
     const int nb = (int)c->box_ptr.size() - 1;
@@ -471,7 +472,7 @@ static int near_blocks_setup(Ctx* c) {
     CK(cudaMalloc(&c->dnbox_ptr, (nb + 1) * sizeof(int)));
     CK(cudaMalloc(&c->dnbox_list, std::max(ne, 1) * sizeof(int)));
     CK(cudaMalloc(&c->dblk_tiles, std::max<size_t>(tiles.size(), 1) * sizeof(int2)));
-    CK(cudaMalloc(&dentry, std::max(ne, 1) * sizeof(int)));
+    CK(ds.alloc(&dentry, std::max(ne, 1) * sizeof(int)));
     CK(cudaMemcpy(c->dblk_off, off.data(), (ne + 1) * sizeof(long long), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->dnbox_ptr, c->nbox_ptr.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->dnbox_list, c->nbox_list.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
@@ -481,7 +482,6 @@ static int near_blocks_setup(Ctx* c) {
                                                   c->dja, c->dZ, c->dZblk);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
-    cudaFree(dentry);
     c->nblk_tiles = (int)tiles.size();
     c->blk_ok = 1;
     return MLF_OK;

@@ -304,6 +304,7 @@ int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStr
 }
 
 int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
+    DevScope ds;
     if (need_tree(c)) return MLF_E_STATE;
     const int nl = c->nlev;
     const Level& leaf = c->lv[nl];
@@ -343,8 +344,8 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     double2* work = nullptr;
     int* dbad = nullptr;
     int* dbases = nullptr;
-    CK(cudaMalloc(&work, slab * batch * sizeof(double2)));
-    CK(cudaMalloc(&dbad, sizeof(int)));
+    CK(ds.alloc(&work, slab * batch * sizeof(double2)));
+    CK(ds.alloc(&dbad, sizeof(int)));
     const int big = 0x7fffffff;
     CK(cudaMemcpy(dbad, &big, sizeof(int), cudaMemcpyHostToDevice));
     dbases = c->dperm;   // the box-sorted basis list
@@ -358,8 +359,6 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     int hbad = 0;
     CK(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    cudaFree(work);
-    cudaFree(dbad);
     *bad_box = hbad == big ? 0 : hbad;
     c->nearinv_ok = *bad_box == 0;
     return MLF_OK;

@@ -599,6 +599,13 @@ int build_octree(Ctx* c) {
         L.ntrans = (int)(L.rab.size() / 3);
     }
     // near CSR rows in basis order (llenarZesparcida, modMLFMA.f90:1594-1634)
+    // the CSR row pointers are int32 (the reference's integer(4) ia_MLFMA)
+    long long total = 0;
+    for (int m = 0; m < N; ++m) total += c->near_ptr[c->box_of[m] + 1] - c->near_ptr[c->box_of[m]];
+    if (total > 2000000000LL) {
+        c->err = "near field larger than 2^31 entries";
+        return MLF_E_ARG;
+    }
     c->ia.assign(N + 1, 0);
     for (int m = 0; m < N; ++m) {
         const int b = c->box_of[m];
@@ -803,16 +810,19 @@ int build_fmm(Ctx* c) {
         c->nbox_ptr.push_back((int)c->nbox_list.size());
     }
     L.ntrans = (int)(L.rab.size() / 3);
+    // the CSR row pointers are int32 (the reference's integer(4) ia_MLFMA)
+    long long total = 0;
+    for (int m = 0; m < N; ++m) total += c->near_ptr[c->box_of[m] + 1] - c->near_ptr[c->box_of[m]];
+    if (total > 2000000000LL) {
+        c->err = "near field larger than 2^31 entries";
+        return MLF_E_ARG;
+    }
     c->ia.assign(N + 1, 0);
     for (int m = 0; m < N; ++m) {
         const int b = c->box_of[m];
         c->ia[m + 1] = c->ia[m] + (c->near_ptr[b + 1] - c->near_ptr[b]);
     }
     c->nnz = c->ia[N];
-    if (c->nnz > 2000000000LL) {
-        c->err = "near field larger than 2^31 entries";
-        return MLF_E_ARG;
-    }
     c->ja.resize(c->nnz);
     for (int m = 0; m < N; ++m) {
         const int b = c->box_of[m];

@@ -515,10 +515,11 @@ __global__ void k_rcs(int N, const double* __restrict__ t_baric, const int* __re
 }
 
 int device_excitation(Ctx* c, const double* dirs, const double2* pols, double2 ctte, int nrhs, double2* b) {
+    DevScope ds;
     double* ddirs = nullptr;
     double2* dpols = nullptr;
-    CK(cudaMalloc(&ddirs, 3 * (size_t)nrhs * sizeof(double)));
-    CK(cudaMalloc(&dpols, 3 * (size_t)nrhs * sizeof(double2)));
+    CK(ds.alloc(&ddirs, 3 * (size_t)nrhs * sizeof(double)));
+    CK(ds.alloc(&dpols, 3 * (size_t)nrhs * sizeof(double2)));
     CK(cudaMemcpyAsync(ddirs, dirs, 3 * (size_t)nrhs * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dpols, pols, 3 * (size_t)nrhs * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
     dim3 g((c->N + 127) / 128, nrhs);
@@ -526,13 +527,12 @@ int device_excitation(Ctx* c, const double* dirs, const double2* pols, double2 c
                                            c->de_po, c->de_long, c->ph.w * c->ph.smue, b);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
-    cudaFree(ddirs);
-    cudaFree(dpols);
     return MLF_OK;
 }
 
 int device_rcs(Ctx* c, const double2* I, const double2* pol, double2 ctte, const double* th, const double* ph,
                int nang, double* sigma) {
+    DevScope ds;
     // calc_RCS (modRCS.f90:109-153): observation radius from the edge-centre
     // bounding box; calc_E uses the triangle centroids
     const int N = c->N;
@@ -562,9 +562,9 @@ int device_rcs(Ctx* c, const double2* I, const double2* pol, double2 ctte, const
         den += vx * vx + vy * vy;
     }
     double *dth = nullptr, *dph = nullptr, *dsig = nullptr;
-    CK(cudaMalloc(&dth, nang * sizeof(double)));
-    CK(cudaMalloc(&dph, nang * sizeof(double)));
-    CK(cudaMalloc(&dsig, nang * sizeof(double)));
+    CK(ds.alloc(&dth, nang * sizeof(double)));
+    CK(ds.alloc(&dph, nang * sizeof(double)));
+    CK(ds.alloc(&dsig, nang * sizeof(double)));
     CK(cudaMemcpyAsync(dth, th, nang * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dph, ph, nang * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     k_rcs<<<nang, 256, 0, c->stream>>>(N, c->dt_baric, c->de_t, c->de_long, I, dth, dph, 0.5 * (maxX + minX),
@@ -573,9 +573,6 @@ int device_rcs(Ctx* c, const double2* I, const double2* pol, double2 ctte, const
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(sigma, dsig, nang * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    cudaFree(dth);
-    cudaFree(dph);
-    cudaFree(dsig);
     return MLF_OK;
 }
 

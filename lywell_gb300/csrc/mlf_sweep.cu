@@ -65,6 +65,7 @@ using namespace mlf;
 extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, double ctte_re, double ctte_im,
                               double tol, int maxit, int precond_kind, int mode, int block, double* sigma, int* iters,
                               int* status_out) {
+    DevScope ds;
     if (!h || nang <= 0 || !sigma || !iters || !status_out || maxit <= 0 || !(tol > 0) || mode < 0 || mode > 2)
         return MLF_E_ARG;
     Ctx* c = &h->c;
@@ -82,9 +83,9 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
     int st = MLF_OK;
     if (mode == 0) {
         double2 *b = nullptr, *x = nullptr, *g = nullptr;
-        CK(cudaMalloc(&b, N * sizeof(double2)));
-        CK(cudaMalloc(&x, N * sizeof(double2)));
-        CK(cudaMalloc(&g, N * sizeof(double2)));
+        CK(ds.alloc(&b, N * sizeof(double2)));
+        CK(ds.alloc(&x, N * sizeof(double2)));
+        CK(ds.alloc(&g, N * sizeof(double2)));
         CK(cudaMemsetAsync(g, 0, N * sizeof(double2), c->stream));
         double prev[3] = {-1., 0., 0.};
         for (int a = 0; a < nang && !st; ++a) {
@@ -102,9 +103,6 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
             CK(cudaMemcpyAsync(g, x, N * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
             prev[0] = d[0]; prev[1] = d[1]; prev[2] = d[2];
         }
-        cudaFree(b);
-        cudaFree(x);
-        cudaFree(g);
         return st;
     }
     int bsel = block;
@@ -119,8 +117,8 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
     }
     const int bs = std::max(1, std::min(bsel, nang));
     double2 *b = nullptr, *x = nullptr;
-    CK(cudaMalloc(&b, (size_t)N * bs * sizeof(double2)));
-    CK(cudaMalloc(&x, (size_t)N * bs * sizeof(double2)));
+    CK(ds.alloc(&b, (size_t)N * bs * sizeof(double2)));
+    CK(ds.alloc(&x, (size_t)N * bs * sizeof(double2)));
     std::vector<double> dirs(3 * (size_t)bs), rr(bs);
     std::vector<double2> pols(3 * (size_t)bs);
     for (int a0 = 0; a0 < nang && !st; a0 += bs) {
@@ -143,7 +141,5 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
             st = device_rcs(c, x + (size_t)q * N, &pols[3 * q], ctte, &th, &ph[a0 + q], 1, &sigma[a0 + q]);
         }
     }
-    cudaFree(b);
-    cudaFree(x);
     return st;
 }
