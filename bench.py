@@ -441,14 +441,40 @@ def learned_at_scale(steps=3000, seed=0):
     run("mixed_exact_neighbourhood", m.nearinv, True, "nearinv")
     run("mixed_learned", learned_setup, True, "nearinv")
     run("fp64_cgs_ilu0_reference", lambda: m.ilu0(), False, "ilu0", maxit=300)
+    # the three additions together: a 722-RHS monostatic sweep on the sphere (phi = 0..180 deg
+    # step 0.5 deg x {VV, HH}), sampled and projected per RHS: the plain FP64 path (the
+    # reference's warm-started sequential CGS, exact neighbourhood inverse) on 3 angles
+    # against mixed + batched (autotuned block) + learned on one block of angles
+    dphi = np.deg2rad(0.5)
+    m.nearinv()
+    torch.cuda.synchronize()
+    t1 = time.time()
+    seq = m.monostatic(3, phis=np.arange(3) * dphi, pol="VV", errmax=1e-4, maxit=4000, precond="nearinv", mode=0)
+    t_seq = time.time() - t1
+    lp.apply_to(m)
+    tune = m.autotune_block()
+    B = int(tune["block"])
+    torch.cuda.synchronize()
+    t1 = time.time()
+    bat = m.monostatic(B, phis=np.arange(B) * dphi, pol="VV", errmax=1e-4, maxit=4000, precond="nearinv", mode=2,
+                       block=B)
+    t_bat = time.time() - t1
     m.close()
+    sweep = {"fp64_sequential_exact": {"angles": 3, "s_per_rhs": t_seq / 3, "iters": [int(v) for v in seq["iters"]]},
+             "mixed_batched_learned": {"angles": B, "s_per_rhs": t_bat / B, "autotune": tune,
+                                       "iters_max": int(np.max(bat["iters"])),
+                                       "status": sorted(set(bat["status"]))},
+             "rcs_db_maxdiff": float(np.abs(bat["sigma_db"][:3] - seq["sigma_db"]).max())}
+    sweep["projected_722_s"] = {"fp64_sequential_exact": 722 * t_seq / 3, "mixed_batched_learned": 722 * t_bat / B}
+    sweep["speedup_projected_722"] = (t_seq / 3) / (t_bat / B)
     base = out["fp64_cgs_exact_neighbourhood"]["time_to_rcs_s"]
     return {"workload": WORKLOADS["sphere6"]["name"] + "; trained on 3 seeded superellipsoids (30720 RWG, same "
                                                        "mesh density)",
             "train_s": t_train, "gamma": lp.gamma, "trace": {str(k): v for k, v in lp.trace.items()},
             "results": out,
             "speedup_vs_fp64_exact": {k: base / v["time_to_rcs_s"] for k, v in out.items()
-                                      if v["status"] == "converged"}}
+                                      if v["status"] == "converged"},
+            "sweep_722": sweep}
 
 
 def main():

@@ -141,6 +141,8 @@ struct Ctx {
     long long* dblk_off = nullptr;
     int *dnbox_ptr = nullptr, *dnbox_list = nullptr;
     int2* dblk_tiles = nullptr;
+    int* dblk_entry = nullptr;        // leaf box of each block entry
+    float2* dMinvblk = nullptr;       // FP32 neighbourhood inverse as near-pattern blocks (batched apply)
     long long nnz = 0;
     std::vector<int> ia, ja;          // 0-based CSR
     // device: leaf
@@ -232,6 +234,8 @@ int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const fl
                         cudaStream_t s);
 void near_blocks_free(Ctx* c);
 int near_blocks_ensure(Ctx* c);
+int device_blocks_from_csr(Ctx* c, const float2* csr, float2** blk);
+int device_near_pattern_apply32(Ctx* c, const float2* Mblk, const float2* xs, int nrhs, float2* out, cudaStream_t s);
 int lp_tokens(Ctx* c, int with_target, float* X, float* T, long long cap, long long* ntok, int* bad_box);
 int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* best_cols, int* best_engine,
                    float* per_rhs_ms);

@@ -504,7 +504,8 @@ extern "C" int mlf_lp_install(mlf_ctx* h, mlf_mlp* net, float scale, int* nonfin
     if (Y) cudaFree(Y);
     if (dbad) cudaFree(dbad);
     if (st) return st;
-    if (c->dMinv32) { cudaFree(c->dMinv32); c->dMinv32 = nullptr; }   // FP32 copy rebuilt on next use
+    if (c->dMinv32) { cudaFree(c->dMinv32); c->dMinv32 = nullptr; }   // FP32 copies rebuilt on next use
+    if (c->dMinvblk) { cudaFree(c->dMinvblk); c->dMinvblk = nullptr; }
     *nonfinite = hbad;
     c->learned = 1;
     return MLF_OK;

@@ -302,13 +302,16 @@ __device__ __forceinline__ void blk_mac(Acc& acc, BlkTile<TC>* stage, const floa
 // The chunks of all near boxes form one sequence, staged through
 // NBK_STAGES shared-memory buffers by cp.async (zero-filled past the block
 // edges): while chunk c is multiplied, chunks c+1 .. c+STAGES-1 are in flight.
-template <int TC, class Acc>
+// OUT = 0: y (FP64 columns, ld) += the product; OUT = 1: out32 (FP32 columns,
+// ld) = the product (a preconditioner with the near pattern).
+template <int TC, class Acc, int OUT>
 __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2* __restrict__ tiles,
                                                     const int* __restrict__ box_ptr, const int* __restrict__ nbox_ptr,
                                                     const int* __restrict__ nbox_list,
                                                     const long long* __restrict__ blk_off,
                                                     const float2* __restrict__ Zblk, const float2* __restrict__ xs,
-                                                    const int* __restrict__ perm, double2* __restrict__ y) {
+                                                    const int* __restrict__ perm, double2* __restrict__ y,
+                                                    float2* __restrict__ out32) {
     constexpr int NC = 8 * TC;
     constexpr int ZPT = NBK_KC * NBK_ROWS / 256;   // Z values per thread per chunk
     constexpr int XPT = NBK_KC * NC / 256;         // x values per thread per chunk
@@ -368,9 +371,13 @@ __global__ void __launch_bounds__(256) k32_near_blk(int nrhs, int ld, const int2
     acc.store(stage[0], [&](int rt, int ct, float2 v) {
         const int row = r0 + rt, col = c0 + ct;
         if (row < ni && col < nrhs) {
-            double2* yp = y + (size_t)col * ld + perm[i0 + row];
-            const double2 o = *yp;
-            *yp = make_double2(o.x + (double)v.x, o.y + (double)v.y);
+            if (OUT == 0) {
+                double2* yp = y + (size_t)col * ld + perm[i0 + row];
+                const double2 o = *yp;
+                *yp = make_double2(o.x + (double)v.x, o.y + (double)v.y);
+            } else {
+                out32[(size_t)col * ld + perm[i0 + row]] = v;
+            }
         }
     });
 }
@@ -441,7 +448,6 @@ __global__ void __launch_bounds__(256) k32_own_blk(int N, int nrhs, const int2* 
 }
 
 static int near_blocks_setup(Ctx* c) {
-    DevScope ds;
     if (c->blk_ok) return MLF_OK;
     if (need_tree(c)) return MLF_E_STATE;
     const int nb = (int)c->box_ptr.size() - 1;
@@ -466,13 +472,13 @@ static int near_blocks_setup(Ctx* c) {
         c->err = "near blocks do not cover the near CSR";
         return MLF_E_STATE;
     }
-    int* dentry = nullptr;
+    int*& dentry = c->dblk_entry;
     CK(cudaMalloc(&c->dZblk, std::max<long long>(c->nnz, 1) * sizeof(float2)));
     CK(cudaMalloc(&c->dblk_off, (ne + 1) * sizeof(long long)));
     CK(cudaMalloc(&c->dnbox_ptr, (nb + 1) * sizeof(int)));
     CK(cudaMalloc(&c->dnbox_list, std::max(ne, 1) * sizeof(int)));
     CK(cudaMalloc(&c->dblk_tiles, std::max<size_t>(tiles.size(), 1) * sizeof(int2)));
-    CK(ds.alloc(&dentry, std::max(ne, 1) * sizeof(int)));
+    CK(cudaMalloc(&dentry, std::max(ne, 1) * sizeof(int)));
     CK(cudaMemcpy(c->dblk_off, off.data(), (ne + 1) * sizeof(long long), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->dnbox_ptr, c->nbox_ptr.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->dnbox_list, c->nbox_list.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
@@ -535,11 +541,37 @@ int device_near_blocks32(Ctx* c, const float2* xs, int ld, int nrhs, double2* y,
     if ((st = near_blocks_setup(c))) return st;
     blk_dispatch(c, nrhs, [&](auto tc, auto acc) {
         constexpr int TC = decltype(tc)::value;
-        const size_t smem = staged_smem(k32_near_blk<TC, decltype(acc)>, sizeof(BlkTile<TC>));
-        k32_near_blk<TC, decltype(acc)><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, smem, s>>>(
-            nrhs, ld, c->dblk_tiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, c->dblk_off, c->dZblk, xs, c->dperm, y);
+        const size_t smem = staged_smem(k32_near_blk<TC, decltype(acc), 0>, sizeof(BlkTile<TC>));
+        k32_near_blk<TC, decltype(acc), 0><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, smem, s>>>(
+            nrhs, ld, c->dblk_tiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, c->dblk_off, c->dZblk, xs, c->dperm, y,
+            nullptr);
     });
     return cuda_ok(c, cudaGetLastError(), "near blocks") ? MLF_OK : MLF_E_CUDA;
+}
+
+// Block copy of a matrix with the near CSR pattern (FP32 values in CSR order)
+int device_blocks_from_csr(Ctx* c, const float2* csr, float2** blk) {
+    int st;
+    if ((st = near_blocks_setup(c))) return st;
+    if (!*blk) CK(cudaMalloc(blk, std::max<long long>(c->nnz, 1) * sizeof(float2)));
+    const int ne = (int)c->nbox_list.size();
+    if (ne) k_blk_fill<<<ne, 256, 0, c->stream>>>(c->dblk_entry, c->dnbox_list, c->dblk_off, c->dbox_ptr, c->dperm,
+                                                  c->dia, c->dja, csr, *blk);
+    return cuda_ok(c, cudaGetLastError(), "block fill") ? MLF_OK : MLF_E_CUDA;
+}
+
+// out (FP32 columns, ld N) = M xs for M given as near-pattern blocks
+int device_near_pattern_apply32(Ctx* c, const float2* Mblk, const float2* xs, int nrhs, float2* out, cudaStream_t s) {
+    int st;
+    if ((st = near_blocks_setup(c))) return st;
+    blk_dispatch(c, nrhs, [&](auto tc, auto acc) {
+        constexpr int TC = decltype(tc)::value;
+        const size_t smem = staged_smem(k32_near_blk<TC, decltype(acc), 1>, sizeof(BlkTile<TC>));
+        k32_near_blk<TC, decltype(acc), 1><<<dim3(c->nblk_tiles, (nrhs + 8 * TC - 1) / (8 * TC)), 256, smem, s>>>(
+            nrhs, c->N, c->dblk_tiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, c->dblk_off, Mblk, xs, c->dperm,
+            nullptr, out);
+    });
+    return cuda_ok(c, cudaGetLastError(), "near-pattern apply") ? MLF_OK : MLF_E_CUDA;
 }
 
 // C (leaf fields, FP32) = R^T x for every leaf box
@@ -587,9 +619,10 @@ int near_blocks_ensure(Ctx* c) { return near_blocks_setup(c); }
 
 void near_blocks_free(Ctx* c) {
     auto F = [](void* p) { if (p) cudaFree(p); };
-    F(c->dZblk); F(c->dblk_off); F(c->dnbox_ptr); F(c->dnbox_list); F(c->dblk_tiles);
+    F(c->dZblk); F(c->dblk_off); F(c->dnbox_ptr); F(c->dnbox_list); F(c->dblk_tiles); F(c->dblk_entry);
+    F(c->dMinvblk);
     c->dZblk = nullptr; c->dblk_off = nullptr; c->dnbox_ptr = nullptr; c->dnbox_list = nullptr;
-    c->dblk_tiles = nullptr;
+    c->dblk_tiles = nullptr; c->dblk_entry = nullptr; c->dMinvblk = nullptr;
     c->blk_ok = 0;
 }
 

@@ -295,6 +295,20 @@ int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStr
         if ((st = device_blk_pack(c, nullptr, y, c->N, nrhs, c->dpre_xs, s))) return st;
         return device_own_blocks32(c, c->dboff, c->dMinv32, c->dpre_xs, nrhs, x, s);
     }
+    if (!c->nearinv_own && nrhs > 1) {
+        // blocks of columns: the near-pattern inverse as box-pair blocks, one GEMM engine pass
+        const size_t need = (size_t)c->N * nrhs;
+        if (c->pre_xs_cap < need) {
+            if (c->dpre_xs) cudaFree(c->dpre_xs);
+            c->dpre_xs = nullptr;
+            CK(cudaMalloc(&c->dpre_xs, need * sizeof(float2)));
+            c->pre_xs_cap = need;
+        }
+        int st;
+        if (!c->dMinvblk && (st = device_blocks_from_csr(c, c->dMinv32, &c->dMinvblk))) return st;
+        if ((st = device_blk_pack(c, nullptr, y, c->N, nrhs, c->dpre_xs, s))) return st;
+        return device_near_pattern_apply32(c, c->dMinvblk, c->dpre_xs, nrhs, x, s);
+    }
     if (c->nearinv_own)
         k32_blockdiag_apply<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
             c->N, nrhs, c->dbox_ptr, c->dbox_of_sorted, c->dperm, c->dboff, c->dMinv32, y, x);
@@ -320,6 +334,8 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     if (c->dMinv) cudaFree(c->dMinv);
     if (c->dboff) cudaFree(c->dboff);
     if (c->dMinv32) cudaFree(c->dMinv32);
+    if (c->dMinvblk) cudaFree(c->dMinvblk);
+    c->dMinvblk = nullptr;
     if (c->dMinv_base) cudaFree(c->dMinv_base);
     c->dMinv_base = nullptr;
     c->dMinv = nullptr;

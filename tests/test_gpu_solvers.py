@@ -173,3 +173,20 @@ def test_own_box_fp32_block_apply(ico4, ncols, engine):
             assert _rel(X[:, k], ref[:, k]) < 1e-4
     finally:
         assert m.nearinv() == 0
+
+
+@pytest.mark.parametrize("engine", [1, 0])
+@pytest.mark.parametrize("ncols", [1, 12, 40])
+def test_neighbourhood_fp32_block_apply(ico4, ncols, engine):
+    """The FP32 neighbourhood inverse of the mixed inner loop: one column by the
+    CSR kernel, blocks of columns as near-pattern box-pair blocks through the
+    GEMM engines; against the FP64 apply of the same preconditioner."""
+    _, m, _ = ico4
+    m.set_block_engine(engine)
+    assert m.nearinv() == 0
+    rng = np.random.default_rng(30 + ncols)
+    Y = rng.standard_normal((m.N, ncols)) + 1j * rng.standard_normal((m.N, ncols))
+    X32 = m.precond_apply32(Y).reshape(m.N, ncols)
+    X64 = m.precond_apply(Y, "nearinv").reshape(m.N, ncols)
+    for k in range(ncols):
+        assert _rel(X32[:, k], X64[:, k]) < 1e-4
