@@ -264,18 +264,23 @@ def batched_rcs_sample(seq_angles=3, block=0, maxit=4000):
     return out
 
 
-def profile_fp32_block(nrhs, steps, engine=-1, cols=0):
+def profile_fp32_block(nrhs, steps, engine=-1, cols=0, mesh="spheroid5"):
     """Profiling aid (not the bench line): the FP32 operator on `nrhs` random
-    columns of a 30720-RWG spheroid with the 122880-RWG spheroid's mesh density
-    (icosphere-5, semi-axes 1.5 x 0.375 x 0.375 lambda, so ~145 bases per leaf
-    box as in the 722-RHS workload) -- small enough for multi-pass ncu."""
+    columns.  mesh "spheroid5": a 30720-RWG spheroid with the 122880-RWG
+    spheroid's mesh density (icosphere-5, semi-axes 1.5 x 0.375 x 0.375 lambda,
+    so ~145 bases per leaf box as in the 722-RHS workload) -- small enough for
+    multi-pass ncu; "sphere6": the 122880-RWG sphere of radius 6 lambda
+    (~11 bases per leaf box)."""
     import ctypes
     import torch
     from lywell_gb300 import MLFMA, RWG, _capi, meshes
 
-    tris = meshes.spheroid(5, (1.5, 0.375, 0.375), noise=0.005, seed=1234)
+    if mesh == "sphere6":
+        tris = meshes.icosphere(6, 6.0)
+    else:
+        tris = meshes.spheroid(5, (1.5, 0.375, 0.375), noise=0.005, seed=1234)
     m = MLFMA(RWG(tris), lam=1.0, ladomax=0.25)
-    if engine >= 0:
+    if engine >= 0 or cols:
         m.set_block_engine(engine, cols)
     lib = _capi.load()
     X = torch.randn(nrhs, m.N, dtype=torch.complex128, device="cuda")
@@ -300,7 +305,7 @@ def profile_fp32_block(nrhs, steps, engine=-1, cols=0):
     stages = [float(v) for v in m.stage_times()]
     m.set_profiling(False)
     print(json.dumps({"profile": "fp32 operator", "stage_ms": stages, "N": m.N, "nrhs": nrhs, "near_nnz": m.nnz, "engine": engine, "cols": cols,
-                      "ms_per_call": e0.elapsed_time(e1) / steps}), flush=True)
+                      "mesh": mesh, "ms_per_call": e0.elapsed_time(e1) / steps}), flush=True)
     m.close()
 
 
@@ -489,15 +494,17 @@ def main():
     ap.add_argument("--rcs-maxit", type=int, default=4000)
     ap.add_argument("--no-batched", action="store_true", help="skip the 722-RHS spheroid sweep sample")
     ap.add_argument("--learned", action="store_true", help="add the learned-preconditioner samples (about 6 min)")
-    ap.add_argument("--block-engine", type=int, default=-1, help="profiling aid: 1 tensor cores, 0 FP32 FMA")
+    ap.add_argument("--block-engine", type=int, default=-1, help="profiling aid: 1 tensor cores, 0 FP32 FMA, 2 warp per basis")
     ap.add_argument("--block-cols", type=int, default=0, help="profiling aid: box-block tile width 8/32/64")
     ap.add_argument("--profile-fp32-block", type=int, default=0,
                     help="profiling aid: time the FP32 operator on this many columns of a small spheroid and exit")
+    ap.add_argument("--profile-mesh", default="spheroid5", choices=["spheroid5", "sphere6"])
     ap.add_argument("--seq-angles", type=int, default=3)
     ap.add_argument("--block", type=int, default=0, help="RHS per block of the batched sweep (0: autotuned)")
     args = ap.parse_args()
     if args.profile_fp32_block > 0:
-        profile_fp32_block(args.profile_fp32_block, args.steps, args.block_engine, args.block_cols)
+        profile_fp32_block(args.profile_fp32_block, args.steps, args.block_engine, args.block_cols,
+                           args.profile_mesh)
         return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -201,22 +201,29 @@ int mlf_set_gs_passes(mlf_ctx* ctx, int passes);
 int mlf_solve_times(mlf_ctx* ctx, double* out4);
 
 /* Autotuner for batched solves: times the FP32 operator on each candidate
- * block of right-hand sides (candidates[ncand], 1..4096) with both box-block
- * GEMM engines and the tile widths 8, 32 and 64 columns, and returns the
- * smallest block whose time
- * per right-hand side is within 5 % of the best, with its tile width (0 for a
- * single column) and engine (best_engine, optional: 1 tensor cores, 0 FP32
- * FMA); both are kept for later operator calls.
+ * block of right-hand sides (candidates[ncand], 1..4096) with each
+ * multi-column engine -- both box-block GEMM engines at the tile widths 8, 32
+ * and 64 columns, and the warp engine -- and returns the smallest block whose
+ * time per right-hand side is within 5 % of the best, with its tile width (0
+ * for a single column or the warp engine) and engine (best_engine, optional:
+ * 1 tensor cores, 0 FP32 FMA, 2 warp engine); both are kept for later
+ * operator and preconditioner calls.
  * per_rhs_ms (optional, ncand) receives the best time per right-hand side of
  * each candidate.  No counterpart in the reference. */
 int mlf_autotune_block(mlf_ctx* ctx, const int* candidates, int ncand, int* best_block, int* best_cols,
                        int* best_engine, float* per_rhs_ms);
 
-/* Box-block GEMM engine of the FP32 operator on blocks of columns: 1 = tensor
- * cores (mma.sync m16n8k8 TF32 with the 3xTF32 split, within a few 1e-6 of
- * FP32; the default), 0 = FP32 FMA; cols = tile width 8, 32 or 64 (0: by the
- * block's width).  mlf_autotune_block sets both.  No counterpart in the
- * reference. */
+/* Multi-column engine of the FP32 operator and of the FP32 preconditioner
+ * applies on blocks of columns:
+ *   1 = box-block GEMMs on tensor cores (mma.sync m16n8k8 TF32 with the
+ *       3xTF32 split, within a few 1e-6 of FP32),
+ *   0 = box-block GEMMs on FP32 FMAs,
+ *   2 = warp engine: one warp per basis over 8 columns, nothing padded (for
+ *       leaf boxes of a few tens of bases),
+ *  -1 = by the mean leaf-box size: 2 below 48 bases per box, else 1 (the
+ *       default).
+ * cols = box-block tile width 8, 32 or 64 (0: by the block's width).
+ * mlf_autotune_block sets both.  No counterpart in the reference. */
 int mlf_set_block_engine(mlf_ctx* ctx, int engine, int cols);
 
 /* y = Z_MLFMA x with the FP32 operator of mode 1 (host or device arrays);

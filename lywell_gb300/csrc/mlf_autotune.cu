@@ -1,9 +1,10 @@
 // Block-size and tile autotuner for batched solves.
 //
-// For each candidate number of right-hand sides per block B, each box-block
-// GEMM engine (tensor-core mma.sync 3xTF32 or FP32 FMA) and each tile width
-// (8, 32 or 64 columns), one FP32 operator application on B random columns is
-// timed with CUDA events (two warm-up calls, three timed).
+// For each candidate number of right-hand sides per block B, each
+// multi-column engine -- the box-block GEMMs (tensor-core mma.sync 3xTF32 or
+// FP32 FMA) at each tile width (8, 32 or 64 columns), and the warp-per-basis
+// engine -- one FP32 operator application on B random columns is timed with
+// CUDA events (two warm-up calls, three timed).
 // The choice minimises operator time per right-hand side; a smaller block is
 // kept when it is within 5 % of the best (it retires columns sooner and holds
 // a smaller Krylov basis).  No counterpart in the reference, whose monostatic
@@ -57,11 +58,12 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
         const int B = cand[q];
         double tq = 1e300;
         const int widths[3] = {8, 32, 64};
-        for (int var = 0; var < 6 && !st; ++var) {
-            const int wv = var % 3, eng = 1 - var / 3;   // tensor-core engine first, then FP32 FMA
+        for (int var = 0; var < 7 && !st; ++var) {
+            // tensor-core box blocks, FP32 FMA box blocks (three widths each), then the warp engine
+            const int wv = var % 3, eng = var == 6 ? 2 : 1 - var / 3;
             if (B == 1 && var) break;   // one column uses the CSR kernels
-            if (wv > 0 && widths[wv - 1] >= B) continue;   // a narrower tile already covers the block
-            c->blk_cols = widths[wv];
+            if (eng != 2 && wv > 0 && widths[wv - 1] >= B) continue;   // a narrower tile already covers the block
+            c->blk_cols = eng == 2 ? 0 : widths[wv];
             c->blk_engine = eng;
             for (int w = 0; w < 2 && !st; ++w) st = device_matvec32(c, x, y, B, c->N, s);
             if (st) break;
@@ -73,7 +75,7 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             const double t = ms / 3.0 / B;
-            if (t < tq) { tq = t; colsel[q] = widths[wv]; engsel[q] = eng; }
+            if (t < tq) { tq = t; colsel[q] = eng == 2 ? 0 : widths[wv]; engsel[q] = eng; }
         }
         per[q] = {tq, B};
         if (per_rhs_ms) per_rhs_ms[q] = (float)tq;
@@ -103,7 +105,7 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
 using namespace mlf;
 
 extern "C" int mlf_set_block_engine(mlf_ctx* h, int engine, int cols) {
-    if (!h || engine < 0 || engine > 1 || (cols != 0 && cols != 8 && cols != 32 && cols != 64)) return MLF_E_ARG;
+    if (!h || engine < -1 || engine > 2 || (cols != 0 && cols != 8 && cols != 32 && cols != 64)) return MLF_E_ARG;
     h->c.blk_engine = engine;
     h->c.blk_cols = cols;
     return MLF_OK;

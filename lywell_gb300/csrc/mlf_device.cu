@@ -582,10 +582,10 @@ int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaSt
     for (int n = nl; n >= 4; --n) {
         Level& Lc = c->lv[n];
         Level& Lp = c->lv[n - 1];
-        const int slab = SEP_SLAB, nslab = chunks(Lp.L, slab);
-        const size_t smem = (size_t)slab * 2 * Lc.L * sizeof(double2);
-        k_interp_sep<double2><<<Lp.nb * nrhs * 2 * nslab, 256, smem, s>>>(
-            Lp.L, Lc.L, nrhs, slab, nslab, Lp.dchild_ptr, Lc.doctant, Lp.dsth, Lp.dwth, Lp.dsph, Lp.dwph, Lp.dshift,
+        const int nslab = chunks(Lp.L, SEP_SLAB);
+        const size_t smem = (size_t)SEP_SLAB * 2 * (Lc.L + Lp.L) * sizeof(double2);   // child rows + parent slab
+        k_interp_sep<double2, 1><<<Lp.nb * nrhs * 2 * nslab, 256, smem, s>>>(
+            Lp.L, Lc.L, nrhs, nslab, Lp.dchild_ptr, Lc.doctant, Lp.dsth, Lp.dwth, Lp.dsph, Lp.dwph, Lp.dshift,
             Lc.dC, Lp.dC);
     }
     if (prof) cudaEventRecord(c->ev[2], s);
@@ -601,7 +601,7 @@ int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaSt
         Level& Lp = c->lv[n - 1];
         const double2* Psrc = (n == 4) ? Lp.dB : Lp.dA;
         const size_t smem = ((size_t)Lp.K + (size_t)Lp.L * 2 * Lc.L) * sizeof(double2);
-        k_anterp_sep<double2><<<Lc.nb * nrhs * 2, 256, smem, s>>>(
+        k_anterp_sep<double2, 1><<<Lc.nb * nrhs * 2, 256, smem, s>>>(
             Lp.L, Lc.L, nrhs, Lc.dparent, Lc.doctant, Lp.dthT_ptr, Lp.dthT_row, Lp.dthT_w, Lp.dphT_ptr,
             Lp.dphT_row, Lp.dphT_w, Lp.dshift, Psrc, Lc.dB, Lc.dA);
     }
@@ -629,7 +629,7 @@ int configure_kernels(Ctx* c) {
     for (int n = 3; n < c->nlev; ++n) {
         mx = std::max(mx, 2 * (size_t)c->lv[n].K * sizeof(double2));
         mx2 = std::max(mx2, ((size_t)c->lv[n].K + (size_t)c->lv[n].L * 2 * c->lv[n + 1].L) * sizeof(double2));
-        mx3 = std::max(mx3, (size_t)SEP_SLAB * 2 * c->lv[n + 1].L * sizeof(double2));
+        mx3 = std::max(mx3, (size_t)SEP_SLAB * 2 * (c->lv[n + 1].L + c->lv[n].L) * sizeof(double2));
     }
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->dev));
@@ -642,8 +642,8 @@ int configure_kernels(Ctx* c) {
     // its own dynamic size), never to one context's need, which would break
     // the launches of an earlier context with larger grids.
     CK(cudaFuncSetAttribute(k_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    CK(cudaFuncSetAttribute(k_anterp_sep<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    CK(cudaFuncSetAttribute(k_interp_sep<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    CK(cudaFuncSetAttribute(k_anterp_sep<double2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    CK(cudaFuncSetAttribute(k_interp_sep<double2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     return MLF_OK;
 }
 

@@ -136,7 +136,9 @@ struct Ctx {
     // 64-row tile of the leaf boxes
     int blk_ok = 0, nblk_tiles = 0;
     int blk_cols = 0;                 // box-block tile width: 0 = by nrhs, else 8, 32 or 64 (autotuner)
-    int blk_engine = 1;               // box-block multiply: 0 FP32 FMA, 1 mma.sync 3xTF32 (autotuner)
+    int blk_engine = -1;              // multi-column engine: 0 box-block FP32 FMA, 1 box-block mma.sync
+                                      // 3xTF32, 2 warp per basis; -1 by mean leaf-box size (autotuner)
+    int* djas = nullptr;              // near CSR columns as box-sorted positions (warp engine)
     float2* dZblk = nullptr;
     long long* dblk_off = nullptr;
     int *dnbox_ptr = nullptr, *dnbox_list = nullptr;
@@ -233,6 +235,16 @@ int device_recv_blocks32(Ctx* c, const float2* R, int K, const float2* A, float 
 int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const float2* xs, int nrhs, float2* out,
                         cudaStream_t s);
 void near_blocks_free(Ctx* c);
+// warp engine (mlf_nearwarp.cu): one warp per basis, for small leaf boxes
+int warp_engine_ensure(Ctx* c);
+void warp_engine_free(Ctx* c);
+int blk_engine_of(const Ctx* c);   // the engine in force (resolves -1)
+int device_agg_warp32(Ctx* c, const float2* R, int K, const float2* xs, int nrhs, float2* C, cudaStream_t s);
+int device_recv_near_warp32(Ctx* c, const float2* R, int K, const float2* A, float facy, const float2* xs, int nrhs,
+                            int ld, double2* y, cudaStream_t s);
+int device_near_pattern_warp32(Ctx* c, const float2* M, const float2* xs, int nrhs, float2* out, cudaStream_t s);
+int device_own_warp32(Ctx* c, const long long* boff, const float2* M, const float2* xs, int nrhs, float2* out,
+                      cudaStream_t s);
 int near_blocks_ensure(Ctx* c);
 int device_blocks_from_csr(Ctx* c, const float2* csr, float2** blk);
 int device_near_pattern_apply32(Ctx* c, const float2* Mblk, const float2* xs, int nrhs, float2* out, cudaStream_t s);

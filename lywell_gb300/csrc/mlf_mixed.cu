@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "mlf_internal.h"
@@ -65,22 +66,45 @@ __global__ void k32_aggregate(int K, int nrhs, int N, const int* __restrict__ bo
     }
 }
 
+// B(:, col, box) = wq * sum over the far boxes of T_tid * C(:, col, src)
+// (llenar_campoCyB, modMLFMA.f90:1838-1852) for both polarisations and columns
+// [c0, c0 + NR): each thread owns one sample k, so each translation value is
+// read once per 2 NR products.
+template <int NR>
 __global__ void k32_translate(int K, int nrhs, int nchunk, const int* __restrict__ far_ptr,
                               const int* __restrict__ far_src, const int* __restrict__ far_tid,
                               const float2* __restrict__ T, const float* __restrict__ wq,
                               const float2* __restrict__ C, float2* __restrict__ B) {
     const int chunk = blockIdx.x % nchunk;
-    const int br = blockIdx.x / nchunk;
-    const int b = br / nrhs, r = br % nrhs;
-    const int q = chunk * blockDim.x + threadIdx.x;
-    if (q >= 2 * K) return;
-    const int k = q >= K ? q - K : q;
-    float2 acc = make_float2(0.f, 0.f);
+    const int b = blockIdx.x / nchunk;
+    const int c0 = blockIdx.y * NR;
+    const int k = chunk * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const size_t K2 = 2 * (size_t)K;
+    float2 a0[NR], a1[NR];
+#pragma unroll
+    for (int u = 0; u < NR; ++u) a0[u] = a1[u] = make_float2(0.f, 0.f);
     const int f1 = far_ptr[b + 1];
-    for (int f = far_ptr[b]; f < f1; ++f)
-        fmac(acc, C[((size_t)far_src[f] * nrhs + r) * 2 * K + q], T[(size_t)far_tid[f] * K + k]);
+    for (int f = far_ptr[b]; f < f1; ++f) {
+        const float2 t = T[(size_t)far_tid[f] * K + k];
+        const float2* cs = C + ((size_t)far_src[f] * nrhs + c0) * K2 + k;
+#pragma unroll
+        for (int u = 0; u < NR; ++u) {
+            if (c0 + u < nrhs) {
+                fmac(a0[u], cs[u * K2], t);
+                fmac(a1[u], cs[u * K2 + K], t);
+            }
+        }
+    }
     const float wk = wq[k];
-    B[((size_t)b * nrhs + r) * 2 * K + q] = make_float2(acc.x * wk, acc.y * wk);
+    float2* bo = B + ((size_t)b * nrhs + c0) * K2 + k;
+#pragma unroll
+    for (int u = 0; u < NR; ++u) {
+        if (c0 + u < nrhs) {
+            bo[u * K2] = make_float2(a0[u].x * wk, a0[u].y * wk);
+            bo[u * K2 + K] = make_float2(a1[u].x * wk, a1[u].y * wk);
+        }
+    }
 }
 
 __global__ void k32_receive_near(int K, int N, int nrhs, int ld, const int* __restrict__ perm,
@@ -160,7 +184,7 @@ int mixed_setup(Ctx* c) {
     size_t mx2 = 0, mx3 = 0;
     for (int n = 3; n < nl; ++n) {
         mx2 = std::max(mx2, ((size_t)c->lv[n].K + (size_t)c->lv[n].L * 2 * c->lv[n + 1].L) * sizeof(float2));
-        mx3 = std::max(mx3, (size_t)SEP_SLAB * 2 * c->lv[n + 1].L * sizeof(float2));
+        mx3 = std::max(mx3, (size_t)SEP_SLAB * 2 * (c->lv[n + 1].L + c->lv[n].L) * sizeof(float2));
     }
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->dev));
@@ -169,8 +193,8 @@ int mixed_setup(Ctx* c) {
         return MLF_E_ARG;
     }
     // kernel-wide limit shared by all contexts: the device maximum (see configure_kernels)
-    CK(cudaFuncSetAttribute(k_anterp_sep<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    CK(cudaFuncSetAttribute(k_interp_sep<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    CK(cudaFuncSetAttribute(k_anterp_sep<float2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    CK(cudaFuncSetAttribute(k_interp_sep<float2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     CK(cudaStreamSynchronize(c->stream));
     c->m32.ready = 1;
     return MLF_OK;
@@ -207,6 +231,19 @@ int device_matvec32_from32(Ctx* c, const float2* x32, double2* y, int nrhs, cuda
     return matvec32_core(c, nullptr, x32, y, nrhs, c->N, s);
 }
 
+// Field slots (columns x polarisations) per CTA of the separable passes: the
+// largest of 8, 4, 2 that divides 2 nrhs and keeps the CTA within 48 KB of
+// shared memory (four CTAs per SM), else 1.  The slots share every index and
+// weight load of the stencils.
+template <class F>
+static void slots_dispatch(int nrhs, size_t per_slot, F f) {
+    const size_t cap = 48 * 1024;
+    if ((2 * nrhs) % 8 == 0 && 8 * per_slot <= cap) f(std::integral_constant<int, 8>());
+    else if ((2 * nrhs) % 4 == 0 && 4 * per_slot <= cap) f(std::integral_constant<int, 4>());
+    else if (2 * per_slot <= cap) f(std::integral_constant<int, 2>());
+    else f(std::integral_constant<int, 1>());
+}
+
 static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y, int nrhs, int ld, cudaStream_t s) {
     int st;
     if (need_tree(c)) return MLF_E_STATE;
@@ -223,36 +260,55 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
                                                      c->m32.lv[nl].C);
     } else {
         // blocks of columns: box-sorted row-major copy, then per-box GEMMs
+        // (or one warp per basis for small boxes)
         if ((st = device_blk_pack(c, x, x32, ld, nrhs, c->m32.xT, s))) return st;
-        if ((st = device_agg_blocks32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s))) return st;
+        st = blk_engine_of(c) == 2 ? device_agg_warp32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s)
+                                   : device_agg_blocks32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s);
+        if (st) return st;
     }
     if (prof) cudaEventRecord(c->ev[1], s);
     for (int n = nl; n >= 4; --n) {
         Level& Lc = c->lv[n];
         Level& Lp = c->lv[n - 1];
-        const int slab = SEP_SLAB, nslab = (Lp.L + slab - 1) / slab;
-        const size_t smem = (size_t)slab * 2 * Lc.L * sizeof(float2);
-        k_interp_sep<float2><<<Lp.nb * nrhs * 2 * nslab, 256, smem, s>>>(
-            Lp.L, Lc.L, nrhs, slab, nslab, Lp.dchild_ptr, Lc.doctant, Lp.dsth, c->m32.lv[n - 1].wth, Lp.dsph,
-            c->m32.lv[n - 1].wph, c->m32.lv[n - 1].shift, c->m32.lv[n].C, c->m32.lv[n - 1].C);
+        const int nslab = (Lp.L + SEP_SLAB - 1) / SEP_SLAB;
+        const size_t per = (size_t)SEP_SLAB * 2 * (Lc.L + Lp.L) * sizeof(float2);   // child rows + parent slab
+        const Mixed32::Lv &mp = c->m32.lv[n - 1], &mc = c->m32.lv[n];
+        slots_dispatch(nrhs, per, [&](auto ns) {
+            constexpr int NS = decltype(ns)::value;
+            k_interp_sep<float2, NS><<<Lp.nb * (2 * nrhs / NS) * nslab, 256, NS * per, s>>>(
+                Lp.L, Lc.L, nrhs, nslab, Lp.dchild_ptr, Lc.doctant, Lp.dsth, mp.wth, Lp.dsph, mp.wph, mp.shift, mc.C,
+                mp.C);
+        });
     }
     if (prof) cudaEventRecord(c->ev[2], s);
     for (int n = 3; n <= nl; ++n) {
         Level& L = c->lv[n];
-        const int bd = 128, nch = (2 * L.K + bd - 1) / bd;
-        k32_translate<<<L.nb * nrhs * nch, bd, 0, s>>>(L.K, nrhs, nch, L.dfar_ptr, L.dfar_src, L.dfar_tid,
-                                                       c->m32.lv[n].T, c->m32.lv[n].wq, c->m32.lv[n].C,
-                                                       c->m32.lv[n].B);
+        const int bd = 128, nch = (L.K + bd - 1) / bd;
+        const int nr = nrhs <= 1 ? 1 : nrhs <= 2 ? 2 : nrhs <= 4 ? 4 : 8;
+        const dim3 grid(L.nb * nch, (nrhs + nr - 1) / nr);
+        const Mixed32::Lv& m = c->m32.lv[n];
+        if (nr == 1)
+            k32_translate<1><<<grid, bd, 0, s>>>(L.K, nrhs, nch, L.dfar_ptr, L.dfar_src, L.dfar_tid, m.T, m.wq, m.C, m.B);
+        else if (nr == 2)
+            k32_translate<2><<<grid, bd, 0, s>>>(L.K, nrhs, nch, L.dfar_ptr, L.dfar_src, L.dfar_tid, m.T, m.wq, m.C, m.B);
+        else if (nr == 4)
+            k32_translate<4><<<grid, bd, 0, s>>>(L.K, nrhs, nch, L.dfar_ptr, L.dfar_src, L.dfar_tid, m.T, m.wq, m.C, m.B);
+        else
+            k32_translate<8><<<grid, bd, 0, s>>>(L.K, nrhs, nch, L.dfar_ptr, L.dfar_src, L.dfar_tid, m.T, m.wq, m.C, m.B);
     }
     if (prof) cudaEventRecord(c->ev[3], s);
     for (int n = 4; n <= nl; ++n) {
         Level& Lc = c->lv[n];
         Level& Lp = c->lv[n - 1];
         const float2* Psrc = (n == 4) ? c->m32.lv[n - 1].B : c->m32.lv[n - 1].A;
-        const size_t smem = ((size_t)Lp.K + (size_t)Lp.L * 2 * Lc.L) * sizeof(float2);
-        k_anterp_sep<float2><<<Lc.nb * nrhs * 2, 256, smem, s>>>(
-            Lp.L, Lc.L, nrhs, Lc.dparent, Lc.doctant, Lp.dthT_ptr, Lp.dthT_row, c->m32.lv[n - 1].thT_w, Lp.dphT_ptr,
-            Lp.dphT_row, c->m32.lv[n - 1].phT_w, c->m32.lv[n - 1].shift, Psrc, c->m32.lv[n].B, c->m32.lv[n].A);
+        const size_t per = ((size_t)Lp.K + (size_t)Lp.L * 2 * Lc.L) * sizeof(float2);
+        const Mixed32::Lv &mp = c->m32.lv[n - 1], &mc = c->m32.lv[n];
+        slots_dispatch(nrhs, per, [&](auto ns) {
+            constexpr int NS = decltype(ns)::value;
+            k_anterp_sep<float2, NS><<<Lc.nb * (2 * nrhs / NS), 256, NS * per, s>>>(
+                Lp.L, Lc.L, nrhs, Lc.dparent, Lc.doctant, Lp.dthT_ptr, Lp.dthT_row, mp.thT_w, Lp.dphT_ptr,
+                Lp.dphT_row, mp.phT_w, mp.shift, Psrc, mc.B, mc.A);
+        });
     }
     if (prof) cudaEventRecord(c->ev[4], s);
     {
@@ -262,6 +318,10 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
             k32_receive_near<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
                 leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, (nl == 3 ? c->m32.lv[nl].B : c->m32.lv[nl].A), c->dia, c->dja,
                 c->dZ, xf, facy, y);
+        } else if (blk_engine_of(c) == 2) {
+            if ((st = device_recv_near_warp32(c, c->m32.R, leaf.K, (nl == 3 ? c->m32.lv[nl].B : c->m32.lv[nl].A), facy,
+                                              c->m32.xT, nrhs, ld, y, s)))
+                return st;
         } else {
             if ((st = device_recv_blocks32(c, c->m32.R, leaf.K, (nl == 3 ? c->m32.lv[nl].B : c->m32.lv[nl].A), facy, nrhs, ld, y, s))) return st;
             if ((st = device_near_blocks32(c, c->m32.xT, ld, nrhs, y, s))) return st;

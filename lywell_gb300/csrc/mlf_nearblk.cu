@@ -516,7 +516,7 @@ static int blk_width(const Ctx* c, int nrhs) {
 template <class F>
 static void blk_dispatch(const Ctx* c, int nrhs, F f) {
     const int w = blk_width(c, nrhs);
-    if (c->blk_engine == 1) {
+    if (blk_engine_of(c) != 0) {   // the mma.sync engine also stands in when the warp engine is set
         if (w == 8) f(std::integral_constant<int, 1>(), MmaAcc<1>());
         else if (w == 32) f(std::integral_constant<int, 4>(), MmaAcc<4>());
         else f(std::integral_constant<int, 8>(), MmaAcc<8>());
@@ -621,6 +621,7 @@ void near_blocks_free(Ctx* c) {
     auto F = [](void* p) { if (p) cudaFree(p); };
     F(c->dZblk); F(c->dblk_off); F(c->dnbox_ptr); F(c->dnbox_list); F(c->dblk_tiles); F(c->dblk_entry);
     F(c->dMinvblk);
+    warp_engine_free(c);
     c->dZblk = nullptr; c->dblk_off = nullptr; c->dnbox_ptr = nullptr; c->dnbox_list = nullptr;
     c->dblk_tiles = nullptr; c->dblk_entry = nullptr; c->dMinvblk = nullptr;
     c->blk_ok = 0;

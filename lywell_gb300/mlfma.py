@@ -27,7 +27,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._capi import CGS_STATUS, FLAG_DENSE_MOM, FLAG_FMM, FLAG_LEGENDRE_RECURRENCE, PRECOND, MLFError, load
+from ._capi import CGS_STATUS, ENGINES, FLAG_DENSE_MOM, FLAG_FMM, FLAG_LEGENDRE_RECURRENCE, PRECOND, MLFError, load
 
 __all__ = ["RWG", "MLFMA", "MoM", "FMM", "MLFError", "FLAG_LEGENDRE_RECURRENCE", "ajustar_polariz", "direction"]
 
@@ -293,8 +293,10 @@ class MLFMA:
         return dict(x=X, iters=it, relres=rr, status=[CGS_STATUS[int(s)] for s in st], outer=outer.value)
 
     def set_block_engine(self, engine: int, cols: int = 0):
-        """Box-block GEMM engine of the batched FP32 operator: 1 tensor cores
-        (3xTF32), 0 FP32 FMA; tile width cols 8, 32, 64 (0: by block width)."""
+        """Multi-column engine of the batched FP32 operator and preconditioner:
+        1 box blocks on tensor cores (3xTF32), 0 box blocks on FP32 FMA, 2 warp
+        per basis, -1 by leaf-box size; tile width cols 8, 32, 64 (0: by block
+        width)."""
         _check(load().mlf_set_block_engine(self._h, int(engine), int(cols)), self._h)
 
     def autotune_block(self, candidates=(8, 16, 32, 64, 128)):
@@ -306,7 +308,7 @@ class MLFMA:
         _check(load().mlf_autotune_block(self._h, _p(cand), cand.size, C.byref(best), C.byref(cols), C.byref(eng),
                                          _p(per)), self._h)
         return dict(block=best.value, tile_cols=cols.value,
-                    engine="tensor cores (3xTF32 mma.sync)" if eng.value == 1 else "FP32 FMA",
+                    engine=ENGINES.get(eng.value, str(eng.value)),
                     per_rhs_ms={int(b): float(t) for b, t in zip(cand, per)})
 
     def precond_apply32(self, y):

@@ -100,8 +100,10 @@ def test_mixed_solve_meets_fp64_test_and_rcs(ico4):
         assert np.abs(s_ref - s_mix).max() < 0.1
 
 
-def test_mixed_multi_rhs(ico4):
+@pytest.mark.parametrize("engine", [2, 1])
+def test_mixed_multi_rhs(ico4, engine):
     _, m, _ = ico4
+    m.set_block_engine(engine)
     assert m.nearinv() == 0
     dirs = np.stack([direction(90.0, a) for a in (0.0, 45.0, 90.0)])
     pols = np.stack([ajustar_polariz(d, "VV") for d in dirs])
@@ -113,12 +115,14 @@ def test_mixed_multi_rhs(ico4):
         assert r < 1e-4
 
 
-@pytest.mark.parametrize("engine", [1, 0])
-@pytest.mark.parametrize("nrhs", [5, 20, 40, 70])
+@pytest.mark.parametrize("engine", [1, 0, 2])
+@pytest.mark.parametrize("nrhs", [2, 3, 5, 20, 40, 70])
 def test_fp32_multi_rhs_columns(ico4, nrhs, engine):
     """The batched FP32 operator (near field, aggregation and receive as dense
     per-box GEMMs on the tensor cores (3xTF32) or FP32 FMAs, 8- and 32-column
-    tiles, ragged last tile) against one column at a time."""
+    tiles, ragged last tile; or one warp per basis over 2, 4 or 8 columns,
+    ragged last chunk; translation over 1, 2, 4 or 8 columns per thread)
+    against one column at a time."""
     _, m, _ = ico4
     m.set_block_engine(engine)
     rng = np.random.default_rng(11 + nrhs)
@@ -148,7 +152,7 @@ def test_own_box_inverse_apply(ico4):
     assert m.nearinv() == 0   # back to the full neighbourhood for the other tests
 
 
-@pytest.mark.parametrize("engine", [1, 0])
+@pytest.mark.parametrize("engine", [1, 0, 2])
 @pytest.mark.parametrize("ncols", [1, 6, 12, 40])
 def test_own_box_fp32_block_apply(ico4, ncols, engine):
     """The FP32 own-box preconditioner of the mixed inner loop (per-box GEMMs
@@ -175,12 +179,13 @@ def test_own_box_fp32_block_apply(ico4, ncols, engine):
         assert m.nearinv() == 0
 
 
-@pytest.mark.parametrize("engine", [1, 0])
-@pytest.mark.parametrize("ncols", [1, 12, 40])
+@pytest.mark.parametrize("engine", [1, 0, 2])
+@pytest.mark.parametrize("ncols", [1, 3, 12, 40])
 def test_neighbourhood_fp32_block_apply(ico4, ncols, engine):
     """The FP32 neighbourhood inverse of the mixed inner loop: one column by the
     CSR kernel, blocks of columns as near-pattern box-pair blocks through the
-    GEMM engines; against the FP64 apply of the same preconditioner."""
+    GEMM engines or one warp per basis on the CSR values; against the FP64
+    apply of the same preconditioner."""
     _, m, _ = ico4
     m.set_block_engine(engine)
     assert m.nearinv() == 0
@@ -190,3 +195,19 @@ def test_neighbourhood_fp32_block_apply(ico4, ncols, engine):
     X64 = m.precond_apply(Y, "nearinv").reshape(m.N, ncols)
     for k in range(ncols):
         assert _rel(X32[:, k], X64[:, k]) < 1e-4
+
+
+def test_autotune_block_covers_all_engines(ico4):
+    """mlf_autotune_block picks a candidate block, an engine among the three and
+    keeps them: a later batched operator call agrees with one column at a time."""
+    _, m, _ = ico4
+    res = m.autotune_block((4, 8, 16))
+    assert res["block"] in (4, 8, 16)
+    assert res["engine"] in ("FP32 FMA", "tensor cores (3xTF32 mma.sync)", "warp per basis")
+    assert all(t > 0 for t in res["per_rhs_ms"].values())
+    rng = np.random.default_rng(77)
+    X = rng.standard_normal((m.N, res["block"])) + 1j * rng.standard_normal((m.N, res["block"]))
+    Y = m.matvec32(X)
+    assert _rel(Y[:, -1], m.matvec32(X[:, -1])) < 5e-6
+    m.set_block_engine(-1)
+
