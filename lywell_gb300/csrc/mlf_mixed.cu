@@ -439,8 +439,9 @@ __global__ void k_mdot32(int N, int nrhs, const float2* __restrict__ V, size_t v
 }
 
 // Block dot products for the FP32 Arnoldi step: each CTA keeps its slice of
-// w (MD_E values per thread) in registers and streams the nvec basis vectors
-// past it, MD_G vectors per block reduction.
+// w (MD_E values per thread) in registers and streams its share of the nvec
+// basis vectors past it (blockIdx.z of gridDim.z shares, so that one column
+// of 10^5 unknowns still fills the GPU), MD_G vectors per block reduction.
 // partial[(i * nrhs + col) * gridDim.x + blockIdx.x] = sum conj(V_i) w over the slice.
 constexpr int MD_E = 8, MD_G = 4;
 __global__ void __launch_bounds__(256) k_mdot32b(int N, int nrhs, int nvec, const float2* __restrict__ V,
@@ -457,13 +458,15 @@ __global__ void __launch_bounds__(256) k_mdot32b(int N, int nrhs, int nvec, cons
         const int e = e0 + u * 256;
         wv[u] = e < N ? w[base + e] : make_float2(0.f, 0.f);
     }
-    for (int i0 = 0; i0 < nvec; i0 += MD_G) {
+    const int vper = ((nvec + gridDim.z - 1) / gridDim.z + MD_G - 1) / MD_G * MD_G;
+    const int iend = min(nvec, (int)(blockIdx.z + 1) * vper);
+    for (int i0 = blockIdx.z * vper; i0 < iend; i0 += MD_G) {
         float sacc[2 * MD_G];
 #pragma unroll
         for (int g = 0; g < MD_G; ++g) {
             float sr = 0.f, si = 0.f;
             const int i = i0 + g;
-            if (i < nvec) {
+            if (i < iend) {
                 const float2* v = V + (size_t)i * vstride + base;
 #pragma unroll
                 for (int u = 0; u < MD_E; ++u) {
@@ -486,7 +489,7 @@ __global__ void __launch_bounds__(256) k_mdot32b(int N, int nrhs, int nvec, cons
 #pragma unroll
             for (int q = 0; q < 2 * MD_G; ++q) red[warp][q] = sacc[q];
         __syncthreads();
-        if (threadIdx.x < MD_G && i0 + (int)threadIdx.x < nvec) {
+        if (threadIdx.x < MD_G && i0 + (int)threadIdx.x < iend) {
             double tr = 0, ti = 0;
             for (int wp = 0; wp < 8; ++wp) {
                 tr += red[wp][2 * threadIdx.x];
@@ -649,6 +652,8 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
     CK(ds.alloc(&r, V1 * sizeof(double2)));
     CK(ds.alloc(&t64, V1 * sizeof(double2)));
     const int md_chunks = (N + 256 * MD_E - 1) / (256 * MD_E);
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev));
     CK(ds.alloc(&partial, (size_t)(m + 1) * nrhs * std::max(GM_BLOCKS, md_chunks) * sizeof(double2)));
     CK(ds.alloc(&dred, (size_t)(m + 1) * nrhs * sizeof(double2)));
     CK(ds.alloc(&dscale, nrhs * sizeof(double)));
@@ -736,7 +741,13 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
             if (prof) cudaEventRecord(c->sev[2], s);
             std::vector<double2> hsum((size_t)(j + 1) * nrhs, make_double2(0, 0));
             for (int pass = 0; pass < c->gs_passes; ++pass) {
-                k_mdot32b<<<dim3(md_chunks, nrhs), 256, 0, s>>>(N, nrhs, j + 1, V, V1, w32, partial);
+                // vector shares when the slices alone leave SMs idle (under two CTAs
+                // per SM): about four CTAs per SM in all, at least MD_G vectors each
+                const int base_ctas = md_chunks * nrhs;
+                const int vz = base_ctas >= 2 * nsm ? 1
+                                                    : std::max(1, std::min((j + 1 + MD_G - 1) / MD_G,
+                                                                           (4 * nsm + base_ctas - 1) / base_ctas));
+                k_mdot32b<<<dim3(md_chunks, nrhs, vz), 256, 0, s>>>(N, nrhs, j + 1, V, V1, w32, partial);
                 k_reduce_partials_n<<<((j + 1) * nrhs + 127) / 128, 128, 0, s>>>((j + 1) * nrhs, md_chunks, partial,
                                                                                   dred);
                 k_gs_update32<<<gc, 256, 0, s>>>(N, nrhs, j + 1, V, V1, dred, w32);
