@@ -195,6 +195,14 @@ int mlf_set_gmres_restart(mlf_ctx* ctx, int m);
  * twice the basis traffic). */
 int mlf_set_gs_passes(mlf_ctx* ctx, int passes);
 
+/* Krylov basis storage of mode 1: 32 (FP32, the default) or 16 (FP16, each
+ * unit basis column stored scaled by sqrt(N), so entries stay within FP16's
+ * range).  FP16 halves the Gram-Schmidt traffic, which streams the basis
+ * twice per step; the arithmetic stays FP32 with FP64 reductions, and the
+ * FP64 refinement keeps the same stopping test.  No counterpart in the
+ * reference. */
+int mlf_set_basis_precision(mlf_ctx* ctx, int bits);
+
 /* Phase times (ms) of the last mixed-precision solve run while profiling was
  * on (mlf_set_profiling): out4 = {preconditioner, FP32 operator,
  * orthogonalisation, wall total}.  No counterpart in the reference. */
@@ -286,9 +294,14 @@ int mlf_rcs(mlf_ctx* ctx, const double* I, const double* pol, double ctte_re, do
  * mode 0: the reference's sequential sweep, CGS on the FP64 operator,
  *         warm start = previous currents x exp(-j k (d_a - d_{a-1}) . r_edge).
  * mode 1: batched, blocks of `block` angles as one multi-RHS FP64 CGS.
- * mode 2: batched mixed precision (mlf_solve mode 1 per block).
- * block <= 0 (modes 1, 2): chosen by mlf_autotune_block among 8..128.
- * Modes 1 and 2 have no counterpart in the reference. */
+ * mode 2: batched mixed precision (mlf_solve mode 1 per block), zero guesses.
+ * mode 3: batched mixed precision with mode 0's warm starts: column q of the
+ *         block sweeps the contiguous run of angles [q n, (q + 1) n),
+ *         n = ceil(nang / block); block k solves the k-th angle of every run,
+ *         each column starting from its previous angle's phase-shifted
+ *         currents.
+ * block <= 0 (modes 1-3): chosen by mlf_autotune_block among 8..128.
+ * Modes 1-3 have no counterpart in the reference. */
 int mlf_monostatic(mlf_ctx* ctx, int nang, const double* phis, int hh, double ctte_re, double ctte_im,
                    double tol, int maxit, int precond_kind, int mode, int block, double* sigma, int* iters,
                    int* status_out);

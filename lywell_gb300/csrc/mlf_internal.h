@@ -113,6 +113,7 @@ struct Ctx {
     int mv_prec = 0;                  // operator precision used by device_matvec: 0 FP64, 1 FP32
     int gmres_m = 800;                // restart length of the mixed-precision GMRES cycles
     int gs_passes = 1;                // classical Gram-Schmidt passes per Arnoldi step (1 or 2)
+    int basis_bits = 32;              // Krylov basis storage of the mixed solve: 32 (FP32) or 16 (FP16)
     Mixed32 m32;
     cudaStream_t stream = nullptr;
     std::string err;

@@ -14,6 +14,7 @@
 // residual estimate drops below inner_tol ||b|| or m steps; x += M^-1 V y in
 // FP64; stop when the FP64 residual ||b - A64 x|| < tol ||b||.  The FP64 residual is the judge, so the result
 // meets the same stopping test as the plain FP64 solve.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,6 +39,17 @@ __device__ __forceinline__ void fmac(float2& acc, float2 a, float2 b) {
     acc.y = fmaf(a.x, b.y, acc.y);
     acc.y = fmaf(a.y, b.x, acc.y);
 }
+
+// Krylov basis storage: FP32, or FP16 scaled by s = sqrt(N) on store (a unit
+// column has every entry within sqrt(N), inside FP16's range) and by 1/s on
+// load.  Arithmetic stays FP32 either way.
+__device__ __forceinline__ float2 bload(const float2* p, float) { return *p; }
+__device__ __forceinline__ float2 bload(const __half2* p, float s) {
+    const float2 v = __half22float2(*p);
+    return make_float2(v.x * s, v.y * s);
+}
+__device__ __forceinline__ void bstore(float2* p, float2 v, float) { *p = v; }
+__device__ __forceinline__ void bstore(__half2* p, float2 v, float s) { *p = __floats2half2_rn(v.x * s, v.y * s); }
 
 __global__ void k32_from64(size_t n, const double2* __restrict__ a, float2* __restrict__ b) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -444,8 +456,9 @@ __global__ void k_mdot32(int N, int nrhs, const float2* __restrict__ V, size_t v
 // of 10^5 unknowns still fills the GPU), MD_G vectors per block reduction.
 // partial[(i * nrhs + col) * gridDim.x + blockIdx.x] = sum conj(V_i) w over the slice.
 constexpr int MD_E = 8, MD_G = 4;
-__global__ void __launch_bounds__(256) k_mdot32b(int N, int nrhs, int nvec, const float2* __restrict__ V,
-                                                 size_t vstride, const float2* __restrict__ w,
+template <class BT>
+__global__ void __launch_bounds__(256) k_mdot32b(int N, int nrhs, int nvec, const BT* __restrict__ V,
+                                                 size_t vstride, float ls, const float2* __restrict__ w,
                                                  double2* __restrict__ partial) {
     const int col = blockIdx.y;
     const size_t base = (size_t)col * N;
@@ -467,12 +480,12 @@ __global__ void __launch_bounds__(256) k_mdot32b(int N, int nrhs, int nvec, cons
             float sr = 0.f, si = 0.f;
             const int i = i0 + g;
             if (i < iend) {
-                const float2* v = V + (size_t)i * vstride + base;
+                const BT* v = V + (size_t)i * vstride + base;
 #pragma unroll
                 for (int u = 0; u < MD_E; ++u) {
                     const int e = e0 + u * 256;
                     if (e < N) {
-                        const float2 a = v[e];
+                        const float2 a = bload(v + e, ls);
                         sr = fmaf(a.x, wv[u].x, sr); sr = fmaf(a.y, wv[u].y, sr);
                         si = fmaf(a.x, wv[u].y, si); si = fmaf(-a.y, wv[u].x, si);
                     }
@@ -481,13 +494,25 @@ __global__ void __launch_bounds__(256) k_mdot32b(int N, int nrhs, int nvec, cons
             sacc[2 * g] = sr;
             sacc[2 * g + 1] = si;
         }
+        // warp sums of the 2 MD_G values by halving exchanges (MD_G = 4: 9
+        // shuffles instead of 40): lane L ends with value (L >> 2)'s total
+        static_assert(2 * MD_G == 8, "the exchange below is written for 8 values");
 #pragma unroll
-        for (int q = 0; q < 2 * MD_G; ++q)
+        for (int st = 0; st < 3; ++st) {
+            const int o = 16 >> st, h = 4 >> st;
+            const bool up = (lane & o) != 0;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) sacc[q] += __shfl_xor_sync(0xffffffff, sacc[q], o);
-        if (lane == 0)
-#pragma unroll
-            for (int q = 0; q < 2 * MD_G; ++q) red[warp][q] = sacc[q];
+            for (int q = 0; q < 4; ++q) {
+                if (q < h) {
+                    const float send = up ? sacc[q] : sacc[q + h];
+                    const float keep = up ? sacc[q + h] : sacc[q];
+                    sacc[q] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+                }
+            }
+        }
+        sacc[0] += __shfl_xor_sync(0xffffffffu, sacc[0], 2);
+        sacc[0] += __shfl_xor_sync(0xffffffffu, sacc[0], 1);
+        if ((lane & 3) == 0) red[warp][lane >> 2] = sacc[0];
         __syncthreads();
         if (threadIdx.x < MD_G && i0 + (int)threadIdx.x < iend) {
             double tr = 0, ti = 0;
@@ -513,7 +538,8 @@ __global__ void k_reduce_partials_n(int nk, int nb, const double2* __restrict__ 
     out[k] = s;
 }
 
-__global__ void k_gs_update32(int N, int nrhs, int nvec, const float2* __restrict__ V, size_t vstride,
+template <class BT>
+__global__ void k_gs_update32(int N, int nrhs, int nvec, const BT* __restrict__ V, size_t vstride, float ls,
                               const double2* __restrict__ h, float2* __restrict__ w) {
     const int col = blockIdx.y;
     __shared__ float2 hs[2048];
@@ -524,11 +550,11 @@ __global__ void k_gs_update32(int N, int nrhs, int nvec, const float2* __restric
     __syncthreads();
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
         float2 acc = w[(size_t)col * N + e];
-        const float2* v = V + (size_t)col * N + e;
+        const BT* v = V + (size_t)col * N + e;
 #pragma unroll 4
         for (int i = 0; i < nvec; ++i) {
             const float2 hv = hs[i];
-            const float2 a = v[(size_t)i * vstride];
+            const float2 a = bload(v + (size_t)i * vstride, ls);
             acc.x -= hv.x * a.x - hv.y * a.y;
             acc.y -= hv.x * a.y + hv.y * a.x;
         }
@@ -536,35 +562,45 @@ __global__ void k_gs_update32(int N, int nrhs, int nvec, const float2* __restric
     }
 }
 
+template <class BT>
 __global__ void k_colscale_df(int N, const double2* __restrict__ src, const double* __restrict__ s,
-                              float2* __restrict__ dst) {
+                              BT* __restrict__ dst, float ss) {
     const int col = blockIdx.y;
     const double f = s[col];
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
         const double2 v = src[(size_t)col * N + e];
-        dst[(size_t)col * N + e] = make_float2((float)(v.x * f), (float)(v.y * f));
+        bstore(dst + (size_t)col * N + e, make_float2((float)(v.x * f), (float)(v.y * f)), ss);
     }
 }
 
+template <class BT>
 __global__ void k_colscale32(int N, const float2* __restrict__ src, const double* __restrict__ s,
-                             float2* __restrict__ dst) {
+                             BT* __restrict__ dst, float ss) {
     const int col = blockIdx.y;
     const float f = (float)s[col];
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
         const float2 v = src[(size_t)col * N + e];
-        dst[(size_t)col * N + e] = make_float2(v.x * f, v.y * f);
+        bstore(dst + (size_t)col * N + e, make_float2(v.x * f, v.y * f), ss);
     }
 }
 
+// FP32 copy of one basis block (the preconditioner's input)
+template <class BT>
+__global__ void k_basis32(size_t n, const BT* __restrict__ src, float ls, float2* __restrict__ dst) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = bload(src + i, ls);
+}
+
 // d[col] = sum_i y[i*nrhs+col] V32_i[col] in double (once per cycle)
-__global__ void k_combine32(int N, int nrhs, int nvec, const float2* __restrict__ V, size_t vstride,
+template <class BT>
+__global__ void k_combine32(int N, int nrhs, int nvec, const BT* __restrict__ V, size_t vstride, float ls,
                             const double2* __restrict__ y, double2* __restrict__ d) {
     const int col = blockIdx.y;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
         double2 acc = make_double2(0, 0);
         for (int i = 0; i < nvec; ++i) {
             const double2 yv = y[i * nrhs + col];
-            const float2 v = V[i * vstride + (size_t)col * N + e];
+            const float2 v = bload(V + i * vstride + (size_t)col * N + e, ls);
             acc.x += yv.x * v.x - yv.y * v.y;
             acc.y += yv.x * v.y + yv.y * v.x;
         }
@@ -635,17 +671,22 @@ static int apply_precond64(Ctx* c, int precond, int nrhs, const double2* in, dou
 // GMRES(m) with an all-FP32 inner loop (basis, Gram-Schmidt, preconditioner,
 // operator; Hessenberg and Givens on the host in double); d = V y in double;
 // x += M^-1 d with the FP64 preconditioner.
-int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
-                       int* iters, double* relres, int precond, int* status, double inner_tol, int* outer) {
+// BT: the Krylov basis storage, float2 or __half2 (mlf_set_basis_precision).
+template <class BT>
+static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
+                         int* iters, double* relres, int precond, int* status, double inner_tol, int* outer) {
     DevScope ds;
     const int N = c->N;
     const int m = std::max(4, std::min(c->gmres_m, 2000));
     const size_t V1 = (size_t)N * nrhs;
     cudaStream_t s = c->stream;
-    float2 *V = nullptr, *w32 = nullptr, *t32 = nullptr;
+    constexpr bool f32 = std::is_same<BT, float2>::value;
+    const float ss = f32 ? 1.f : (float)std::sqrt((double)N), ls = 1.f / ss;   // store / load scales
+    BT* V = nullptr;
+    float2 *w32 = nullptr, *t32 = nullptr;
     double2 *w = nullptr, *r = nullptr, *t64 = nullptr, *partial = nullptr, *dred = nullptr;
     double* dscale = nullptr;
-    CK(ds.alloc(&V, (size_t)(m + 1) * V1 * sizeof(float2)));
+    CK(ds.alloc(&V, (size_t)(m + 1) * V1 * sizeof(BT)));
     CK(ds.alloc(&w32, V1 * sizeof(float2)));
     CK(ds.alloc(&t32, V1 * sizeof(float2)));
     CK(ds.alloc(&w, V1 * sizeof(double2)));
@@ -694,7 +735,7 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
         if (all || !budget) break;
         for (int col = 0; col < nrhs; ++col) scl[col] = (!done[col] && beta[col] > 0) ? 1.0 / beta[col] : 0.0;
         CK(cudaMemcpyAsync(dscale, scl.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
-        k_colscale_df<<<gc, 256, 0, s>>>(N, r, dscale, V);
+        k_colscale_df<BT><<<gc, 256, 0, s>>>(N, r, dscale, V, ss);
         std::fill(H.begin(), H.end(), cx(0, 0));
         std::fill(G.begin(), G.end(), cx(0, 0));
         for (int col = 0; col < nrhs; ++col) G[(size_t)col * (m + 1)] = cx(done[col] ? 0.0 : beta[col], 0);
@@ -705,8 +746,14 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
             bool any = false;
             for (int col = 0; col < nrhs; ++col) any = any || live[col];
             if (!any) break;
-            const float2* vj = V + (size_t)j * V1;
             if (prof) cudaEventRecord(c->sev[0], s);
+            const float2* vj;
+            if (f32) {
+                vj = reinterpret_cast<const float2*>(V + (size_t)j * V1);
+            } else {   // w32 is free until the operator writes it below
+                k_basis32<BT><<<4096, 256, 0, s>>>(V1, V + (size_t)j * V1, ls, w32);
+                vj = w32;
+            }
             if (precond == 2) {
                 if ((st = device_nearinv_apply32(c, vj, t32, nrhs, s))) break;
             } else if (precond == 1) {
@@ -747,10 +794,10 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
                 const int vz = base_ctas >= 2 * nsm ? 1
                                                     : std::max(1, std::min((j + 1 + MD_G - 1) / MD_G,
                                                                            (4 * nsm + base_ctas - 1) / base_ctas));
-                k_mdot32b<<<dim3(md_chunks, nrhs, vz), 256, 0, s>>>(N, nrhs, j + 1, V, V1, w32, partial);
+                k_mdot32b<BT><<<dim3(md_chunks, nrhs, vz), 256, 0, s>>>(N, nrhs, j + 1, V, V1, ls, w32, partial);
                 k_reduce_partials_n<<<((j + 1) * nrhs + 127) / 128, 128, 0, s>>>((j + 1) * nrhs, md_chunks, partial,
                                                                                   dred);
-                k_gs_update32<<<gc, 256, 0, s>>>(N, nrhs, j + 1, V, V1, dred, w32);
+                k_gs_update32<BT><<<gc, 256, 0, s>>>(N, nrhs, j + 1, V, V1, ls, dred, w32);
                 CK(cudaMemcpyAsync(hbuf.data(), dred, (size_t)(j + 1) * nrhs * sizeof(double2), cudaMemcpyDeviceToHost, s));
                 CK(cudaStreamSynchronize(s));
                 for (size_t q = 0; q < (size_t)(j + 1) * nrhs; ++q) { hsum[q].x += hbuf[q].x; hsum[q].y += hbuf[q].y; }
@@ -759,7 +806,7 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
             if ((st = col_norms32(c, nrhs, w32, partial, dred, hbuf, hn, s))) break;
             for (int col = 0; col < nrhs; ++col) scl[col] = (live[col] && hn[col] > 1e-300) ? 1.0 / hn[col] : 0.0;
             CK(cudaMemcpyAsync(dscale, scl.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
-            k_colscale32<<<gc, 256, 0, s>>>(N, w32, dscale, V + (size_t)(j + 1) * V1);
+            k_colscale32<BT><<<gc, 256, 0, s>>>(N, w32, dscale, V + (size_t)(j + 1) * V1, ss);
             if (prof) {
                 cudaEventRecord(c->sev[3], s);
                 cudaEventSynchronize(c->sev[3]);
@@ -813,7 +860,7 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
         }
         if (jmax == 0) break;
         CK(cudaMemcpyAsync(dred, y.data(), (size_t)jmax * nrhs * sizeof(double2), cudaMemcpyHostToDevice, s));
-        k_combine32<<<gc, 256, 0, s>>>(N, nrhs, jmax, V, V1, dred, w);
+        k_combine32<BT><<<gc, 256, 0, s>>>(N, nrhs, jmax, V, V1, ls, dred, w);
         if ((st = apply_precond64(c, precond, nrhs, w, t64, s))) break;
         k_axpy1<<<4096, 256, 0, s>>>(V1, t64, x);
         CK(cudaGetLastError());
@@ -827,6 +874,13 @@ int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, 
         c->solve_ms[3] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
     }
     return st;
+}
+
+int device_solve_mixed(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
+                       int* iters, double* relres, int precond, int* status, double inner_tol, int* outer) {
+    if (c->basis_bits == 16)
+        return solve_mixed_t<__half2>(c, b, x0, tol, maxit, nrhs, x, iters, relres, precond, status, inner_tol, outer);
+    return solve_mixed_t<float2>(c, b, x0, tol, maxit, nrhs, x, iters, relres, precond, status, inner_tol, outer);
 }
 
 }  // namespace mlf
@@ -848,6 +902,12 @@ int mlf_set_gmres_restart(mlf_ctx* h, int m) {
 int mlf_set_gs_passes(mlf_ctx* h, int passes) {
     if (!h || passes < 1 || passes > 2) return MLF_E_ARG;
     h->c.gs_passes = passes;
+    return MLF_OK;
+}
+
+int mlf_set_basis_precision(mlf_ctx* h, int bits) {
+    if (!h || (bits != 16 && bits != 32)) return MLF_E_ARG;
+    h->c.basis_bits = bits;
     return MLF_OK;
 }
 

@@ -13,6 +13,12 @@
 //   retire independently).
 // mode 2 — batched mixed precision: blocks solved by mlf_solve mode 1
 //   (FP64 refinement around GMRES on the FP32 operator).
+// mode 3 — batched mixed precision with the reference's warm starts: the
+//   angles are dealt to the block's columns in contiguous runs (column q
+//   sweeps angles [q * nrun, (q + 1) * nrun), nrun = ceil(nang / block)),
+//   block k solves the k-th angle of every run, and each column starts from
+//   its previous angle's currents phase-shifted as in mode 0.  Runs end
+//   together except the last ones, so a block's live columns are a prefix.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -66,7 +72,7 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
                               double tol, int maxit, int precond_kind, int mode, int block, double* sigma, int* iters,
                               int* status_out) {
     DevScope ds;
-    if (!h || nang <= 0 || !sigma || !iters || !status_out || maxit <= 0 || !(tol > 0) || mode < 0 || mode > 2)
+    if (!h || nang <= 0 || !sigma || !iters || !status_out || maxit <= 0 || !(tol > 0) || mode < 0 || mode > 3)
         return MLF_E_ARG;
     Ctx* c = &h->c;
     if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
@@ -116,6 +122,43 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
         if ((st = autotune_block(c, cand.data(), (int)cand.size(), &bsel, &cols, nullptr, nullptr))) return st;
     }
     const int bs = std::max(1, std::min(bsel, nang));
+    if (mode == 3) {
+        const int nrun = (nang + bs - 1) / bs;
+        double2 *b = nullptr, *x = nullptr, *g = nullptr;
+        CK(ds.alloc(&b, (size_t)N * bs * sizeof(double2)));
+        CK(ds.alloc(&x, (size_t)N * bs * sizeof(double2)));
+        CK(ds.alloc(&g, (size_t)N * bs * sizeof(double2)));
+        std::vector<double> dirs(3 * (size_t)bs), prev(3 * (size_t)bs), rr(bs);
+        std::vector<double2> pols(3 * (size_t)bs);
+        std::vector<int> it(bs), stc(bs);
+        for (int k = 0; k < nrun && !st; ++k) {
+            int nb = 0;
+            while (nb < bs && nb * nrun + k < nang) ++nb;   // live columns: a prefix
+            for (int q = 0; q < nb; ++q) {
+                mono_dir(ph[q * nrun + k], &dirs[3 * q]);
+                mono_pol(&dirs[3 * q], hh, &pols[3 * q]);
+                if (k > 0)
+                    k_phase_shift<<<(N + 255) / 256, 256, 0, c->stream>>>(
+                        N, c->de_centro, dirs[3 * q] - prev[3 * q], dirs[3 * q + 1] - prev[3 * q + 1],
+                        dirs[3 * q + 2] - prev[3 * q + 2], c->ph.kappa, g + (size_t)q * N);
+            }
+            if ((st = device_excitation(c, dirs.data(), pols.data(), ctte, nb, b))) break;
+            int outer = 0;
+            if ((st = device_solve_mixed(c, b, k > 0 ? g : nullptr, tol, maxit, nb, x, it.data(), rr.data(),
+                                         precond_kind, stc.data(), 0.5 * tol, &outer)))
+                break;
+            for (int q = 0; q < nb && !st; ++q) {
+                const int a = q * nrun + k;
+                const double th = PI / 2.;
+                iters[a] = it[q];
+                status_out[a] = stc[q];
+                st = device_rcs(c, x + (size_t)q * N, &pols[3 * q], ctte, &th, &ph[a], 1, &sigma[a]);
+            }
+            CK(cudaMemcpyAsync(g, x, (size_t)N * nb * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
+            std::copy(dirs.begin(), dirs.begin() + 3 * nb, prev.begin());
+        }
+        return st;
+    }
     double2 *b = nullptr, *x = nullptr;
     CK(ds.alloc(&b, (size_t)N * bs * sizeof(double2)));
     CK(ds.alloc(&x, (size_t)N * bs * sizeof(double2)));

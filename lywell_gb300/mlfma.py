@@ -333,6 +333,10 @@ class MLFMA:
     def set_gs_passes(self, passes: int):
         _check(load().mlf_set_gs_passes(self._h, int(passes)), self._h)
 
+    def set_basis_precision(self, bits: int):
+        """Krylov basis storage of the mixed solve: 32 (FP32) or 16 (FP16)."""
+        _check(load().mlf_set_basis_precision(self._h, int(bits)), self._h)
+
     def matvec32(self, x):
         x = np.asarray(x, dtype=np.complex128)
         single = x.ndim == 1
@@ -377,7 +381,8 @@ class MLFMA:
                    ctte=1.0):
         """Monostatic sweep (gen_rcs_monostatica).  Returns dict(phi, sigma_db, iters, status).
         mode 0: the reference's warm-started sequential sweep; 1: batched FP64 CGS;
-        2: batched mixed precision."""
+        2: batched mixed precision; 3: batched mixed precision, each block
+        column sweeping a contiguous run of angles with mode 0's warm starts."""
         if isinstance(precond, str):
             precond = PRECOND[precond]
         ph = None if phis is None else np.ascontiguousarray(phis, dtype=np.float64)

@@ -245,9 +245,16 @@ def test_monostatic_batched_modes(ico3):
     ref = m.monostatic(12, pol="HH", errmax=1e-6, maxit=3000, mode=0)
     b1 = m.monostatic(12, pol="HH", errmax=1e-6, maxit=3000, mode=1, block=5)
     b2 = m.monostatic(12, pol="HH", errmax=1e-6, maxit=3000, mode=2, block=5)
-    for out in (b1, b2):
+    # mode 3, block 5: runs of 3 angles (the last column has none), a ragged
+    # last block; warm-started columns
+    b3 = m.monostatic(12, pol="HH", errmax=1e-6, maxit=3000, mode=3, block=5)
+    for out in (b1, b2, b3):
         assert all(s == "converged" for s in out["status"])
         assert np.abs(out["sigma_db"] - ref["sigma_db"]).max() < 0.01
+    # the warm-started angles (the 2nd and 3rd of every run) take fewer
+    # iterations than the same angles solved cold in mode 2
+    warm = [a for a in range(12) if a % 3]
+    assert b3["iters"][warm].sum() < b2["iters"][warm].sum()
 
 
 def test_five_level_octree_against_binary(gpu_lib):

@@ -211,3 +211,30 @@ def test_autotune_block_covers_all_engines(ico4):
     assert _rel(Y[:, -1], m.matvec32(X[:, -1])) < 5e-6
     m.set_block_engine(-1)
 
+
+
+@pytest.mark.parametrize("nrhs", [1, 3])
+def test_fp16_basis_meets_fp64_test_and_rcs(ico4, nrhs):
+    """Mode 1 with the Krylov basis stored in FP16 (scaled by sqrt(N)): every
+    column still meets the FP64 residual test, and the RCS stays within
+    0.1 dB of the FP64 CGS solve's."""
+    _, m, _ = ico4
+    m.set_block_engine(-1)
+    assert m.nearinv() == 0
+    dirs = np.stack([direction(90.0, a) for a in (0.0, 60.0, 120.0)[:nrhs]])
+    pols = np.stack([ajustar_polariz(d, "VV") for d in dirs])
+    B = m.excitation(dirs, pols).reshape(m.N, nrhs)
+    try:
+        m.set_basis_precision(16)
+        mix = m.solve(B, errmax=1e-4, maxit=3000, precond="nearinv", mixed=True)
+    finally:
+        m.set_basis_precision(32)
+    X = np.asarray(mix["x"]).reshape(m.N, nrhs)
+    th = np.deg2rad(np.arange(0, 181, 2.0))
+    for k in range(nrhs):
+        assert mix["status"][k] == "converged"   # 2-D right-hand sides give per-column lists
+        assert np.linalg.norm(m.matvec(X[:, k]) - B[:, k]) / np.linalg.norm(B[:, k]) < 1e-4
+        ref = m.solve(B[:, k], errmax=1e-4, maxit=3000, precond="nearinv", mixed=False)
+        s_ref = 10 * np.log10(m.rcs(ref["x"], pols[k], th, np.zeros_like(th)))
+        s_mix = 10 * np.log10(m.rcs(X[:, k], pols[k], th, np.zeros_like(th)))
+        assert np.abs(s_ref - s_mix).max() < 0.1
