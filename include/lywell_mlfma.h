@@ -203,6 +203,13 @@ int mlf_set_gs_passes(mlf_ctx* ctx, int passes);
  * reference. */
 int mlf_set_basis_precision(mlf_ctx* ctx, int bits);
 
+/* FP32 translation stage (mode 1 and mlf_matvec32*): boxes = 2 or 4 = one
+ * thread per sample for that many consecutive boxes over the merged list of
+ * their far boxes, each source value read once for all of them; 1 = one box
+ * at a time; 0 (the default) = 2 for one column, 4 for blocks of columns.
+ * The same sums in another order.  No counterpart in the reference. */
+int mlf_set_translation_group(mlf_ctx* ctx, int boxes);
+
 /* Phase times (ms) of the last mixed-precision solve run while profiling was
  * on (mlf_set_profiling): out4 = {preconditioner, FP32 operator,
  * orthogonalisation, wall total}.  No counterpart in the reference. */

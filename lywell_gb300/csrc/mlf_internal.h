@@ -103,6 +103,12 @@ struct Mixed32 {
         float2 *T = nullptr, *shift = nullptr, *C = nullptr, *B = nullptr, *A = nullptr;
         float* wq = nullptr;
         float *wth = nullptr, *wph = nullptr, *thT_w = nullptr, *phT_w = nullptr;
+        // translation by groups of G = 2 (grp[0]) or 4 (grp[1]) consecutive boxes:
+        // merged far lists, sources ascending, tid = the source's translation
+        // index for each box of the group (-1: not far)
+        struct Grp {
+            int *ptr = nullptr, *src = nullptr, *tid = nullptr;
+        } grp[2];
     } lv[32];
 };
 
@@ -113,6 +119,7 @@ struct Ctx {
     int mv_prec = 0;                  // operator precision used by device_matvec: 0 FP64, 1 FP32
     int gmres_m = 800;                // restart length of the mixed-precision GMRES cycles
     int gs_passes = 1;                // classical Gram-Schmidt passes per Arnoldi step (1 or 2)
+    int tr_group = 0;                 // FP32 translation: boxes per thread (1, 2, 4; 0: 2 for one column, else 4)
     int basis_bits = 32;              // Krylov basis storage of the mixed solve: 32 (FP32) or 16 (FP16)
     Mixed32 m32;
     cudaStream_t stream = nullptr;

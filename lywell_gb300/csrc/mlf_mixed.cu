@@ -119,6 +119,67 @@ __global__ void k32_translate(int K, int nrhs, int nchunk, const int* __restrict
     }
 }
 
+// The same sums for a group of G consecutive boxes (G i .. G i + G - 1, in
+// depth-first order and mostly siblings) over the merged list of their far
+// boxes: each source value read from L2 serves every box of the group that
+// has it, so the stage's L2 traffic, which bounds it, drops.  One thread per
+// sample k, both polarisations, NR columns and the G boxes in registers.
+template <int NR, int G>
+__global__ void k32_translate_grp(int K, int nb, int nrhs, int nchunk, const int* __restrict__ gptr,
+                                  const int* __restrict__ gsrc, const int* __restrict__ gtid,
+                                  const float2* __restrict__ T, const float* __restrict__ wq,
+                                  const float2* __restrict__ C, float2* __restrict__ B) {
+    const int chunk = blockIdx.x % nchunk;
+    const int gr = blockIdx.x / nchunk;
+    const int c0 = blockIdx.y * NR;
+    const int k = chunk * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const size_t K2 = 2 * (size_t)K;
+    float2 acc[G][2][NR];
+#pragma unroll
+    for (int h = 0; h < G; ++h)
+#pragma unroll
+        for (int u = 0; u < NR; ++u) acc[h][0][u] = acc[h][1][u] = make_float2(0.f, 0.f);
+    const int e1 = gptr[gr + 1];
+    for (int e = gptr[gr]; e < e1; ++e) {
+        int t[G];   // the same for the whole CTA: uniform branches
+        if (G == 4) {
+            const int4 q = reinterpret_cast<const int4*>(gtid)[e];
+            t[0] = q.x; t[1] = q.y; t[2 % G] = q.z; t[3 % G] = q.w;
+        } else {
+            const int2 q = reinterpret_cast<const int2*>(gtid)[e];
+            t[0] = q.x; t[1 % G] = q.y;
+        }
+        const float2* cs = C + ((size_t)gsrc[e] * nrhs + c0) * K2 + k;
+        float2 tv[G];
+#pragma unroll
+        for (int h = 0; h < G; ++h) tv[h] = t[h] >= 0 ? T[(size_t)t[h] * K + k] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < NR; ++u) {
+            if (c0 + u < nrhs) {
+                const float2 p = cs[u * K2], q = cs[u * K2 + K];
+#pragma unroll
+                for (int h = 0; h < G; ++h)
+                    if (t[h] >= 0) { fmac(acc[h][0][u], p, tv[h]); fmac(acc[h][1][u], q, tv[h]); }
+            }
+        }
+    }
+    const float wk = wq[k];
+#pragma unroll
+    for (int h = 0; h < G; ++h) {
+        const int b = G * gr + h;
+        if (b >= nb) break;
+        float2* bo = B + ((size_t)b * nrhs + c0) * K2 + k;
+#pragma unroll
+        for (int u = 0; u < NR; ++u) {
+            if (c0 + u < nrhs) {
+                bo[u * K2] = make_float2(acc[h][0][u].x * wk, acc[h][0][u].y * wk);
+                bo[u * K2 + K] = make_float2(acc[h][1][u].x * wk, acc[h][1][u].y * wk);
+            }
+        }
+    }
+}
+
 __global__ void k32_receive_near(int K, int N, int nrhs, int ld, const int* __restrict__ perm,
                                  const int* __restrict__ box_of_sorted, const float2* __restrict__ R,
                                  const float2* __restrict__ A, const int* __restrict__ ia, const int* __restrict__ ja,
@@ -170,6 +231,43 @@ static int conv32(Ctx* c, float2** dst, const double2* src, size_t n) {
     return MLF_OK;
 }
 
+// Merged far lists of the box groups (G i .. G i + G - 1) of one level,
+// sources ascending, with each source's translation index per box (-1 where
+// it is not far from that box).
+static int group_lists(Ctx* c, const Level& L, int G, Mixed32::Lv::Grp& M) {
+    const int ng = (L.nb + G - 1) / G;
+    std::vector<int> gptr(ng + 1, 0), gsrc, gtid;
+    std::vector<std::pair<int, int>> ent;   // (source, box within the group), then the translation
+    std::vector<int> etid;
+    for (int g = 0; g < ng; ++g) {
+        ent.clear();
+        etid.clear();
+        for (int h = 0; h < G && G * g + h < L.nb; ++h) {
+            const int b = G * g + h;
+            for (int f = L.far_ptr[b]; f < L.far_ptr[b + 1]; ++f) ent.push_back({L.far_src[f], (h << 20) | (int)etid.size()}), etid.push_back(L.far_tid[f]);
+        }
+        std::sort(ent.begin(), ent.end());
+        for (size_t q = 0; q < ent.size(); ++q) {
+            const int h = ent[q].second >> 20, t = etid[ent[q].second & 0xfffff];
+            if (q == 0 || ent[q].first != ent[q - 1].first) {
+                gsrc.push_back(ent[q].first);
+                gtid.insert(gtid.end(), G, -1);
+            }
+            gtid[gtid.size() - G + h] = t;
+        }
+        gptr[g + 1] = (int)gsrc.size();
+    }
+    CK(cudaMalloc(&M.ptr, gptr.size() * sizeof(int)));
+    CK(cudaMalloc(&M.src, std::max<size_t>(gsrc.size(), 1) * sizeof(int)));
+    CK(cudaMalloc(&M.tid, std::max<size_t>(gtid.size(), 4) * sizeof(int)));
+    CK(cudaMemcpy(M.ptr, gptr.data(), gptr.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (!gsrc.empty()) {
+        CK(cudaMemcpy(M.src, gsrc.data(), gsrc.size() * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(M.tid, gtid.data(), gtid.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    return MLF_OK;
+}
+
 int mixed_setup(Ctx* c) {
     if (c->m32.ready) return MLF_OK;
     const int nl = c->nlev;
@@ -180,6 +278,8 @@ int mixed_setup(Ctx* c) {
         Mixed32::Lv& M = c->m32.lv[n];
         if ((st = conv32(c, &M.T, L.dT, (size_t)L.ntrans * L.K))) return st;
         if ((st = up32(c, &M.wq, L.wq))) return st;
+        if ((st = group_lists(c, L, 2, M.grp[0]))) return st;
+        if ((st = group_lists(c, L, 4, M.grp[1]))) return st;
         if (n < nl) {
             if ((st = up32(c, &M.wth, L.wth))) return st;
             if ((st = up32(c, &M.wph, L.wph))) return st;
@@ -299,6 +399,22 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
         const int nr = nrhs <= 1 ? 1 : nrhs <= 2 ? 2 : nrhs <= 4 ? 4 : 8;
         const dim3 grid(L.nb * nch, (nrhs + nr - 1) / nr);
         const Mixed32::Lv& m = c->m32.lv[n];
+        const int G = c->tr_group ? c->tr_group : (nrhs == 1 ? 2 : 4);
+        if (G > 1 && m.grp[G / 4].ptr) {
+            // box groups: at most 8 sums of each box's two polarisations per thread
+            const Mixed32::Lv::Grp& gl = m.grp[G / 4];
+            const int ng = (L.nb + G - 1) / G, nrg = std::min(nr, G == 4 ? 2 : 4);
+            const dim3 gg(ng * nch, (nrhs + nrg - 1) / nrg);
+#define TGRP(NR_, G_) k32_translate_grp<NR_, G_><<<gg, bd, 0, s>>>(L.K, L.nb, nrhs, nch, gl.ptr, gl.src, gl.tid, \
+                                                                  m.T, m.wq, m.C, m.B)
+            if (G == 4) {
+                if (nrg == 1) TGRP(1, 4); else TGRP(2, 4);
+            } else {
+                if (nrg == 1) TGRP(1, 2); else if (nrg == 2) TGRP(2, 2); else TGRP(4, 2);
+            }
+#undef TGRP
+            continue;
+        }
         if (nr == 1)
             k32_translate<1><<<grid, bd, 0, s>>>(L.K, nrhs, nch, L.dfar_ptr, L.dfar_src, L.dfar_tid, m.T, m.wq, m.C, m.B);
         else if (nr == 2)
@@ -355,6 +471,7 @@ void mixed_free(Ctx* c) {
         Mixed32::Lv& M = c->m32.lv[n];
         F(M.T); F(M.wq); F(M.shift); F(M.C); F(M.B); F(M.A);
         F(M.wth); F(M.wph); F(M.thT_w); F(M.phT_w);
+        for (auto& g : M.grp) { F(g.ptr); F(g.src); F(g.tid); }
     }
 }
 
@@ -902,6 +1019,12 @@ int mlf_set_gmres_restart(mlf_ctx* h, int m) {
 int mlf_set_gs_passes(mlf_ctx* h, int passes) {
     if (!h || passes < 1 || passes > 2) return MLF_E_ARG;
     h->c.gs_passes = passes;
+    return MLF_OK;
+}
+
+int mlf_set_translation_group(mlf_ctx* h, int boxes) {
+    if (!h || (boxes != 0 && boxes != 1 && boxes != 2 && boxes != 4)) return MLF_E_ARG;
+    h->c.tr_group = boxes;
     return MLF_OK;
 }
 

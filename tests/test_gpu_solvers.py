@@ -238,3 +238,23 @@ def test_fp16_basis_meets_fp64_test_and_rcs(ico4, nrhs):
         s_ref = 10 * np.log10(m.rcs(ref["x"], pols[k], th, np.zeros_like(th)))
         s_mix = 10 * np.log10(m.rcs(X[:, k], pols[k], th, np.zeros_like(th)))
         assert np.abs(s_ref - s_mix).max() < 0.1
+
+
+@pytest.mark.parametrize("boxes", [2, 4])
+@pytest.mark.parametrize("nrhs", [1, 2, 3, 8, 11])
+def test_translation_groups_match_per_box(ico4, nrhs, boxes):
+    """FP32 translation by groups of consecutive boxes over their merged far
+    lists against one box at a time: the same sums in another order, 1e-6."""
+    _, m, _ = ico4
+    rng = np.random.default_rng(90 + nrhs)
+    X = rng.standard_normal((m.N, nrhs)) + 1j * rng.standard_normal((m.N, nrhs))
+    try:
+        m.set_translation_group(boxes)
+        Yg = m.matvec32(X).reshape(m.N, nrhs)
+        m.set_translation_group(1)
+        Yb = m.matvec32(X).reshape(m.N, nrhs)
+    finally:
+        m.set_translation_group(0)
+    for k in range(nrhs):
+        assert _rel(Yg[:, k], Yb[:, k]) < 1e-6
+        assert _rel(Yg[:, k], m.matvec(X[:, k])) < 2e-5
