@@ -153,6 +153,48 @@ module lywell_mlfma_cabi
             integer(c_int), value :: nang
             real(c_double), intent(out) :: sigma(*)
         end function
+
+        ! tuning of the mixed-precision and batched paths (optional; no counterpart
+        ! in the reference)
+        integer(c_int) function mlf_autotune_block(ctx, candidates, ncand, best_block, best_cols, &
+                                                   best_engine, per_rhs_ms) bind(C)
+            import :: c_int, c_float, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), intent(in) :: candidates(*)
+            integer(c_int), value :: ncand
+            integer(c_int), intent(out) :: best_block, best_cols, best_engine
+            real(c_float), intent(out) :: per_rhs_ms(*)
+        end function
+
+        integer(c_int) function mlf_set_block_engine(ctx, engine, cols) bind(C)
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: engine, cols
+        end function
+
+        integer(c_int) function mlf_set_gmres_restart(ctx, m) bind(C)
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: m
+        end function
+
+        integer(c_int) function mlf_set_gs_passes(ctx, passes) bind(C)
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: passes
+        end function
+
+        integer(c_int) function mlf_set_basis_precision(ctx, bits) bind(C)
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: bits
+        end function
+
+        integer(c_int) function mlf_set_translation_group(ctx, boxes) bind(C)
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: boxes
+        end function
     end interface
 
 contains
