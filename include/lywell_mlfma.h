@@ -174,11 +174,12 @@ int mlf_cgs(mlf_ctx* ctx, const double* b, const double* x0, double tol, int max
 /* Solve Z_MLFMA x = b for nrhs columns.  mode 0: CGS on the FP64 operator
  * (exactly mlf_cgs).  mode 1: mixed precision — iterative refinement whose
  * residual r = b - Z x is formed with the FP64 operator and whose
- * corrections come from one right-preconditioned GMRES(m) cycle (m = 800 by
- * default, mlf_set_gmres_restart) on the FP32
+ * corrections come from one right-preconditioned GMRES(m) cycle (m set by
+ * mlf_set_gmres_restart, or by default 1600 while the basis fits in 16 GB,
+ * down to 800 for wide blocks) on the FP32
  * operator (patterns, translations, interpolation and fields in float;
  * complex(4) near field), stopped when its residual estimate drops below
- * inner_tol ||b|| (<= 0: tol/2).  Stops when the FP64 residual satisfies
+ * inner_tol ||b|| (<= 0: 0.9 tol).  Stops when the FP64 residual satisfies
  * ||b - Z x|| < tol ||b||, the same test as CGSold (modIterativo.f90:472).
  * iters: inner GMRES steps (FP32 matvecs) per column; *outer: refinement
  * steps (FP64 matvecs).  No counterpart in the reference for mode 1. */
@@ -186,8 +187,9 @@ int mlf_solve(mlf_ctx* ctx, const double* b, const double* x0, double tol, int m
               int precond_kind, int mode, double inner_tol, double* x, int* iters, double* relres,
               int* status_out, int* outer);
 
-/* Restart length m of mode 1's GMRES cycles (4..2000; memory (m+1) N nrhs
- * complex(8) values). */
+/* Restart length m of mode 1's GMRES cycles (4..2000, or 0 = automatic:
+ * 1600 while the basis fits in 16 GB, down to 800; memory (m+1) N nrhs
+ * FP32 complex values). */
 int mlf_set_gmres_restart(mlf_ctx* ctx, int m);
 
 /* Classical Gram-Schmidt passes per Arnoldi step of mode 1 (1, the default:

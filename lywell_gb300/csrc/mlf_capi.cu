@@ -295,7 +295,7 @@ int mlf_solve(mlf_ctx* h, const double* b, const double* x0, double tol, int max
     int outer_k = 0;
     if (!st)
         st = device_solve_mixed(c, db, dx0, tol, maxit, nrhs, dx, iters, relres, precond_kind, status_out,
-                                inner_tol > 0 ? inner_tol : 0.5 * tol, &outer_k);
+                                inner_tol > 0 ? inner_tol : 0.9 * tol, &outer_k);
     if (outer) *outer = outer_k;
     if (!st) st = d2h_cols(c, x, dx, nrhs, c->N);
     if (!st) CK(cudaStreamSynchronize(c->stream));

@@ -117,7 +117,7 @@ struct Ctx {
     int dense = 0;                    // dense MoM operator instead of the octree (MLF_FLAG_DENSE_MOM)
     double2* dZdense = nullptr;       // N x N row-major, FP64
     int mv_prec = 0;                  // operator precision used by device_matvec: 0 FP64, 1 FP32
-    int gmres_m = 800;                // restart length of the mixed-precision GMRES cycles
+    int gmres_m = 0;                  // restart length of the mixed-precision GMRES cycles (0: automatic)
     int gs_passes = 1;                // classical Gram-Schmidt passes per Arnoldi step (1 or 2)
     int tr_group = 0;                 // FP32 translation: boxes per thread (1, 2, 4; 0: 2 for one column, else 4)
     int basis_bits = 32;              // Krylov basis storage of the mixed solve: 32 (FP32) or 16 (FP16)

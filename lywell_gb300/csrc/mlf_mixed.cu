@@ -794,7 +794,12 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
                          int* iters, double* relres, int precond, int* status, double inner_tol, int* outer) {
     DevScope ds;
     const int N = c->N;
-    const int m = std::max(4, std::min(c->gmres_m, 2000));
+    // restart length: the one set, else 1600 while the basis fits in 16 GB,
+    // down to 800 for wide blocks (a cold solve of the bench workloads takes
+    // 1200-1600 steps; warm-started ones 500-800)
+    const size_t colbytes = (size_t)N * nrhs * sizeof(BT);
+    const int m_auto = (int)std::max<size_t>(800, std::min<size_t>(1600, ((size_t)16 << 30) / colbytes - 1));
+    const int m = std::max(4, std::min(c->gmres_m > 0 ? c->gmres_m : m_auto, 2000));
     const size_t V1 = (size_t)N * nrhs;
     cudaStream_t s = c->stream;
     constexpr bool f32 = std::is_same<BT, float2>::value;
@@ -1011,7 +1016,7 @@ extern "C" int mlf_solve_times(mlf_ctx* h, double* out4) {
 }
 
 int mlf_set_gmres_restart(mlf_ctx* h, int m) {
-    if (!h || m < 4 || m > 2000) return MLF_E_ARG;
+    if (!h || (m != 0 && (m < 4 || m > 2000))) return MLF_E_ARG;
     h->c.gmres_m = m;
     return MLF_OK;
 }

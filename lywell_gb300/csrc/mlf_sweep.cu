@@ -145,7 +145,7 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
             if ((st = device_excitation(c, dirs.data(), pols.data(), ctte, nb, b))) break;
             int outer = 0;
             if ((st = device_solve_mixed(c, b, k > 0 ? g : nullptr, tol, maxit, nb, x, it.data(), rr.data(),
-                                         precond_kind, stc.data(), 0.5 * tol, &outer)))
+                                         precond_kind, stc.data(), 0.9 * tol, &outer)))
                 break;
             for (int q = 0; q < nb && !st; ++q) {
                 const int a = q * nrun + k;
@@ -176,7 +176,7 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
         } else {
             int outer = 0;
             st = device_solve_mixed(c, b, nullptr, tol, maxit, nb, x, &iters[a0], rr.data(), precond_kind,
-                                    &status_out[a0], 0.5 * tol, &outer);
+                                    &status_out[a0], 0.9 * tol, &outer);
         }
         if (st) break;
         for (int q = 0; q < nb && !st; ++q) {
