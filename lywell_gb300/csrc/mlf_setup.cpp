@@ -148,21 +148,19 @@ extern "C" int mlf_rwg_build(const double* tris, int T, int* N_out, int* P_out, 
         la[3 * t + 1] = tp[3 * t]; lb[3 * t + 1] = tp[3 * t + 2];
         la[3 * t + 2] = tp[3 * t + 1]; lb[3 * t + 2] = tp[3 * t + 2];
     }
-    std::vector<int> order(M);
-    for (int i = 0; i < M; ++i) order[i] = i;
-    auto key = [&](int i) {
+    // sides sorted by (node pair, side index): equal pairs are adjacent, in side order
+    std::vector<std::pair<uint64_t, int>> ks(M);
+    for (int i = 0; i < M; ++i) {
         const uint64_t a = (uint64_t)std::min(la[i], lb[i]), b = (uint64_t)std::max(la[i], lb[i]);
-        return (a << 32) | b;
-    };
-    std::sort(order.begin(), order.end(), [&](int x, int y) {
-        const uint64_t kx = key(x), ky = key(y);
-        return kx != ky ? kx < ky : x < y;
-    });
+        ks[i] = {(a << 32) | b, i};
+    }
+    std::sort(ks.begin(), ks.end());
     std::vector<std::pair<int, int>> pairs;
+    pairs.reserve(M / 2);
     for (int s = 0; s < M;) {
         int e = s;
-        while (e + 1 < M && key(order[e + 1]) == key(order[s])) ++e;
-        for (int q = s; q + 1 <= e; q += 2) pairs.emplace_back(order[q], order[q + 1]);
+        while (e + 1 < M && ks[e + 1].first == ks[s].first) ++e;
+        for (int q = s; q + 1 <= e; q += 2) pairs.emplace_back(ks[q].second, ks[q + 1].second);
         s = e + 1;
     }
     std::sort(pairs.begin(), pairs.end());

@@ -53,24 +53,29 @@ class RWG:
         tris = np.ascontiguousarray(tris, dtype=np.float64).reshape(-1, 3, 3)
         L = load()
         T = tris.shape[0]
+        # one call with the arrays sized for the bounds (P <= 3T nodes, N <= 3T/2
+        # edges: every edge pairs two triangle sides), then trimmed
+        Pm, Nm = 3 * T, (3 * T) // 2
         N = C.c_int()
         P = C.c_int()
-        _check(L.mlf_rwg_build(_p(tris), T, C.byref(N), C.byref(P), *([None] * 10)))
-        N, P = N.value, P.value
-        self.N, self.P, self.T = N, P, T
-        self.p_coord = np.zeros((P, 3))
+        p_coord = np.zeros((Pm, 3))
         self.t_p = np.zeros((T, 3), dtype=np.int32)
-        self.e_p = np.zeros((N, 2), dtype=np.int32)
-        self.e_t = np.zeros((N, 2), dtype=np.int32)
-        self.e_po = np.zeros((N, 2), dtype=np.int32)
-        self.e_long = np.zeros(N)
-        self.e_centro = np.zeros((N, 3))
+        e_p = np.zeros((Nm, 2), dtype=np.int32)
+        e_t = np.zeros((Nm, 2), dtype=np.int32)
+        e_po = np.zeros((Nm, 2), dtype=np.int32)
+        e_long = np.zeros(Nm)
+        e_centro = np.zeros((Nm, 3))
         self.t_area = np.zeros(T)
         self.t_baric = np.zeros((T, 3))
         self.t_baric_sub = np.zeros((T, 9, 3))
-        _check(L.mlf_rwg_build(_p(tris), T, C.byref(C.c_int()), C.byref(C.c_int()), _p(self.p_coord),
-                               _p(self.t_p), _p(self.e_p), _p(self.e_t), _p(self.e_po), _p(self.e_long),
-                               _p(self.e_centro), _p(self.t_area), _p(self.t_baric), _p(self.t_baric_sub)))
+        _check(L.mlf_rwg_build(_p(tris), T, C.byref(N), C.byref(P), _p(p_coord), _p(self.t_p), _p(e_p), _p(e_t),
+                               _p(e_po), _p(e_long), _p(e_centro), _p(self.t_area), _p(self.t_baric),
+                               _p(self.t_baric_sub)))
+        N, P = N.value, P.value
+        self.N, self.P, self.T = N, P, T
+        self.p_coord = p_coord[:P]
+        self.e_p, self.e_t, self.e_po = e_p[:N], e_t[:N], e_po[:N]
+        self.e_long, self.e_centro = e_long[:N], e_centro[:N]
         # 0-based views
         self.t_p -= 1
         self.e_p -= 1
