@@ -244,7 +244,6 @@ int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const fl
                         cudaStream_t s);
 void near_blocks_free(Ctx* c);
 // warp engine (mlf_nearwarp.cu): one warp per basis, for small leaf boxes
-int warp_engine_ensure(Ctx* c);
 void warp_engine_free(Ctx* c);
 int blk_engine_of(const Ctx* c);   // the engine in force (resolves -1)
 int device_agg_warp32(Ctx* c, const float2* R, int K, const float2* xs, int nrhs, float2* C, cudaStream_t s);
@@ -253,7 +252,6 @@ int device_recv_near_warp32(Ctx* c, const float2* R, int K, const float2* A, flo
 int device_near_pattern_warp32(Ctx* c, const float2* M, const float2* xs, int nrhs, float2* out, cudaStream_t s);
 int device_own_warp32(Ctx* c, const long long* boff, const float2* M, const float2* xs, int nrhs, float2* out,
                       cudaStream_t s);
-int near_blocks_ensure(Ctx* c);
 int device_blocks_from_csr(Ctx* c, const float2* csr, float2** blk);
 int device_near_pattern_apply32(Ctx* c, const float2* Mblk, const float2* xs, int nrhs, float2* out, cudaStream_t s);
 int lp_tokens(Ctx* c, int with_target, float* X, float* T, long long cap, long long* ntok, int* bad_box);

@@ -615,8 +615,6 @@ int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const fl
     return cuda_ok(c, cudaGetLastError(), "own-box blocks") ? MLF_OK : MLF_E_CUDA;
 }
 
-int near_blocks_ensure(Ctx* c) { return near_blocks_setup(c); }
-
 void near_blocks_free(Ctx* c) {
     auto F = [](void* p) { if (p) cudaFree(p); };
     F(c->dZblk); F(c->dblk_off); F(c->dnbox_ptr); F(c->dnbox_list); F(c->dblk_tiles); F(c->dblk_entry);

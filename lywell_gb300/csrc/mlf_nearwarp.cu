@@ -226,8 +226,6 @@ static int warp_setup(Ctx* c) {
     return MLF_OK;
 }
 
-int warp_engine_ensure(Ctx* c) { return warp_setup(c); }
-
 // The engine in force: the one set (mlf_set_block_engine, the autotuner),
 // else the warp engine when leaf boxes hold fewer than 48 bases on average.
 int blk_engine_of(const Ctx* c) {
