@@ -222,17 +222,19 @@ def project_sequential(t_sample, iters, nang=722):
     return t_sample / it.sum() * (it[0] + (nang - 1) * it[1:].mean())
 
 
-def project_batched_warm(t_sample, iters, block, nrun_sample=3, nang=722):
-    """mlf_monostatic mode 3 over nang angles, from a sample of nrun_sample
+def project_batched_warm(t_sample, iters, block, nrun_sample=4, nang=722, steady_from=2):
+    """mlf_monostatic mode 3/4 over nang angles, from a sample of nrun_sample
     blocks (runs of nrun_sample angles per column): a block's time is split
     by its slowest column's iteration count (the block steps until every
-    column has converged); the first block starts cold, every later one
-    warm."""
+    column has converged).  Blocks before `steady_from` are counted once (the
+    cold start; in mode 4 also the first warm block, which has only one
+    previous angle to start from), every later block of the full sweep as the
+    mean of the sampled later ones."""
     it = np.asarray(iters, dtype=float).reshape(block, nrun_sample)   # [column, step of its run]
     per_block = it.max(axis=0)
     t_blk = t_sample * per_block / per_block.sum()
     nrun = -(-nang // block)
-    return float(t_blk[0] + (nrun - 1) * t_blk[1:].mean())
+    return float(t_blk[:steady_from].sum() + (nrun - steady_from) * t_blk[steady_from:].mean())
 
 
 def batched_rcs_sample(seq_angles=3, block=0, maxit=4000):
@@ -255,14 +257,15 @@ def batched_rcs_sample(seq_angles=3, block=0, maxit=4000):
     nang_total, dphi = 722, np.deg2rad(0.5)
     tune = m.autotune_block() if block <= 0 else dict(block=block, tile_cols=0, per_rhs_ms={})
     B = int(tune["block"])
-    # mode 3 on 3 x B angles: each column sweeps a run of 3 angles 0.5 deg apart,
-    # the first cold and two warm, as the first three blocks of the full sweep
-    nrs = 3
+    # mode 4 on 4 x B angles: each column sweeps a run of 4 angles 0.5 deg apart
+    # (cold, warm from one previous angle, then extrapolated from two), as the
+    # first four blocks of the full sweep
+    nrs = 4
     phis = np.arange(nrs * B) * dphi
     torch.cuda.synchronize()
     m.set_profiling(True)
     t0 = time.time()
-    mix = m.monostatic(nrs * B, phis=phis, pol="VV", errmax=1e-4, maxit=maxit, precond="nearinv", mode=3, block=B)
+    mix = m.monostatic(nrs * B, phis=phis, pol="VV", errmax=1e-4, maxit=maxit, precond="nearinv", mode=4, block=B)
     t_mix = time.time() - t0
     phases = m.solve_times()
     m.set_profiling(False)
@@ -276,7 +279,7 @@ def batched_rcs_sample(seq_angles=3, block=0, maxit=4000):
     db = np.abs(mix["sigma_db"][:seq_angles] - seq["sigma_db"])
     out = {"workload": SPHEROID["name"], "N": m.N, "near_nnz": m.nnz, "setup_s": t_tree, "precond_setup_s": t_pre,
            "precond": "own-box near-field inverse", "nearinv_bad_box": bad, "autotune": tune, "block": B,
-           "mixed_batched": {"mode": 3, "angles": nrs * B, "blocks": nrs, "seconds": t_mix,
+           "mixed_batched": {"mode": 4, "angles": nrs * B, "blocks": nrs, "seconds": t_mix,
                              "iters": [int(v) for v in mix["iters"]], "status": sorted(set(mix["status"])),
                              "phases_ms": phases},
            "fp64_sequential": {"angles": seq_angles, "seconds": t_seq,
@@ -284,9 +287,9 @@ def batched_rcs_sample(seq_angles=3, block=0, maxit=4000):
            "projected_722_s": {"mixed_batched": t_tree + t_pre + proj_mix,
                                "fp64_sequential": t_tree + t_pre + proj_seq},
            "rcs_db_maxdiff_vs_fp64": float(db.max()),
-           "note": "solve times measured on samples of the 722-RHS sweep (3 sequential angles; 3 blocks of the "
-                   "batched sweep) and projected with one cold start and warm starts after it, time split by "
-                   "iteration count"}
+           "note": "solve times measured on samples of the 722-RHS sweep (3 sequential angles; 4 blocks of the "
+                   "batched sweep) and projected with the cold start (and, batched, the first warm block) once "
+                   "and the later steps as sampled, time split by iteration count"}
     out["s_per_rhs_projected"] = {k: v / nang_total for k, v in out["projected_722_s"].items()}
     out["speedup_projected_722"] = out["projected_722_s"]["fp64_sequential"] / out["projected_722_s"]["mixed_batched"]
     m.close()
@@ -490,20 +493,20 @@ def learned_at_scale(steps=3000, seed=0):
     B = int(tune["block"])
     torch.cuda.synchronize()
     t1 = time.time()
-    bat = m.monostatic(3 * B, phis=np.arange(3 * B) * dphi, pol="VV", errmax=1e-4, maxit=4000, precond="nearinv",
-                       mode=3, block=B)
+    bat = m.monostatic(4 * B, phis=np.arange(4 * B) * dphi, pol="VV", errmax=1e-4, maxit=4000, precond="nearinv",
+                       mode=4, block=B)
     t_bat = time.time() - t1
     m.close()
     p_seq = project_sequential(t_seq, seq["iters"])
-    p_bat = project_batched_warm(t_bat, bat["iters"], B, 3)
+    p_bat = project_batched_warm(t_bat, bat["iters"], B, 4)
     sweep = {"fp64_sequential_exact": {"angles": 3, "seconds": t_seq, "iters": [int(v) for v in seq["iters"]],
                                        "s_per_rhs_projected": p_seq / 722},
-             "mixed_batched_learned": {"mode": 3, "angles": 3 * B, "blocks": 3, "seconds": t_bat, "autotune": tune,
+             "mixed_batched_learned": {"mode": 4, "angles": 4 * B, "blocks": 4, "seconds": t_bat, "autotune": tune,
                                        "iters": [int(v) for v in bat["iters"]],
                                        "status": sorted(set(bat["status"])), "s_per_rhs_projected": p_bat / 722},
              "rcs_db_maxdiff": float(np.abs(bat["sigma_db"][:3] - seq["sigma_db"]).max()),
-             "note": "projected from 3 sequential angles and 3 batched blocks: one cold start, warm starts after "
-                     "it, time split by iteration count"}
+             "note": "projected from 3 sequential angles and 4 batched blocks: the cold start (and, batched, the "
+                     "first warm block) once, the later steps as sampled, time split by iteration count"}
     sweep["projected_722_s"] = {"fp64_sequential_exact": p_seq, "mixed_batched_learned": p_bat}
     sweep["speedup_projected_722"] = p_seq / p_bat
     base = out["fp64_cgs_exact_neighbourhood"]["time_to_rcs_s"]

@@ -309,8 +309,11 @@ int mlf_rcs(mlf_ctx* ctx, const double* I, const double* pol, double ctte_re, do
  *         n = ceil(nang / block); block k solves the k-th angle of every run,
  *         each column starting from its previous angle's phase-shifted
  *         currents.
- * block <= 0 (modes 1-3): chosen by mlf_autotune_block among 8..128.
- * Modes 1-3 have no counterpart in the reference. */
+ * mode 4: mode 3 with each column's start extrapolated linearly from its
+ *         two previous angles' currents, both phase-shifted to the new
+ *         direction (x0 = 2 x_{k-1} - x_{k-2}).
+ * block <= 0 (modes 1-4): chosen by mlf_autotune_block among 8..128.
+ * Modes 1-4 have no counterpart in the reference. */
 int mlf_monostatic(mlf_ctx* ctx, int nang, const double* phis, int hh, double ctte_re, double ctte_im,
                    double tol, int maxit, int precond_kind, int mode, int block, double* sigma, int* iters,
                    int* status_out);

@@ -19,6 +19,9 @@
 //   block k solves the k-th angle of every run, and each column starts from
 //   its previous angle's currents phase-shifted as in mode 0.  Runs end
 //   together except the last ones, so a block's live columns are a prefix.
+// mode 4 — mode 3 with each column's start extrapolated from its two previous
+//   angles: the currents are a slowly varying amplitude times the incident
+//   phase, so with both shifted to the new direction, x0 = 2 x_{k-1} - x_{k-2}.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -47,6 +50,12 @@ __global__ void k_phase_shift(int N, const double* __restrict__ e_centro, double
     x[i] = make_double2(v.x * co + v.y * s, v.y * co - v.x * s);
 }
 
+// b = 2 a - b
+__global__ void k_extrapolate(size_t n, const double2* __restrict__ a, double2* __restrict__ b) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = make_double2(2. * a[i].x - b[i].x, 2. * a[i].y - b[i].y);
+}
+
 static void mono_dir(double phi, double* d) {
     d[0] = -std::cos(phi);
     d[1] = -std::sin(phi);
@@ -72,7 +81,7 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
                               double tol, int maxit, int precond_kind, int mode, int block, double* sigma, int* iters,
                               int* status_out) {
     DevScope ds;
-    if (!h || nang <= 0 || !sigma || !iters || !status_out || maxit <= 0 || !(tol > 0) || mode < 0 || mode > 3)
+    if (!h || nang <= 0 || !sigma || !iters || !status_out || maxit <= 0 || !(tol > 0) || mode < 0 || mode > 4)
         return MLF_E_ARG;
     Ctx* c = &h->c;
     if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
@@ -122,12 +131,14 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
         if ((st = autotune_block(c, cand.data(), (int)cand.size(), &bsel, &cols, nullptr, nullptr))) return st;
     }
     const int bs = std::max(1, std::min(bsel, nang));
-    if (mode == 3) {
+    if (mode >= 3) {
         const int nrun = (nang + bs - 1) / bs;
-        double2 *b = nullptr, *x = nullptr, *g = nullptr;
+        double2 *b = nullptr, *x = nullptr, *g = nullptr, *g2 = nullptr;
         CK(ds.alloc(&b, (size_t)N * bs * sizeof(double2)));
         CK(ds.alloc(&x, (size_t)N * bs * sizeof(double2)));
-        CK(ds.alloc(&g, (size_t)N * bs * sizeof(double2)));
+        CK(ds.alloc(&g, (size_t)N * bs * sizeof(double2)));    // previous angle's currents
+        if (mode == 4) CK(ds.alloc(&g2, (size_t)N * bs * sizeof(double2)));   // the one before
+        const size_t nbytes_col = (size_t)N * sizeof(double2);
         std::vector<double> dirs(3 * (size_t)bs), prev(3 * (size_t)bs), rr(bs);
         std::vector<double2> pols(3 * (size_t)bs);
         std::vector<int> it(bs), stc(bs);
@@ -141,11 +152,22 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
                     k_phase_shift<<<(N + 255) / 256, 256, 0, c->stream>>>(
                         N, c->de_centro, dirs[3 * q] - prev[3 * q], dirs[3 * q + 1] - prev[3 * q + 1],
                         dirs[3 * q + 2] - prev[3 * q + 2], c->ph.kappa, g + (size_t)q * N);
+                if (k > 1 && g2)
+                    k_phase_shift<<<(N + 255) / 256, 256, 0, c->stream>>>(
+                        N, c->de_centro, dirs[3 * q] - prev[3 * q], dirs[3 * q + 1] - prev[3 * q + 1],
+                        dirs[3 * q + 2] - prev[3 * q + 2], c->ph.kappa, g2 + (size_t)q * N);
+            }
+            // mode 4: the two previous angles' currents, both phase-shifted to this
+            // angle, extrapolated linearly (x0 = 2 x_{k-1} - x_{k-2}, into g2)
+            const double2* x0 = k > 0 ? g : nullptr;
+            if (k > 1 && g2) {
+                k_extrapolate<<<4096, 256, 0, c->stream>>>((size_t)N * nb, g, g2);
+                x0 = g2;
             }
             if ((st = device_excitation(c, dirs.data(), pols.data(), ctte, nb, b))) break;
             int outer = 0;
-            if ((st = device_solve_mixed(c, b, k > 0 ? g : nullptr, tol, maxit, nb, x, it.data(), rr.data(),
-                                         precond_kind, stc.data(), 0.9 * tol, &outer)))
+            if ((st = device_solve_mixed(c, b, x0, tol, maxit, nb, x, it.data(), rr.data(), precond_kind,
+                                         stc.data(), 0.9 * tol, &outer)))
                 break;
             for (int q = 0; q < nb && !st; ++q) {
                 const int a = q * nrun + k;
@@ -154,7 +176,8 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
                 status_out[a] = stc[q];
                 st = device_rcs(c, x + (size_t)q * N, &pols[3 * q], ctte, &th, &ph[a], 1, &sigma[a]);
             }
-            CK(cudaMemcpyAsync(g, x, (size_t)N * nb * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
+            if (g2 && k > 0) std::swap(g, g2);   // g2 <- x_{k-1} in this angle's frame
+            CK(cudaMemcpyAsync(g, x, nbytes_col * nb, cudaMemcpyDeviceToDevice, c->stream));
             std::copy(dirs.begin(), dirs.begin() + 3 * nb, prev.begin());
         }
         return st;

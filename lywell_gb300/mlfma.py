@@ -393,7 +393,8 @@ class MLFMA:
         """Monostatic sweep (gen_rcs_monostatica).  Returns dict(phi, sigma_db, iters, status).
         mode 0: the reference's warm-started sequential sweep; 1: batched FP64 CGS;
         2: batched mixed precision; 3: batched mixed precision, each block
-        column sweeping a contiguous run of angles with mode 0's warm starts."""
+        column sweeping a contiguous run of angles with mode 0's warm starts;
+        4: as 3, starts extrapolated from each column's two previous angles."""
         if isinstance(precond, str):
             precond = PRECOND[precond]
         ph = None if phis is None else np.ascontiguousarray(phis, dtype=np.float64)

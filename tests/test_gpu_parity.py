@@ -248,7 +248,8 @@ def test_monostatic_batched_modes(ico3):
     # mode 3, block 5: runs of 3 angles (the last column has none), a ragged
     # last block; warm-started columns
     b3 = m.monostatic(12, pol="HH", errmax=1e-6, maxit=3000, mode=3, block=5)
-    for out in (b1, b2, b3):
+    b4 = m.monostatic(12, pol="HH", errmax=1e-6, maxit=3000, mode=4, block=5)
+    for out in (b1, b2, b3, b4):
         assert all(s == "converged" for s in out["status"])
         assert np.abs(out["sigma_db"] - ref["sigma_db"]).max() < 0.01
     # the warm-started angles (the 2nd and 3rd of every run) take fewer
