@@ -106,9 +106,27 @@ __global__ void __launch_bounds__(256) k32_near_warp(int N, int nrhs, int ld, in
     const int n = perm[pos];
     float tr = 0.f, ti = 0.f;
     {
+        // four entries per lane in flight: each is a chain of two dependent
+        // loads (the column's sorted position, then x), so unrolling is what
+        // hides their latency
+        constexpr int G = 32 / NR;
         const float2* xc = xs + c0 + r;
         const int q1 = ia[n + 1];
-        for (int q = ia[n] + g; q < q1; q += 32 / NR) {
+        int q = ia[n] + g;
+        for (; q + 3 * G < q1; q += 4 * G) {
+            float2 z[4], v[4];
+            int j[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) { z[u] = Z[q + u * G]; j[u] = jas[q + u * G]; }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = live ? xc[(size_t)j[u] * nrhs] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                tr = fmaf(z[u].x, v[u].x, tr); tr = fmaf(-z[u].y, v[u].y, tr);
+                ti = fmaf(z[u].x, v[u].y, ti); ti = fmaf(z[u].y, v[u].x, ti);
+            }
+        }
+        for (; q < q1; q += G) {
             const float2 z = Z[q];
             const float2 v = live ? xc[(size_t)jas[q] * nrhs] : make_float2(0.f, 0.f);
             tr = fmaf(z.x, v.x, tr); tr = fmaf(-z.y, v.y, tr);
@@ -161,7 +179,22 @@ __global__ void __launch_bounds__(128) k32_agg_warp(int K2, int nrhs, const int*
         float ax[NR], ay[NR];
 #pragma unroll
         for (int u = 0; u < NR; ++u) ax[u] = ay[u] = 0.f;
-        for (int t = j0; t < j1; ++t) {
+        int t = j0;
+        for (; t + 1 < j1; t += 2) {   // two pattern rows in flight
+            const float2 a0 = R[(size_t)t * K2 + k], a1 = R[(size_t)(t + 1) * K2 + k];
+            const float2* xv = xs + (size_t)t * nrhs + c0;
+#pragma unroll
+            for (int u = 0; u < NR; ++u) {
+                if (c0 + u < nrhs) {
+                    const float2 w = xv[u], w1 = xv[nrhs + u];
+                    ax[u] = fmaf(a0.x, w.x, ax[u]); ax[u] = fmaf(-a0.y, w.y, ax[u]);
+                    ay[u] = fmaf(a0.x, w.y, ay[u]); ay[u] = fmaf(a0.y, w.x, ay[u]);
+                    ax[u] = fmaf(a1.x, w1.x, ax[u]); ax[u] = fmaf(-a1.y, w1.y, ax[u]);
+                    ay[u] = fmaf(a1.x, w1.y, ay[u]); ay[u] = fmaf(a1.y, w1.x, ay[u]);
+                }
+            }
+        }
+        for (; t < j1; ++t) {
             const float2 a = R[(size_t)t * K2 + k];
             const float2* xv = xs + (size_t)t * nrhs + c0;
 #pragma unroll
