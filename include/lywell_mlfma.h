@@ -209,8 +209,10 @@ int mlf_set_basis_precision(mlf_ctx* ctx, int bits);
  * thread per sample for that many consecutive boxes over the merged list of
  * their far boxes, each source value read once for all of them; 1 = one box
  * at a time; 0 (the default) = 2 for one column, 4 for blocks of columns.
- * The same sums in another order.  No counterpart in the reference. */
-int mlf_set_translation_group(mlf_ctx* ctx, int boxes);
+ * cols = columns per thread with grouped boxes (1, 2 or 4; 0, the default:
+ * 2 with 4 boxes, else 4).  The same sums in another order.  No counterpart
+ * in the reference. */
+int mlf_set_translation_group(mlf_ctx* ctx, int boxes, int cols);
 
 /* Phase times (ms) of the last mixed-precision solve run while profiling was
  * on (mlf_set_profiling): out4 = {preconditioner, FP32 operator,

@@ -39,7 +39,7 @@ SIGNATURES = {
     "mlf_set_gmres_restart": (C.c_int, [vp, C.c_int]),
     "mlf_set_gs_passes": (C.c_int, [vp, C.c_int]),
     "mlf_set_basis_precision": (C.c_int, [vp, C.c_int]),
-    "mlf_set_translation_group": (C.c_int, [vp, C.c_int]),
+    "mlf_set_translation_group": (C.c_int, [vp, C.c_int, C.c_int]),
     "mlf_solve_times": (C.c_int, [vp, vp]),
     "mlf_precond_apply32": (C.c_int, [vp, vp, vp, C.c_int]),
     "mlf_autotune_block": (C.c_int, [vp, vp, C.c_int, vp, vp, vp, vp]),

@@ -120,6 +120,7 @@ struct Ctx {
     int gmres_m = 0;                  // restart length of the mixed-precision GMRES cycles (0: automatic)
     int gs_passes = 1;                // classical Gram-Schmidt passes per Arnoldi step (1 or 2)
     int tr_group = 0;                 // FP32 translation: boxes per thread (1, 2, 4; 0: 2 for one column, else 4)
+    int tr_cols = 0;                  // ... and columns per thread for grouped boxes (1, 2, 4; 0: 2 with 4 boxes, else 4)
     int basis_bits = 32;              // Krylov basis storage of the mixed solve: 32 (FP32) or 16 (FP16)
     Mixed32 m32;
     cudaStream_t stream = nullptr;

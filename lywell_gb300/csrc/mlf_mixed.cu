@@ -403,12 +403,13 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
         if (G > 1 && m.grp[G / 4].ptr) {
             // box groups: at most 8 sums of each box's two polarisations per thread
             const Mixed32::Lv::Grp& gl = m.grp[G / 4];
-            const int ng = (L.nb + G - 1) / G, nrg = std::min(nr, G == 4 ? 2 : 4);
+            const int nrg = std::min(nr, c->tr_cols ? c->tr_cols : (G == 4 ? 2 : 4));
+            const int ng = (L.nb + G - 1) / G;
             const dim3 gg(ng * nch, (nrhs + nrg - 1) / nrg);
 #define TGRP(NR_, G_) k32_translate_grp<NR_, G_><<<gg, bd, 0, s>>>(L.K, L.nb, nrhs, nch, gl.ptr, gl.src, gl.tid, \
                                                                   m.T, m.wq, m.C, m.B)
             if (G == 4) {
-                if (nrg == 1) TGRP(1, 4); else TGRP(2, 4);
+                if (nrg == 1) TGRP(1, 4); else if (nrg == 2) TGRP(2, 4); else TGRP(4, 4);
             } else {
                 if (nrg == 1) TGRP(1, 2); else if (nrg == 2) TGRP(2, 2); else TGRP(4, 2);
             }
@@ -1027,9 +1028,11 @@ int mlf_set_gs_passes(mlf_ctx* h, int passes) {
     return MLF_OK;
 }
 
-int mlf_set_translation_group(mlf_ctx* h, int boxes) {
-    if (!h || (boxes != 0 && boxes != 1 && boxes != 2 && boxes != 4)) return MLF_E_ARG;
+int mlf_set_translation_group(mlf_ctx* h, int boxes, int cols) {
+    if (!h || (boxes != 0 && boxes != 1 && boxes != 2 && boxes != 4) || (cols != 0 && cols != 1 && cols != 2 && cols != 4))
+        return MLF_E_ARG;
     h->c.tr_group = boxes;
+    h->c.tr_cols = cols;
     return MLF_OK;
 }
 

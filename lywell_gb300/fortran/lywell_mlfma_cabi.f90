@@ -190,10 +190,10 @@ module lywell_mlfma_cabi
             integer(c_int), value :: bits
         end function
 
-        integer(c_int) function mlf_set_translation_group(ctx, boxes) bind(C)
+        integer(c_int) function mlf_set_translation_group(ctx, boxes, cols) bind(C)
             import :: c_int, c_ptr
             type(c_ptr), value :: ctx
-            integer(c_int), value :: boxes
+            integer(c_int), value :: boxes, cols
         end function
     end interface
 

@@ -342,11 +342,12 @@ class MLFMA:
         """Krylov basis storage of the mixed solve: 32 (FP32) or 16 (FP16)."""
         _check(load().mlf_set_basis_precision(self._h, int(bits)), self._h)
 
-    def set_translation_group(self, boxes: int = 0):
+    def set_translation_group(self, boxes: int = 0, cols: int = 0):
         """FP32 translation over the merged far lists of 2 or 4 consecutive
         boxes per thread, 1 box at a time, or 0 (the default): 2 for one
-        column, 4 for blocks."""
-        _check(load().mlf_set_translation_group(self._h, int(boxes)), self._h)
+        column, 4 for blocks; cols = columns per thread with grouped boxes
+        (0: automatic)."""
+        _check(load().mlf_set_translation_group(self._h, int(boxes), int(cols)), self._h)
 
     def matvec32(self, x):
         x = np.asarray(x, dtype=np.complex128)

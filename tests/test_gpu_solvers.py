@@ -240,16 +240,16 @@ def test_fp16_basis_meets_fp64_test_and_rcs(ico4, nrhs):
         assert np.abs(s_ref - s_mix).max() < 0.1
 
 
-@pytest.mark.parametrize("boxes", [2, 4])
+@pytest.mark.parametrize("boxes,cols", [(2, 0), (4, 0), (4, 4)])
 @pytest.mark.parametrize("nrhs", [1, 2, 3, 8, 11])
-def test_translation_groups_match_per_box(ico4, nrhs, boxes):
+def test_translation_groups_match_per_box(ico4, nrhs, boxes, cols):
     """FP32 translation by groups of consecutive boxes over their merged far
     lists against one box at a time: the same sums in another order, 1e-6."""
     _, m, _ = ico4
     rng = np.random.default_rng(90 + nrhs)
     X = rng.standard_normal((m.N, nrhs)) + 1j * rng.standard_normal((m.N, nrhs))
     try:
-        m.set_translation_group(boxes)
+        m.set_translation_group(boxes, cols)
         Yg = m.matvec32(X).reshape(m.N, nrhs)
         m.set_translation_group(1)
         Yb = m.matvec32(X).reshape(m.N, nrhs)
