@@ -12,7 +12,7 @@
 // of right-preconditioned GMRES(m) solves A d = r with an FP32 inner loop
 // (operator, preconditioner, Krylov basis and Gram-Schmidt in float) until its
 // residual estimate drops below inner_tol ||b|| or m steps; x += M^-1 V y in
-// FP64; stop when the FP64 residual ||b - A64 x|| < tol ||b||.  The FP64 residual is the judge, so the result
+// FP64; stop when the FP64 residual ||b - A64 x|| < tol ||b||.  The FP64 residual decides, so the result
 // meets the same stopping test as the plain FP64 solve.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -478,7 +478,8 @@ void mixed_free(Ctx* c) {
 
 // ---------------------------------------------------------------------------
 // GMRES-IR: FP64 iterative refinement, each step one right-preconditioned
-// GMRES(m) cycle on the FP32 operator (classical Gram-Schmidt applied twice).
+// GMRES(m) cycle on the FP32 operator (classical Gram-Schmidt, one pass by
+// default, two with mlf_set_gs_passes).
 // The reference's CGS (kept as mode 0) is too erratic to tolerate an
 // operator perturbed at the 1e-7 level; GMRES minimises the residual over
 // the Krylov space and cannot diverge.

@@ -9,7 +9,7 @@ pattern and apply cost as M1, still linear.  Training, inference and
 gradients run in the library's own CUDA kernels (mlf_mlp_*); tokens and the
 2-ring targets come from mlf_lp_tokens; gamma is chosen from CGS traces on
 the training bodies; solve_with_fallback switches to ILU0 when the learned
-solve has not converged within the unpreconditioned iteration count, judged
+solve has not converged within the unpreconditioned iteration count, measured
 by the true FP64 MLFMA residual.  Device buffers are torch CUDA tensors
 (memory only).  No counterpart in the reference.
 """
@@ -181,7 +181,7 @@ def train(contexts, excitations, steps=4000, batch=8192, lr=1e-3, seed=0, gammas
 
 def solve_with_fallback(m, b, lp: LearnedPreconditioner, plain_iters: int, errmax=1e-4, maxit=5000,
                         install_first=True):
-    """CGS with the learned preconditioner, judged by the true FP64 MLFMA
+    """CGS with the learned preconditioner, checked against the true FP64 MLFMA
     residual; if it has not converged within `plain_iters` iterations (the
     count of the solve without a preconditioner), solve again with ILU0, the
     reference's preconditioner.  install_first=False when lp is already
