@@ -225,7 +225,7 @@ int mlf_solve_times(mlf_ctx* ctx, double* out4);
  * and 64 columns, and the warp engine -- and returns the smallest block whose
  * time per right-hand side is within 5 % of the best, with its tile width (0
  * for a single column or the warp engine) and engine (best_engine, optional:
- * 1 tensor cores, 0 FP32 FMA, 2 warp engine); both are kept for later
+ * 1 tensor cores, 0 FP32 FMA, 2 or 3 warp engine); both are kept for later
  * operator and preconditioner calls.
  * per_rhs_ms (optional, ncand) receives the best time per right-hand side of
  * each candidate.  No counterpart in the reference. */
@@ -238,7 +238,9 @@ int mlf_autotune_block(mlf_ctx* ctx, const int* candidates, int ncand, int* best
  *       3xTF32 split, within a few 1e-6 of FP32),
  *   0 = box-block GEMMs on FP32 FMAs,
  *   2 = warp engine: one warp per basis over 8 columns, nothing padded (for
- *       leaf boxes of a few tens of bases),
+ *       leaf boxes of a few tens of bases), the leaf receive by one CTA per
+ *       box with the box's fields in shared memory,
+ *   3 = warp engine with the leaf receive also one warp per basis,
  *  -1 = by the mean leaf-box size: 2 below 48 bases per box, else 1 (the
  *       default).
  * cols = box-block tile width 8, 32 or 64 (0: by the block's width).

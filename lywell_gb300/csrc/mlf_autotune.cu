@@ -58,12 +58,13 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
         const int B = cand[q];
         double tq = 1e300;
         const int widths[3] = {8, 32, 64};
-        for (int var = 0; var < 7 && !st; ++var) {
-            // tensor-core box blocks, FP32 FMA box blocks (three widths each), then the warp engine
-            const int wv = var % 3, eng = var == 6 ? 2 : 1 - var / 3;
+        for (int var = 0; var < 8 && !st; ++var) {
+            // tensor-core box blocks, FP32 FMA box blocks (three widths each), then the warp
+            // engine with its per-box and its per-basis receive
+            const int wv = var % 3, eng = var >= 6 ? var - 4 : 1 - var / 3;
             if (B == 1 && var) break;   // one column uses the CSR kernels
-            if (eng != 2 && wv > 0 && widths[wv - 1] >= B) continue;   // a narrower tile already covers the block
-            c->blk_cols = eng == 2 ? 0 : widths[wv];
+            if (eng < 2 && wv > 0 && widths[wv - 1] >= B) continue;   // a narrower tile already covers the block
+            c->blk_cols = eng >= 2 ? 0 : widths[wv];
             c->blk_engine = eng;
             for (int w = 0; w < 2 && !st; ++w) st = device_matvec32(c, x, y, B, c->N, s);
             if (st) break;
@@ -75,7 +76,7 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             const double t = ms / 3.0 / B;
-            if (t < tq) { tq = t; colsel[q] = eng == 2 ? 0 : widths[wv]; engsel[q] = eng; }
+            if (t < tq) { tq = t; colsel[q] = eng >= 2 ? 0 : widths[wv]; engsel[q] = eng; }
         }
         per[q] = {tq, B};
         if (per_rhs_ms) per_rhs_ms[q] = (float)tq;
@@ -105,7 +106,7 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
 using namespace mlf;
 
 extern "C" int mlf_set_block_engine(mlf_ctx* h, int engine, int cols) {
-    if (!h || engine < -1 || engine > 2 || (cols != 0 && cols != 8 && cols != 32 && cols != 64)) return MLF_E_ARG;
+    if (!h || engine < -1 || engine > 3 || (cols != 0 && cols != 8 && cols != 32 && cols != 64)) return MLF_E_ARG;
     h->c.blk_engine = engine;
     h->c.blk_cols = cols;
     return MLF_OK;

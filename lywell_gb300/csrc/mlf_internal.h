@@ -146,7 +146,8 @@ struct Ctx {
     int blk_ok = 0, nblk_tiles = 0;
     int blk_cols = 0;                 // box-block tile width: 0 = by nrhs, else 8, 32 or 64 (autotuner)
     int blk_engine = -1;              // multi-column engine: 0 box-block FP32 FMA, 1 box-block mma.sync
-                                      // 3xTF32, 2 warp per basis; -1 by mean leaf-box size (autotuner)
+                                      // 3xTF32, 2 warp per basis with a per-box receive, 3 warp per basis
+                                      // throughout; -1 by mean leaf-box size (autotuner)
     int* djas = nullptr;              // near CSR columns as box-sorted positions (warp engine)
     float2* dZblk = nullptr;
     long long* dblk_off = nullptr;

@@ -82,6 +82,70 @@ template <> struct Log2<2> { static constexpr int v = 1; };
 template <> struct Log2<4> { static constexpr int v = 2; };
 template <> struct Log2<8> { static constexpr int v = 3; };
 
+// Near-field sum of CSR row n for column c0 + r over the warp's entry slots
+// (lane = slot g x column r), returned summed over the slots in every lane.
+// Four entries per lane in flight: each is a chain of two dependent loads
+// (the column's sorted position, then x), so unrolling is what hides their
+// latency.
+template <int NR>
+__device__ __forceinline__ void near_row(int n, int g, int r, bool live, int c0, int nrhs,
+                                         const int* __restrict__ ia, const int* __restrict__ jas,
+                                         const float2* __restrict__ Z, const float2* __restrict__ xs, float& tr,
+                                         float& ti) {
+    constexpr int G = 32 / NR;
+    const float2* xc = xs + c0 + r;
+    const int q1 = ia[n + 1];
+    int q = ia[n] + g;
+    tr = 0.f;
+    ti = 0.f;
+    for (; q + 3 * G < q1; q += 4 * G) {
+        float2 z[4], v[4];
+        int j[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { z[u] = Z[q + u * G]; j[u] = jas[q + u * G]; }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = live ? xc[(size_t)j[u] * nrhs] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            tr = fmaf(z[u].x, v[u].x, tr); tr = fmaf(-z[u].y, v[u].y, tr);
+            ti = fmaf(z[u].x, v[u].y, ti); ti = fmaf(z[u].y, v[u].x, ti);
+        }
+    }
+    for (; q < q1; q += G) {
+        const float2 z = Z[q];
+        const float2 v = live ? xc[(size_t)jas[q] * nrhs] : make_float2(0.f, 0.f);
+        tr = fmaf(z.x, v.x, tr); tr = fmaf(-z.y, v.y, tr);
+        ti = fmaf(z.x, v.y, ti); ti = fmaf(z.y, v.x, ti);
+    }
+    tr = slot_sum<NR>(tr);
+    ti = slot_sum<NR>(ti);
+}
+
+// Receive sum sum_k conj(R_n[k]) A(k, col) for columns c0 .. c0 + NR - 1,
+// A(:, u) at Ab + u * K2; lane r ends with column r's (Re, Im).
+template <int NR>
+__device__ __forceinline__ void recv_row(const float2* __restrict__ Rn, const float2* Ab, int K2, int lane, int r,
+                                         int ncol, float& sr, float& si) {
+    float v[2 * NR];   // Re, then Im, of sum conj(R) A for each column
+#pragma unroll
+    for (int u = 0; u < 2 * NR; ++u) v[u] = 0.f;
+    for (int k = lane; k < K2; k += 32) {
+        const float2 a = Rn[k];
+#pragma unroll
+        for (int u = 0; u < NR; ++u) {
+            if (u < ncol) {
+                const float2 w = Ab[(size_t)u * K2 + k];
+                v[u] = fmaf(a.x, w.x, v[u]); v[u] = fmaf(a.y, w.y, v[u]);
+                v[NR + u] = fmaf(a.x, w.y, v[NR + u]); v[NR + u] = fmaf(-a.y, w.x, v[NR + u]);
+            }
+        }
+    }
+    const float s = warp_split_sum<2 * NR>(v, lane);
+    constexpr int sh = 5 - (Log2<NR>::v + 1);
+    sr = __shfl_sync(0xffffffffu, s, r << sh);
+    si = __shfl_sync(0xffffffffu, s, (NR + r) << sh);
+}
+
 // For the bases in box-sorted order (one warp each) and columns
 // [c0, c0 + NR), c0 = blockIdx.y * NR:
 //   t(n, col) = sum_q Z[q] x(ja[q], col)                       (near CSR row n)
@@ -104,65 +168,53 @@ __global__ void __launch_bounds__(256) k32_near_warp(int N, int nrhs, int ld, in
     const int g = lane / NR, r = lane % NR;   // entry slot, column
     const bool live = c0 + r < nrhs;
     const int n = perm[pos];
-    float tr = 0.f, ti = 0.f;
-    {
-        // four entries per lane in flight: each is a chain of two dependent
-        // loads (the column's sorted position, then x), so unrolling is what
-        // hides their latency
-        constexpr int G = 32 / NR;
-        const float2* xc = xs + c0 + r;
-        const int q1 = ia[n + 1];
-        int q = ia[n] + g;
-        for (; q + 3 * G < q1; q += 4 * G) {
-            float2 z[4], v[4];
-            int j[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) { z[u] = Z[q + u * G]; j[u] = jas[q + u * G]; }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) v[u] = live ? xc[(size_t)j[u] * nrhs] : make_float2(0.f, 0.f);
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                tr = fmaf(z[u].x, v[u].x, tr); tr = fmaf(-z[u].y, v[u].y, tr);
-                ti = fmaf(z[u].x, v[u].y, ti); ti = fmaf(z[u].y, v[u].x, ti);
-            }
-        }
-        for (; q < q1; q += G) {
-            const float2 z = Z[q];
-            const float2 v = live ? xc[(size_t)jas[q] * nrhs] : make_float2(0.f, 0.f);
-            tr = fmaf(z.x, v.x, tr); tr = fmaf(-z.y, v.y, tr);
-            ti = fmaf(z.x, v.y, ti); ti = fmaf(z.y, v.x, ti);
-        }
-        tr = slot_sum<NR>(tr);
-        ti = slot_sum<NR>(ti);
-    }
+    float tr, ti;
+    near_row<NR>(n, g, r, live, c0, nrhs, ia, jas, Z, xs, tr, ti);
     if (OUT == 0 && R) {
         const int b = box_of_sorted[pos];
-        const float2* Rn = R + (size_t)pos * K2;
-        const float2* Ab = A + ((size_t)b * nrhs + c0) * K2;
-        float v[2 * NR];   // Re, then Im, of sum conj(R) A for each column
-#pragma unroll
-        for (int u = 0; u < 2 * NR; ++u) v[u] = 0.f;
-        for (int k = lane; k < K2; k += 32) {
-            const float2 a = Rn[k];
-#pragma unroll
-            for (int u = 0; u < NR; ++u) {
-                if (c0 + u < nrhs) {
-                    const float2 w = Ab[(size_t)u * K2 + k];
-                    v[u] = fmaf(a.x, w.x, v[u]); v[u] = fmaf(a.y, w.y, v[u]);
-                    v[NR + u] = fmaf(a.x, w.y, v[NR + u]); v[NR + u] = fmaf(-a.y, w.x, v[NR + u]);
-                }
-            }
-        }
-        const float s = warp_split_sum<2 * NR>(v, lane);
-        constexpr int sh = 5 - (Log2<NR>::v + 1);
-        const float sr = __shfl_sync(0xffffffffu, s, r << sh);
-        const float si = __shfl_sync(0xffffffffu, s, (NR + r) << sh);
+        float sr, si;
+        recv_row<NR>(R + (size_t)pos * K2, A + ((size_t)b * nrhs + c0) * K2, K2, lane, r, nrhs - c0, sr, si);
         tr = fmaf(-facy, si, tr);
         ti = fmaf(facy, sr, ti);
     }
     if (g == 0 && live) {
         if (OUT == 0) y[(size_t)(c0 + r) * ld + n] = make_double2((double)tr, (double)ti);
         else out32[(size_t)(c0 + r) * ld + n] = make_float2(tr, ti);
+    }
+}
+
+// The same near field + receive with one CTA per leaf box: the box's A
+// fields for the NR columns are staged once in shared memory, and the CTA's
+// warps walk the box's bases.  The sums are the per-basis kernel's, in the
+// same order.
+template <int NR>
+__global__ void __launch_bounds__(128) k32_nearrecv_box(int nrhs, int ld, int K2, float facy,
+                                                        const int* __restrict__ box_ptr,
+                                                        const int* __restrict__ perm, const float2* __restrict__ R,
+                                                        const float2* __restrict__ A, const int* __restrict__ ia,
+                                                        const int* __restrict__ jas, const float2* __restrict__ Z,
+                                                        const float2* __restrict__ xs, double2* __restrict__ y) {
+    extern __shared__ __align__(16) unsigned char box_smem[];
+    float2* As = reinterpret_cast<float2*>(box_smem);   // NR x K2
+    const int b = blockIdx.x, c0 = blockIdx.y * NR;
+    const float2* Ab = A + ((size_t)b * nrhs + c0) * K2;
+    for (int i = threadIdx.x; i < NR * K2; i += blockDim.x) {
+        const int u = i / K2;
+        As[i] = c0 + u < nrhs ? Ab[i] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int g = lane / NR, r = lane % NR;
+    const bool live = c0 + r < nrhs;
+    const int j1 = box_ptr[b + 1];
+    for (int pos = box_ptr[b] + (threadIdx.x >> 5); pos < j1; pos += nw) {   // warp-uniform
+        const int n = perm[pos];
+        float tr, ti, sr, si;
+        near_row<NR>(n, g, r, live, c0, nrhs, ia, jas, Z, xs, tr, ti);
+        recv_row<NR>(R + (size_t)pos * K2, As, K2, lane, r, nrhs - c0, sr, si);
+        tr = fmaf(-facy, si, tr);
+        ti = fmaf(facy, sr, ti);
+        if (g == 0 && live) y[(size_t)(c0 + r) * ld + n] = make_double2((double)tr, (double)ti);
     }
 }
 
@@ -296,10 +348,17 @@ int device_recv_near_warp32(Ctx* c, const float2* R, int K, const float2* A, flo
     int st;
     if ((st = warp_setup(c))) return st;
     const unsigned grid = (unsigned)(((size_t)c->N * 32 + 255) / 256);
+    const int nb = (int)c->box_ptr.size() - 1;
     nr_dispatch(nrhs, [&](auto nr) {
         constexpr int NR = decltype(nr)::value;
-        k32_near_warp<NR, 0><<<dim3(grid, (nrhs + NR - 1) / NR), 256, 0, s>>>(
-            c->N, nrhs, ld, 2 * K, facy, c->dperm, c->dbox_of_sorted, R, A, c->dia, c->djas, c->dZ, xs, y, nullptr);
+        const size_t smem = (size_t)NR * 2 * K * sizeof(float2);
+        if (blk_engine_of(c) == 2 && smem <= 48 * 1024)   // the box's A fields in shared memory
+            k32_nearrecv_box<NR><<<dim3(nb, (nrhs + NR - 1) / NR), 128, smem, s>>>(
+                nrhs, ld, 2 * K, facy, c->dbox_ptr, c->dperm, R, A, c->dia, c->djas, c->dZ, xs, y);
+        else
+            k32_near_warp<NR, 0><<<dim3(grid, (nrhs + NR - 1) / NR), 256, 0, s>>>(
+                c->N, nrhs, ld, 2 * K, facy, c->dperm, c->dbox_of_sorted, R, A, c->dia, c->djas, c->dZ, xs, y,
+                nullptr);
     });
     return cuda_ok(c, cudaGetLastError(), "near + receive (warp)") ? MLF_OK : MLF_E_CUDA;
 }

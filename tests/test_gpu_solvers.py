@@ -115,7 +115,7 @@ def test_mixed_multi_rhs(ico4, engine):
         assert r < 1e-4
 
 
-@pytest.mark.parametrize("engine", [1, 0, 2])
+@pytest.mark.parametrize("engine", [1, 0, 2, 3])
 @pytest.mark.parametrize("nrhs", [2, 3, 5, 20, 40, 70])
 def test_fp32_multi_rhs_columns(ico4, nrhs, engine):
     """The batched FP32 operator (near field, aggregation and receive as dense
@@ -203,7 +203,8 @@ def test_autotune_block_covers_all_engines(ico4):
     _, m, _ = ico4
     res = m.autotune_block((4, 8, 16))
     assert res["block"] in (4, 8, 16)
-    assert res["engine"] in ("FP32 FMA", "tensor cores (3xTF32 mma.sync)", "warp per basis")
+    assert res["engine"] in ("FP32 FMA", "tensor cores (3xTF32 mma.sync)", "warp per basis",
+                             "warp per basis, per-basis receive")
     assert all(t > 0 for t in res["per_rhs_ms"].values())
     rng = np.random.default_rng(77)
     X = rng.standard_normal((m.N, res["block"])) + 1j * rng.standard_normal((m.N, res["block"]))
