@@ -77,6 +77,29 @@ def test_rwg_builder_shared_node_topology(lib):
         assert not np.any(a.e_po[:, s] == a.e_p[:, 0]) and not np.any(a.e_po[:, s] == a.e_p[:, 1])
 
 
+def test_rwg_builder_open_and_degenerate_meshes(lib):
+    """The one-call builder sizes its outputs by the bounds (P <= 3T, N <= 3T/2)
+    and trims them: a lone triangle has no edge, an open strip's boundary
+    sides make none, and a side shared by three triangles pairs the first two
+    listings (the reference's first-occurrence rule) -- as the oracle does."""
+    from lywell_gb300 import RWG
+    from oracle.rwg import RWG as ORWG
+    one = np.array([[[0, 0, 0], [1, 0, 0], [0, 1, 0]]], float)
+    a = RWG(one)
+    assert (a.N, a.P) == (0, 3) and a.e_p.shape == (0, 2) and a.p_coord.shape == (3, 3)
+    fan = np.array([[[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 0, 0], [1, 0, 0], [0, -1, 0]],
+                    [[0, 0, 0], [1, 0, 0], [0, 0, 1]]], float)
+    strip = np.array([[[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[1, 0, 0], [1, 1, 0], [0, 1, 0]],
+                      [[1, 0, 0], [2, 0, 0], [1, 1, 0]]], float)
+    for t in (fan, strip):
+        a, b = RWG(t), ORWG(t)
+        assert a.N == b.N
+        for k in ("e_t", "e_po", "e_long", "e_centro"):
+            assert np.array_equal(getattr(a, k), getattr(b, k)), k
+        assert np.array_equal(a.p_coord[a.e_p], b.p_coord[b.e_p])
+    assert RWG(fan).e_t.tolist() == [[0, 1]]
+
+
 def test_init_without_gpu_reports_no_device(lib):
     from conftest import has_gpu
     if has_gpu():
