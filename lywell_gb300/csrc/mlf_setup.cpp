@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <unordered_map>
 
 #include "mlf_internal.h"
@@ -380,28 +381,32 @@ struct Builder {
         static const int sz[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
         const double half = side / 2., quarter = side / 4.;
         Level& ch = c->lv[level + 1];
-        std::vector<int> rest;
-        rest.reserve(bases.size());
+        double cc[8][3], lo[8][3], hi[8][3];
         for (int i = 0; i < 8; ++i) {
-            double cc[3];
-            cc[0] = sx[i] < 0 ? centre[0] - quarter : centre[0] + quarter;
-            cc[1] = sy[i] < 0 ? centre[1] - quarter : centre[1] + quarter;
-            cc[2] = sz[i] < 0 ? centre[2] - quarter : centre[2] + quarter;
+            cc[i][0] = sx[i] < 0 ? centre[0] - quarter : centre[0] + quarter;
+            cc[i][1] = sy[i] < 0 ? centre[1] - quarter : centre[1] + quarter;
+            cc[i][2] = sz[i] < 0 ? centre[2] - quarter : centre[2] + quarter;
             const double q = half / 2.;
-            const double xmax = cc[0] + q, xmin = cc[0] - q, ymax = cc[1] + q, ymin = cc[1] - q;
-            const double zmax = cc[2] + q, zmin = cc[2] - q;
-            std::vector<int> found;
-            rest.clear();
-            for (int b : bases) {
-                const double* e = &c->e_centro[3 * (size_t)b];
-                if (e[0] <= xmax && e[0] >= xmin && e[1] <= ymax && e[1] >= ymin && e[2] <= zmax &&
-                    e[2] >= zmin)
-                    found.push_back(b);
-                else
-                    rest.push_back(b);
+            for (int d = 0; d < 3; ++d) { hi[i][d] = cc[i][d] + q; lo[i][d] = cc[i][d] - q; }
+        }
+        // one pass: each basis to the first child (in the fixed order) whose
+        // closed box holds it -- what filtering child by child gives -- in
+        // the order of `bases`
+        std::array<std::vector<int>, 8> kids;
+        for (int b : bases) {
+            const double* e = &c->e_centro[3 * (size_t)b];
+            for (int i = 0; i < 8; ++i) {
+                if (e[0] <= hi[i][0] && e[0] >= lo[i][0] && e[1] <= hi[i][1] && e[1] >= lo[i][1] &&
+                    e[2] <= hi[i][2] && e[2] >= lo[i][2]) {
+                    kids[i].push_back(b);
+                    break;
+                }
             }
+        }
+        for (int i = 0; i < 8; ++i) {
+            std::vector<int>& found = kids[i];
             if (found.empty()) continue;
-            ch.centre.insert(ch.centre.end(), cc, cc + 3);
+            ch.centre.insert(ch.centre.end(), cc[i], cc[i] + 3);
             ch.parent.push_back(cur_parent[level]);
             ch.octant.push_back(i);
             ch.nb++;
@@ -411,13 +416,31 @@ struct Builder {
             }
             const int saved = cur_parent[level + 1];
             cur_parent[level + 1] = ch.nb - 1;
-            split(cc, half, found, level + 1);
+            split(cc[i], half, found, level + 1);
             cur_parent[level + 1] = saved;
-            bases.swap(rest);
         }
     }
     int cur_parent[33]{};
 };
+
+// f(i) for i in [0, n) on up to 16 host threads in contiguous ranges; the
+// calls must be independent
+template <class F>
+void parallel_for(int n, F f) {
+    const int nt = (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency()));
+    if (nt == 1 || n < 4096) {
+        for (int i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(nt);
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back([&, t] {
+            const int i0 = (int)((long long)n * t / nt), i1 = (int)((long long)n * (t + 1) / nt);
+            for (int i = i0; i < i1; ++i) f(i);
+        });
+    for (auto& x : th) x.join();
+}
 
 inline long long cell_key(int a, int b, int cc) {
     return ((long long)(a + 1) << 42) | ((long long)(b + 1) << 21) | (long long)(cc + 1);
@@ -530,11 +553,38 @@ int build_octree(Ctx* c) {
     for (int n = 3; n <= nl; ++n) {
         Level& L = c->lv[n];
         const Level& Lp = c->lv[n - 1];
+        // parent cells: a dense grid (2^(n-2) per axis) while it has at most
+        // 2^21 cells, else a hash map
+        const long long G = 1LL << (n - 2);
+        const bool dense = G * G * G <= (1LL << 21);
+        std::vector<int> pgrid;
         std::unordered_map<long long, int> pcell;
-        pcell.reserve(2 * (size_t)Lp.nb);
-        for (int b = 0; b < Lp.nb; ++b)
-            pcell[cell_key(cells[n - 1][3 * b], cells[n - 1][3 * b + 1], cells[n - 1][3 * b + 2])] = b;
-        std::unordered_map<long long, int> tid_of;
+        if (dense) {
+            pgrid.assign((size_t)(G * G * G), -1);
+            for (int b = 0; b < Lp.nb; ++b) {
+                const int* q = &cells[n - 1][3 * b];
+                if (q[0] >= 0 && q[0] < G && q[1] >= 0 && q[1] < G && q[2] >= 0 && q[2] < G)
+                    pgrid[(size_t)((q[0] * G + q[1]) * G + q[2])] = b;
+                else
+                    pcell[cell_key(q[0], q[1], q[2])] = b;   // outside the grid: kept in the map
+            }
+        } else {
+            pcell.reserve(2 * (size_t)Lp.nb);
+            for (int b = 0; b < Lp.nb; ++b)
+                pcell[cell_key(cells[n - 1][3 * b], cells[n - 1][3 * b + 1], cells[n - 1][3 * b + 2])] = b;
+        }
+        auto parent_at = [&](int x, int y, int z) -> int {
+            if (dense && x >= 0 && x < G && y >= 0 && y < G && z >= 0 && z < G)
+                return pgrid[(size_t)((x * G + y) * G + z)];
+            if (pcell.empty()) return -1;
+            auto it = pcell.find(cell_key(x, y, z));
+            return it == pcell.end() ? -1 : it->second;
+        };
+        // translation index by cell offset (children of the parent's neighbours
+        // lie within +-3 cells; numbered in order of first appearance)
+        constexpr int OFF = 8, SPAN = 2 * OFF + 1;
+        std::vector<int> tid_lut(SPAN * SPAN * SPAN, -1);
+        std::unordered_map<long long, int> tid_of;   // offsets beyond the table (not expected)
         L.far_ptr.assign(1, 0);
         L.far_src.clear();
         L.far_tid.clear();
@@ -544,16 +594,20 @@ int build_octree(Ctx* c) {
             const int ip = L.parent[i];
             cand.clear();
             const int* pc = &cells[n - 1][3 * ip];
+            // children of distinct parents are disjoint contiguous ranges, so
+            // ordering the ranges by their start orders the candidates
+            int nrg = 0;
+            std::array<int, 27> rg;
             for (int dx = -1; dx <= 1; ++dx)
                 for (int dy = -1; dy <= 1; ++dy)
                     for (int dz = -1; dz <= 1; ++dz) {
-                        auto it = pcell.find(cell_key(pc[0] + dx, pc[1] + dy, pc[2] + dz));
-                        if (it == pcell.end()) continue;
-                        for (int j = Lp.child_ptr[it->second]; j < Lp.child_ptr[it->second + 1]; ++j)
-                            cand.push_back(j);
+                        const int pb = parent_at(pc[0] + dx, pc[1] + dy, pc[2] + dz);
+                        if (pb >= 0 && Lp.child_ptr[pb + 1] > Lp.child_ptr[pb]) rg[nrg++] = pb;
                     }
-            std::sort(cand.begin(), cand.end());
-            const size_t near_start = c->near_bases.size();
+            std::sort(rg.begin(), rg.begin() + nrg,
+                      [&](int a, int b2) { return Lp.child_ptr[a] < Lp.child_ptr[b2]; });
+            for (int q = 0; q < nrg; ++q)
+                for (int j = Lp.child_ptr[rg[q]]; j < Lp.child_ptr[rg[q] + 1]; ++j) cand.push_back(j);
             for (int j : cand) {
                 const int jp = L.parent[j];
                 double rp[3], rh[3];
@@ -563,38 +617,65 @@ int build_octree(Ctx* c) {
                 for (int d = 0; d < 3; ++d) rh[d] = L.centre[3 * i + d] - L.centre[3 * j + d];
                 const double nh = std::sqrt(rh[0] * rh[0] + rh[1] * rh[1] + rh[2] * rh[2]);
                 if (nh >= (2 * L.side - tol)) {
-                    const long long k = cell_key(cells[n][3 * i] - cells[n][3 * j] + 8,
-                                                 cells[n][3 * i + 1] - cells[n][3 * j + 1] + 8,
-                                                 cells[n][3 * i + 2] - cells[n][3 * j + 2] + 8);
-                    auto it = tid_of.find(k);
-                    int tid;
-                    if (it == tid_of.end()) {
+                    const int ox_ = cells[n][3 * i] - cells[n][3 * j] + OFF,
+                              oy_ = cells[n][3 * i + 1] - cells[n][3 * j + 1] + OFF,
+                              oz_ = cells[n][3 * i + 2] - cells[n][3 * j + 2] + OFF;
+                    const bool in_lut = ox_ >= 0 && ox_ < SPAN && oy_ >= 0 && oy_ < SPAN && oz_ >= 0 && oz_ < SPAN;
+                    int* slot = in_lut ? &tid_lut[(ox_ * SPAN + oy_) * SPAN + oz_] : nullptr;
+                    int tid = -1;
+                    if (slot) {
+                        tid = *slot;
+                    } else {
+                        auto it = tid_of.find(cell_key(ox_, oy_, oz_));
+                        if (it != tid_of.end()) tid = it->second;
+                    }
+                    if (tid < 0) {
                         tid = (int)(L.rab.size() / 3);
                         if (tid >= 316) {
                             c->err = "more than 316 distinct translation vectors on a level";
                             return MLF_E_TABLE;
                         }
-                        tid_of.emplace(k, tid);
+                        if (slot) *slot = tid;
+                        else tid_of.emplace(cell_key(ox_, oy_, oz_), tid);
                         L.rab.insert(L.rab.end(), rh, rh + 3);
-                    } else {
-                        tid = it->second;
                     }
                     L.far_src.push_back(j);
                     L.far_tid.push_back(tid);
                 } else if (n == nl) {
                     c->nbox_list.push_back(j);
-                    c->near_bases.insert(c->near_bases.end(), c->box_bases.begin() + c->box_ptr[j],
-                                         c->box_bases.begin() + c->box_ptr[j + 1]);
                 }
             }
             L.far_ptr.push_back((int)L.far_src.size());
-            if (n == nl) {
-                std::sort(c->near_bases.begin() + near_start, c->near_bases.end());
-                c->near_ptr.push_back((int)c->near_bases.size());
-                c->nbox_ptr.push_back((int)c->nbox_list.size());
-            }
+            if (n == nl) c->nbox_ptr.push_back((int)c->nbox_list.size());
         }
         L.ntrans = (int)(L.rab.size() / 3);
+    }
+    // near bases of each leaf box: its near boxes' bases, ascending (boxes
+    // are independent: sized by a prefix sum, then filled and sorted in parallel)
+    {
+        const int nbl = c->lv[nl].nb;
+        c->near_ptr.assign(nbl + 1, 0);
+        for (int i = 0; i < nbl; ++i) {
+            long long cnt = 0;
+            for (int e = c->nbox_ptr[i]; e < c->nbox_ptr[i + 1]; ++e) {
+                const int j = c->nbox_list[e];
+                cnt += c->box_ptr[j + 1] - c->box_ptr[j];
+            }
+            if (c->near_ptr[i] + cnt > 2000000000LL) {
+                c->err = "near lists larger than 2^31 entries";
+                return MLF_E_ARG;
+            }
+            c->near_ptr[i + 1] = c->near_ptr[i] + (int)cnt;
+        }
+        c->near_bases.resize(c->near_ptr[nbl]);
+        parallel_for(nbl, [&](int i) {
+            int* out = c->near_bases.data() + c->near_ptr[i];
+            for (int e = c->nbox_ptr[i]; e < c->nbox_ptr[i + 1]; ++e) {
+                const int j = c->nbox_list[e];
+                out = std::copy(c->box_bases.begin() + c->box_ptr[j], c->box_bases.begin() + c->box_ptr[j + 1], out);
+            }
+            std::sort(c->near_bases.begin() + c->near_ptr[i], c->near_bases.begin() + c->near_ptr[i + 1]);
+        });
     }
     // near CSR rows in basis order (llenarZesparcida, modMLFMA.f90:1594-1634)
     // the CSR row pointers are int32 (the reference's integer(4) ia_MLFMA)
@@ -611,11 +692,11 @@ int build_octree(Ctx* c) {
     }
     c->nnz = c->ia[N];
     c->ja.resize(c->nnz);
-    for (int m = 0; m < N; ++m) {
+    parallel_for(N, [&](int m) {
         const int b = c->box_of[m];
         std::copy(c->near_bases.begin() + c->near_ptr[b], c->near_bases.begin() + c->near_ptr[b + 1],
                   c->ja.begin() + c->ia[m]);
-    }
+    });
     // interpolation tables and their transposes
     for (int n = 3; n < nl; ++n) {
         Level& L = c->lv[n];
@@ -822,11 +903,11 @@ int build_fmm(Ctx* c) {
     }
     c->nnz = c->ia[N];
     c->ja.resize(c->nnz);
-    for (int m = 0; m < N; ++m) {
+    parallel_for(N, [&](int m) {
         const int b = c->box_of[m];
         std::copy(c->near_bases.begin() + c->near_ptr[b], c->near_bases.begin() + c->near_ptr[b + 1],
                   c->ja.begin() + c->ia[m]);
-    }
+    });
     return MLF_OK;
 }
 
