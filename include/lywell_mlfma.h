@@ -140,6 +140,24 @@ int mlf_near_csr(mlf_ctx* ctx, long long* nnz, float* a, int* ja, int* ia);
  * (modIterativo.f90:1805-1976). */
 int mlf_ilu0(mlf_ctx* ctx, int* ierr_row);
 
+/* ILU(0) of a host CSR matrix with the reference routine's own arguments:
+ * ilu0C(n, a, ja, ia, alu, jlu, ju, iw, ierr) (modIterativo.f90:1805-1976),
+ * the work array iw kept inside.  a: nnz complex(4) values (interleaved
+ * floats); ja, ia: 1-based CSR, columns strictly ascending in each row.
+ * Outputs in ilu0C's MSR layout: alu (nnz+1 complex(4)), jlu (nnz+1), ju (n).
+ * *ierr = 0, or k > 0 when a zero pivot was met at row k (a row without a
+ * diagonal entry counts as one).  A malformed CSR (ia(1) != 1, ia
+ * decreasing, a column outside 1..n or out of order) returns MLF_E_ARG and
+ * names the row in mlf_last_error(NULL); the reference checks none of this.
+ * Host code only: no CUDA device is needed. */
+int mlf_ilu0_csr(int n, const float* a, const int* ja, const int* ia, float* alu, int* jlu, int* ju, int* ierr);
+
+/* Overwrite the context's complex(4) near-field values (nnz, in the order of
+ * mlf_near_csr), as the reference's host may overwrite its public
+ * Zesparcida_MLFMA (modMLFMA.f90:12) before crear_precond.  ILU and
+ * neighbourhood preconditioners built earlier are dropped: build them again. */
+int mlf_set_near_values(mlf_ctx* ctx, const float* a);
+
 /* ILUT (dual threshold) of the near-field block, the reference's default
  * preconditioner: lfil = ceiling(0.01 fill_in_prc N), drop tolerance
  * droptol (ilut.fillin / ilut.droptol; defaults 5 and 1e-3).  The factors
@@ -170,6 +188,14 @@ int mlf_ilu0_solve(mlf_ctx* ctx, const double* y, double* x, int nrhs);
  * Replaces: CGSold (modIterativo.f90:331-493). */
 int mlf_cgs(mlf_ctx* ctx, const double* b, const double* x0, double tol, int maxit, int nrhs,
             double* x, int* iters, double* relres, int precond_kind, int* status_out);
+
+/* Stagnation detector of mlf_cgs, mlf_solve and mlf_monostatic: a column
+ * whose relative residual has set no new minimum within `window` iterations
+ * stops with status MLF_CGS_STAGNATED (mlf_solve mode 1: the FP64 residual
+ * of each refinement step, the window counted in inner steps).  0, the
+ * default, turns it off, as in the reference, whose CGSold iterates until
+ * it converges (modIterativo.f90:384-490). */
+int mlf_set_stagnation(mlf_ctx* ctx, int window);
 
 /* Solve Z_MLFMA x = b for nrhs columns.  mode 0: CGS on the FP64 operator
  * (exactly mlf_cgs).  mode 1: mixed precision — iterative refinement whose

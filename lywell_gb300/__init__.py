@@ -6,6 +6,6 @@ include/lywell_mlfma.h; :mod:`lywell_gb300.mlfma` is the host-side mirror of
 the reference's Fortran interface, :mod:`lywell_gb300.meshes` makes the
 synthetic PEC bodies.
 """
-from .mlfma import FMM, MLFMA, RWG, MLFError, MoM, ajustar_polariz, direction  # noqa: F401
+from .mlfma import FMM, MLFMA, RWG, MLFError, MoM, ajustar_polariz, direction, ilu0C  # noqa: F401
 
-__all__ = ["MLFMA", "FMM", "MoM", "RWG", "MLFError", "ajustar_polariz", "direction"]
+__all__ = ["MLFMA", "FMM", "MoM", "RWG", "MLFError", "ajustar_polariz", "direction", "ilu0C"]

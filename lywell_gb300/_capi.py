@@ -29,6 +29,9 @@ SIGNATURES = {
     "mlf_ilut": (C.c_int, [vp, C.c_double, C.c_double, ip]),
     "mlf_ilu_size": (C.c_int, [vp, C.POINTER(C.c_longlong)]),
     "mlf_ilu0_solve": (C.c_int, [vp, vp, vp, C.c_int]),
+    "mlf_ilu0_csr": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, vp, ip]),
+    "mlf_set_near_values": (C.c_int, [vp, vp]),
+    "mlf_set_stagnation": (C.c_int, [vp, C.c_int]),
     "mlf_cgs": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp]),
     "mlf_nearinv": (C.c_int, [vp, ip]),
     "mlf_nearinv_own": (C.c_int, [vp, ip]),

@@ -182,6 +182,64 @@ int mlf_ilu0(mlf_ctx* h, int* ierr_row) {
     return MLF_OK;
 }
 
+int mlf_ilu0_csr(int n, const float* a, const int* ja, const int* ia, float* alu, int* jlu, int* ju, int* ierr) {
+    g_init_error.clear();
+    if (n <= 0 || !a || !ja || !ia || !alu || !jlu || !ju || !ierr) {
+        g_init_error = "invalid argument";
+        return MLF_E_ARG;
+    }
+    // the CSR must be well formed: ia(1) = 1, ia non-decreasing, columns in
+    // 1..n and strictly ascending within each row (ilu0C relies on the L
+    // entries preceding the diagonal and checks none of this)
+    if (ia[0] != 1) {
+        g_init_error = "ia(1) must be 1";
+        return MLF_E_ARG;
+    }
+    for (int i = 0; i < n; ++i) {
+        if (ia[i + 1] < ia[i]) {
+            g_init_error = "ia decreases at row " + std::to_string(i + 1);
+            return MLF_E_ARG;
+        }
+        for (int q = ia[i] - 1; q < ia[i + 1] - 1; ++q) {
+            if (ja[q] < 1 || ja[q] > n) {
+                g_init_error = "column index out of range in row " + std::to_string(i + 1);
+                return MLF_E_ARG;
+            }
+            if (q > ia[i] - 1 && ja[q] <= ja[q - 1]) {
+                g_init_error = "columns not strictly ascending in row " + std::to_string(i + 1);
+                return MLF_E_ARG;
+            }
+        }
+    }
+    const long long nnz = (long long)ia[n] - 1;
+    std::vector<int> ia0(n + 1), ja0(nnz);
+    for (int i = 0; i <= n; ++i) ia0[i] = ia[i] - 1;
+    for (long long q = 0; q < nnz; ++q) ja0[q] = ja[q] - 1;
+    std::vector<float2> aluv(nnz + 2, make_float2(0.f, 0.f));
+    std::vector<int> jluv(nnz + 2, 0), juv(n + 1, 0);
+    *ierr = ilu0_msr(n, ia0.data(), ja0.data(), reinterpret_cast<const float2*>(a), aluv.data(), jluv.data(),
+                     juv.data());
+    // element k of the Fortran arrays alu(nnz+1), jlu(nnz+1), ju(n) is index k here
+    std::memcpy(alu, aluv.data() + 1, (size_t)(nnz + 1) * sizeof(float2));
+    std::memcpy(jlu, jluv.data() + 1, (size_t)(nnz + 1) * sizeof(int));
+    std::memcpy(ju, juv.data() + 1, (size_t)n * sizeof(int));
+    return MLF_OK;
+}
+
+int mlf_set_near_values(mlf_ctx* h, const float* a) {
+    if (!h || !a) return MLF_E_ARG;
+    Ctx* c = &h->c;
+    if (need_tree(c)) return MLF_E_STATE;
+    if (!bind_device(c)) return MLF_E_CUDA;
+    return device_set_near(c, reinterpret_cast<const float2*>(a));
+}
+
+int mlf_set_stagnation(mlf_ctx* h, int window) {
+    if (!h || window < 0) return MLF_E_ARG;
+    h->c.stag_window = window;
+    return MLF_OK;
+}
+
 int mlf_ilut(mlf_ctx* h, double fill_in_prc, double droptol, int* ierr_out) {
     if (!h || !ierr_out || fill_in_prc < 0 || droptol < 0) return MLF_E_ARG;
     Ctx* c = &h->c;

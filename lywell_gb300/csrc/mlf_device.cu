@@ -388,6 +388,25 @@ int fetch_near_values(Ctx* c, std::vector<float2>& out) {
     return MLF_OK;
 }
 
+// Replace the complex(4) near-field values (the reference's public
+// Zesparcida_MLFMA, which its host may overwrite before crear_precond) and
+// drop everything derived from them: the complex(8) copy is rebuilt, the
+// box-pair blocks are rebuilt on their next use, and the ILU / neighbourhood
+// preconditioners must be built again.
+int device_set_near(Ctx* c, const float2* host_vals) {
+    CK(cudaMemcpyAsync(c->dZ, host_vals, c->nnz * sizeof(float2), cudaMemcpyHostToDevice, c->stream));
+    k_f2d<<<4096, 256, 0, c->stream>>>((size_t)c->nnz, c->dZ, c->dZd);
+    int st;
+    if ((st = launch_check(c, "k_f2d"))) return st;
+    CK(cudaStreamSynchronize(c->stream));
+    near_blocks_free(c);
+    c->ilu_ok = 0;
+    c->nearinv_ok = 0;
+    c->nearinv_own = 0;
+    c->learned = 0;
+    return MLF_OK;
+}
+
 int need_tree(Ctx* c) {
     if (!c->dense) return 0;
     c->err = "this call needs the MLFMA octree; the context holds the dense MoM operator";

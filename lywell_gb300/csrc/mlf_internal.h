@@ -122,6 +122,8 @@ struct Ctx {
     int tr_group = 0;                 // FP32 translation: boxes per thread (1, 2, 4; 0: 2 for one column, else 4)
     int tr_cols = 0;                  // ... and columns per thread for grouped boxes (1, 2, 4; 0: 2 with 4 boxes, else 4)
     int basis_bits = 32;              // Krylov basis storage of the mixed solve: 32 (FP32) or 16 (FP16)
+    int stag_window = 0;              // stagnation window in iterations (0: off): a column whose residual
+                                      // sets no new minimum within this many iterations stops as stagnated
     Mixed32 m32;
     cudaStream_t stream = nullptr;
     std::string err;
@@ -214,11 +216,16 @@ int build_fmm(Ctx* c);             // single-level FMM grid as a one-level tree 
 void sph_bessel(int nmax, double x, double* j, double* y);
 void binomial_squares(int nmax, std::vector<double>& out);  // (n!/(i!(n-i)!))^2, [n*(nmax+1)+i]
 int ilu0_factor(Ctx* c);           // host ILU(0), fills alu/jlu/ju, returns ierr
+// ILU(0) of an n x n CSR matrix (0-based ia/ja, columns ascending in each row)
+// into MSR arrays with 1-based content (alu, jlu: nnz + 2 entries, ju: n + 1;
+// element 0 unused); returns 0 or the zero-pivot row (1-based)
+int ilu0_msr(int n, const int* ia, const int* ja, const float2* a, float2* alu, int* jlu, int* ju);
 int ilut_factor(Ctx* c, int lfil, double tol);  // host ILUT, same MSR layout
 void ilu_levels(Ctx* c);           // level schedules of the forward/backward sweeps
 
 // device set-up and operators (mlf_device.cu)
 int device_setup(Ctx* c);          // uploads tables, computes T, patterns, near field
+int device_set_near(Ctx* c, const float2* host_vals);   // replace the near values, drop what derives from them
 void device_free(Ctx* c);
 int ensure_fields(Ctx* c, int nrhs);
 int configure_kernels(Ctx* c);

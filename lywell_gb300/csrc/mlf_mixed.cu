@@ -831,6 +831,9 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
     if (int st = col_norms(c, nrhs, b, partial, dred, hbuf, bn, s)) return st;
     std::fill(iters, iters + nrhs, 0);
     std::vector<int> done(nrhs, 0);
+    // stagnation: the best FP64 residual of each column and the inner step count that reached it
+    std::vector<double> sbest(nrhs, HUGE_VAL);
+    std::vector<int> sbest_it(nrhs, 0);
     std::vector<Cx> H((size_t)nrhs * (m + 1) * m), G((size_t)nrhs * (m + 1)), CS((size_t)nrhs * m), SN((size_t)nrhs * m);
     auto Hc = [&](int col, int i, int j) -> Cx& { return H[((size_t)col * m + j) * (m + 1) + i]; };
     int st = MLF_OK, k = 0;
@@ -853,6 +856,15 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
             relres[col] = bn[col] > 0 ? beta[col] / bn[col] : 0.0;
             if (!done[col] && (relres[col] < tol || bn[col] == 0)) { done[col] = 1; status[col] = MLF_CGS_CONVERGED; }
             if (!std::isfinite(relres[col]) && !done[col]) { done[col] = 1; status[col] = MLF_CGS_NOT_FINITE; }
+            if (c->stag_window > 0 && !done[col]) {
+                if (relres[col] < sbest[col]) {
+                    sbest[col] = relres[col];
+                    sbest_it[col] = iters[col];
+                } else if (iters[col] - sbest_it[col] >= c->stag_window) {
+                    done[col] = 1;
+                    status[col] = MLF_CGS_STAGNATED;
+                }
+            }
             all = all && done[col];
             budget = budget || (!done[col] && iters[col] < maxit);
         }

@@ -923,29 +923,22 @@ inline float2 mulf(float2 a, float2 b) {
 }
 }  // namespace
 
-// ilu0C, modIterativo.f90:1805-1976 (Saad's ILU(0), IKJ on the CSR pattern).
-// MSR output with 1-based content: alu[1..n] inverted diagonal, jlu[1] = n+2,
-// row i of L then U in [jlu[i], jlu[i+1]), ju[i] = start of U.  Factors are
-// complex(4); the update alu(jw) - tl*alu(jj) runs in double, tl = alu(j) *
-// alu(jrow) in single, as in the reference.  Returns 0 or the zero-pivot row.
-int ilu0_factor(Ctx* c) {
-    const int n = c->N;
-    const long long nnz = c->nnz;
-    c->alu.assign(nnz + 2, make_float2(0.f, 0.f));
-    c->jlu.assign(nnz + 2, 0);
-    c->ju.assign(n + 1, 0);
-    std::vector<float2> zf;
-    if (fetch_near_values(c, zf) != MLF_OK) return -1;
+// ilu0C, modIterativo.f90:1805-1976: Saad's ILU(0) (SPARSKIT ilu0), IKJ on the
+// CSR pattern, restated step by step because the tests hold the complex(4)
+// factors bit-exact against the reference's.  MSR output with 1-based
+// content: alu[1..n] inverted diagonal, jlu[1] = n+2, row i of L then U in
+// [jlu[i], jlu[i+1]), ju[i] = start of U.  Factors are complex(4); the update
+// alu(jw) - tl*alu(jj) runs in double, tl = alu(j) * alu(jrow) in single, as
+// in the reference.  A row without a diagonal entry keeps alu[i] = 0 and is
+// reported as that zero pivot.  Returns 0 or the zero-pivot row.
+int ilu0_msr(int n, const int* ia, const int* ja, const float2* zf, float2* alu, int* jlu, int* ju) {
     std::vector<int> iw(n + 1, 0);
-    float2* alu = c->alu.data();
-    int* jlu = c->jlu.data();
-    int* ju = c->ju.data();
     long long ju0 = n + 2;
     jlu[1] = (int)ju0;
     for (int ii = 1; ii <= n; ++ii) {
         const long long js = ju0;
-        for (long long j = c->ia[ii - 1]; j < c->ia[ii]; ++j) {
-            const int jcol = c->ja[j] + 1;
+        for (long long j = ia[ii - 1]; j < ia[ii]; ++j) {
+            const int jcol = ja[j] + 1;
             if (jcol == ii) {
                 alu[ii] = zf[j];
                 iw[jcol] = ii;
@@ -982,6 +975,20 @@ int ilu0_factor(Ctx* c) {
         for (long long i = js; i <= jf; ++i) iw[jlu[i]] = 0;
     }
     return 0;
+}
+
+// ILU(0) of the context's near field (crear_precond ILU0 branch,
+// main.f90:851-902): the device values are fetched and factorised on the host
+// as the reference does.  Returns 0, the zero-pivot row, or -1 on a CUDA error.
+int ilu0_factor(Ctx* c) {
+    const int n = c->N;
+    const long long nnz = c->nnz;
+    c->alu.assign(nnz + 2, make_float2(0.f, 0.f));
+    c->jlu.assign(nnz + 2, 0);
+    c->ju.assign(n + 1, 0);
+    std::vector<float2> zf;
+    if (fetch_near_values(c, zf) != MLF_OK) return -1;
+    return ilu0_msr(n, c->ia.data(), c->ja.data(), zf.data(), c->alu.data(), c->jlu.data(), c->ju.data());
 }
 
 // ilutC, modIterativo.f90:2432-2883 (Saad's dual-threshold ILUT as adapted

@@ -386,6 +386,9 @@ int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxi
     std::vector<double> hscal((size_t)nrhs * S_NSCAL);
     c->cgs_hist.clear();
     c->cgs_hist_nrhs = nrhs;
+    // stagnation: the best residual of each column and the iteration that set it
+    std::vector<double> best(nrhs, HUGE_VAL);
+    std::vector<int> best_it(nrhs, 0);
     int it = 0;
     for (; it < maxit; ++it) {
         k_dot_partial<<<rg, RED_THREADS, 0, s>>>(N, r, Rt, 0, flags, partials);
@@ -405,10 +408,25 @@ int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxi
         CK(cudaMemcpyAsync(hflags.data(), flags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
         CK(cudaMemcpyAsync(hscal.data(), scal, hscal.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
+        bool stalled = false;
         for (int col = 0; col < nrhs; ++col) {
             const double bb = hscal[col * S_NSCAL + S_BB];
-            c->cgs_hist.push_back(bb > 0 ? std::sqrt(hscal[col * S_NSCAL + S_RR] / bb) : 0.0);
+            const double rel = bb > 0 ? std::sqrt(hscal[col * S_NSCAL + S_RR] / bb) : 0.0;
+            c->cgs_hist.push_back(rel);
+            int* fl = &hflags[col * F_NFLAG];
+            if (c->stag_window <= 0 || fl[F_DONE]) continue;
+            if (rel < best[col]) {
+                best[col] = rel;
+                best_it[col] = fl[F_ITERS];
+            } else if (fl[F_ITERS] - best_it[col] >= c->stag_window) {
+                fl[F_DONE] = 1;
+                fl[F_STATUS] = MLF_CGS_STAGNATED;
+                stalled = true;
+            }
         }
+        // retire the stagnated columns on the device (the update kernels skip done columns)
+        if (stalled)
+            CK(cudaMemcpyAsync(flags, hflags.data(), hflags.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         bool all = true;
         for (int col = 0; col < nrhs; ++col) all = all && hflags[col * F_NFLAG + F_DONE];
         if (all) break;

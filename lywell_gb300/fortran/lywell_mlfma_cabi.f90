@@ -77,6 +77,29 @@ module lywell_mlfma_cabi
             integer(c_int), intent(out) :: ierr_row
         end function
 
+        ! ilu0C(n, a, ja, ia, alu, jlu, ju, iw, ierr) on host arrays (iw kept inside)
+        integer(c_int) function mlf_ilu0_csr(n, a, ja, ia, alu, jlu, ju, ierr) bind(C)
+            import :: c_int, c_float_complex
+            integer(c_int), value :: n
+            complex(c_float_complex), intent(in) :: a(*)
+            integer(c_int), intent(in) :: ja(*), ia(*)
+            complex(c_float_complex), intent(out) :: alu(*)
+            integer(c_int), intent(out) :: jlu(*), ju(*), ierr
+        end function
+
+        ! overwrite Zesparcida_MLFMA's values on the device
+        integer(c_int) function mlf_set_near_values(ctx, a) bind(C)
+            import :: c_int, c_float_complex, c_ptr
+            type(c_ptr), value :: ctx
+            complex(c_float_complex), intent(in) :: a(*)
+        end function
+
+        integer(c_int) function mlf_set_stagnation(ctx, window) bind(C)
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: window
+        end function
+
         integer(c_int) function mlf_ilu0_solve(ctx, y, x, nrhs) bind(C)
             import :: c_int, c_double_complex, c_ptr
             type(c_ptr), value :: ctx

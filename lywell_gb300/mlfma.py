@@ -11,6 +11,7 @@ inicializar_MLFMA            ``MLFMA(rwg, lam, ladomax)``                   mlf_
 MatxVec_MLFMA                ``MLFMA.MatxVec_MLFMA(x)`` / ``matvec``        mlf_matvec
 Zesparcida_MLFMA, ia, ja     ``MLFMA.near_csr()``                           mlf_near_csr
 crear_precond -> ilu0C       ``MLFMA.ilu0C()`` (returns ierr)               mlf_ilu0
+ilu0C on a host CSR          ``ilu0C(n, a, ja, ia)``                        mlf_ilu0_csr
 lusol0C                      ``MLFMA.lusol0C(y)``                           mlf_ilu0_solve
 CGSold                       ``MLFMA.CGSold(b, guess, errmax, ...)``        mlf_cgs
 generar_onda                 ``MLFMA.generar_onda(dir, pol, ctte)``         mlf_excitation
@@ -29,7 +30,7 @@ import numpy as np
 
 from ._capi import CGS_STATUS, ENGINES, FLAG_DENSE_MOM, FLAG_FMM, FLAG_LEGENDRE_RECURRENCE, PRECOND, MLFError, load
 
-__all__ = ["RWG", "MLFMA", "MoM", "FMM", "MLFError", "FLAG_LEGENDRE_RECURRENCE", "ajustar_polariz", "direction"]
+__all__ = ["RWG", "MLFMA", "MoM", "FMM", "MLFError", "FLAG_LEGENDRE_RECURRENCE", "ajustar_polariz", "direction", "ilu0C"]
 
 
 def _p(a):
@@ -101,6 +102,30 @@ def ajustar_polariz(d, kind: str) -> np.ndarray:
         return np.array([0, 0, 1], dtype=np.complex128)
     v = np.array([d[1], -d[0], 0.0])
     return (v / np.sqrt(np.sum(v * v))).astype(np.complex128)
+
+
+def ilu0C(n: int, a, ja, ia):
+    """ilu0C (modIterativo.f90:1805-1976) on a host CSR matrix: a complex64
+    values, ja / ia 1-based.  Returns (alu, jlu, ju, ierr) in the reference's
+    MSR layout; raises MLFError on a malformed CSR."""
+    L = load()
+    a = np.ascontiguousarray(a, dtype=np.complex64)
+    ja = np.ascontiguousarray(ja, dtype=np.int32)
+    ia = np.ascontiguousarray(ia, dtype=np.int32)
+    if ia.size != n + 1 or a.size != ja.size:
+        raise ValueError("ia must hold n + 1 entries and a, ja the same count")
+    nnz = int(ia[-1]) - 1 if ia.size else 0
+    if nnz != a.size:
+        raise ValueError("ia(n+1) - 1 must equal the number of values")
+    alu = np.zeros(nnz + 1, dtype=np.complex64)
+    jlu = np.zeros(nnz + 1, dtype=np.int32)
+    ju = np.zeros(n, dtype=np.int32)
+    ierr = C.c_int()
+    code = L.mlf_ilu0_csr(int(n), _p(a), _p(ja), _p(ia), _p(alu), _p(jlu), _p(ju), C.byref(ierr))
+    if code != 0:
+        msg = L.mlf_last_error(None)
+        raise MLFError(code, msg.decode() if msg else "")
+    return alu, jlu, ju, int(ierr.value)
 
 
 class MLFMA:
@@ -188,6 +213,14 @@ class MLFMA:
         _check(load().mlf_near_csr(self._h, C.byref(nnz), _p(a), _p(ja), _p(ia)), self._h)
         return ia, ja, a
 
+    def set_near_values(self, a):
+        """Overwrite the complex(4) near-field values (Zesparcida_MLFMA) in
+        near_csr()'s order; preconditioners built before must be built again."""
+        a = np.ascontiguousarray(a, dtype=np.complex64)
+        if a.size != self.nnz:
+            raise ValueError(f"expected {self.nnz} near values, got {a.size}")
+        _check(load().mlf_set_near_values(self._h, _p(a)), self._h)
+
     # -- preconditioner
     def ilu0(self) -> int:
         ierr = C.c_int()
@@ -266,6 +299,11 @@ class MLFMA:
         if single:
             return dict(x=X[:, 0], iters=int(it[0]), relres=float(rr[0]), status=CGS_STATUS[int(st[0])])
         return dict(x=X, iters=it, relres=rr, status=[CGS_STATUS[int(s)] for s in st])
+
+    def set_stagnation(self, window: int):
+        """Stop a column as 'stagnated' when its residual has set no new
+        minimum within `window` iterations (0: off, the default)."""
+        _check(load().mlf_set_stagnation(self._h, int(window)), self._h)
 
     def cgs_history(self, col: int = 0):
         n = C.c_int()

@@ -129,9 +129,9 @@ def test_learned_preconditioner_gain(gpu_lib):
     of the held-out body), pick the damping from CGS traces, and solve the
     held-out superellipsoid (exponent 4, 2 x 1 x 1 lambda) from -z,
     x-polarised.  The learned preconditioner must converge, beat ILU0 and the
-    unpreconditioned solve, and not lose against the exact neighbourhood
-    inverse it corrects (the damping falls back to 0 when the correction does
-    not pay on the training bodies)."""
+    unpreconditioned solve, and take strictly fewer iterations than the exact
+    neighbourhood inverse M1 it corrects: the gain of the network over the
+    method without it."""
     from lywell_gb300 import MLFMA, RWG, meshes
     from lywell_gb300.learned import solve_with_fallback, train
     rng = np.random.default_rng(7)
@@ -165,5 +165,6 @@ def test_learned_preconditioner_gain(gpu_lib):
     assert out["true_relres"] < 1.01e-4
     assert out["iters"] < plain
     assert ilu["status"] != "converged" or out["iters"] < ilu["iters"]
-    assert out["iters"] <= 1.1 * exact["iters"]
+    assert exact["status"] == "converged"
+    assert out["iters"] < exact["iters"]
     m.close()

@@ -211,20 +211,6 @@ def test_cgs_multi_rhs_per_column(ico3):
         np.testing.assert_allclose(out["x"][:, k], one["x"], rtol=1e-10, atol=1e-16)
 
 
-@pytest.mark.slow
-def test_cfg2_sphere_matvec_vs_oracle(gpu_lib):
-    """Icosphere-5, r = 3 lambda (30720 RWG, 6 levels): 2 seeded vectors."""
-    tris = meshes.icosphere(5, 3.0)
-    m = MLFMA(RWG(tris), lam=1.0, ladomax=0.25)
-    o = core.OracleMLFMA(ORWG(tris), lam=1.0, ladomax=0.25)
-    assert m.nlev == 6
-    _, _, a = m.near_csr()
-    o.set_near(a)
-    for x in _vectors(m.N, [0, 1]):
-        assert _rel(m.matvec(x), o.matvec(x)) < 1e-12
-    m.close()
-
-
 def test_monostatic_reference_sweep(ico3):
     """mlf_monostatic mode 0 against the oracle's sweep and the binary's RCSMONO file."""
     tris, m, o = ico3

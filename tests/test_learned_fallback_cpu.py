@@ -1,0 +1,83 @@
+"""Host logic of the learned preconditioner's fallback (no GPU): a stand-in
+operator records the calls that solve_with_fallback makes.
+
+The rule: keep the learned solve when it converged within the
+unpreconditioned iteration count AND its true residual ||b - Z x|| / ||b||
+meets the tolerance; otherwise solve again with ILU0 (the reference's
+preconditioner, crear_precond main.f90:851-902), or without a preconditioner
+when ILU0 meets a zero pivot."""
+import numpy as np
+import pytest
+
+from lywell_gb300.learned import solve_with_fallback
+
+
+class FakeOperator:
+    """Z = 2 I.  cgs() returns the scripted result for each preconditioner."""
+
+    def __init__(self, n, learned_status="converged", learned_x_scale=1.0, ilu0_ierr=0):
+        self.n = n
+        self.calls = []
+        self.learned_status = learned_status
+        self.learned_x_scale = learned_x_scale
+        self.ilu0_ierr = ilu0_ierr
+
+    def matvec(self, x):
+        return 2.0 * x
+
+    def ilu0(self):
+        self.calls.append("ilu0")
+        return self.ilu0_ierr
+
+    def cgs(self, b, errmax=1e-4, maxit=1000, precond=0):
+        self.calls.append(("cgs", precond, maxit))
+        if precond == "nearinv":
+            return dict(x=self.learned_x_scale * b / 2.0, iters=min(maxit, 7), relres=0.0,
+                        status=self.learned_status)
+        return dict(x=b / 2.0, iters=11, relres=0.0, status="converged")
+
+
+class FakeLearned:
+    def __init__(self):
+        self.installed = 0
+
+    def apply_to(self, m):
+        self.installed += 1
+        return 0
+
+
+@pytest.fixture
+def b():
+    rng = np.random.default_rng(0)
+    return rng.standard_normal(50) + 1j * rng.standard_normal(50)
+
+
+def test_learned_kept_when_converged(b):
+    m, lp = FakeOperator(50), FakeLearned()
+    out = solve_with_fallback(m, b, lp, plain_iters=30)
+    assert out["used"] == "learned" and lp.installed == 1
+    assert m.calls == [("cgs", "nearinv", 30)]
+    assert out["true_relres"] < 1e-15
+
+
+def test_falls_back_to_ilu0_past_the_plain_count(b):
+    m, lp = FakeOperator(50, learned_status="maxit"), FakeLearned()
+    out = solve_with_fallback(m, b, lp, plain_iters=1, maxit=900)
+    assert out["used"] == "ilu0"
+    assert m.calls == [("cgs", "nearinv", 1), "ilu0", ("cgs", "ilu0", 900)]
+    assert out["true_relres"] < 1e-15
+
+
+def test_falls_back_when_true_residual_misses(b):
+    # the recursion claims convergence but the currents are 10 % off
+    m, lp = FakeOperator(50, learned_x_scale=1.1), FakeLearned()
+    out = solve_with_fallback(m, b, lp, plain_iters=30, errmax=1e-4)
+    assert out["used"] == "ilu0"
+    assert "ilu0" in m.calls
+
+
+def test_no_preconditioner_when_ilu0_has_a_zero_pivot(b):
+    m, lp = FakeOperator(50, learned_status="stagnated", ilu0_ierr=17), FakeLearned()
+    out = solve_with_fallback(m, b, lp, plain_iters=5)
+    assert out["used"] == "none"
+    assert m.calls[-1] == ("cgs", "none", 5000)
