@@ -119,14 +119,16 @@ int mlf_matvec_device(mlf_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, in
  * reference.  It is for callers that must not allocate device memory
  * while they solve: hosts that record their iteration into a CUDA graph,
  * or hosts whose device memory belongs to another runtime or a fixed
- * pool.  It runs the same kernels as mlf_matvec_device but keeps the
- * multipole fields in one fixed 64 MiB device array inside the library
- * (held by every GPU that loads it, until exit) and never calls
- * cudaMalloc/cudaFree.  Octrees whose C, B and A fields together exceed
- * 4,194,304 complex values are rejected with MLF_E_ARG.  The first call on
- * a device looks up the array's address; make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race.
- * stream NULL = the context's stream. */
+ * pool.  It issues the same FP64-operator launches as mlf_matvec_device,
+ * with bit-identical results, but keeps the multipole fields in one fixed
+ * 64 MiB device array inside the library (held by every GPU that loads it,
+ * until exit) and never calls cudaMalloc/cudaFree.  Octrees whose C, B and
+ * A fields together exceed 4,194,304 complex values are rejected with
+ * MLF_E_ARG.  The first call on a device looks up the array's address and
+ * keeps it for the process; make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race.  The caller's
+ * current device is restored on return.  stream NULL = the context's
+ * stream. */
 int mlf_matvec_device_noalloc(mlf_ctx* ctx, const void* x_dev, void* y_dev, void* stream);
 
 /* Near-field block in CSR (1-based), values complex(4) interleaved floats.

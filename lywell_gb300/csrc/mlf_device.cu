@@ -22,8 +22,9 @@
 //                     phi pass then theta pass (mlf_sep.cuh)   (:1857-1897)
 //   k_receive_near_d  y = fac sum conj(R) A + Znear x, near values in
 //                     complex(8)                               (:1915-1942)
-//   k_interp_up, k_anterp_down, k_receive_near: the 9-tap forms, used by the
-//                     allocation-free entry point (mlf_noalloc.cu)
+// fp64_matvec_launch issues these on given field buffers: the context's own
+// (device_matvec) or the allocation-free entry point's fixed scratch
+// (mlf_noalloc.cu).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -187,36 +188,6 @@ __global__ void k_aggregate(int K, int nrhs, int ld, const int* __restrict__ box
     }
 }
 
-// parent level (coarse) Kp samples, child level Kc; blockIdx.x = (parent*nrhs + r)*nchunk + chunk
-__global__ void k_interp_up(int Kp, int Kc, int nrhs, int nchunk, const int* __restrict__ child_ptr,
-                            const int* __restrict__ octant, const double* __restrict__ iw,
-                            const int* __restrict__ iidx, const double2* __restrict__ shift,
-                            const double2* __restrict__ Cc, double2* __restrict__ Cp) {
-    const int chunk = blockIdx.x % nchunk;
-    const int pr = blockIdx.x / nchunk;
-    const int P = pr / nrhs, r = pr % nrhs;
-    const int q = chunk * blockDim.x + threadIdx.x;
-    if (q >= 2 * Kp) return;
-    const int pol = q >= Kp, m = q - pol * Kp;
-    double w9[9];
-    int i9[9];
-#pragma unroll
-    for (int t = 0; t < 9; ++t) { w9[t] = iw[9 * m + t]; i9[t] = iidx[9 * m + t] + pol * Kc; }
-    double2 acc = make_double2(0, 0);
-    for (int cb = child_ptr[P]; cb < child_ptr[P + 1]; ++cb) {
-        const double2* src = Cc + ((size_t)cb * nrhs + r) * 2 * Kc;
-        double2 v = make_double2(0, 0);
-#pragma unroll
-        for (int t = 0; t < 9; ++t) {
-            const double2 s = src[i9[t]];
-            v.x = fma(w9[t], s.x, v.x);
-            v.y = fma(w9[t], s.y, v.y);
-        }
-        cmac(acc, v, shift[octant[cb] * Kp + m]);
-    }
-    Cp[((size_t)P * nrhs + r) * 2 * Kp + q] = acc;
-}
-
 // blockIdx.x = (box*nrhs + r)*nchunk + chunk
 __global__ void k_translate(int K, int nrhs, int nchunk, const int* __restrict__ far_ptr,
                             const int* __restrict__ far_src, const int* __restrict__ far_tid,
@@ -238,86 +209,10 @@ __global__ void k_translate(int K, int nrhs, int nchunk, const int* __restrict__
     B[((size_t)b * nrhs + r) * 2 * K + q] = make_double2(acc.x * wk, acc.y * wk);
 }
 
-// child level (fine) Kc, parent level Kp. One block per (child, rhs): stage
-// D = P(parent) * conj(shift_oct) in shared memory, then gather the
-// transposed interpolation taps.  Dynamic smem: 2*Kp double2.
-__global__ void k_anterp_down(int Kp, int Kc, int nrhs, const int* __restrict__ parent,
-                              const int* __restrict__ octant, const int* __restrict__ ant_ptr,
-                              const int* __restrict__ ant_row, const double* __restrict__ ant_w,
-                              const double2* __restrict__ shift, const double2* __restrict__ Psrc,
-                              const double2* __restrict__ Bc, double2* __restrict__ Ac) {
-    extern __shared__ double2 D[];
-    const int cb = blockIdx.x / nrhs, r = blockIdx.x % nrhs;
-    const int P = parent[cb];
-    const double2* sh = shift + (size_t)octant[cb] * Kp;
-    const double2* src = Psrc + ((size_t)P * nrhs + r) * 2 * Kp;
-    for (int q = threadIdx.x; q < 2 * Kp; q += blockDim.x) {
-        const int m = q >= Kp ? q - Kp : q;
-        const double2 s = sh[m];
-        const double2 v = src[q];
-        D[q] = make_double2(v.x * s.x + v.y * s.y, v.y * s.x - v.x * s.y);   // v * conj(s)
-    }
-    __syncthreads();
-    const size_t off = ((size_t)cb * nrhs + r) * 2 * Kc;
-    for (int q = threadIdx.x; q < 2 * Kc; q += blockDim.x) {
-        const int pol = q >= Kc, k = q - pol * Kc;
-        double2 acc = make_double2(0, 0);
-        const int e1 = ant_ptr[k + 1];
-        for (int e = ant_ptr[k]; e < e1; ++e) {
-            const double w = ant_w[e];
-            const double2 d = D[ant_row[e] + pol * Kp];
-            acc.x = fma(w, d.x, acc.x);
-            acc.y = fma(w, d.y, acc.y);
-        }
-        const double2 bv = Bc[off + q];
-        Ac[off + q] = make_double2(bv.x + acc.x, bv.y + acc.y);
-    }
-}
-
-// One warp per (sorted basis j, rhs): y[perm[j]] = fac * sum conj(R_j) A_box + sum_near Z x.
-__global__ void k_receive_near(int K, int N, int nrhs, int ld, const int* __restrict__ perm,
-                               const int* __restrict__ box_of_sorted, const double2* __restrict__ R,
-                               const double2* __restrict__ A, const int* __restrict__ ia,
-                               const int* __restrict__ ja, const float2* __restrict__ Z,
-                               const double2* __restrict__ x, double facy, double2* __restrict__ y) {
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (gw >= N * nrhs) return;
-    const int j = gw / nrhs, r = gw % nrhs;
-    const int n = perm[j], b = box_of_sorted[j];
-    const double2* Rj = R + (size_t)j * 2 * K;
-    const double2* Ab = A + ((size_t)b * nrhs + r) * 2 * K;
-    double sr = 0, si = 0;
-    for (int q = lane; q < 2 * K; q += 32) {
-        const double2 a = Rj[q], v = Ab[q];
-        // conj(a) * v
-        sr = fma(a.x, v.x, sr); sr = fma(a.y, v.y, sr);
-        si = fma(a.x, v.y, si); si = fma(-a.y, v.x, si);
-    }
-    const double2* xr = x + (size_t)r * ld;
-    double nr = 0, ni = 0;
-    for (int q = ia[n] + lane; q < ia[n + 1]; q += 32) {
-        const float2 z = Z[q];
-        const double2 xv = xr[ja[q]];
-        nr = fma(xv.x, (double)z.x, nr); nr = fma(-xv.y, (double)z.y, nr);
-        ni = fma(xv.x, (double)z.y, ni); ni = fma(xv.y, (double)z.x, ni);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        sr += __shfl_xor_sync(0xffffffff, sr, o);
-        si += __shfl_xor_sync(0xffffffff, si, o);
-        nr += __shfl_xor_sync(0xffffffff, nr, o);
-        ni += __shfl_xor_sync(0xffffffff, ni, o);
-    }
-    if (lane == 0) {
-        // (s) * (j*facy) = (-facy*si, facy*sr)
-        y[(size_t)r * ld + n] = make_double2(-facy * si + nr, facy * sr + ni);
-    }
-}
-
-// Same with the near field held as complex(8): the complex(4) values of the
-// reference converted once at set-up, so the SpMV spends no FP64-pipe slots
-// on float -> double conversions.
+// One warp per (sorted basis j, rhs): y[perm[j]] = fac * sum conj(R_j) A_box
+// + sum_near Z x, with the near field held as complex(8): the complex(4)
+// values of the reference converted once at set-up, so the SpMV spends no
+// FP64-pipe slots on float -> double conversions.
 __global__ void k_receive_near_d(int K, int N, int nrhs, int ld, const int* __restrict__ perm,
                                  const int* __restrict__ box_of_sorted, const double2* __restrict__ R,
                                  const double2* __restrict__ A, const int* __restrict__ ia,
@@ -456,11 +351,6 @@ int device_setup(Ctx* c) {
         if ((st = upload(c, &L.doctant, L.octant))) return st;
         if (n < nl) {
             if ((st = upload(c, &L.dchild_ptr, L.child_ptr))) return st;
-            if ((st = upload(c, &L.diw, L.iw))) return st;
-            if ((st = upload(c, &L.diidx, L.iidx))) return st;
-            if ((st = upload(c, &L.dant_ptr, L.ant_ptr))) return st;
-            if ((st = upload(c, &L.dant_row, L.ant_row))) return st;
-            if ((st = upload(c, &L.dant_w, L.ant_w))) return st;
             if ((st = upload(c, &L.dsth, L.sth))) return st;
             if ((st = upload(c, &L.dsph, L.sph))) return st;
             if ((st = upload(c, &L.dwth, L.wth))) return st;
@@ -586,18 +476,18 @@ int device_setup(Ctx* c) {
 
 static inline int chunks(int n, int bd) { return (n + bd - 1) / bd; }
 
-int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s) {
-    if (c->dense) return dense_matvec(c, x, y, nrhs, ld, s);
-    if (c->mv_prec == 1) return device_matvec32(c, x, y, nrhs, ld, s);
-    int st;
-    if ((st = ensure_fields(c, nrhs))) return st;
-    c->last_nrhs = nrhs;
+// The FP64 operator's launches on the given field buffers (level n: Cf[n],
+// Bf[n], Af[n], each double2[nb_n][nrhs][2][K_n]).  device_matvec passes the
+// context's buffers; mlf_matvec_device_noalloc passes buffers carved from its
+// fixed scratch, so both run the same kernels in the same order.  ev: six
+// events recorded between the stages (profiling), or nullptr.
+int fp64_matvec_launch(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s,
+                       double2* const* Cf, double2* const* Bf, double2* const* Af, cudaEvent_t* ev) {
     const int nl = c->nlev;
     Level& leaf = c->lv[nl];
-    const bool prof = c->profiling != 0;
-    if (prof) cudaEventRecord(c->ev[0], s);
-    k_aggregate<<<leaf.nb * nrhs, 256, 0, s>>>(leaf.K, nrhs, ld, c->dbox_ptr, c->dperm, c->dR, x, leaf.dC);
-    if (prof) cudaEventRecord(c->ev[1], s);
+    if (ev) cudaEventRecord(ev[0], s);
+    k_aggregate<<<leaf.nb * nrhs, 256, 0, s>>>(leaf.K, nrhs, ld, c->dbox_ptr, c->dperm, c->dR, x, Cf[nl]);
+    if (ev) cudaEventRecord(ev[1], s);
     for (int n = nl; n >= 4; --n) {
         Level& Lc = c->lv[n];
         Level& Lp = c->lv[n - 1];
@@ -605,36 +495,54 @@ int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaSt
         const size_t smem = (size_t)SEP_SLAB * 2 * (Lc.L + Lp.L) * sizeof(double2);   // child rows + parent slab
         k_interp_sep<double2, 1><<<Lp.nb * nrhs * 2 * nslab, 256, smem, s>>>(
             Lp.L, Lc.L, nrhs, nslab, Lp.dchild_ptr, Lc.doctant, Lp.dsth, Lp.dwth, Lp.dsph, Lp.dwph, Lp.dshift,
-            Lc.dC, Lp.dC);
+            Cf[n], Cf[n - 1]);
     }
-    if (prof) cudaEventRecord(c->ev[2], s);
+    if (ev) cudaEventRecord(ev[2], s);
     for (int n = 3; n <= nl; ++n) {
         Level& L = c->lv[n];
         const int bd = 128, nch = chunks(2 * L.K, bd);
         k_translate<<<L.nb * nrhs * nch, bd, 0, s>>>(L.K, nrhs, nch, L.dfar_ptr, L.dfar_src, L.dfar_tid,
-                                                     L.dT, L.dwq, L.dC, L.dB);
+                                                     L.dT, L.dwq, Cf[n], Bf[n]);
     }
-    if (prof) cudaEventRecord(c->ev[3], s);
+    if (ev) cudaEventRecord(ev[3], s);
     for (int n = 4; n <= nl; ++n) {
         Level& Lc = c->lv[n];
         Level& Lp = c->lv[n - 1];
-        const double2* Psrc = (n == 4) ? Lp.dB : Lp.dA;
+        const double2* Psrc = (n == 4) ? Bf[n - 1] : Af[n - 1];
         const size_t smem = ((size_t)Lp.K + (size_t)Lp.L * 2 * Lc.L) * sizeof(double2);
         k_anterp_sep<double2, 1><<<Lc.nb * nrhs * 2, 256, smem, s>>>(
             Lp.L, Lc.L, nrhs, Lc.dparent, Lc.doctant, Lp.dthT_ptr, Lp.dthT_row, Lp.dthT_w, Lp.dphT_ptr,
-            Lp.dphT_row, Lp.dphT_w, Lp.dshift, Psrc, Lc.dB, Lc.dA);
+            Lp.dphT_row, Lp.dphT_w, Lp.dshift, Psrc, Bf[n], Af[n]);
     }
-    if (prof) cudaEventRecord(c->ev[4], s);
+    if (ev) cudaEventRecord(ev[4], s);
     {
         const int warps = c->N * nrhs;
         const double facy = c->ph.w * MU / (4. * PI);
         k_receive_near_d<<<chunks(warps * 32, 256), 256, 0, s>>>(leaf.K, c->N, nrhs, ld, c->dperm,
                                                                   c->dbox_of_sorted, c->dR,
-                                                                  nl == 3 ? leaf.dB : leaf.dA, c->dia,
+                                                                  nl == 3 ? Bf[nl] : Af[nl], c->dia,
                                                                   c->dja, c->dZd, x, facy, y);
     }
-    if (prof) cudaEventRecord(c->ev[5], s);
-    if ((st = launch_check(c, "matvec"))) return st;
+    if (ev) cudaEventRecord(ev[5], s);
+    return launch_check(c, "matvec");
+}
+
+int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s) {
+    if (c->dense) return dense_matvec(c, x, y, nrhs, ld, s);
+    if (c->mv_prec == 1) return device_matvec32(c, x, y, nrhs, ld, s);
+    int st;
+    if ((st = ensure_fields(c, nrhs))) return st;
+    c->last_nrhs = nrhs;
+    double2* Cf[32] = {nullptr};
+    double2* Bf[32] = {nullptr};
+    double2* Af[32] = {nullptr};
+    for (int n = 3; n <= c->nlev; ++n) {
+        Cf[n] = c->lv[n].dC;
+        Bf[n] = c->lv[n].dB;
+        Af[n] = c->lv[n].dA;
+    }
+    const bool prof = c->profiling != 0;
+    if ((st = fp64_matvec_launch(c, x, y, nrhs, ld, s, Cf, Bf, Af, prof ? c->ev : nullptr))) return st;
     if (prof) {
         CK(cudaEventSynchronize(c->ev[5]));
         for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&c->stage_ms[i], c->ev[i], c->ev[i + 1]);
@@ -644,15 +552,14 @@ int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaSt
 
 // anterpolation smem: the largest parent grid decides; opt in above 48 KB
 int configure_kernels(Ctx* c) {
-    size_t mx = 0, mx2 = 0, mx3 = 0;
+    size_t mx2 = 0, mx3 = 0;
     for (int n = 3; n < c->nlev; ++n) {
-        mx = std::max(mx, 2 * (size_t)c->lv[n].K * sizeof(double2));
         mx2 = std::max(mx2, ((size_t)c->lv[n].K + (size_t)c->lv[n].L * 2 * c->lv[n + 1].L) * sizeof(double2));
         mx3 = std::max(mx3, (size_t)SEP_SLAB * 2 * (c->lv[n + 1].L + c->lv[n].L) * sizeof(double2));
     }
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->dev));
-    if (mx > (size_t)optin || mx2 > (size_t)optin || mx3 > (size_t)optin) {
+    if (mx2 > (size_t)optin || mx3 > (size_t)optin) {
         c->err = "parent sampling grid too large for the shared-memory interpolation stages";
         return MLF_E_ARG;
     }
@@ -660,7 +567,6 @@ int configure_kernels(Ctx* c) {
     // process: raise it to the device maximum (what a launch actually uses is
     // its own dynamic size), never to one context's need, which would break
     // the launches of an earlier context with larger grids.
-    CK(cudaFuncSetAttribute(k_anterp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     CK(cudaFuncSetAttribute(k_anterp_sep<double2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     CK(cudaFuncSetAttribute(k_interp_sep<double2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     return MLF_OK;
@@ -671,7 +577,7 @@ void device_free(Ctx* c) {
     for (int n = 1; n <= c->nlev && n < 32; ++n) {
         Level& L = c->lv[n];
         F(L.dC); F(L.dB); F(L.dA); F(L.dT); F(L.dwq); F(L.dfar_ptr); F(L.dfar_src); F(L.dfar_tid);
-        F(L.diw); F(L.diidx); F(L.dant_ptr); F(L.dant_row); F(L.dant_w); F(L.dshift);
+        F(L.dshift);
         F(L.dchild_ptr); F(L.dparent); F(L.doctant); F(L.dkap); F(L.dath); F(L.daph); F(L.dcentre);
         F(L.dsth); F(L.dsph); F(L.dwth); F(L.dwph); F(L.dthT_ptr); F(L.dthT_row); F(L.dthT_w); F(L.dphT_ptr);
         F(L.dphT_row); F(L.dphT_w);

@@ -80,10 +80,6 @@ struct Level {
     double2* dT = nullptr;
     double* dwq = nullptr;
     int *dfar_ptr = nullptr, *dfar_src = nullptr, *dfar_tid = nullptr;
-    double* diw = nullptr;
-    int* diidx = nullptr;
-    int *dant_ptr = nullptr, *dant_row = nullptr;
-    double* dant_w = nullptr;
     int *dsth = nullptr, *dsph = nullptr, *dthT_ptr = nullptr, *dthT_row = nullptr, *dphT_ptr = nullptr,
         *dphT_row = nullptr;
     double *dwth = nullptr, *dwph = nullptr, *dthT_w = nullptr, *dphT_w = nullptr;
@@ -231,6 +227,8 @@ int ensure_fields(Ctx* c, int nrhs);
 int configure_kernels(Ctx* c);
 int ensure_work(Ctx* c, size_t n_double2);
 int device_matvec(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s);
+int fp64_matvec_launch(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s,
+                       double2* const* Cf, double2* const* Bf, double2* const* Af, cudaEvent_t* ev);
 int device_ilu_upload(Ctx* c);
 int device_ilu_solve(Ctx* c, const double2* y, double2* x, cudaStream_t s);
 int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs,

@@ -853,9 +853,12 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
         if ((st = col_norms(c, nrhs, r, partial, dred, hbuf, beta, s))) break;
         bool all = true, budget = false;
         for (int col = 0; col < nrhs; ++col) {
-            relres[col] = bn[col] > 0 ? beta[col] / bn[col] : 0.0;
+            // a NaN or Inf in b or in the residual ends the column first
+            // (bn > 0 is false for a NaN norm, which would read as converged)
+            const bool finite = std::isfinite(bn[col]) && std::isfinite(beta[col]);
+            relres[col] = !finite ? beta[col] / bn[col] : (bn[col] > 0 ? beta[col] / bn[col] : 0.0);
+            if (!finite && !done[col]) { done[col] = 1; status[col] = MLF_CGS_NOT_FINITE; }
             if (!done[col] && (relres[col] < tol || bn[col] == 0)) { done[col] = 1; status[col] = MLF_CGS_CONVERGED; }
-            if (!std::isfinite(relres[col]) && !done[col]) { done[col] = 1; status[col] = MLF_CGS_NOT_FINITE; }
             if (c->stag_window > 0 && !done[col]) {
                 if (relres[col] < sbest[col]) {
                     sbest[col] = relres[col];

@@ -432,13 +432,25 @@ void parallel_for(int n, F f) {
         for (int i = 0; i < n; ++i) f(i);
         return;
     }
+    // chunk t of nt covers [n t / nt, n (t + 1) / nt); chunks run on threads,
+    // and any chunk whose thread could not be created (a process or container
+    // thread limit: std::system_error) runs here, so no exception crosses the
+    // C ABI and the result does not depend on how many threads started
+    auto chunk = [&](int t) {
+        const int i0 = (int)((long long)n * t / nt), i1 = (int)((long long)n * (t + 1) / nt);
+        for (int i = i0; i < i1; ++i) f(i);
+    };
     std::vector<std::thread> th;
     th.reserve(nt);
-    for (int t = 0; t < nt; ++t)
-        th.emplace_back([&, t] {
-            const int i0 = (int)((long long)n * t / nt), i1 = (int)((long long)n * (t + 1) / nt);
-            for (int i = i0; i < i1; ++i) f(i);
-        });
+    int started = 0;
+    for (; started < nt; ++started) {
+        try {
+            th.emplace_back(chunk, started);
+        } catch (...) {
+            break;
+        }
+    }
+    for (int t = started; t < nt; ++t) chunk(t);
     for (auto& x : th) x.join();
 }
 
