@@ -250,10 +250,11 @@ int mlf_solve_times(mlf_ctx* ctx, double* out4);
 /* Autotuner for batched solves: times the FP32 operator on each candidate
  * block of right-hand sides (candidates[ncand], 1..4096) with each
  * multi-column engine -- both box-block GEMM engines at the tile widths 8, 32
- * and 64 columns, and the warp engine -- and returns the smallest block whose
- * time per right-hand side is within 5 % of the best, with its tile width (0
- * for a single column or the warp engine) and engine (best_engine, optional:
- * 1 tensor cores, 0 FP32 FMA, 2 or 3 warp engine); both are kept for later
+ * and 64 columns, the warp engine and the tcgen05 near field -- and returns
+ * the smallest block whose time per right-hand side is within 5 % of the
+ * best, with its tile width (0 for a single column or the warp engine) and
+ * engine (best_engine, optional: 1 tensor cores (mma.sync), 0 FP32 FMA, 2 or
+ * 3 warp engine, 4 tensor cores (tcgen05)); both are kept for later
  * operator and preconditioner calls.
  * per_rhs_ms (optional, ncand) receives the best time per right-hand side of
  * each candidate.  No counterpart in the reference. */

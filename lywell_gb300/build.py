@@ -21,7 +21,7 @@ OUT = os.path.join(OUT_DIR, "liblywell_mlfma.so")
 OBJ_DIR = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["mlf_setup.cpp", "mlf_device.cu", "mlf_solver.cu", "mlf_capi.cu", "mlf_noalloc.cu", "mlf_precond.cu", "mlf_mixed.cu", "mlf_sweep.cu", "mlf_nearblk.cu", "mlf_nearwarp.cu", "mlf_autotune.cu", "mlf_mlp.cu", "mlf_learned.cu", "mlf_mom.cu"]
+SOURCES = ["mlf_setup.cpp", "mlf_device.cu", "mlf_solver.cu", "mlf_capi.cu", "mlf_noalloc.cu", "mlf_precond.cu", "mlf_mixed.cu", "mlf_sweep.cu", "mlf_nearblk.cu", "mlf_nearwarp.cu", "mlf_autotune.cu", "mlf_mlp.cu", "mlf_learned.cu", "mlf_mom.cu", "mlf_tc.cu"]
 
 
 def _nvcc():
@@ -34,7 +34,7 @@ def _nvcc():
 def _compile(src: str) -> str:
     obj = os.path.join(OBJ_DIR, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
-    deps = [path, os.path.join(CSRC, "mlf_internal.h"),
+    deps = [path, os.path.join(CSRC, "mlf_internal.h"), os.path.join(CSRC, "mlf_tcgen05.h"),
             os.path.join(os.path.dirname(HERE), "include", "lywell_mlfma.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj

@@ -2,9 +2,10 @@
 //
 // For each candidate number of right-hand sides per block B, each
 // multi-column engine -- the box-block GEMMs (tensor-core mma.sync 3xTF32 or
-// FP32 FMA) at each tile width (8, 32 or 64 columns), and the warp-per-basis
-// engine -- one FP32 operator application on B random columns is timed with
-// CUDA events (two warm-up calls, three timed).
+// FP32 FMA) at each tile width (8, 32 or 64 columns), the warp-per-basis
+// engine, and the box blocks with the near field on tcgen05 -- one FP32
+// operator application on B random columns is timed with CUDA events (two
+// warm-up calls, three timed).
 // The choice minimises operator time per right-hand side; a smaller block is
 // kept when it is within 5 % of the best (it retires columns sooner and holds
 // a smaller Krylov basis).  No counterpart in the reference, whose monostatic
@@ -58,9 +59,9 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
         const int B = cand[q];
         double tq = 1e300;
         const int widths[3] = {8, 32, 64};
-        for (int var = 0; var < 8 && !st; ++var) {
-            // tensor-core box blocks, FP32 FMA box blocks (three widths each), then the warp
-            // engine with its per-box and its per-basis receive
+        for (int var = 0; var < 9 && !st; ++var) {
+            // mma.sync box blocks, FP32 FMA box blocks (three widths each), the warp engine
+            // with its per-box and its per-basis receive, then the tcgen05 near field
             const int wv = var % 3, eng = var >= 6 ? var - 4 : 1 - var / 3;
             if (B == 1 && var) break;   // one column uses the CSR kernels
             if (eng < 2 && wv > 0 && widths[wv - 1] >= B) continue;   // a narrower tile already covers the block
@@ -73,6 +74,7 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
             cudaEventRecord(e1, s);
             if (st) break;
             if (!cuda_ok(c, cudaEventSynchronize(e1), "autotune")) { st = MLF_E_CUDA; break; }
+            if (eng == 4 && (st = tc_check(c))) break;
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             const double t = ms / 3.0 / B;
@@ -106,7 +108,7 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
 using namespace mlf;
 
 extern "C" int mlf_set_block_engine(mlf_ctx* h, int engine, int cols) {
-    if (!h || engine < -1 || engine > 3 || (cols != 0 && cols != 8 && cols != 32 && cols != 64)) return MLF_E_ARG;
+    if (!h || engine < -1 || engine > 4 || (cols != 0 && cols != 8 && cols != 32 && cols != 64)) return MLF_E_ARG;
     h->c.blk_engine = engine;
     h->c.blk_cols = cols;
     return MLF_OK;

@@ -371,7 +371,7 @@ int mlf_matvec32(mlf_ctx* h, const double* x, double* y, int nrhs, int ld) {
     if ((st = device_matvec32(c, c->dx_io, c->dy_io, nrhs, c->N, c->stream))) return st;
     if ((st = d2h_cols(c, y, c->dy_io, nrhs, ld))) return st;
     CK(cudaStreamSynchronize(c->stream));
-    return MLF_OK;
+    return blk_engine_of(c) == 4 ? tc_check(c) : MLF_OK;
 }
 
 int mlf_cgs_history(mlf_ctx* h, int col, double* hist, int cap, int* n) {

@@ -16,6 +16,8 @@
 
 namespace mlf {
 
+struct TcState;   // tensor-core near-field engine (mlf_tc.cu)
+
 // Device allocations of one call, released when the call returns (error
 // returns included).
 struct DevScope {
@@ -145,7 +147,9 @@ struct Ctx {
     int blk_cols = 0;                 // box-block tile width: 0 = by nrhs, else 8, 32 or 64 (autotuner)
     int blk_engine = -1;              // multi-column engine: 0 box-block FP32 FMA, 1 box-block mma.sync
                                       // 3xTF32, 2 warp per basis with a per-box receive, 3 warp per basis
-                                      // throughout; -1 by mean leaf-box size (autotuner)
+                                      // throughout, 4 box blocks with the near field on tcgen05 (3xTF32,
+                                      // TMEM accumulators) and the rest as 1; -1 by mean leaf-box size
+    TcState* tc = nullptr;            // engine 4's operand layouts and tensor maps, built on first use
     int* djas = nullptr;              // near CSR columns as box-sorted positions (warp engine)
     float2* dZblk = nullptr;
     long long* dblk_off = nullptr;
@@ -253,6 +257,12 @@ void near_blocks_free(Ctx* c);
 // warp engine (mlf_nearwarp.cu): one warp per basis, for small leaf boxes
 void warp_engine_free(Ctx* c);
 int blk_engine_of(const Ctx* c);   // the engine in force (resolves -1)
+inline bool warp_engine(int e) { return e == 2 || e == 3; }
+// tensor-core engine (mlf_tc.cu)
+int device_blocks_ready(Ctx* c);   // box-pair blocks of the near field built
+int device_near_tc(Ctx* c, const float2* xs, int ld, int nrhs, double2* y, cudaStream_t s);
+int tc_check(Ctx* c);              // MLF_E_CUDA if a tensor-core CTA gave up a wait since the last check
+void tc_free(Ctx* c);
 int device_agg_warp32(Ctx* c, const float2* R, int K, const float2* xs, int nrhs, float2* C, cudaStream_t s);
 int device_recv_near_warp32(Ctx* c, const float2* R, int K, const float2* A, float facy, const float2* xs, int nrhs,
                             int ld, double2* y, cudaStream_t s);

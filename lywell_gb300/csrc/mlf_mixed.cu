@@ -374,7 +374,7 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
         // blocks of columns: box-sorted row-major copy, then per-box GEMMs
         // (or one warp per basis for small boxes)
         if ((st = device_blk_pack(c, x, x32, ld, nrhs, c->m32.xT, s))) return st;
-        st = blk_engine_of(c) >= 2 ? device_agg_warp32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s)
+        st = warp_engine(blk_engine_of(c)) ? device_agg_warp32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s)
                                    : device_agg_blocks32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s);
         if (st) return st;
     }
@@ -447,13 +447,15 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
             k32_receive_near<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
                 leaf.K, c->N, nrhs, ld, c->dperm, c->dbox_of_sorted, c->m32.R, (nl == 3 ? c->m32.lv[nl].B : c->m32.lv[nl].A), c->dia, c->dja,
                 c->dZ, xf, facy, y);
-        } else if (blk_engine_of(c) >= 2) {
+        } else if (warp_engine(blk_engine_of(c))) {
             if ((st = device_recv_near_warp32(c, c->m32.R, leaf.K, (nl == 3 ? c->m32.lv[nl].B : c->m32.lv[nl].A), facy,
                                               c->m32.xT, nrhs, ld, y, s)))
                 return st;
         } else {
             if ((st = device_recv_blocks32(c, c->m32.R, leaf.K, (nl == 3 ? c->m32.lv[nl].B : c->m32.lv[nl].A), facy, nrhs, ld, y, s))) return st;
-            if ((st = device_near_blocks32(c, c->m32.xT, ld, nrhs, y, s))) return st;
+            st = blk_engine_of(c) == 4 ? device_near_tc(c, c->m32.xT, ld, nrhs, y, s)
+                                       : device_near_blocks32(c, c->m32.xT, ld, nrhs, y, s);
+            if (st) return st;
         }
     }
     if (prof) cudaEventRecord(c->ev[5], s);
@@ -1008,6 +1010,7 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
     for (int col = 0; col < nrhs; ++col)
         if (!done[col]) status[col] = MLF_CGS_MAXIT;
     *outer = k;
+    if (!st && blk_engine_of(c) == 4) st = tc_check(c);
     if (prof) {
         cudaStreamSynchronize(s);
         c->solve_ms[3] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();

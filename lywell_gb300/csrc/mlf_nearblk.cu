@@ -516,7 +516,7 @@ static int blk_width(const Ctx* c, int nrhs) {
 template <class F>
 static void blk_dispatch(const Ctx* c, int nrhs, F f) {
     const int w = blk_width(c, nrhs);
-    if (blk_engine_of(c) != 0) {   // the mma.sync engine also stands in when the warp engine is set
+    if (blk_engine_of(c) != 0) {   // the mma.sync engine also stands in for the warp and tensor-core engines
         if (w == 8) f(std::integral_constant<int, 1>(), MmaAcc<1>());
         else if (w == 32) f(std::integral_constant<int, 4>(), MmaAcc<4>());
         else f(std::integral_constant<int, 8>(), MmaAcc<8>());
@@ -615,7 +615,10 @@ int device_own_blocks32(Ctx* c, const long long* boff, const float2* M, const fl
     return cuda_ok(c, cudaGetLastError(), "own-box blocks") ? MLF_OK : MLF_E_CUDA;
 }
 
+int device_blocks_ready(Ctx* c) { return near_blocks_setup(c); }
+
 void near_blocks_free(Ctx* c) {
+    tc_free(c);
     auto F = [](void* p) { if (p) cudaFree(p); };
     F(c->dZblk); F(c->dblk_off); F(c->dnbox_ptr); F(c->dnbox_list); F(c->dblk_tiles); F(c->dblk_entry);
     F(c->dMinvblk);

@@ -293,7 +293,7 @@ int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStr
         }
         int st;
         if ((st = device_blk_pack(c, nullptr, y, c->N, nrhs, c->dpre_xs, s))) return st;
-        if (blk_engine_of(c) >= 2) return device_own_warp32(c, c->dboff, c->dMinv32, c->dpre_xs, nrhs, x, s);
+        if (warp_engine(blk_engine_of(c))) return device_own_warp32(c, c->dboff, c->dMinv32, c->dpre_xs, nrhs, x, s);
         return device_own_blocks32(c, c->dboff, c->dMinv32, c->dpre_xs, nrhs, x, s);
     }
     if (!c->nearinv_own && nrhs > 1) {
@@ -306,7 +306,7 @@ int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStr
             c->pre_xs_cap = need;
         }
         int st;
-        if (blk_engine_of(c) >= 2) {   // one warp per basis on the CSR values
+        if (warp_engine(blk_engine_of(c))) {   // one warp per basis on the CSR values
             if ((st = device_blk_pack(c, nullptr, y, c->N, nrhs, c->dpre_xs, s))) return st;
             return device_near_pattern_warp32(c, c->dMinv32, c->dpre_xs, nrhs, x, s);
         }

@@ -1,0 +1,470 @@
+// Near-field box-pair GEMMs of the FP32 operator on the fifth-generation
+// tensor cores (block engine 4): tcgen05.mma with TMEM accumulators, operands
+// staged into shared memory by TMA (cp.async.bulk.tensor) through tensor maps
+// over this GPU's own memory, 3xTF32 for FP32 accuracy.
+//
+// The near matrix (llenarZesparcida, modMLFMA.f90:1594-1634) is a union of
+// dense box-pair blocks Z_ij (bases of leaf box i x bases of near box j).  For
+// a block of right-hand sides, leaf box i needs Y_i = sum_j Z_ij X_j.  Here it
+// is computed transposed, as a real GEMM whose M side is the right-hand sides:
+//   D (2 nrhs x n_i) = A (2 nrhs x 2 n_j) * B^T,   B = [Zr Zi] interleaved
+// with the complex product written as a real one on the contraction side:
+//   A row 2c   = [ Xr(t,c), -Xi(t,c) ]_t   -> D row 2c   = Re Y(:, c)
+//   A row 2c+1 = [ Xi(t,c),  Xr(t,c) ]_t   -> D row 2c+1 = Im Y(:, c)
+//   B row p    = [ Zr(p,t),  Zi(p,t) ]_t   (the complex(4) row of Z, as stored)
+// so that M = 128 covers 64 right-hand sides exactly and N = the box's bases
+// (padded to 16), with no padding of the rows to 128.
+//
+// Layouts in HBM (built once per context; the X operand once per call):
+//   Z operand: per block e = (i, j) and chunk kc of 16 columns t, the n_i
+//     rows p of 32 floats [re, im] x 16 (zero past n_j), rows of all blocks
+//     and chunks stacked: one 2-D tensor map [rows][32 floats], boxes of 32
+//     rows; split into TF32 hi and lo copies.
+//   X operand: per column tile of 64 right-hand sides, per box j and chunk kc,
+//     128 rows of 32 floats as above, hi and lo; one tensor map, boxes of 128
+//     rows.
+// Each TMA box is written with 128-byte swizzling, which is the canonical
+// K-major SWIZZLE_128B layout tcgen05.mma reads (8-row atoms of 1024 bytes).
+//
+// One CTA (4 warps) per (tile of at most 256 rows of box i, 64 columns).
+// Thread 0 issues the TMA loads of a 2-stage ring and the MMAs: per chunk of
+// 32 real K, 4 K-steps x 3 products (A_lo B_hi, A_hi B_lo, A_hi B_hi) into a
+// 128 x N FP32 accumulator in TMEM; tcgen05.commit frees a stage when its MMAs
+// are done.  The four warps then read their 32 TMEM lanes each (tcgen05.ld),
+// pair the real and imaginary rows with one shuffle and add into y.
+//
+// Every wait on an mbarrier is bounded; on a timeout the CTA records an error
+// flag, lets its loads in flight land, frees its TMEM and skips the output.
+// The host checks the flag after the solve (tc_check).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "mlf_internal.h"
+#include "mlf_tcgen05.h"
+
+namespace mlf {
+
+#define CK(call)                                             \
+    do {                                                     \
+        if (!cuda_ok(c, (call), #call)) return MLF_E_CUDA;   \
+    } while (0)
+
+constexpr int TC_STAGES = 2;
+constexpr int TC_ROWS = 256;                 // bases of box i per tile (MMA N <= 256)
+constexpr int TC_KCH = 16;                   // complex contraction values per chunk (128-byte rows)
+constexpr int TC_COLS = 64;                  // right-hand sides per column tile (MMA M = 128)
+constexpr int TC_ZBOX = 32;                  // rows per TMA box of the Z operand
+constexpr int TC_ABYTES = 128 * 128;         // one A tile: 128 rows x 128 bytes
+constexpr int TC_BBYTES = TC_ROWS * 128;     // one B tile at most
+constexpr int TC_STAGE_BYTES = 2 * TC_ABYTES + 2 * TC_BBYTES;
+constexpr size_t TC_SMEM = (size_t)TC_STAGES * TC_STAGE_BYTES + 1024;   // + alignment of the ring
+constexpr uint32_t TC_TMEM_COLS = 256;
+constexpr uint32_t TC_SPIN = 1u << 20;       // mbarrier polls before a wait gives up
+
+struct TcOperand {
+    float* hi = nullptr;
+    float* lo = nullptr;
+    CUtensorMap mhi, mlo;
+};
+
+struct TcState {
+    int ntiles = 0, nchunk = 0;     // tiles of the near GEMM; chunks of 16 bases over all boxes
+    long long zrows = 0;            // rows of the Z-operand layout
+    int4* dtiles = nullptr;         // (box, first row, rows, instruction descriptor)
+    int* dzrow = nullptr;           // per block entry e: first Z-operand row (chunk 0)
+    int* dcbase = nullptr;          // per box: its first chunk
+    int2* dchunk = nullptr;         // per chunk: (first box-sorted position, bases in it)
+    int* derr = nullptr;            // set by a CTA whose wait gave up
+    TcOperand Z;
+    float *xhi = nullptr, *xlo = nullptr;
+    long long xrows_cap = 0;
+    CUtensorMap mxhi, mxlo;
+};
+
+// ---------------------------------------------------------------------------
+// operand layouts
+// ---------------------------------------------------------------------------
+
+// Z operand of block entry e (one CTA each) from the box-pair blocks (column-
+// major n_i x n_j at blk_off[e]): row zrow[e] + kc n_i + p holds
+// Z(p, 16 kc + u), u = 0..15, as (re, im) pairs, split into TF32 hi and lo.
+__global__ void k_tc_fill_z(const int* __restrict__ entry_box, const int* __restrict__ nbox_list,
+                            const long long* __restrict__ blk_off, const int* __restrict__ box_ptr,
+                            const int* __restrict__ zrow, const float2* __restrict__ blk, float* __restrict__ zhi,
+                            float* __restrict__ zlo) {
+    const int e = blockIdx.x;
+    const int i = entry_box[e], j = nbox_list[e];
+    const int ni = box_ptr[i + 1] - box_ptr[i], nj = box_ptr[j + 1] - box_ptr[j];
+    const int nkc = (nj + TC_KCH - 1) / TC_KCH;
+    const float2* src = blk + blk_off[e];
+    const size_t base = (size_t)zrow[e] * 32;
+    for (int q = threadIdx.x; q < nkc * ni * TC_KCH; q += blockDim.x) {
+        const int u = q % TC_KCH, rp = q / TC_KCH;     // rp = kc n_i + p
+        const int kc = rp / ni, p = rp - kc * ni;
+        const int t = kc * TC_KCH + u;
+        const float2 v = t < nj ? src[(size_t)t * ni + p] : make_float2(0.f, 0.f);
+        const float hr = tc::tf32_rna(v.x), hi_ = tc::tf32_rna(v.y);
+        const size_t o = base + (size_t)rp * 32 + 2 * u;
+        zhi[o] = hr;
+        zhi[o + 1] = hi_;
+        zlo[o] = tc::tf32_rna(v.x - hr);
+        zlo[o + 1] = tc::tf32_rna(v.y - hi_);
+    }
+}
+
+// X operand of one (column tile, chunk) per CTA from xs (box-sorted rows,
+// row-major N x nrhs): rows 2c and 2c+1 of the chunk's 128 as in the header.
+__global__ void __launch_bounds__(256) k_tc_pack_x(int nchunk, int nrhs, const int2* __restrict__ chunk,
+                                                   const float2* __restrict__ xs, float* __restrict__ xhi,
+                                                   float* __restrict__ xlo) {
+    __shared__ float2 xsm[TC_KCH][TC_COLS + 1];
+    const int ch = blockIdx.x, ct = blockIdx.y;
+    const int2 cd = chunk[ch];
+    for (int q = threadIdx.x; q < TC_KCH * TC_COLS; q += blockDim.x) {
+        const int u = q / TC_COLS, cl = q - u * TC_COLS, col = ct * TC_COLS + cl;
+        xsm[u][cl] = (u < cd.y && col < nrhs) ? xs[(size_t)(cd.x + u) * nrhs + col] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const size_t base = ((size_t)ct * nchunk + ch) * 128 * 32;
+    for (int q = threadIdx.x; q < 128 * TC_KCH; q += blockDim.x) {
+        const int row = q / TC_KCH, u = q - row * TC_KCH;
+        const float2 v = xsm[u][row >> 1];
+        const float a = (row & 1) ? v.y : v.x, b = (row & 1) ? v.x : -v.y;
+        const float ha = tc::tf32_rna(a), hb = tc::tf32_rna(b);
+        const size_t o = base + (size_t)row * 32 + 2 * u;
+        *reinterpret_cast<float2*>(xhi + o) = make_float2(ha, hb);
+        *reinterpret_cast<float2*>(xlo + o) = make_float2(tc::tf32_rna(a - ha), tc::tf32_rna(b - hb));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the GEMM
+// ---------------------------------------------------------------------------
+
+// OUT = 0: y (FP64 columns, ld) += Z X;  OUT = 1: out32 (FP32 columns, ld) = Z X
+template <int OUT>
+__global__ void __launch_bounds__(128, 1)
+    k_tc_near(const __grid_constant__ CUtensorMap mzhi, const __grid_constant__ CUtensorMap mzlo,
+              const __grid_constant__ CUtensorMap mxhi, const __grid_constant__ CUtensorMap mxlo,
+              const int4* __restrict__ tiles, const int* __restrict__ box_ptr, const int* __restrict__ nbox_ptr,
+              const int* __restrict__ nbox_list, const int* __restrict__ zrow, const int* __restrict__ cbase,
+              int nchunk, int nrhs, int ld, const int* __restrict__ perm, double2* __restrict__ y,
+              float2* __restrict__ out32, int* __restrict__ err) {
+    extern __shared__ unsigned char tc_raw[];
+    __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int skip;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t raw = tc::smem_u32(tc_raw);
+    unsigned char* ring = tc_raw + (((raw + 1023u) & ~1023u) - raw);   // 1024-aligned swizzle atoms
+    const int4 tl = tiles[blockIdx.x];
+    const int i = tl.x, r0 = tl.y, nrow = tl.z;
+    const uint32_t idesc = (uint32_t)tl.w;
+    const int ct = blockIdx.y;
+    const int i0 = box_ptr[i], ni = box_ptr[i + 1] - i0;
+    const int e_beg = nbox_ptr[i], e_end = nbox_ptr[i + 1];
+    if (tid == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(&done, 1);
+        skip = 0;
+        tc::fence_barrier_init();
+        tc::tma_prefetch_desc(&mzhi);
+        tc::tma_prefetch_desc(&mzlo);
+        tc::tma_prefetch_desc(&mxhi);
+        tc::tma_prefetch_desc(&mxlo);
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tmem_base, TC_TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    tc::tc_fence_after_sync();
+    const uint32_t tmem = tmem_base;
+
+    if (tid == 0) {
+        const int nB = (nrow + TC_ZBOX - 1) / TC_ZBOX * TC_ZBOX;          // B rows staged
+        const uint32_t bytes = 2u * TC_ABYTES + 2u * (uint32_t)nB * 128u;
+        int nch = 0;
+        for (int e = e_beg; e < e_end; ++e) {
+            const int j = nbox_list[e];
+            nch += (box_ptr[j + 1] - box_ptr[j] + TC_KCH - 1) / TC_KCH;
+        }
+        int le = e_beg, lkc = 0, issued = 0, consumed = 0;
+        bool ok = true;
+        // once any CTA has given up a wait, the rest skip their work (the call fails anyway)
+        if (*reinterpret_cast<volatile int*>(err)) nch = 0;
+        for (int cI = 0; cI < nch + TC_STAGES - 1 && nch > 0; ++cI) {
+            if (cI < nch) {   // load chunk cI into stage cI % STAGES once its previous MMAs are done
+                const int s = cI % TC_STAGES;
+                if (cI >= TC_STAGES && !tc::mbar_wait(&empty[s], ((cI / TC_STAGES) - 1) & 1, TC_SPIN)) {
+                    ok = false;
+                    break;
+                }
+                unsigned char* st = ring + (size_t)s * TC_STAGE_BYTES;
+                tc::mbar_arrive_expect_tx(&full[s], bytes);
+                const int j = nbox_list[le];
+                const int nj = box_ptr[j + 1] - box_ptr[j];
+                const int xr = (ct * nchunk + cbase[j] + lkc) * 128;
+                tc::tma_load_2d(st, &mxhi, 0, xr, &full[s]);
+                tc::tma_load_2d(st + TC_ABYTES, &mxlo, 0, xr, &full[s]);
+                const int zr = zrow[le] + lkc * ni + r0;
+                for (int q = 0; q < nB; q += TC_ZBOX) {
+                    tc::tma_load_2d(st + 2 * TC_ABYTES + q * 128, &mzhi, 0, zr + q, &full[s]);
+                    tc::tma_load_2d(st + 2 * TC_ABYTES + TC_BBYTES + q * 128, &mzlo, 0, zr + q, &full[s]);
+                }
+                ++issued;
+                if (++lkc * TC_KCH >= nj) {
+                    lkc = 0;
+                    ++le;
+                }
+            }
+            const int cc = cI - (TC_STAGES - 1);
+            if (cc >= 0) {    // the MMAs of chunk cc
+                const int s = cc % TC_STAGES;
+                if (!tc::mbar_wait(&full[s], (cc / TC_STAGES) & 1, TC_SPIN)) {
+                    ok = false;
+                    break;
+                }
+                ++consumed;
+                tc::tc_fence_after_sync();
+                const uint32_t a = tc::smem_u32(ring + (size_t)s * TC_STAGE_BYTES);
+                const uint32_t ahi = a, alo = a + TC_ABYTES, bhi = a + 2 * TC_ABYTES, blo = bhi + TC_BBYTES;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {   // K steps of 8 TF32 = 32 bytes of the 128-byte rows
+                    const uint32_t ko = 32u * q;
+                    tc::mma_tf32(tmem, tc::kmajor_sw128_desc(alo + ko), tc::kmajor_sw128_desc(bhi + ko), idesc,
+                                 (cc | q) != 0);
+                    tc::mma_tf32(tmem, tc::kmajor_sw128_desc(ahi + ko), tc::kmajor_sw128_desc(blo + ko), idesc, 1);
+                    tc::mma_tf32(tmem, tc::kmajor_sw128_desc(ahi + ko), tc::kmajor_sw128_desc(bhi + ko), idesc, 1);
+                }
+                tc::mma_commit(&empty[s]);
+            }
+        }
+        tc::mma_commit(&done);   // every MMA issued above
+        if (!tc::mbar_wait(&done, 0, TC_SPIN)) ok = false;
+        if (!ok) {
+            // loads still in flight land before the shared memory is given up
+            for (int k = consumed; k < issued; ++k)
+                tc::mbar_wait(&full[k % TC_STAGES], (k / TC_STAGES) & 1, TC_SPIN);
+            atomicExch(err, 1);
+        }
+        skip = (!ok || nch == 0) ? 1 : 0;
+    }
+    __syncthreads();
+    tc::tc_fence_after_sync();
+    if (!skip) {
+        const int m = 32 * warp + lane;                 // D row = TMEM lane
+        const int col = ct * TC_COLS + (m >> 1);
+        const bool writer = (lane & 1) == 0 && col < nrhs;
+        for (int n0 = 0; n0 < nrow; n0 += 32) {
+            float v[32];
+            tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)n0, v);
+#pragma unroll
+            for (int u = 0; u < 32; ++u) {
+                const float im = __shfl_xor_sync(0xffffffffu, v[u], 1);
+                const int p = n0 + u;
+                if (writer && p < nrow) {
+                    const int g = perm[i0 + r0 + p];
+                    if (OUT == 0) {
+                        double2* yp = y + (size_t)col * ld + g;
+                        const double2 o = *yp;
+                        *yp = make_double2(o.x + (double)v[u], o.y + (double)im);
+                    } else {
+                        out32[(size_t)col * ld + g] = make_float2(v[u], im);
+                    }
+                }
+            }
+        }
+    }
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder(Ctx* c) {
+    static std::mutex mu;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p) {
+            c->err = "cuTensorMapEncodeTiled is not available from the driver";
+            return nullptr;
+        }
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 2-D map over rows of 32 floats (128 bytes), boxes of 32 floats x box_rows,
+// 128-byte swizzle, zero fill past the last row
+int make_rows_map(Ctx* c, CUtensorMap* m, const float* base, long long rows, int box_rows) {
+    auto enc = tensor_map_encoder(c);
+    if (!enc) return MLF_E_CUDA;
+    const cuuint64_t dims[2] = {32, (cuuint64_t)std::max<long long>(rows, 1)};
+    const cuuint64_t strides[1] = {128};
+    const cuuint32_t box[2] = {32, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        c->err = "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")";
+        return MLF_E_CUDA;
+    }
+    return MLF_OK;
+}
+
+}  // namespace
+
+void tc_free(Ctx* c) {
+    TcState* t = c->tc;
+    if (!t) return;
+    auto F = [](void* p) { if (p) cudaFree(p); };
+    F(t->dtiles); F(t->dzrow); F(t->dcbase); F(t->dchunk); F(t->derr);
+    F(t->Z.hi); F(t->Z.lo); F(t->xhi); F(t->xlo);
+    delete t;
+    c->tc = nullptr;
+}
+
+// tiles, chunk tables and the Z operand (needs the box-pair blocks)
+static int tc_setup(Ctx* c) {
+    if (c->tc) return MLF_OK;
+    int st;
+    if ((st = device_blocks_ready(c))) return st;
+    const int nb = (int)c->box_ptr.size() - 1;
+    const int ne = c->nbox_ptr[nb];
+    std::vector<int4> tiles;
+    for (int i = 0; i < nb; ++i) {
+        const int ni = c->box_ptr[i + 1] - c->box_ptr[i];
+        if (ni <= 0) continue;
+        const int nt = (ni + TC_ROWS - 1) / TC_ROWS;
+        const int per = ((ni + nt - 1) / nt + 15) / 16 * 16;   // rows per tile, multiple of 16
+        for (int r0 = 0; r0 < ni; r0 += per) {
+            const int nrow = std::min(per, ni - r0);
+            const int N = (nrow + 15) / 16 * 16;
+            if (!tc::valid_shape(128, N)) {
+                c->err = "tensor-core near field: invalid tile shape";
+                return MLF_E_STATE;
+            }
+            tiles.push_back(make_int4(i, r0, nrow, (int)tc::instr_desc_f32acc(tc::FMT_TF32, 128, N)));
+        }
+    }
+    std::vector<int> cbase(nb + 1, 0);
+    std::vector<int2> chunk;
+    for (int j = 0; j < nb; ++j) {
+        const int j0 = c->box_ptr[j], nj = c->box_ptr[j + 1] - j0;
+        cbase[j] = (int)chunk.size();
+        for (int kc = 0; kc * TC_KCH < nj; ++kc) chunk.push_back(make_int2(j0 + kc * TC_KCH, std::min(TC_KCH, nj - kc * TC_KCH)));
+    }
+    cbase[nb] = (int)chunk.size();
+    std::vector<int> zrow(std::max(ne, 1), 0);
+    long long rows = 0;
+    for (int i = 0; i < nb; ++i) {
+        const int ni = c->box_ptr[i + 1] - c->box_ptr[i];
+        for (int e = c->nbox_ptr[i]; e < c->nbox_ptr[i + 1]; ++e) {
+            const int j = c->nbox_list[e];
+            zrow[e] = (int)rows;
+            rows += (long long)ni * ((c->box_ptr[j + 1] - c->box_ptr[j] + TC_KCH - 1) / TC_KCH);
+        }
+    }
+    if (rows >= (1LL << 31) - TC_ROWS || (long long)chunk.size() * 2 * 128 >= (1LL << 31)) {
+        c->err = "tensor-core near field: operand layout exceeds 2^31 rows";
+        return MLF_E_STATE;
+    }
+    TcState* t = new TcState();
+    c->tc = t;
+    t->ntiles = (int)tiles.size();
+    t->nchunk = (int)chunk.size();
+    t->zrows = rows;
+    CK(cudaMalloc(&t->dtiles, std::max<size_t>(tiles.size(), 1) * sizeof(int4)));
+    CK(cudaMalloc(&t->dzrow, zrow.size() * sizeof(int)));
+    CK(cudaMalloc(&t->dcbase, cbase.size() * sizeof(int)));
+    CK(cudaMalloc(&t->dchunk, std::max<size_t>(chunk.size(), 1) * sizeof(int2)));
+    CK(cudaMalloc(&t->derr, sizeof(int)));
+    CK(cudaMemcpy(t->dtiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(t->dzrow, zrow.data(), zrow.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(t->dcbase, cbase.data(), cbase.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(t->dchunk, chunk.data(), chunk.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    CK(cudaMemset(t->derr, 0, sizeof(int)));
+    const size_t zfl = (size_t)std::max<long long>(rows, 1) * 32;
+    CK(cudaMalloc(&t->Z.hi, zfl * sizeof(float)));
+    CK(cudaMalloc(&t->Z.lo, zfl * sizeof(float)));
+    if (ne)
+        k_tc_fill_z<<<ne, 256, 0, c->stream>>>(c->dblk_entry, c->dnbox_list, c->dblk_off, c->dbox_ptr, t->dzrow,
+                                               c->dZblk, t->Z.hi, t->Z.lo);
+    CK(cudaGetLastError());
+    if ((st = make_rows_map(c, &t->Z.mhi, t->Z.hi, rows, TC_ZBOX))) return st;
+    if ((st = make_rows_map(c, &t->Z.mlo, t->Z.lo, rows, TC_ZBOX))) return st;
+    CK(cudaFuncSetAttribute(k_tc_near<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+    CK(cudaFuncSetAttribute(k_tc_near<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+    CK(cudaStreamSynchronize(c->stream));
+    return MLF_OK;
+}
+
+// X operand buffers for nrhs columns (grown on demand; maps re-encoded)
+static int tc_x_buffers(Ctx* c, int nrhs) {
+    TcState* t = c->tc;
+    const int nct = (nrhs + TC_COLS - 1) / TC_COLS;
+    const long long rows = (long long)nct * t->nchunk * 128;
+    if (rows <= t->xrows_cap) return MLF_OK;
+    if (t->xhi) cudaFree(t->xhi);
+    if (t->xlo) cudaFree(t->xlo);
+    t->xhi = t->xlo = nullptr;
+    t->xrows_cap = 0;
+    CK(cudaMalloc(&t->xhi, (size_t)rows * 32 * sizeof(float)));
+    CK(cudaMalloc(&t->xlo, (size_t)rows * 32 * sizeof(float)));
+    int st;
+    if ((st = make_rows_map(c, &t->mxhi, t->xhi, rows, 128))) return st;
+    if ((st = make_rows_map(c, &t->mxlo, t->xlo, rows, 128))) return st;
+    t->xrows_cap = rows;
+    return MLF_OK;
+}
+
+// y(:, 0:nrhs) += Z_near xs on the tensor cores (engine 4)
+int device_near_tc(Ctx* c, const float2* xs, int ld, int nrhs, double2* y, cudaStream_t s) {
+    int st;
+    if ((st = tc_setup(c))) return st;
+    if ((st = tc_x_buffers(c, nrhs))) return st;
+    TcState* t = c->tc;
+    const int nct = (nrhs + TC_COLS - 1) / TC_COLS;
+    k_tc_pack_x<<<dim3(t->nchunk, nct), 256, 0, s>>>(t->nchunk, nrhs, t->dchunk, xs, t->xhi, t->xlo);
+    k_tc_near<0><<<dim3(t->ntiles, nct), 128, TC_SMEM, s>>>(
+        t->Z.mhi, t->Z.mlo, t->mxhi, t->mxlo, t->dtiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, t->dzrow,
+        t->dcbase, t->nchunk, nrhs, ld, c->dperm, y, nullptr, t->derr);
+    return cuda_ok(c, cudaGetLastError(), "tensor-core near field") ? MLF_OK : MLF_E_CUDA;
+}
+
+// error flag of the tensor-core kernels since the last check (0: none)
+int tc_check(Ctx* c) {
+    TcState* t = c->tc;
+    if (!t) return MLF_OK;
+    int h = 0;
+    CK(cudaMemcpy(&h, t->derr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        CK(cudaMemset(t->derr, 0, sizeof(int)));
+        c->err = "tensor-core near field: an mbarrier wait gave up (output skipped)";
+        return MLF_E_CUDA;
+    }
+    return MLF_OK;
+}
+
+}  // namespace mlf

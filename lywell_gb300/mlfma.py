@@ -337,9 +337,11 @@ class MLFMA:
 
     def set_block_engine(self, engine: int, cols: int = 0):
         """Multi-column engine of the batched FP32 operator and preconditioner:
-        1 box blocks on tensor cores (3xTF32), 0 box blocks on FP32 FMA, 2 warp
-        per basis (receive per box), 3 warp per basis throughout, -1 by
-        leaf-box size; tile width cols 8, 32, 64 (0: by block width)."""
+        1 box blocks on tensor cores (3xTF32 mma.sync), 0 box blocks on FP32
+        FMA, 2 warp per basis (receive per box), 3 warp per basis throughout,
+        4 box blocks with the near field on tcgen05 (3xTF32, TMEM
+        accumulators, TMA-staged operands), -1 by leaf-box size; tile width
+        cols 8, 32, 64 (0: by block width)."""
         _check(load().mlf_set_block_engine(self._h, int(engine), int(cols)), self._h)
 
     def autotune_block(self, candidates=(8, 16, 32, 64, 128)):
