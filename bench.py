@@ -296,51 +296,6 @@ def batched_rcs_sample(seq_angles=3, block=0, maxit=4000):
     return out
 
 
-def profile_fp32_block(nrhs, steps, engine=-1, cols=0, mesh="spheroid5"):
-    """Profiling aid (not the bench line): the FP32 operator on `nrhs` random
-    columns.  mesh "spheroid5": a 30720-RWG spheroid with the 122880-RWG
-    spheroid's mesh density (icosphere-5, semi-axes 1.5 x 0.375 x 0.375 lambda,
-    so ~145 bases per leaf box as in the 722-RHS workload) -- small enough for
-    multi-pass ncu; "sphere6": the 122880-RWG sphere of radius 6 lambda
-    (~11 bases per leaf box)."""
-    import ctypes
-    import torch
-    from lywell_gb300 import MLFMA, RWG, _capi, meshes
-
-    if mesh == "sphere6":
-        tris = meshes.icosphere(6, 6.0)
-    else:
-        tris = meshes.spheroid(5, (1.5, 0.375, 0.375), noise=0.005, seed=1234)
-    m = MLFMA(RWG(tris), lam=1.0, ladomax=0.25)
-    if engine >= 0 or cols:
-        m.set_block_engine(engine, cols)
-    lib = _capi.load()
-    X = torch.randn(nrhs, m.N, dtype=torch.complex128, device="cuda")
-    Y = torch.empty_like(X)
-    stream = torch.cuda.Stream()            # a real stream handle (the default stream's is 0)
-    torch.cuda.set_stream(stream)
-    s = stream.cuda_stream
-    call = lambda: lib.mlf_matvec32_device(m.handle, ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(Y.data_ptr()),
-                                           nrhs, m.N, ctypes.c_void_p(s))
-    for _ in range(2):
-        assert call() == 0
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(steps):
-        call()
-    e1.record()
-    torch.cuda.synchronize()
-    m.set_profiling(True)
-    call()
-    torch.cuda.synchronize()
-    stages = [float(v) for v in m.stage_times()]
-    m.set_profiling(False)
-    print(json.dumps({"profile": "fp32 operator", "stage_ms": stages, "N": m.N, "nrhs": nrhs, "near_nnz": m.nnz, "engine": engine, "cols": cols,
-                      "mesh": mesh, "ms_per_call": e0.elapsed_time(e1) / steps}), flush=True)
-    m.close()
-
-
 def learned_sample(steps=3000, seed=0):
     """Learned preconditioner: trained on three seeded superellipsoids
     (exponent U[2, 6], semi-axes (2, 1, 1) lambda x U[0.85, 1.15], 7680 RWG)
@@ -531,18 +486,9 @@ def main():
     ap.add_argument("--rcs-maxit", type=int, default=4000)
     ap.add_argument("--no-batched", action="store_true", help="skip the 722-RHS spheroid sweep sample")
     ap.add_argument("--learned", action="store_true", help="add the learned-preconditioner samples (about 6 min)")
-    ap.add_argument("--block-engine", type=int, default=-1, help="profiling aid: 1 tensor cores, 0 FP32 FMA, 2 warp per basis")
-    ap.add_argument("--block-cols", type=int, default=0, help="profiling aid: box-block tile width 8/32/64")
-    ap.add_argument("--profile-fp32-block", type=int, default=0,
-                    help="profiling aid: time the FP32 operator on this many columns of a small spheroid and exit")
-    ap.add_argument("--profile-mesh", default="spheroid5", choices=["spheroid5", "sphere6"])
     ap.add_argument("--seq-angles", type=int, default=3)
     ap.add_argument("--block", type=int, default=0, help="RHS per block of the batched sweep (0: autotuned)")
     args = ap.parse_args()
-    if args.profile_fp32_block > 0:
-        profile_fp32_block(args.profile_fp32_block, args.steps, args.block_engine, args.block_cols,
-                           args.profile_mesh)
-        return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, wl)
@@ -624,10 +570,11 @@ def main():
     total_tflops = cnt["flops_total"] / (t / args.steps * ws) / 1e12
     roof = {"bound": "fp64", "kernel": "k_translate (5 launches/matvec)", "achieved": achieved, "peak": fp64,
             "unit": "TFLOP/s", "frac": achieved / fp64,
-            # DRAM bytes of the stage's 5 launches in one matvec (ncu dram__bytes_read.sum +
-            # dram__bytes_write.sum on this workload, profiles/matvec_launches_sphere6_fp64.md)
             "traffic": (TRANSLATE6_DRAM_BYTES if wl is WORKLOADS["sphere6"] else None),
             "traffic_unit": "bytes per matvec (5 launches)",
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's launches in one "
+                               "matvec of this workload, from a separate capture of the same kernels (not "
+                               "measured in this run)" if wl is WORKLOADS["sphere6"] else None),
             "peak_source": "measured here: cuBLAS DGEMM 4096^3 (GB300 FP64 pipe)",
             "algorithmic_flops_per_matvec": tr_flops,
             "hbm": {"achieved_gbs": cnt["translation_bytes"] / tr_s / 1e9, "peak_gbs": hbm,

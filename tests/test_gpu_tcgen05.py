@@ -8,7 +8,9 @@ per 0.25 lambda leaf box), and the same body with 0.5 lambda leaf boxes
 
 Tolerances: the 3xTF32 products of both tensor-core engines drop the lo x lo
 term, so a batched column agrees with the other engine's to 5e-6 relative,
-and with the FP64 operator to the FP32 operator's 2e-5.
+and with the FP64 operator to the FP32 operator's own accuracy: 2e-5 with
+0.25 lambda leaves, 1e-4 with 0.5 lambda leaves (larger sampling grids and
+longer FP32 translation sums; measured 8e-5 with either engine).
 """
 import numpy as np
 import pytest
@@ -32,7 +34,7 @@ def spheroid(request, gpu_lib):
 
 @pytest.mark.parametrize("nrhs", [2, 64, 70, 128])
 def test_tc_engine_matches_mma_engine(spheroid, nrhs):
-    _, m = spheroid
+    side, m = spheroid
     rng = np.random.default_rng(100 + nrhs)
     X = rng.standard_normal((m.N, nrhs)) + 1j * rng.standard_normal((m.N, nrhs))
     m.set_block_engine(1)
@@ -46,7 +48,7 @@ def test_tc_engine_matches_mma_engine(spheroid, nrhs):
     print(f"nrhs {nrhs}: tcgen05 vs mma.sync worst column {worst:.2e}")
     assert worst < 5e-6
     for k in sorted({0, nrhs - 1}):
-        assert _rel(Y4[:, k], m.matvec(X[:, k])) < 2e-5
+        assert _rel(Y4[:, k], m.matvec(X[:, k])) < (2e-5 if side == 0.25 else 1e-4)
 
 
 def test_tc_engine_mixed_solve(spheroid):
