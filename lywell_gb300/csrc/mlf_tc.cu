@@ -26,12 +26,13 @@
 // Each TMA box is written with 128-byte swizzling, which is the canonical
 // K-major SWIZZLE_128B layout tcgen05.mma reads (8-row atoms of 1024 bytes).
 //
-// One CTA (4 warps) per (tile of at most 256 rows of box i, 64 columns).
-// Thread 0 issues the TMA loads of a 2-stage ring and the MMAs: per chunk of
-// 32 real K, 4 K-steps x 3 products (A_lo B_hi, A_hi B_lo, A_hi B_hi) into a
-// 128 x N FP32 accumulator in TMEM; tcgen05.commit frees a stage when its MMAs
-// are done.  The four warps then read their 32 TMEM lanes each (tcgen05.ld),
-// pair the real and imaginary rows with one shuffle and add into y.
+// One CTA (4 warps) per (tile of at most 160 rows of box i, 64 columns).
+// Thread 0 (warp 0) issues the TMA loads of a 3-stage ring; thread 32
+// (warp 1) issues the MMAs: per chunk of 32 real K, 4 K-steps x 3 products
+// (A_lo B_hi, A_hi B_lo, A_hi B_hi) into a 128 x N FP32 accumulator in TMEM,
+// and tcgen05.commit frees a stage once its MMAs are done.  The four warps
+// then read their 32 TMEM lanes each (tcgen05.ld), pair the real and
+// imaginary rows with one shuffle and add into y.
 //
 // Every wait on an mbarrier is bounded; on a timeout the CTA records an error
 // flag, lets its loads in flight land, frees its TMEM and skips the output.
@@ -54,8 +55,8 @@ namespace mlf {
         if (!cuda_ok(c, (call), #call)) return MLF_E_CUDA;   \
     } while (0)
 
-constexpr int TC_STAGES = 2;
-constexpr int TC_ROWS = 256;                 // bases of box i per tile (MMA N <= 256)
+constexpr int TC_STAGES = 3;
+constexpr int TC_ROWS = 160;                 // bases of box i per tile (MMA N <= 160 here)
 constexpr int TC_KCH = 16;                   // complex contraction values per chunk (128-byte rows)
 constexpr int TC_COLS = 64;                  // right-hand sides per column tile (MMA M = 128)
 constexpr int TC_ZBOX = 32;                  // rows per TMA box of the Z operand
@@ -158,7 +159,7 @@ __global__ void __launch_bounds__(128, 1)
     extern __shared__ unsigned char tc_raw[];
     __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], done;
     __shared__ uint32_t tmem_base;
-    __shared__ int skip;
+    __shared__ int nch_s, fail_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t raw = tc::smem_u32(tc_raw);
     unsigned char* ring = tc_raw + (((raw + 1023u) & ~1023u) - raw);   // 1024-aligned swizzle atoms
@@ -174,12 +175,16 @@ __global__ void __launch_bounds__(128, 1)
             tc::mbar_init(&empty[s], 1);
         }
         tc::mbar_init(&done, 1);
-        skip = 0;
         tc::fence_barrier_init();
-        tc::tma_prefetch_desc(&mzhi);
-        tc::tma_prefetch_desc(&mzlo);
-        tc::tma_prefetch_desc(&mxhi);
-        tc::tma_prefetch_desc(&mxlo);
+        int nch = 0;
+        for (int e = e_beg; e < e_end; ++e) {
+            const int j = nbox_list[e];
+            nch += (box_ptr[j + 1] - box_ptr[j] + TC_KCH - 1) / TC_KCH;
+        }
+        // once any CTA has given up a wait, the rest skip their work (the call fails anyway)
+        if (*reinterpret_cast<volatile int*>(err)) nch = 0;
+        nch_s = nch;
+        fail_s = 0;
     }
     if (warp == 0) {
         tc::tmem_alloc(&tmem_base, TC_TMEM_COLS);
@@ -189,78 +194,78 @@ __global__ void __launch_bounds__(128, 1)
     __syncthreads();
     tc::tc_fence_after_sync();
     const uint32_t tmem = tmem_base;
+    const int nch = nch_s;
 
-    if (tid == 0) {
+    if (tid == 0 && nch > 0) {
+        // producer: TMA loads of chunk c into stage c % STAGES once that stage's MMAs are done
+        tc::tma_prefetch_desc(&mzhi);
+        tc::tma_prefetch_desc(&mzlo);
+        tc::tma_prefetch_desc(&mxhi);
+        tc::tma_prefetch_desc(&mxlo);
         const int nB = (nrow + TC_ZBOX - 1) / TC_ZBOX * TC_ZBOX;          // B rows staged
         const uint32_t bytes = 2u * TC_ABYTES + 2u * (uint32_t)nB * 128u;
-        int nch = 0;
-        for (int e = e_beg; e < e_end; ++e) {
-            const int j = nbox_list[e];
-            nch += (box_ptr[j + 1] - box_ptr[j] + TC_KCH - 1) / TC_KCH;
+        int le = e_beg, lkc = 0;
+        for (int cI = 0; cI < nch; ++cI) {
+            const int s = cI % TC_STAGES;
+            if (cI >= TC_STAGES && !tc::mbar_wait(&empty[s], ((cI / TC_STAGES) - 1) & 1, TC_SPIN)) {
+                fail_s = 1;   // the MMA thread then gives up on this stage's full barrier too
+                break;
+            }
+            unsigned char* st = ring + (size_t)s * TC_STAGE_BYTES;
+            tc::mbar_arrive_expect_tx(&full[s], bytes);
+            const int j = nbox_list[le];
+            const int nj = box_ptr[j + 1] - box_ptr[j];
+            const int xr = (ct * nchunk + cbase[j] + lkc) * 128;
+            tc::tma_load_2d(st, &mxhi, 0, xr, &full[s]);
+            tc::tma_load_2d(st + TC_ABYTES, &mxlo, 0, xr, &full[s]);
+            const int zr = zrow[le] + lkc * ni + r0;
+            for (int q = 0; q < nB; q += TC_ZBOX) {
+                tc::tma_load_2d(st + 2 * TC_ABYTES + q * 128, &mzhi, 0, zr + q, &full[s]);
+                tc::tma_load_2d(st + 2 * TC_ABYTES + TC_BBYTES + q * 128, &mzlo, 0, zr + q, &full[s]);
+            }
+            if (++lkc * TC_KCH >= nj) {
+                lkc = 0;
+                ++le;
+            }
         }
-        int le = e_beg, lkc = 0, issued = 0, consumed = 0;
+    } else if (tid == 32 && nch > 0) {
+        // MMA issuer: per chunk 4 K steps x 3 products into the TMEM accumulator
+        int consumed = 0;
         bool ok = true;
-        // once any CTA has given up a wait, the rest skip their work (the call fails anyway)
-        if (*reinterpret_cast<volatile int*>(err)) nch = 0;
-        for (int cI = 0; cI < nch + TC_STAGES - 1 && nch > 0; ++cI) {
-            if (cI < nch) {   // load chunk cI into stage cI % STAGES once its previous MMAs are done
-                const int s = cI % TC_STAGES;
-                if (cI >= TC_STAGES && !tc::mbar_wait(&empty[s], ((cI / TC_STAGES) - 1) & 1, TC_SPIN)) {
-                    ok = false;
-                    break;
-                }
-                unsigned char* st = ring + (size_t)s * TC_STAGE_BYTES;
-                tc::mbar_arrive_expect_tx(&full[s], bytes);
-                const int j = nbox_list[le];
-                const int nj = box_ptr[j + 1] - box_ptr[j];
-                const int xr = (ct * nchunk + cbase[j] + lkc) * 128;
-                tc::tma_load_2d(st, &mxhi, 0, xr, &full[s]);
-                tc::tma_load_2d(st + TC_ABYTES, &mxlo, 0, xr, &full[s]);
-                const int zr = zrow[le] + lkc * ni + r0;
-                for (int q = 0; q < nB; q += TC_ZBOX) {
-                    tc::tma_load_2d(st + 2 * TC_ABYTES + q * 128, &mzhi, 0, zr + q, &full[s]);
-                    tc::tma_load_2d(st + 2 * TC_ABYTES + TC_BBYTES + q * 128, &mzlo, 0, zr + q, &full[s]);
-                }
-                ++issued;
-                if (++lkc * TC_KCH >= nj) {
-                    lkc = 0;
-                    ++le;
-                }
+        for (int cc = 0; cc < nch; ++cc) {
+            const int s = cc % TC_STAGES;
+            if (!tc::mbar_wait(&full[s], (cc / TC_STAGES) & 1, TC_SPIN)) {
+                ok = false;
+                break;
             }
-            const int cc = cI - (TC_STAGES - 1);
-            if (cc >= 0) {    // the MMAs of chunk cc
-                const int s = cc % TC_STAGES;
-                if (!tc::mbar_wait(&full[s], (cc / TC_STAGES) & 1, TC_SPIN)) {
-                    ok = false;
-                    break;
-                }
-                ++consumed;
-                tc::tc_fence_after_sync();
-                const uint32_t a = tc::smem_u32(ring + (size_t)s * TC_STAGE_BYTES);
-                const uint32_t ahi = a, alo = a + TC_ABYTES, bhi = a + 2 * TC_ABYTES, blo = bhi + TC_BBYTES;
+            ++consumed;
+            tc::tc_fence_after_sync();
+            const uint32_t a = tc::smem_u32(ring + (size_t)s * TC_STAGE_BYTES);
+            const uint32_t ahi = a, alo = a + TC_ABYTES, bhi = a + 2 * TC_ABYTES, blo = bhi + TC_BBYTES;
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {   // K steps of 8 TF32 = 32 bytes of the 128-byte rows
-                    const uint32_t ko = 32u * q;
-                    tc::mma_tf32(tmem, tc::kmajor_sw128_desc(alo + ko), tc::kmajor_sw128_desc(bhi + ko), idesc,
-                                 (cc | q) != 0);
-                    tc::mma_tf32(tmem, tc::kmajor_sw128_desc(ahi + ko), tc::kmajor_sw128_desc(blo + ko), idesc, 1);
-                    tc::mma_tf32(tmem, tc::kmajor_sw128_desc(ahi + ko), tc::kmajor_sw128_desc(bhi + ko), idesc, 1);
-                }
-                tc::mma_commit(&empty[s]);
+            for (int q = 0; q < 4; ++q) {   // K steps of 8 TF32 = 32 bytes of the 128-byte rows
+                const uint32_t ko = 32u * q;
+                tc::mma_tf32(tmem, tc::kmajor_sw128_desc(alo + ko), tc::kmajor_sw128_desc(bhi + ko), idesc,
+                             (cc | q) != 0);
+                tc::mma_tf32(tmem, tc::kmajor_sw128_desc(ahi + ko), tc::kmajor_sw128_desc(blo + ko), idesc, 1);
+                tc::mma_tf32(tmem, tc::kmajor_sw128_desc(ahi + ko), tc::kmajor_sw128_desc(bhi + ko), idesc, 1);
             }
+            tc::mma_commit(&empty[s]);
         }
         tc::mma_commit(&done);   // every MMA issued above
         if (!tc::mbar_wait(&done, 0, TC_SPIN)) ok = false;
         if (!ok) {
-            // loads still in flight land before the shared memory is given up
-            for (int k = consumed; k < issued; ++k)
+            // loads already issued land before the shared memory is given up: the
+            // producer issues at most STAGES chunks beyond the last one consumed
+            for (int k = consumed; k < nch && k < consumed + TC_STAGES; ++k)
                 tc::mbar_wait(&full[k % TC_STAGES], (k / TC_STAGES) & 1, TC_SPIN);
-            atomicExch(err, 1);
+            fail_s = 1;
         }
-        skip = (!ok || nch == 0) ? 1 : 0;
     }
     __syncthreads();
     tc::tc_fence_after_sync();
+    const bool skip = fail_s != 0 || nch == 0;
+    if (tid == 0 && fail_s) atomicExch(err, 1);
     if (!skip) {
         const int m = 32 * warp + lane;                 // D row = TMEM lane
         const int col = ct * TC_COLS + (m >> 1);
@@ -386,7 +391,7 @@ static int tc_setup(Ctx* c) {
             rows += (long long)ni * ((c->box_ptr[j + 1] - c->box_ptr[j] + TC_KCH - 1) / TC_KCH);
         }
     }
-    if (rows >= (1LL << 31) - TC_ROWS || (long long)chunk.size() * 2 * 128 >= (1LL << 31)) {
+    if (rows >= (1LL << 31) - 256 || (long long)chunk.size() * 2 * 128 >= (1LL << 31)) {
         c->err = "tensor-core near field: operand layout exceeds 2^31 rows";
         return MLF_E_STATE;
     }
