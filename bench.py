@@ -222,76 +222,74 @@ def project_sequential(t_sample, iters, nang=722):
     return t_sample / it.sum() * (it[0] + (nang - 1) * it[1:].mean())
 
 
-def project_batched_warm(t_sample, iters, block, nrun_sample=4, nang=722, steady_from=2):
-    """mlf_monostatic mode 3/4 over nang angles, from a sample of nrun_sample
-    blocks (runs of nrun_sample angles per column): a block's time is split
-    by its slowest column's iteration count (the block steps until every
-    column has converged).  Blocks before `steady_from` are counted once (the
-    cold start; in mode 4 also the first warm block, which has only one
-    previous angle to start from), every later block of the full sweep as the
-    mean of the sampled later ones."""
-    it = np.asarray(iters, dtype=float).reshape(block, nrun_sample)   # [column, step of its run]
-    per_block = it.max(axis=0)
-    t_blk = t_sample * per_block / per_block.sum()
-    nrun = -(-nang // block)
-    return float(t_blk[:steady_from].sum() + (nrun - steady_from) * t_blk[steady_from:].mean())
-
-
-def batched_rcs_sample(seq_angles=3, block=0, maxit=4000):
-    """722-RHS monostatic sweep on the spheroid, sampled: one autotuned block of
-    angles solved as a batched mixed-precision GMRES-IR (FP32 operator, FP64
-    residual), against the plain FP64 GPU path -- the reference's sequential,
-    warm-started CGS sweep on the FP64 operator -- on the first `seq_angles`
-    angles.  Both use the own-box near-field inverse as preconditioner.  Times
-    per right-hand side are projected to the 722 RHS."""
+def batched_rcs_722(seq_angles=3, block=0, maxit=4000):
+    """The 722-RHS monostatic sweep on the spheroid, measured end to end:
+    phi = 0..180 deg in 0.5 deg steps (361 angles) x {VV, HH}, theta = 90 deg,
+    solved as mixed-precision GMRES-IR (FP32 operator, FP64 residual to 1e-4)
+    in blocks of right-hand sides (autotuned block size and engine), each
+    block column sweeping a run of angles with extrapolated warm starts
+    (mlf_monostatic mode 4).  Time to RCS = geometry and operator set-up +
+    preconditioner set-up (own-box near-field inverse) + autotuning + the two
+    sweeps, which include the backscatter RCS of every angle.  The plain FP64
+    GPU path -- the reference's sequential warm-started CGS sweep
+    (gen_rcs_monostatica, main.f90:967-1089) on the FP64 operator, same
+    preconditioner -- is run on the first `seq_angles` angles of each
+    polarisation, which also give the per-angle RCS check, and projected to
+    the 722 angles (its full run would take over an hour)."""
     import torch
     from lywell_gb300 import MLFMA, RWG, meshes
 
     t0 = time.time()
     tris = meshes.spheroid(SPHEROID["level"], SPHEROID["axes"], noise=SPHEROID["noise"], seed=SPHEROID["seed"])
     m = MLFMA(RWG(tris), lam=SPHEROID["lam"], ladomax=SPHEROID["ladomax"])
+    torch.cuda.synchronize()
     t_tree = time.time() - t0
     t0 = time.time()
     bad = m.nearinv(own_only=True)
     t_pre = time.time() - t0
-    nang_total, dphi = 722, np.deg2rad(0.5)
+    t0 = time.time()
     tune = m.autotune_block() if block <= 0 else dict(block=block, tile_cols=0, per_rhs_ms={})
+    t_tune = time.time() - t0
     B = int(tune["block"])
-    # mode 4 on 4 x B angles: each column sweeps a run of 4 angles 0.5 deg apart
-    # (cold, warm from one previous angle, then extrapolated from two), as the
-    # first four blocks of the full sweep
-    nrs = 4
-    phis = np.arange(nrs * B) * dphi
-    torch.cuda.synchronize()
-    m.set_profiling(True)
+    nang = 361
+    phis = np.arange(nang) * np.deg2rad(0.5)
+    sweeps = {}
     t0 = time.time()
-    mix = m.monostatic(nrs * B, phis=phis, pol="VV", errmax=1e-4, maxit=maxit, precond="nearinv", mode=4, block=B)
-    t_mix = time.time() - t0
-    phases = m.solve_times()
-    m.set_profiling(False)
+    for pol in ("VV", "HH"):
+        sweeps[pol] = m.monostatic(nang, phis=phis, pol=pol, errmax=1e-4, maxit=maxit, precond="nearinv", mode=4,
+                                   block=B)
+    t_sweep = time.time() - t0
+    nrun = -(-nang // B)
+    blocks = {pol: [int(max(sweeps[pol]["iters"][q * nrun + k] for q in range(B) if q * nrun + k < nang))
+                    for k in range(nrun)] for pol in sweeps}
     t0 = time.time()
-    seq = m.monostatic(seq_angles, phis=phis[:seq_angles], pol="VV", errmax=1e-4, maxit=maxit,
-                       precond="nearinv", mode=0)
-    t_seq = time.time() - t0
-    proj_mix = project_batched_warm(t_mix, mix["iters"], B, nrs, nang_total)
-    proj_seq = project_sequential(t_seq, seq["iters"], nang_total)
-    # column 0 of the batched sample sweeps the sequential sample's angles
-    db = np.abs(mix["sigma_db"][:seq_angles] - seq["sigma_db"])
+    seq, t_seq = {}, {}
+    for pol in ("VV", "HH"):
+        t1 = time.time()
+        seq[pol] = m.monostatic(seq_angles, phis=phis[:seq_angles], pol=pol, errmax=1e-4, maxit=maxit,
+                                precond="nearinv", mode=0)
+        t_seq[pol] = time.time() - t1
+    # column 0 of every block sweeps the first angles, as the sequential sample
+    db = np.concatenate([np.abs(sweeps[pol]["sigma_db"][:seq_angles] - seq[pol]["sigma_db"]) for pol in seq])
+    proj_seq = sum(project_sequential(t_seq[pol], seq[pol]["iters"], nang) for pol in seq)
+    status = sorted({s for pol in sweeps for s in sweeps[pol]["status"]})
+    ttr = t_tree + t_pre + t_tune + t_sweep
     out = {"workload": SPHEROID["name"], "N": m.N, "near_nnz": m.nnz, "setup_s": t_tree, "precond_setup_s": t_pre,
-           "precond": "own-box near-field inverse", "nearinv_bad_box": bad, "autotune": tune, "block": B,
-           "mixed_batched": {"mode": 4, "angles": nrs * B, "blocks": nrs, "seconds": t_mix,
-                             "iters": [int(v) for v in mix["iters"]], "status": sorted(set(mix["status"])),
-                             "phases_ms": phases},
-           "fp64_sequential": {"angles": seq_angles, "seconds": t_seq,
-                               "iters": [int(v) for v in seq["iters"]], "status": sorted(set(seq["status"]))},
-           "projected_722_s": {"mixed_batched": t_tree + t_pre + proj_mix,
-                               "fp64_sequential": t_tree + t_pre + proj_seq},
+           "precond": "own-box near-field inverse", "nearinv_bad_box": bad, "autotune": tune, "autotune_s": t_tune,
+           "block": B,
+           "measured_722": {"mode": 4, "angles": 2 * nang, "sweep_s": t_sweep, "time_to_rcs_s": ttr,
+                            "status": status, "iters_per_block": blocks,
+                            "iters_per_angle": {pol: [int(v) for v in sweeps[pol]["iters"]] for pol in sweeps}},
+           "fp64_sequential_sample": {"angles_per_pol": seq_angles, "seconds": t_seq,
+                                      "iters": {pol: [int(v) for v in seq[pol]["iters"]] for pol in seq},
+                                      "status": sorted({s for pol in seq for s in seq[pol]["status"]}),
+                                      "projected_722_s": t_tree + t_pre + proj_seq,
+                                      "note": "projected: the sampled angles' time split by iteration count, "
+                                              "the cold first angle of each polarisation once, every later "
+                                              "angle as the sampled warm ones"},
+           "rcs_db_vs_fp64_per_angle": [float(v) for v in db],
            "rcs_db_maxdiff_vs_fp64": float(db.max()),
-           "note": "solve times measured on samples of the 722-RHS sweep (3 sequential angles; 4 blocks of the "
-                   "batched sweep) and projected with the cold start (and, batched, the first warm block) once "
-                   "and the later steps as sampled, time split by iteration count"}
-    out["s_per_rhs_projected"] = {k: v / nang_total for k, v in out["projected_722_s"].items()}
-    out["speedup_projected_722"] = out["projected_722_s"]["fp64_sequential"] / out["projected_722_s"]["mixed_batched"]
+           "speedup_vs_fp64_projected": (t_tree + t_pre + proj_seq) / ttr}
     m.close()
     return out
 
@@ -433,37 +431,57 @@ def learned_at_scale(steps=3000, seed=0):
     run("mixed_exact_neighbourhood", m.nearinv, True, "nearinv")
     run("mixed_learned", learned_setup, True, "nearinv")
     run("fp64_cgs_ilu0_reference", lambda: m.ilu0(), False, "ilu0", maxit=300)
-    # the three additions together: a 722-RHS monostatic sweep on the sphere (phi = 0..180 deg
-    # step 0.5 deg x {VV, HH}), sampled and projected per RHS: the plain FP64 path (the
-    # reference's warm-started sequential CGS, exact neighbourhood inverse) on 3 angles
-    # against mixed + batched (autotuned block) + learned on one block of angles
-    dphi = np.deg2rad(0.5)
-    m.nearinv()
-    torch.cuda.synchronize()
+    # the three additions together: the 722-RHS monostatic sweep on the sphere (phi = 0..180 deg
+    # step 0.5 deg x {VV, HH}), mixed + batched (autotuned block) + learned, measured over all
+    # 722 angles; the plain FP64 path (the reference's warm-started sequential CGS, exact
+    # neighbourhood inverse) on the first 3 angles of each polarisation, projected
+    nang = 361
+    phis = np.arange(nang) * np.deg2rad(0.5)
     t1 = time.time()
-    seq = m.monostatic(3, phis=np.arange(3) * dphi, pol="VV", errmax=1e-4, maxit=4000, precond="nearinv", mode=0)
-    t_seq = time.time() - t1
+    m.nearinv()
+    t_exact = time.time() - t1
+    seq, t_seq = {}, {}
+    for pol in ("VV", "HH"):
+        torch.cuda.synchronize()
+        t1 = time.time()
+        seq[pol] = m.monostatic(3, phis=phis[:3], pol=pol, errmax=1e-4, maxit=4000, precond="nearinv", mode=0)
+        t_seq[pol] = time.time() - t1
+    t1 = time.time()
     lp.apply_to(m)
+    t_inst = time.time() - t1
+    t1 = time.time()
     tune = m.autotune_block()
+    t_tune = time.time() - t1
     B = int(tune["block"])
     torch.cuda.synchronize()
+    bat = {}
     t1 = time.time()
-    bat = m.monostatic(4 * B, phis=np.arange(4 * B) * dphi, pol="VV", errmax=1e-4, maxit=4000, precond="nearinv",
-                       mode=4, block=B)
+    for pol in ("VV", "HH"):
+        bat[pol] = m.monostatic(nang, phis=phis, pol=pol, errmax=1e-4, maxit=4000, precond="nearinv", mode=4,
+                                block=B)
     t_bat = time.time() - t1
     m.close()
-    p_seq = project_sequential(t_seq, seq["iters"])
-    p_bat = project_batched_warm(t_bat, bat["iters"], B, 4)
-    sweep = {"fp64_sequential_exact": {"angles": 3, "seconds": t_seq, "iters": [int(v) for v in seq["iters"]],
-                                       "s_per_rhs_projected": p_seq / 722},
-             "mixed_batched_learned": {"mode": 4, "angles": 4 * B, "blocks": 4, "seconds": t_bat, "autotune": tune,
-                                       "iters": [int(v) for v in bat["iters"]],
-                                       "status": sorted(set(bat["status"])), "s_per_rhs_projected": p_bat / 722},
-             "rcs_db_maxdiff": float(np.abs(bat["sigma_db"][:3] - seq["sigma_db"]).max()),
-             "note": "projected from 3 sequential angles and 4 batched blocks: the cold start (and, batched, the "
-                     "first warm block) once, the later steps as sampled, time split by iteration count"}
-    sweep["projected_722_s"] = {"fp64_sequential_exact": p_seq, "mixed_batched_learned": p_bat}
-    sweep["speedup_projected_722"] = p_seq / p_bat
+    nrun = -(-nang // B)
+    p_seq = t_exact + sum(project_sequential(t_seq[pol], seq[pol]["iters"], nang) for pol in seq)
+    ttr = t_exact + t_inst + t_tune + t_bat
+    db = np.concatenate([np.abs(bat[pol]["sigma_db"][:3] - seq[pol]["sigma_db"]) for pol in seq])
+    sweep = {"fp64_sequential_exact": {"angles_per_pol": 3, "seconds": t_seq,
+                                       "iters": {pol: [int(v) for v in seq[pol]["iters"]] for pol in seq},
+                                       "projected_722_s": p_seq,
+                                       "note": "projected: the cold first angle of each polarisation once, every "
+                                               "later angle as the sampled warm ones, time split by iteration "
+                                               "count; + the exact neighbourhood inverse set-up"},
+             "mixed_batched_learned": {"mode": 4, "angles": 2 * nang, "block": B, "autotune": tune,
+                                       "sweep_s": t_bat, "time_to_rcs_s": ttr,
+                                       "setup_s": {"exact_inverse": t_exact, "learned_install": t_inst,
+                                                   "autotune": t_tune},
+                                       "status": sorted({v for pol in bat for v in bat[pol]["status"]}),
+                                       "iters_per_block": {pol: [int(max(bat[pol]["iters"][q * nrun + k]
+                                                                         for q in range(B) if q * nrun + k < nang))
+                                                                 for k in range(nrun)] for pol in bat}},
+             "rcs_db_vs_fp64_per_angle": [float(v) for v in db],
+             "rcs_db_maxdiff": float(db.max())}
+    sweep["speedup_vs_fp64_projected"] = p_seq / ttr
     base = out["fp64_cgs_exact_neighbourhood"]["time_to_rcs_s"]
     return {"workload": WORKLOADS["sphere6"]["name"] + "; trained on 3 seeded superellipsoids (30720 RWG, same "
                                                        "mesh density)",
@@ -484,7 +502,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-time-to-rcs", action="store_true")
     ap.add_argument("--rcs-maxit", type=int, default=4000)
-    ap.add_argument("--no-batched", action="store_true", help="skip the 722-RHS spheroid sweep sample")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 722-RHS spheroid sweep")
     ap.add_argument("--learned", action="store_true", help="add the learned-preconditioner samples (about 6 min)")
     ap.add_argument("--seq-angles", type=int, default=3)
     ap.add_argument("--block", type=int, default=0, help="RHS per block of the batched sweep (0: autotuned)")
@@ -625,7 +643,7 @@ def main():
 
     batched = None
     if not args.no_batched and rank == 0:
-        batched = batched_rcs_sample(args.seq_angles, args.block, args.rcs_maxit)
+        batched = batched_rcs_722(args.seq_angles, args.block, args.rcs_maxit)
 
     learned = None
     if args.learned and rank == 0:
