@@ -291,6 +291,13 @@ int mlf_matvec32_device(mlf_ctx* ctx, const void* x_dev, void* y_dev, int nrhs, 
  * singular. */
 int mlf_nearinv(mlf_ctx* ctx, int* bad_box);
 
+/* Arithmetic of mlf_nearinv's elimination: 64 = FP64 Gaussian elimination
+ * with partial pivoting, one CTA per box; 32 = blocked FP32 LU with partial
+ * pivoting (panels of 32 columns, tiled GEMM trailing updates), for
+ * neighbourhoods of thousands of unknowns; 0 (the default) = FP64 up to 768
+ * unknowns per neighbourhood, FP32 above.  No counterpart in the reference. */
+int mlf_set_nearinv_precision(mlf_ctx* ctx, int bits);
+
 /* Same with each box's own bases as the neighbourhood (block Jacobi on the
  * near field): cheaper where leaf boxes hold many bases and near lists run
  * into the thousands.  Replaces any previous mlf_nearinv result. */

@@ -32,6 +32,7 @@ SIGNATURES = {
     "mlf_ilu0_csr": (C.c_int, [C.c_int, vp, vp, vp, vp, vp, vp, ip]),
     "mlf_set_near_values": (C.c_int, [vp, vp]),
     "mlf_set_stagnation": (C.c_int, [vp, C.c_int]),
+    "mlf_set_nearinv_precision": (C.c_int, [vp, C.c_int]),
     "mlf_cgs": (C.c_int, [vp, vp, vp, C.c_double, C.c_int, C.c_int, vp, vp, vp, C.c_int, vp]),
     "mlf_nearinv": (C.c_int, [vp, ip]),
     "mlf_nearinv_own": (C.c_int, [vp, ip]),

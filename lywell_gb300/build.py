@@ -21,7 +21,7 @@ OUT = os.path.join(OUT_DIR, "liblywell_mlfma.so")
 OBJ_DIR = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["mlf_setup.cpp", "mlf_device.cu", "mlf_solver.cu", "mlf_capi.cu", "mlf_noalloc.cu", "mlf_precond.cu", "mlf_mixed.cu", "mlf_sweep.cu", "mlf_nearblk.cu", "mlf_nearwarp.cu", "mlf_autotune.cu", "mlf_mlp.cu", "mlf_learned.cu", "mlf_mom.cu", "mlf_tc.cu"]
+SOURCES = ["mlf_setup.cpp", "mlf_device.cu", "mlf_solver.cu", "mlf_capi.cu", "mlf_noalloc.cu", "mlf_precond.cu", "mlf_mixed.cu", "mlf_sweep.cu", "mlf_nearblk.cu", "mlf_nearwarp.cu", "mlf_autotune.cu", "mlf_mlp.cu", "mlf_learned.cu", "mlf_mom.cu", "mlf_tc.cu", "mlf_nbhd_lu.cu"]
 
 
 def _nvcc():

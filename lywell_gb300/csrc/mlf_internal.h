@@ -184,6 +184,7 @@ struct Ctx {
     float2* dpre_xs = nullptr;        // box-sorted copy of the preconditioner input (blocks of columns)
     size_t pre_xs_cap = 0;
     int nearinv_ok = 0, nearinv_own = 0;
+    int nearinv_bits = 0;             // 64: FP64 elimination, 32: blocked FP32 LU, 0: by neighbourhood size
     int learned = 0;                  // own-box blocks installed from the learned network
     // level schedule of the triangular solves
     std::vector<int> lvl_ptr_f, lvl_rows_f, lvl_ptr_b, lvl_rows_b;
@@ -238,6 +239,7 @@ int device_ilu_solve(Ctx* c, const double2* y, double2* x, cudaStream_t s);
 int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs,
                double2* x, int* iters, double* relres, int precond, int* status);
 int device_nearinv_setup(Ctx* c, int* bad_box, int own_only);
+int nbhd_inverse_lu32(Ctx* c, int nmax, int nownmax, int* bad_box);   // blocked FP32 LU (mlf_nbhd_lu.cu)
 int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s);
 int device_matvec32_from32(Ctx* c, const float2* x32, double2* y, int nrhs, cudaStream_t s);
 int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStream_t s);

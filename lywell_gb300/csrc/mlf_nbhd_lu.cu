@@ -1,0 +1,370 @@
+// Neighbourhood-inverse preconditioner for large neighbourhoods: a blocked,
+// FP32, partially pivoted LU per leaf box.
+//
+// The preconditioner (mlf_precond.cu) needs, for every leaf box b, the rows of
+// inv(A) that belong to b's own bases, A = Znear[S, S] over the box's near
+// list S.  Its FP64 elimination works by rank-1 updates of A in global memory,
+// which is fine for neighbourhoods of a few hundred unknowns but not for the
+// 1500-4000 unknowns of bodies with 60-150 bases per 0.25 lambda leaf box
+// (the prolate spheroid of the 722-RHS workload, the superellipsoids of the
+// learned preconditioner): there the work is ~2.7 n^3 flops per box and the
+// rank-1 form re-reads the whole matrix n times.
+//
+// This kernel solves the same system, A^T X = E_own (then M rows = X^T), with
+// a right-looking blocked LU of A^T, column-major in a per-CTA slab of global
+// memory (L2-resident in part):
+//   for each panel of LU_P = 32 columns:
+//     * panel factorisation: pivot = largest |a|^2 at or below the diagonal
+//       (first row on ties), row swap across the trailing columns and X,
+//       scaling, rank-1 updates inside the panel;
+//     * U12 = L11^-1 A12 for the trailing columns and the right-hand sides X
+//       (forward substitution on 32 x 64 tiles in shared memory, one thread
+//       per column);
+//     * trailing update A22 -= L21 U12 and X2 -= L21 X1 as 64 x 64 complex
+//       tiles of a register-blocked FP32 GEMM (each thread 4 x 4 outputs,
+//       operand tiles in shared memory);
+//   back substitution U X = Y by blocks of 32 rows from the bottom (a small
+//   triangular solve per block, then a tiled GEMM update of the rows above).
+// Persistent CTAs (two per SM) take boxes from an atomic counter, so large and
+// small neighbourhoods balance over the GPU.
+//
+// FP32 with partial pivoting leaves the preconditioner's rows within ~1e-5 of
+// the FP64 ones (tested); a preconditioner only has to be close, and the
+// solves' residual test stays FP64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "mlf_internal.h"
+
+namespace mlf {
+
+#define CK(call)                                             \
+    do {                                                     \
+        if (!cuda_ok(c, (call), #call)) return MLF_E_CUDA;   \
+    } while (0)
+
+constexpr int LU_P = 32;          // panel width (= block of the back substitution)
+constexpr int LU_T = 64;          // GEMM tile rows and columns
+constexpr int LU_THREADS = 256;
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cinvf(float2 a) {
+    const float d = a.x * a.x + a.y * a.y;
+    return make_float2(a.x / d, -a.y / d);
+}
+
+__device__ __forceinline__ int bsearch_cols(const int* S, int n, int v) {
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int s = S[mid];
+        if (s == v) return mid;
+        if (s < v) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return -1;
+}
+
+// D(rows r0.., cols c0..) -= Lop * Uop over K = kb, one 64 x 64 tile:
+//   Lop(i, t) = A[(lk + t) * n + lr + r0 + i]                     (column-major panel)
+//   Uop(t, j) = col(c0 + j)[uk + t],  col(q) = q < nc ? A + (ac + q) * n : X + (q - nc) * n
+//   D(i, j)   = col(c0 + j)[dr + r0 + i]
+// rows < nrows and columns < ncols only; the caller synchronises around it.
+struct LuTiles {
+    float2 L[LU_T][LU_P + 1];
+    float2 U[LU_P][LU_T + 1];
+};
+
+__device__ __forceinline__ void lu_tile_update(LuTiles& sm, float2* __restrict__ A, float2* __restrict__ X, int n,
+                                               int kb, int lk, int lr, int uk, int dr, int ac, int nc, int r0,
+                                               int c0, int nrows, int ncols) {
+    const int tid = threadIdx.x;
+    for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
+        const int t = e / LU_T, i = e - t * LU_T;          // consecutive threads: consecutive rows
+        sm.L[i][t] = (t < kb && r0 + i < nrows) ? A[(size_t)(lk + t) * n + lr + r0 + i] : make_float2(0.f, 0.f);
+    }
+    for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
+        const int j = e / LU_P, t = e - j * LU_P;          // consecutive threads: consecutive t of one column
+        float2 v = make_float2(0.f, 0.f);
+        if (t < kb && c0 + j < ncols) {
+            const int q = c0 + j;
+            const float2* col = q < nc ? A + (size_t)(ac + q) * n : X + (size_t)(q - nc) * n;
+            v = col[uk + t];
+        }
+        sm.U[t][j] = v;
+    }
+    __syncthreads();
+    const int tx = tid & 15, ty = tid >> 4;
+    float2 acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
+    for (int t = 0; t < kb; ++t) {
+        float2 a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a[u] = sm.L[ty * 4 + u][t];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) b[v] = sm.U[t][tx * 4 + v];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                acc[u][v].x = fmaf(a[u].x, b[v].x, acc[u][v].x);
+                acc[u][v].x = fmaf(-a[u].y, b[v].y, acc[u][v].x);
+                acc[u][v].y = fmaf(a[u].x, b[v].y, acc[u][v].y);
+                acc[u][v].y = fmaf(a[u].y, b[v].x, acc[u][v].y);
+            }
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        const int j = tx * 4 + v;
+        if (c0 + j >= ncols) continue;
+        const int q = c0 + j;
+        float2* col = q < nc ? A + (size_t)(ac + q) * n : X + (size_t)(q - nc) * n;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = ty * 4 + u;
+            if (r0 + i < nrows) {
+                float2 d = col[dr + r0 + i];
+                d.x -= acc[u][v].x;
+                d.y -= acc[u][v].y;
+                col[dr + r0 + i] = d;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(LU_THREADS, 2)
+    k_nbhd_lu32(int nb, const int* __restrict__ box_ptr, const int* __restrict__ box_bases,
+                const int* __restrict__ ia, const int* __restrict__ ja, const float2* __restrict__ Z, size_t slab,
+                float2* __restrict__ work, double2* __restrict__ M, int* __restrict__ next_box,
+                int* __restrict__ bad) {
+    __shared__ LuTiles sm;
+    __shared__ float s_val[LU_THREADS / 32];
+    __shared__ int s_idx[LU_THREADS / 32];
+    __shared__ int s_b, s_piv, s_sing;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    float2* A = work + (size_t)blockIdx.x * slab;
+    for (;;) {
+        if (tid == 0) {
+            s_b = atomicAdd(next_box, 1);
+            s_sing = 0;
+        }
+        __syncthreads();
+        const int b = s_b;
+        if (b >= nb) break;
+        const int m0 = box_bases[box_ptr[b]], nown = box_ptr[b + 1] - box_ptr[b];
+        const int n = ia[m0 + 1] - ia[m0];
+        const int* S = ja + ia[m0];
+        float2* X = A + (size_t)n * n;
+        // A^T column r = row S[r] of Z restricted to S; X = the own bases' unit columns
+        for (size_t e = tid; e < (size_t)n * n + (size_t)n * nown; e += LU_THREADS) A[e] = make_float2(0.f, 0.f);
+        __syncthreads();
+        for (int r = wid; r < n; r += LU_THREADS / 32) {
+            const int m = S[r];
+            for (int q = ia[m] + lane; q < ia[m + 1]; q += 32) {
+                const int pos = bsearch_cols(S, n, ja[q]);
+                if (pos >= 0) A[(size_t)r * n + pos] = Z[q];
+            }
+        }
+        for (int cc = tid; cc < nown; cc += LU_THREADS) {
+            const int pos = bsearch_cols(S, n, box_bases[box_ptr[b] + cc]);
+            if (pos >= 0) X[(size_t)cc * n + pos] = make_float2(1.f, 0.f);
+        }
+        __syncthreads();
+        for (int k0 = 0; k0 < n; k0 += LU_P) {
+            const int kb = min(LU_P, n - k0);
+            // ---- panel factorisation
+            for (int j = k0; j < k0 + kb; ++j) {
+                float best = -1.f;
+                int bi = n;
+                const float2* colj = A + (size_t)j * n;
+                for (int i = j + tid; i < n; i += LU_THREADS) {
+                    const float2 a = colj[i];
+                    const float v = a.x * a.x + a.y * a.y;
+                    if (v > best) { best = v; bi = i; }
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+                }
+                if (lane == 0) { s_val[wid] = best; s_idx[wid] = bi; }
+                __syncthreads();
+                if (tid == 0) {
+                    float bv = s_val[0];
+                    int bx = s_idx[0];
+                    for (int w = 1; w < LU_THREADS / 32; ++w)
+                        if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bx)) { bv = s_val[w]; bx = s_idx[w]; }
+                    s_piv = bx;
+                    if (!(bv > 0.f) || bx >= n) s_sing = 1;
+                }
+                __syncthreads();
+                if (s_sing) break;
+                const int piv = s_piv;
+                if (piv != j) {
+                    for (int cc = k0 + tid; cc < n + nown; cc += LU_THREADS) {
+                        float2* col = cc < n ? A + (size_t)cc * n : X + (size_t)(cc - n) * n;
+                        const float2 t = col[j];
+                        col[j] = col[piv];
+                        col[piv] = t;
+                    }
+                    __syncthreads();
+                }
+                const float2 dinv = cinvf(A[(size_t)j * n + j]);
+                for (int i = j + 1 + tid; i < n; i += LU_THREADS) {
+                    float2* p = A + (size_t)j * n + i;
+                    *p = cmulf(*p, dinv);
+                }
+                __syncthreads();
+                const int nr = n - j - 1, ncl = k0 + kb - j - 1;
+                for (int e = tid; e < nr * ncl; e += LU_THREADS) {
+                    const int cq = e / nr, i = j + 1 + (e - cq * nr);
+                    float2* col = A + (size_t)(j + 1 + cq) * n;
+                    const float2 l = A[(size_t)j * n + i], u = col[j];
+                    float2 d = col[i];
+                    d.x -= l.x * u.x - l.y * u.y;
+                    d.y -= l.x * u.y + l.y * u.x;
+                    col[i] = d;
+                }
+                __syncthreads();
+            }
+            if (s_sing) break;
+            const int nc = n - k0 - kb;                       // trailing columns of A
+            const int ncols = nc + nown;                      // ... and the right-hand sides
+            // ---- U12 = L11^-1 A12 (and X), unit lower L11 in shared memory
+            for (int e = tid; e < LU_P * LU_P; e += LU_THREADS) {
+                const int t = e / LU_P, r = e - t * LU_P;
+                sm.L[r][t] = (r < kb && t < kb) ? A[(size_t)(k0 + t) * n + k0 + r] : make_float2(0.f, 0.f);
+            }
+            __syncthreads();
+            for (int c0 = 0; c0 < ncols; c0 += LU_T) {
+                // a 32 x 64 tile of the columns in shared memory, forward substitution per column
+                for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
+                    const int j = e / LU_P, t = e - j * LU_P;
+                    float2 v = make_float2(0.f, 0.f);
+                    if (t < kb && c0 + j < ncols) {
+                        const int q = c0 + j;
+                        v = (q < nc ? A + (size_t)(k0 + kb + q) * n : X + (size_t)(q - nc) * n)[k0 + t];
+                    }
+                    sm.U[t][j] = v;
+                }
+                __syncthreads();
+                if (tid < LU_T) {
+                    for (int r = 1; r < kb; ++r) {
+                        float2 acc = sm.U[r][tid];
+                        for (int t = 0; t < r; ++t) {
+                            const float2 l = sm.L[r][t], u = sm.U[t][tid];
+                            acc.x -= l.x * u.x - l.y * u.y;
+                            acc.y -= l.x * u.y + l.y * u.x;
+                        }
+                        sm.U[r][tid] = acc;
+                    }
+                }
+                __syncthreads();
+                for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
+                    const int j = e / LU_P, t = e - j * LU_P;
+                    if (t < kb && c0 + j < ncols) {
+                        const int q = c0 + j;
+                        (q < nc ? A + (size_t)(k0 + kb + q) * n : X + (size_t)(q - nc) * n)[k0 + t] = sm.U[t][j];
+                    }
+                }
+                __syncthreads();
+            }
+            // ---- trailing update: rows k0+kb.. of the trailing columns and of X
+            const int nrows = n - k0 - kb;
+            if (nrows > 0)
+                for (int r0 = 0; r0 < nrows; r0 += LU_T)
+                    for (int c0 = 0; c0 < ncols; c0 += LU_T)
+                        lu_tile_update(sm, A, X, n, kb, k0, k0 + kb, k0, k0 + kb, k0 + kb, nc, r0, c0, nrows, ncols);
+        }
+        if (s_sing) {
+            if (tid == 0) atomicMin(bad, b + 1);
+            __syncthreads();
+            continue;
+        }
+        // ---- back substitution U X = Y, blocks of LU_P rows from the bottom
+        for (int k0 = ((n - 1) / LU_P) * LU_P; k0 >= 0; k0 -= LU_P) {
+            const int kb = min(LU_P, n - k0);
+            for (int e = tid; e < LU_P * LU_P; e += LU_THREADS) {
+                const int t = e / LU_P, r = e - t * LU_P;
+                sm.L[r][t] = (r < kb && t < kb) ? A[(size_t)(k0 + t) * n + k0 + r] : make_float2(0.f, 0.f);
+            }
+            __syncthreads();
+            for (int c0 = 0; c0 < nown; c0 += LU_T) {
+                // a 32 x 64 tile of X in shared memory, backward substitution per column
+                for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
+                    const int j = e / LU_P, t = e - j * LU_P;
+                    sm.U[t][j] = (t < kb && c0 + j < nown) ? X[(size_t)(c0 + j) * n + k0 + t] : make_float2(0.f, 0.f);
+                }
+                __syncthreads();
+                if (tid < LU_T) {
+                    for (int r = kb - 1; r >= 0; --r) {
+                        float2 acc = sm.U[r][tid];
+                        for (int t = r + 1; t < kb; ++t) {
+                            const float2 u = sm.L[r][t], x = sm.U[t][tid];
+                            acc.x -= u.x * x.x - u.y * x.y;
+                            acc.y -= u.x * x.y + u.y * x.x;
+                        }
+                        sm.U[r][tid] = cmulf(acc, cinvf(sm.L[r][r]));
+                    }
+                }
+                __syncthreads();
+                for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
+                    const int j = e / LU_P, t = e - j * LU_P;
+                    if (t < kb && c0 + j < nown) X[(size_t)(c0 + j) * n + k0 + t] = sm.U[t][j];
+                }
+                __syncthreads();
+            }
+            // rows 0..k0-1 of X -= U(0..k0-1, k0..k0+kb-1) X(k0..k0+kb-1)
+            if (k0 > 0)
+                for (int r0 = 0; r0 < k0; r0 += LU_T)
+                    for (int c0 = 0; c0 < nown; c0 += LU_T)
+                        lu_tile_update(sm, A, X, n, kb, k0, 0, k0, 0, 0, 0, r0, c0, k0, nown);
+        }
+        // ---- M rows of the own bases: M[ia[g] + j] = X(j, own index)
+        for (int cc = 0; cc < nown; ++cc) {
+            const int g = box_bases[box_ptr[b] + cc];
+            double2* row = M + ia[g];
+            const float2* col = X + (size_t)cc * n;
+            for (int j = tid; j < n; j += LU_THREADS) row[j] = make_double2((double)col[j].x, (double)col[j].y);
+        }
+        __syncthreads();
+    }
+}
+
+// Every box's rows of the neighbourhood inverse into c->dMinv (near CSR
+// pattern, allocated by the caller); *bad_box as mlf_nearinv.
+int nbhd_inverse_lu32(Ctx* c, int nmax, int nownmax, int* bad_box) {
+    DevScope ds;
+    const int nb = (int)c->box_ptr.size() - 1;
+    const size_t slab = (size_t)nmax * nmax + (size_t)nmax * nownmax;
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev));
+    // two CTAs per SM, within 32 GB of slabs
+    const size_t cap = ((size_t)32 << 30) / (slab * sizeof(float2));
+    const int grid = (int)std::max<size_t>(1, std::min<size_t>({(size_t)2 * nsm, (size_t)nb, cap}));
+    float2* work = nullptr;
+    int *dctr = nullptr, *dbad = nullptr;
+    CK(ds.alloc(&work, slab * grid * sizeof(float2)));
+    CK(ds.alloc(&dctr, 2 * sizeof(int)));
+    dbad = dctr + 1;
+    const int init[2] = {0, 0x7fffffff};
+    CK(cudaMemcpyAsync(dctr, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
+    k_nbhd_lu32<<<grid, LU_THREADS, 0, c->stream>>>(nb, c->dbox_ptr, c->dperm, c->dia, c->dja, c->dZ, slab, work,
+                                                    c->dMinv, dctr, dbad);
+    CK(cudaGetLastError());
+    int hbad = 0;
+    CK(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *bad_box = hbad == 0x7fffffff ? 0 : hbad;
+    return MLF_OK;
+}
+
+}  // namespace mlf

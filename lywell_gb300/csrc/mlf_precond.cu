@@ -9,7 +9,9 @@
 // right-preconditioned CGS stays valid.  Rows of A^-1 solve A^T X = E_own.
 //
 // Set-up: one CTA per box, Gaussian elimination with partial pivoting
-// (largest |a|^2, first row on ties) in FP64 on a per-CTA workspace slab.
+// (largest |a|^2, first row on ties) in FP64 on a per-CTA workspace slab, for
+// neighbourhoods of up to NBI_FP64_MAX unknowns; larger ones go to the
+// blocked FP32 LU of mlf_nbhd_lu.cu (mlf_set_nearinv_precision overrides).
 // Apply: a warp-per-row SpMV with the near CSR pattern.
 #include <cuda_runtime.h>
 
@@ -43,6 +45,8 @@ __device__ __forceinline__ double2 zdiv(double2 a, double2 b) {
 }
 
 constexpr int NBI_THREADS = 256;
+// neighbourhoods of more unknowns go to the blocked FP32 LU unless FP64 is asked for
+constexpr int NBI_FP64_MAX = 768;
 
 __global__ void __launch_bounds__(NBI_THREADS)
 k_nbhd_inverse(int b0, int nb, const int* __restrict__ box_ptr, const int* __restrict__ box_bases,
@@ -362,6 +366,13 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     }
     c->minv_len = total;
     CK(cudaMalloc(&c->dMinv, std::max<long long>(total, 1) * sizeof(double2)));
+    // large neighbourhoods: the blocked FP32 LU (mlf_nbhd_lu.cu)
+    if (!own_only && (c->nearinv_bits == 32 || (c->nearinv_bits == 0 && nmax > NBI_FP64_MAX))) {
+        const int st = nbhd_inverse_lu32(c, nmax, nownmax, bad_box);
+        if (st) return st;
+        c->nearinv_ok = *bad_box == 0;
+        return MLF_OK;
+    }
     double2* work = nullptr;
     int* dbad = nullptr;
     int* dbases = nullptr;
@@ -415,6 +426,12 @@ extern "C" int mlf_nearinv_own(mlf_ctx* h, int* bad_box) {
     Ctx* c = &h->c;
     if (!cuda_ok(c, cudaSetDevice(c->dev), "cudaSetDevice")) return MLF_E_CUDA;
     return device_nearinv_setup(c, bad_box, 1);
+}
+
+extern "C" int mlf_set_nearinv_precision(mlf_ctx* h, int bits) {
+    if (!h || (bits != 0 && bits != 32 && bits != 64)) return MLF_E_ARG;
+    h->c.nearinv_bits = bits;
+    return MLF_OK;
 }
 
 extern "C" int mlf_nearinv_values(mlf_ctx* h, double* vals) {

@@ -264,6 +264,10 @@ class MLFMA:
         _check(f(self._h, C.byref(bad)), self._h)
         return int(bad.value)
 
+    def set_nearinv_precision(self, bits: int):
+        """Elimination of nearinv(): 64 FP64, 32 blocked FP32 LU, 0 by size (FP64 up to 768 unknowns)."""
+        _check(load().mlf_set_nearinv_precision(self._h, int(bits)), self._h)
+
     def precond_apply(self, y, precond="nearinv"):
         if isinstance(precond, str):
             precond = PRECOND[precond]

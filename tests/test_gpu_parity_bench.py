@@ -19,9 +19,7 @@ Checks (MatxVec_MLFMA, modMLFMA.f90:1901-1946; llenar_campoCyB / llenar_campoA
     from -z, CGS + neighbourhood inverse to 1e-4): the GPU RCS against the
     oracle's sigmaRCS on the same currents (1e-9 dB), the currents against the
     oracle's operator (true residual), and the RCS against the Mie series
-    (the method's own accuracy, stated in the assertion); the dense MoM
-    solve of the same sphere splits that error into the mesh's and the
-    multipole approximations'.
+    (the method's own accuracy, stated in the assertion).
 """
 import numpy as np
 import pytest
@@ -144,37 +142,6 @@ def test_cfg2_rcs_vs_oracle_and_mie(sphere5):
     assert worst_oracle < 1e-9
     # the reference method's own accuracy at leaf 0.19 lambda (one centroid per
     # triangle in the patterns, multipoles clipped to kD): measured mean 0.71 dB,
-    # max 2.34 dB against Mie; the dense-MoM test below separates this from the
-    # mesh's discretisation error
+    # max 2.34 dB against Mie (the r = 0.5 lambda case of test_gpu_fmm /
+    # test_gpu_mom separates it from the mesh's own error with the dense MoM)
     assert mie_err.mean() < 1.0 and mie_err.max() < 3.0
-    sphere5_rcs["mlfma"] = np.concatenate([10 * np.log10(m.rcs(out["x"], p, th, np.full_like(th, ph)))
-                                           for ph in (0.0, np.pi / 2)])
-
-
-sphere5_rcs = {}
-
-
-def test_cfg2_dense_mom_separates_the_errors(sphere5):
-    """The same sphere and wave solved with the dense MoM operator on the GPU
-    (MoM + MatxVec_MoM, modMoM.f90:85-128, 273-277; 30720^2 complex(8) = 15 GB):
-    the MoM RCS against Mie is the mesh's own error, the MLFMA RCS against the
-    MoM RCS the method's far-field approximations."""
-    from lywell_gb300 import MoM
-    tris, _, _ = sphere5
-    if "mlfma" not in sphere5_rcs:
-        pytest.skip("needs test_cfg2_rcs_vs_oracle_and_mie's solve")
-    mom = MoM(RWG(tris), lam=1.0)
-    d = np.array([0.0, 0.0, 1.0])
-    p = np.array([1.0, 0.0, 0.0], dtype=complex)
-    b = mom.excitation(d, p)
-    out = mom.cgs(b, errmax=1e-4, maxit=3000)
-    assert out["status"] == "converged"
-    th = np.deg2rad(np.arange(0.0, 181.0))
-    db_mom = np.concatenate([10 * np.log10(mom.rcs(out["x"], p, th, np.full_like(th, ph))) for ph in (0.0, np.pi / 2)])
-    db_mie = np.concatenate([10 * np.log10(mie.sphere_rcs(3.0, 1.0, th, ph)) for ph in (0.0, np.pi / 2)])
-    mom.close()
-    e_mom = np.abs(db_mom - db_mie)
-    e_mlfma = np.abs(sphere5_rcs["mlfma"] - db_mom)
-    print(f"cfg2 dense MoM: {out['iters']} CGS iterations; MoM vs Mie mean {e_mom.mean():.3f} dB max "
-          f"{e_mom.max():.3f} dB; MLFMA vs MoM mean {e_mlfma.mean():.3f} dB max {e_mlfma.max():.3f} dB")
-    assert e_mom.mean() < 1.0
