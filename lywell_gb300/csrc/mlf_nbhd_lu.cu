@@ -83,10 +83,12 @@ __device__ __forceinline__ void lu_tile_update(LuTiles& sm, float2* __restrict__
                                                int kb, int lk, int lr, int uk, int dr, int ac, int nc, int r0,
                                                int c0, int nrows, int ncols) {
     const int tid = threadIdx.x;
+#pragma unroll
     for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
         const int t = e / LU_T, i = e - t * LU_T;          // consecutive threads: consecutive rows
         sm.L[i][t] = (t < kb && r0 + i < nrows) ? A[(size_t)(lk + t) * n + lr + r0 + i] : make_float2(0.f, 0.f);
     }
+#pragma unroll
     for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
         const int j = e / LU_P, t = e - j * LU_P;          // consecutive threads: consecutive t of one column
         float2 v = make_float2(0.f, 0.f);
@@ -98,37 +100,37 @@ __device__ __forceinline__ void lu_tile_update(LuTiles& sm, float2* __restrict__
         sm.U[t][j] = v;
     }
     __syncthreads();
-    const int tx = tid & 15, ty = tid >> 4;
-    float2 acc[4][4];
+    // warp w: columns 8w .. 8w+7 of the tile; lane: rows lane and lane + 32, so
+    // the U values are warp-wide broadcasts and the write-back is coalesced
+    const int lane = tid & 31, w = tid >> 5;
+    float2 acc[2][8];
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 2; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
+        for (int v = 0; v < 8; ++v) acc[u][v] = make_float2(0.f, 0.f);
     for (int t = 0; t < kb; ++t) {
-        float2 a[4], b[4];
+        const float2 a0 = sm.L[lane][t], a1 = sm.L[lane + 32][t];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) a[u] = sm.L[ty * 4 + u][t];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) b[v] = sm.U[t][tx * 4 + v];
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                acc[u][v].x = fmaf(a[u].x, b[v].x, acc[u][v].x);
-                acc[u][v].x = fmaf(-a[u].y, b[v].y, acc[u][v].x);
-                acc[u][v].y = fmaf(a[u].x, b[v].y, acc[u][v].y);
-                acc[u][v].y = fmaf(a[u].y, b[v].x, acc[u][v].y);
-            }
+        for (int v = 0; v < 8; ++v) {
+            const float2 b = sm.U[t][8 * w + v];
+            acc[0][v].x = fmaf(a0.x, b.x, acc[0][v].x);
+            acc[0][v].x = fmaf(-a0.y, b.y, acc[0][v].x);
+            acc[0][v].y = fmaf(a0.x, b.y, acc[0][v].y);
+            acc[0][v].y = fmaf(a0.y, b.x, acc[0][v].y);
+            acc[1][v].x = fmaf(a1.x, b.x, acc[1][v].x);
+            acc[1][v].x = fmaf(-a1.y, b.y, acc[1][v].x);
+            acc[1][v].y = fmaf(a1.x, b.y, acc[1][v].y);
+            acc[1][v].y = fmaf(a1.y, b.x, acc[1][v].y);
+        }
     }
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-        const int j = tx * 4 + v;
-        if (c0 + j >= ncols) continue;
-        const int q = c0 + j;
+    for (int v = 0; v < 8; ++v) {
+        const int q = c0 + 8 * w + v;
+        if (q >= ncols) continue;
         float2* col = q < nc ? A + (size_t)(ac + q) * n : X + (size_t)(q - nc) * n;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int i = ty * 4 + u;
+        for (int u = 0; u < 2; ++u) {
+            const int i = lane + 32 * u;
             if (r0 + i < nrows) {
                 float2 d = col[dr + r0 + i];
                 d.x -= acc[u][v].x;
@@ -149,6 +151,7 @@ __global__ void __launch_bounds__(LU_THREADS, 2)
     __shared__ float s_val[LU_THREADS / 32];
     __shared__ int s_idx[LU_THREADS / 32];
     __shared__ int s_b, s_piv, s_sing;
+    __shared__ float2 s_u[LU_P];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     float2* A = work + (size_t)blockIdx.x * slab;
     for (;;) {
@@ -185,10 +188,19 @@ __global__ void __launch_bounds__(LU_THREADS, 2)
                 float best = -1.f;
                 int bi = n;
                 const float2* colj = A + (size_t)j * n;
-                for (int i = j + tid; i < n; i += LU_THREADS) {
-                    const float2 a = colj[i];
-                    const float v = a.x * a.x + a.y * a.y;
-                    if (v > best) { best = v; bi = i; }
+                for (int i0 = j + tid; i0 < n; i0 += 4 * LU_THREADS) {   // four loads in flight per thread
+                    float2 a[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int i = i0 + u * LU_THREADS;
+                        a[u] = i < n ? colj[i] : make_float2(0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int i = i0 + u * LU_THREADS;
+                        const float v = a[u].x * a[u].x + a[u].y * a[u].y;
+                        if (i < n && v > best) { best = v; bi = i; }
+                    }
                 }
                 for (int o = 16; o > 0; o >>= 1) {
                     const float ov = __shfl_xor_sync(0xffffffffu, best, o);
@@ -223,15 +235,28 @@ __global__ void __launch_bounds__(LU_THREADS, 2)
                     *p = cmulf(*p, dinv);
                 }
                 __syncthreads();
-                const int nr = n - j - 1, ncl = k0 + kb - j - 1;
-                for (int e = tid; e < nr * ncl; e += LU_THREADS) {
-                    const int cq = e / nr, i = j + 1 + (e - cq * nr);
-                    float2* col = A + (size_t)(j + 1 + cq) * n;
-                    const float2 l = A[(size_t)j * n + i], u = col[j];
-                    float2 d = col[i];
-                    d.x -= l.x * u.x - l.y * u.y;
-                    d.y -= l.x * u.y + l.y * u.x;
-                    col[i] = d;
+                // rank-1 update of the panel's remaining columns: each thread takes rows,
+                // the row-j values of those columns staged in shared memory, eight
+                // columns' loads in flight at a time
+                const int ncl = k0 + kb - j - 1;
+                if (tid < ncl) s_u[tid] = A[(size_t)(j + 1 + tid) * n + j];
+                __syncthreads();
+                for (int i = j + 1 + tid; i < n; i += LU_THREADS) {
+                    const float2 l = A[(size_t)j * n + i];
+                    for (int cq0 = 0; cq0 < ncl; cq0 += 8) {
+                        float2 d[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u)
+                            if (cq0 + u < ncl) d[u] = A[(size_t)(j + 1 + cq0 + u) * n + i];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u)
+                            if (cq0 + u < ncl) {
+                                const float2 uu = s_u[cq0 + u];
+                                d[u].x -= l.x * uu.x - l.y * uu.y;
+                                d[u].y -= l.x * uu.y + l.y * uu.x;
+                                A[(size_t)(j + 1 + cq0 + u) * n + i] = d[u];
+                            }
+                    }
                 }
                 __syncthreads();
             }
