@@ -25,8 +25,8 @@
 //       operand tiles in shared memory);
 //   back substitution U X = Y by blocks of 32 rows from the bottom (a small
 //   triangular solve per block, then a tiled GEMM update of the rows above).
-// Persistent CTAs (two per SM) take boxes from an atomic counter, so large and
-// small neighbourhoods balance over the GPU.
+// Persistent CTAs (two per SM) take boxes from an atomic counter, largest
+// neighbourhoods first, so large and small neighbourhoods balance over the GPU.
 //
 // FP32 with partial pivoting leaves the preconditioner's rows within ~1e-5 of
 // the FP64 ones (tested); a preconditioner only has to be close, and the
@@ -145,8 +145,8 @@ __device__ __forceinline__ void lu_tile_update(LuTiles& sm, float2* __restrict__
 __global__ void __launch_bounds__(LU_THREADS, 2)
     k_nbhd_lu32(int nb, const int* __restrict__ box_ptr, const int* __restrict__ box_bases,
                 const int* __restrict__ ia, const int* __restrict__ ja, const float2* __restrict__ Z, size_t slab,
-                float2* __restrict__ work, double2* __restrict__ M, int* __restrict__ next_box,
-                int* __restrict__ bad) {
+                float2* __restrict__ work, double2* __restrict__ M, const int* __restrict__ order,
+                int* __restrict__ next_box, int* __restrict__ bad) {
     __shared__ LuTiles sm;
     __shared__ float s_val[LU_THREADS / 32];
     __shared__ int s_idx[LU_THREADS / 32];
@@ -156,7 +156,8 @@ __global__ void __launch_bounds__(LU_THREADS, 2)
     float2* A = work + (size_t)blockIdx.x * slab;
     for (;;) {
         if (tid == 0) {
-            s_b = atomicAdd(next_box, 1);
+            const int k = atomicAdd(next_box, 1);
+            s_b = k < nb ? order[k] : nb;      // largest neighbourhoods first
             s_sing = 0;
         }
         __syncthreads();
@@ -372,18 +373,28 @@ int nbhd_inverse_lu32(Ctx* c, int nmax, int nownmax, int* bad_box) {
     const size_t slab = (size_t)nmax * nmax + (size_t)nmax * nownmax;
     int nsm = 0;
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev));
-    // two CTAs per SM, within 32 GB of slabs
-    const size_t cap = ((size_t)32 << 30) / (slab * sizeof(float2));
+    // two CTAs per SM, the slabs within half of the free device memory
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    const size_t cap = (fr / 2) / (slab * sizeof(float2));
     const int grid = (int)std::max<size_t>(1, std::min<size_t>({(size_t)2 * nsm, (size_t)nb, cap}));
+    // boxes by decreasing neighbourhood size, so that the largest do not finish last
+    std::vector<int> order(nb);
+    for (int b = 0; b < nb; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b2) {
+        return c->near_ptr[a + 1] - c->near_ptr[a] > c->near_ptr[b2 + 1] - c->near_ptr[b2];
+    });
     float2* work = nullptr;
-    int *dctr = nullptr, *dbad = nullptr;
+    int *dctr = nullptr, *dbad = nullptr, *dorder = nullptr;
     CK(ds.alloc(&work, slab * grid * sizeof(float2)));
+    CK(ds.alloc(&dorder, std::max(nb, 1) * sizeof(int)));
+    CK(cudaMemcpyAsync(dorder, order.data(), nb * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     CK(ds.alloc(&dctr, 2 * sizeof(int)));
     dbad = dctr + 1;
     const int init[2] = {0, 0x7fffffff};
     CK(cudaMemcpyAsync(dctr, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
     k_nbhd_lu32<<<grid, LU_THREADS, 0, c->stream>>>(nb, c->dbox_ptr, c->dperm, c->dia, c->dja, c->dZ, slab, work,
-                                                    c->dMinv, dctr, dbad);
+                                                    c->dMinv, dorder, dctr, dbad);
     CK(cudaGetLastError());
     int hbad = 0;
     CK(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
