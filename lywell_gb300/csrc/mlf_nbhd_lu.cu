@@ -20,9 +20,10 @@
 //     * U12 = L11^-1 A12 for the trailing columns and the right-hand sides X
 //       (forward substitution on 32 x 64 tiles in shared memory, one thread
 //       per column);
-//     * trailing update A22 -= L21 U12 and X2 -= L21 X1 as 64 x 64 complex
-//       tiles of a register-blocked FP32 GEMM (each thread 4 x 4 outputs,
-//       operand tiles in shared memory);
+//     * trailing update A22 -= L21 U12 and X2 -= L21 X1 by strips of 64
+//       rows: a register-blocked FP32 GEMM over 64 x 64 complex tiles (each
+//       thread 2 x 8 outputs), L staged once per strip, the next U tile and
+//       the current output tile loaded while the FMAs run;
 //   back substitution U X = Y by blocks of 32 rows from the bottom (a small
 //   triangular solve per block, then a tiled GEMM update of the rows above).
 // Persistent CTAs (two per SM) take boxes from an atomic counter, largest
@@ -69,77 +70,107 @@ __device__ __forceinline__ int bsearch_cols(const int* S, int n, int v) {
     return -1;
 }
 
-// D(rows r0.., cols c0..) -= Lop * Uop over K = kb, one 64 x 64 tile:
+// One 64-row strip of D -= Lop * Uop over K = kb, 64 columns at a time:
 //   Lop(i, t) = A[(lk + t) * n + lr + r0 + i]                     (column-major panel)
-//   Uop(t, j) = col(c0 + j)[uk + t],  col(q) = q < nc ? A + (ac + q) * n : X + (q - nc) * n
-//   D(i, j)   = col(c0 + j)[dr + r0 + i]
-// rows < nrows and columns < ncols only; the caller synchronises around it.
+//   Uop(t, j) = col(j)[uk + t],  col(q) = q < nc ? A + (ac + q) * n : X + (q - nc) * n
+//   D(i, j)   = col(j)[dr + r0 + i]
+// rows r0 .. r0+63 (< nrows), all columns < ncols.  The L tile is staged once
+// per strip; while a column tile is multiplied, the next tile's U values and
+// the current tile's D values are already in flight (registers), so the loads
+// overlap the FMAs.  Warp w owns columns 8w .. 8w+7 of a tile and each lane
+// rows lane and lane + 32: the U values are warp-wide broadcasts and the D
+// accesses coalesced.  The caller synchronises before; this ends synchronised.
 struct LuTiles {
     float2 L[LU_T][LU_P + 1];
-    float2 U[LU_P][LU_T + 1];
+    float2 U[2][LU_P][LU_T + 1];
 };
 
-__device__ __forceinline__ void lu_tile_update(LuTiles& sm, float2* __restrict__ A, float2* __restrict__ X, int n,
-                                               int kb, int lk, int lr, int uk, int dr, int ac, int nc, int r0,
-                                               int c0, int nrows, int ncols) {
-    const int tid = threadIdx.x;
+__device__ __forceinline__ float2* lu_col(float2* A, float2* X, int n, int ac, int nc, int q) {
+    return q < nc ? A + (size_t)(ac + q) * n : X + (size_t)(q - nc) * n;
+}
+
+__device__ __forceinline__ void lu_strip_update(LuTiles& sm, float2* __restrict__ A, float2* __restrict__ X, int n,
+                                                int kb, int lk, int lr, int uk, int dr, int ac, int nc, int r0,
+                                                int nrows, int ncols) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    constexpr int PER = LU_T * LU_P / LU_THREADS;   // U values per thread per tile (8)
 #pragma unroll
     for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
         const int t = e / LU_T, i = e - t * LU_T;          // consecutive threads: consecutive rows
         sm.L[i][t] = (t < kb && r0 + i < nrows) ? A[(size_t)(lk + t) * n + lr + r0 + i] : make_float2(0.f, 0.f);
     }
+    float2 un[PER];
+    auto load_u = [&](int c0) {
 #pragma unroll
-    for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
-        const int j = e / LU_P, t = e - j * LU_P;          // consecutive threads: consecutive t of one column
-        float2 v = make_float2(0.f, 0.f);
-        if (t < kb && c0 + j < ncols) {
-            const int q = c0 + j;
-            const float2* col = q < nc ? A + (size_t)(ac + q) * n : X + (size_t)(q - nc) * n;
-            v = col[uk + t];
+        for (int k = 0; k < PER; ++k) {
+            const int e = tid + k * LU_THREADS;
+            const int j = e / LU_P, t = e - j * LU_P;      // consecutive threads: consecutive t of one column
+            un[k] = (t < kb && c0 + j < ncols) ? lu_col(A, X, n, ac, nc, c0 + j)[uk + t] : make_float2(0.f, 0.f);
         }
-        sm.U[t][j] = v;
-    }
+    };
+    auto stage_u = [&](int buf) {
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int e = tid + k * LU_THREADS;
+            const int j = e / LU_P, t = e - j * LU_P;
+            sm.U[buf][t][j] = un[k];
+        }
+    };
+    load_u(0);
+    stage_u(0);
     __syncthreads();
-    // warp w: columns 8w .. 8w+7 of the tile; lane: rows lane and lane + 32, so
-    // the U values are warp-wide broadcasts and the write-back is coalesced
-    const int lane = tid & 31, w = tid >> 5;
-    float2 acc[2][8];
-#pragma unroll
-    for (int u = 0; u < 2; ++u)
-#pragma unroll
-        for (int v = 0; v < 8; ++v) acc[u][v] = make_float2(0.f, 0.f);
-    for (int t = 0; t < kb; ++t) {
-        const float2 a0 = sm.L[lane][t], a1 = sm.L[lane + 32][t];
+    int buf = 0;
+    for (int c0 = 0; c0 < ncols; c0 += LU_T) {
+        // in flight during the FMAs: the next tile's U values and this tile's D values
+        if (c0 + LU_T < ncols) load_u(c0 + LU_T);
+        float2 d[2][8];
 #pragma unroll
         for (int v = 0; v < 8; ++v) {
-            const float2 b = sm.U[t][8 * w + v];
-            acc[0][v].x = fmaf(a0.x, b.x, acc[0][v].x);
-            acc[0][v].x = fmaf(-a0.y, b.y, acc[0][v].x);
-            acc[0][v].y = fmaf(a0.x, b.y, acc[0][v].y);
-            acc[0][v].y = fmaf(a0.y, b.x, acc[0][v].y);
-            acc[1][v].x = fmaf(a1.x, b.x, acc[1][v].x);
-            acc[1][v].x = fmaf(-a1.y, b.y, acc[1][v].x);
-            acc[1][v].y = fmaf(a1.x, b.y, acc[1][v].y);
-            acc[1][v].y = fmaf(a1.y, b.x, acc[1][v].y);
-        }
-    }
+            const int q = c0 + 8 * w + v;
 #pragma unroll
-    for (int v = 0; v < 8; ++v) {
-        const int q = c0 + 8 * w + v;
-        if (q >= ncols) continue;
-        float2* col = q < nc ? A + (size_t)(ac + q) * n : X + (size_t)(q - nc) * n;
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const int i = lane + 32 * u;
-            if (r0 + i < nrows) {
-                float2 d = col[dr + r0 + i];
-                d.x -= acc[u][v].x;
-                d.y -= acc[u][v].y;
-                col[dr + r0 + i] = d;
+            for (int u = 0; u < 2; ++u) {
+                const int i = lane + 32 * u;
+                d[u][v] = (q < ncols && r0 + i < nrows) ? lu_col(A, X, n, ac, nc, q)[dr + r0 + i]
+                                                        : make_float2(0.f, 0.f);
             }
         }
+        // the K-sum accumulates on its own and is subtracted once (the
+        // in-place form rounds each product against the larger D value)
+        float2 acc[2][8];
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int v = 0; v < 8; ++v) acc[u][v] = make_float2(0.f, 0.f);
+        for (int t = 0; t < kb; ++t) {
+            const float2 a0 = sm.L[lane][t], a1 = sm.L[lane + 32][t];
+#pragma unroll
+            for (int v = 0; v < 8; ++v) {
+                const float2 b = sm.U[buf][t][8 * w + v];
+                acc[0][v].x = fmaf(a0.x, b.x, acc[0][v].x);
+                acc[0][v].x = fmaf(-a0.y, b.y, acc[0][v].x);
+                acc[0][v].y = fmaf(a0.x, b.y, acc[0][v].y);
+                acc[0][v].y = fmaf(a0.y, b.x, acc[0][v].y);
+                acc[1][v].x = fmaf(a1.x, b.x, acc[1][v].x);
+                acc[1][v].x = fmaf(-a1.y, b.y, acc[1][v].x);
+                acc[1][v].y = fmaf(a1.x, b.y, acc[1][v].y);
+                acc[1][v].y = fmaf(a1.y, b.x, acc[1][v].y);
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+            const int q = c0 + 8 * w + v;
+            if (q >= ncols) continue;
+            float2* col = lu_col(A, X, n, ac, nc, q);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int i = lane + 32 * u;
+                if (r0 + i < nrows) col[dr + r0 + i] = make_float2(d[u][v].x - acc[u][v].x, d[u][v].y - acc[u][v].y);
+            }
+        }
+        if (c0 + LU_T < ncols) stage_u(buf ^ 1);
+        __syncthreads();
+        buf ^= 1;
     }
-    __syncthreads();
 }
 
 __global__ void __launch_bounds__(LU_THREADS, 2)
@@ -279,18 +310,18 @@ __global__ void __launch_bounds__(LU_THREADS, 2)
                         const int q = c0 + j;
                         v = (q < nc ? A + (size_t)(k0 + kb + q) * n : X + (size_t)(q - nc) * n)[k0 + t];
                     }
-                    sm.U[t][j] = v;
+                    sm.U[0][t][j] = v;
                 }
                 __syncthreads();
                 if (tid < LU_T) {
                     for (int r = 1; r < kb; ++r) {
-                        float2 acc = sm.U[r][tid];
+                        float2 acc = sm.U[0][r][tid];
                         for (int t = 0; t < r; ++t) {
-                            const float2 l = sm.L[r][t], u = sm.U[t][tid];
+                            const float2 l = sm.L[r][t], u = sm.U[0][t][tid];
                             acc.x -= l.x * u.x - l.y * u.y;
                             acc.y -= l.x * u.y + l.y * u.x;
                         }
-                        sm.U[r][tid] = acc;
+                        sm.U[0][r][tid] = acc;
                     }
                 }
                 __syncthreads();
@@ -298,17 +329,15 @@ __global__ void __launch_bounds__(LU_THREADS, 2)
                     const int j = e / LU_P, t = e - j * LU_P;
                     if (t < kb && c0 + j < ncols) {
                         const int q = c0 + j;
-                        (q < nc ? A + (size_t)(k0 + kb + q) * n : X + (size_t)(q - nc) * n)[k0 + t] = sm.U[t][j];
+                        (q < nc ? A + (size_t)(k0 + kb + q) * n : X + (size_t)(q - nc) * n)[k0 + t] = sm.U[0][t][j];
                     }
                 }
                 __syncthreads();
             }
             // ---- trailing update: rows k0+kb.. of the trailing columns and of X
             const int nrows = n - k0 - kb;
-            if (nrows > 0)
-                for (int r0 = 0; r0 < nrows; r0 += LU_T)
-                    for (int c0 = 0; c0 < ncols; c0 += LU_T)
-                        lu_tile_update(sm, A, X, n, kb, k0, k0 + kb, k0, k0 + kb, k0 + kb, nc, r0, c0, nrows, ncols);
+            for (int r0 = 0; r0 < nrows; r0 += LU_T)
+                lu_strip_update(sm, A, X, n, kb, k0, k0 + kb, k0, k0 + kb, k0 + kb, nc, r0, nrows, ncols);
         }
         if (s_sing) {
             if (tid == 0) atomicMin(bad, b + 1);
@@ -327,32 +356,30 @@ __global__ void __launch_bounds__(LU_THREADS, 2)
                 // a 32 x 64 tile of X in shared memory, backward substitution per column
                 for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
                     const int j = e / LU_P, t = e - j * LU_P;
-                    sm.U[t][j] = (t < kb && c0 + j < nown) ? X[(size_t)(c0 + j) * n + k0 + t] : make_float2(0.f, 0.f);
+                    sm.U[0][t][j] = (t < kb && c0 + j < nown) ? X[(size_t)(c0 + j) * n + k0 + t] : make_float2(0.f, 0.f);
                 }
                 __syncthreads();
                 if (tid < LU_T) {
                     for (int r = kb - 1; r >= 0; --r) {
-                        float2 acc = sm.U[r][tid];
+                        float2 acc = sm.U[0][r][tid];
                         for (int t = r + 1; t < kb; ++t) {
-                            const float2 u = sm.L[r][t], x = sm.U[t][tid];
+                            const float2 u = sm.L[r][t], x = sm.U[0][t][tid];
                             acc.x -= u.x * x.x - u.y * x.y;
                             acc.y -= u.x * x.y + u.y * x.x;
                         }
-                        sm.U[r][tid] = cmulf(acc, cinvf(sm.L[r][r]));
+                        sm.U[0][r][tid] = cmulf(acc, cinvf(sm.L[r][r]));
                     }
                 }
                 __syncthreads();
                 for (int e = tid; e < LU_T * LU_P; e += LU_THREADS) {
                     const int j = e / LU_P, t = e - j * LU_P;
-                    if (t < kb && c0 + j < nown) X[(size_t)(c0 + j) * n + k0 + t] = sm.U[t][j];
+                    if (t < kb && c0 + j < nown) X[(size_t)(c0 + j) * n + k0 + t] = sm.U[0][t][j];
                 }
                 __syncthreads();
             }
             // rows 0..k0-1 of X -= U(0..k0-1, k0..k0+kb-1) X(k0..k0+kb-1)
-            if (k0 > 0)
-                for (int r0 = 0; r0 < k0; r0 += LU_T)
-                    for (int c0 = 0; c0 < nown; c0 += LU_T)
-                        lu_tile_update(sm, A, X, n, kb, k0, 0, k0, 0, 0, 0, r0, c0, k0, nown);
+            for (int r0 = 0; r0 < k0; r0 += LU_T)
+                lu_strip_update(sm, A, X, n, kb, k0, 0, k0, 0, 0, 0, r0, k0, nown);
         }
         // ---- M rows of the own bases: M[ia[g] + j] = X(j, own index)
         for (int cc = 0; cc < nown; ++cc) {
