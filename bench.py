@@ -229,7 +229,7 @@ def batched_rcs_722(seq_angles=3, block=0, maxit=4000):
     in blocks of right-hand sides (autotuned block size and engine), each
     block column sweeping a run of angles with extrapolated warm starts
     (mlf_monostatic mode 4).  Time to RCS = geometry and operator set-up +
-    preconditioner set-up (own-box near-field inverse) + autotuning + the two
+    preconditioner set-up (27-box neighbourhood inverse, blocked FP32 LU) + autotuning + the two
     sweeps, which include the backscatter RCS of every angle.  The plain FP64
     GPU path -- the reference's sequential warm-started CGS sweep
     (gen_rcs_monostatica, main.f90:967-1089) on the FP64 operator, same
@@ -245,7 +245,8 @@ def batched_rcs_722(seq_angles=3, block=0, maxit=4000):
     torch.cuda.synchronize()
     t_tree = time.time() - t0
     t0 = time.time()
-    bad = m.nearinv(own_only=True)
+    bad = m.nearinv()
+    torch.cuda.synchronize()
     t_pre = time.time() - t0
     t0 = time.time()
     tune = m.autotune_block() if block <= 0 else dict(block=block, tile_cols=0, per_rhs_ms={})
@@ -275,7 +276,8 @@ def batched_rcs_722(seq_angles=3, block=0, maxit=4000):
     status = sorted({s for pol in sweeps for s in sweeps[pol]["status"]})
     ttr = t_tree + t_pre + t_tune + t_sweep
     out = {"workload": SPHEROID["name"], "N": m.N, "near_nnz": m.nnz, "setup_s": t_tree, "precond_setup_s": t_pre,
-           "precond": "own-box near-field inverse", "nearinv_bad_box": bad, "autotune": tune, "autotune_s": t_tune,
+           "precond": "27-box neighbourhood inverse (blocked FP32 LU per leaf box)", "nearinv_bad_box": bad,
+           "autotune": tune, "autotune_s": t_tune,
            "block": B,
            "measured_722": {"mode": 4, "angles": 2 * nang, "sweep_s": t_sweep, "time_to_rcs_s": ttr,
                             "status": status, "iters_per_block": blocks,
