@@ -437,6 +437,7 @@ int mlf_precond_apply32(mlf_ctx* h, const double* y, double* x, int nrhs) {
         st = d2h_cols(c, x, c->dy_io, nrhs, c->N);
     }
     if (!st && !cuda_ok(c, cudaStreamSynchronize(c->stream), "precond32")) st = MLF_E_CUDA;
+    if (!st && blk_engine_of(c) == 4) st = tc_check(c);
     return st;
 }
 

@@ -506,6 +506,7 @@ extern "C" int mlf_lp_install(mlf_ctx* h, mlf_mlp* net, float scale, int* nonfin
     if (st) return st;
     if (c->dMinv32) { cudaFree(c->dMinv32); c->dMinv32 = nullptr; }   // FP32 copies rebuilt on next use
     if (c->dMinvblk) { cudaFree(c->dMinvblk); c->dMinvblk = nullptr; }
+    tc_drop_precond(c);
     *nonfinite = hbad;
     c->learned = 1;
     return MLF_OK;

@@ -314,8 +314,12 @@ int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStr
             if ((st = device_blk_pack(c, nullptr, y, c->N, nrhs, c->dpre_xs, s))) return st;
             return device_near_pattern_warp32(c, c->dMinv32, c->dpre_xs, nrhs, x, s);
         }
-        if (!c->dMinvblk && (st = device_blocks_from_csr(c, c->dMinv32, &c->dMinvblk))) return st;
+        if (!c->dMinvblk) {
+            if ((st = device_blocks_from_csr(c, c->dMinv32, &c->dMinvblk))) return st;
+            tc_drop_precond(c);
+        }
         if ((st = device_blk_pack(c, nullptr, y, c->N, nrhs, c->dpre_xs, s))) return st;
+        if (blk_engine_of(c) == 4) return device_near_pattern_tc(c, c->dMinvblk, c->dpre_xs, nrhs, x, s);
         return device_near_pattern_apply32(c, c->dMinvblk, c->dpre_xs, nrhs, x, s);
     }
     if (c->nearinv_own)
@@ -345,6 +349,7 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     if (c->dMinv32) cudaFree(c->dMinv32);
     if (c->dMinvblk) cudaFree(c->dMinvblk);
     c->dMinvblk = nullptr;
+    tc_drop_precond(c);
     if (c->dMinv_base) cudaFree(c->dMinv_base);
     c->dMinv_base = nullptr;
     c->dMinv = nullptr;

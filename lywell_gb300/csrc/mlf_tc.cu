@@ -82,6 +82,7 @@ struct TcState {
     int2* dchunk = nullptr;         // per chunk: (first box-sorted position, bases in it)
     int* derr = nullptr;            // set by a CTA whose wait gave up
     TcOperand Z;
+    TcOperand M;                    // the neighbourhood-inverse preconditioner on the near pattern (hi null: not built)
     float *xhi = nullptr, *xlo = nullptr;
     long long xrows_cap = 0;
     CUtensorMap mxhi, mxlo;
@@ -345,7 +346,7 @@ void tc_free(Ctx* c) {
     if (!t) return;
     auto F = [](void* p) { if (p) cudaFree(p); };
     F(t->dtiles); F(t->dzrow); F(t->dcbase); F(t->dchunk); F(t->derr);
-    F(t->Z.hi); F(t->Z.lo); F(t->xhi); F(t->xlo);
+    F(t->Z.hi); F(t->Z.lo); F(t->M.hi); F(t->M.lo); F(t->xhi); F(t->xlo);
     delete t;
     c->tc = nullptr;
 }
@@ -456,6 +457,43 @@ int device_near_tc(Ctx* c, const float2* xs, int ld, int nrhs, double2* y, cudaS
         t->Z.mhi, t->Z.mlo, t->mxhi, t->mxlo, t->dtiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, t->dzrow,
         t->dcbase, t->nchunk, nrhs, ld, c->dperm, y, nullptr, t->derr);
     return cuda_ok(c, cudaGetLastError(), "tensor-core near field") ? MLF_OK : MLF_E_CUDA;
+}
+
+// out (FP32 columns, ld N) = M xs for the near-pattern preconditioner M, given
+// as box-pair blocks (the layout of the near field's): the same kernel with M
+// in place of Z, its operand layout built on first use after each rebuild of M
+int device_near_pattern_tc(Ctx* c, const float2* Mblk, const float2* xs, int nrhs, float2* out, cudaStream_t s) {
+    int st;
+    if ((st = tc_setup(c))) return st;
+    if ((st = tc_x_buffers(c, nrhs))) return st;
+    TcState* t = c->tc;
+    if (!t->M.hi) {
+        const size_t zfl = (size_t)std::max<long long>(t->zrows, 1) * 32;
+        CK(cudaMalloc(&t->M.hi, zfl * sizeof(float)));
+        CK(cudaMalloc(&t->M.lo, zfl * sizeof(float)));
+        const int ne = (int)c->nbox_list.size();
+        if (ne)
+            k_tc_fill_z<<<ne, 256, 0, s>>>(c->dblk_entry, c->dnbox_list, c->dblk_off, c->dbox_ptr, t->dzrow, Mblk,
+                                           t->M.hi, t->M.lo);
+        CK(cudaGetLastError());
+        if ((st = make_rows_map(c, &t->M.mhi, t->M.hi, t->zrows, TC_ZBOX))) return st;
+        if ((st = make_rows_map(c, &t->M.mlo, t->M.lo, t->zrows, TC_ZBOX))) return st;
+    }
+    const int nct = (nrhs + TC_COLS - 1) / TC_COLS;
+    k_tc_pack_x<<<dim3(t->nchunk, nct), 256, 0, s>>>(t->nchunk, nrhs, t->dchunk, xs, t->xhi, t->xlo);
+    k_tc_near<1><<<dim3(t->ntiles, nct), 128, TC_SMEM, s>>>(
+        t->M.mhi, t->M.mlo, t->mxhi, t->mxlo, t->dtiles, c->dbox_ptr, c->dnbox_ptr, c->dnbox_list, t->dzrow,
+        t->dcbase, t->nchunk, nrhs, c->N, c->dperm, nullptr, out, t->derr);
+    return cuda_ok(c, cudaGetLastError(), "tensor-core near-pattern preconditioner") ? MLF_OK : MLF_E_CUDA;
+}
+
+// the preconditioner's operand layout is stale once its blocks are rebuilt
+void tc_drop_precond(Ctx* c) {
+    TcState* t = c->tc;
+    if (!t) return;
+    if (t->M.hi) cudaFree(t->M.hi);
+    if (t->M.lo) cudaFree(t->M.lo);
+    t->M.hi = t->M.lo = nullptr;
 }
 
 // error flag of the tensor-core kernels since the last check (0: none)

@@ -179,7 +179,7 @@ def test_own_box_fp32_block_apply(ico4, ncols, engine):
         assert m.nearinv() == 0
 
 
-@pytest.mark.parametrize("engine", [1, 0, 2])
+@pytest.mark.parametrize("engine", [1, 0, 2, 4])
 @pytest.mark.parametrize("ncols", [1, 3, 12, 40])
 def test_neighbourhood_fp32_block_apply(ico4, ncols, engine):
     """The FP32 neighbourhood inverse of the mixed inner loop: one column by the
