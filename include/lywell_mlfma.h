@@ -209,8 +209,10 @@ int mlf_set_stagnation(mlf_ctx* ctx, int window);
  * complex(4) near field), stopped when its residual estimate drops below
  * inner_tol ||b|| (<= 0: 0.9 tol).  Stops when the FP64 residual satisfies
  * ||b - Z x|| < tol ||b||, the same test as CGSold (modIterativo.f90:472).
- * iters: inner GMRES steps (FP32 matvecs) per column; *outer: refinement
- * steps (FP64 matvecs).  No counterpart in the reference for mode 1. */
+ * The first cycle's right-hand side needs no FP64 operator: it is b itself
+ * without x0, and b - Z32 x0 (FP32 operator) with x0, on which no column is
+ * declared converged.  iters: inner GMRES steps (FP32 matvecs) per column;
+ * *outer: refinement cycles.  No counterpart in the reference for mode 1. */
 int mlf_solve(mlf_ctx* ctx, const double* b, const double* x0, double tol, int maxit, int nrhs,
               int precond_kind, int mode, double inner_tol, double* x, int* iters, double* relres,
               int* status_out, int* outer);
@@ -352,7 +354,9 @@ int mlf_rcs(mlf_ctx* ctx, const double* I, const double* pol, double ctte_re, do
  * mode 4: mode 3 with each column's start extrapolated linearly from its
  *         two previous angles' currents, both phase-shifted to the new
  *         direction (x0 = 2 x_{k-1} - x_{k-2}).
- * block <= 0 (modes 1-4): chosen by mlf_autotune_block among 8..128.
+ * block <= 0 (modes 1-4): chosen by mlf_autotune_block among 8..128 (modes
+ * 3 and 4: at most nang / 4, so that every column sweeps at least four
+ * angles).
  * Modes 1-4 have no counterpart in the reference. */
 int mlf_monostatic(mlf_ctx* ctx, int nang, const double* phis, int hh, double ctte_re, double ctte_im,
                    double tol, int maxit, int precond_kind, int mode, int block, double* sigma, int* iters,

@@ -849,9 +849,22 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
     }
     const auto t_start = std::chrono::steady_clock::now();
     for (; k < max_outer; ++k) {
-        c->mv_prec = 0;
-        if ((st = device_matvec(c, x, t64, nrhs, N, s))) break;
-        k_resid<<<4096, 256, 0, s>>>(V1, b, t64, r);
+        // The residual that decides convergence is always FP64.  Two first
+        // steps need no FP64 operator: with no initial guess r = b exactly;
+        // with a warm start, the first cycle's right-hand side b - Z x0 is
+        // formed with the FP32 operator and only feeds the inner solve (no
+        // column is declared converged on it), the FP64 residual after the
+        // cycle deciding as always.
+        const bool provisional = k == 0 && x0 != nullptr;
+        if (k == 0 && !x0) {
+            CK(cudaMemcpyAsync(r, b, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        } else {
+            c->mv_prec = provisional ? 1 : 0;
+            st = device_matvec(c, x, t64, nrhs, N, s);
+            c->mv_prec = 0;
+            if (st) break;
+            k_resid<<<4096, 256, 0, s>>>(V1, b, t64, r);
+        }
         if ((st = col_norms(c, nrhs, r, partial, dred, hbuf, beta, s))) break;
         bool all = true, budget = false;
         for (int col = 0; col < nrhs; ++col) {
@@ -860,8 +873,11 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
             const bool finite = std::isfinite(bn[col]) && std::isfinite(beta[col]);
             relres[col] = !finite ? beta[col] / bn[col] : (bn[col] > 0 ? beta[col] / bn[col] : 0.0);
             if (!finite && !done[col]) { done[col] = 1; status[col] = MLF_CGS_NOT_FINITE; }
-            if (!done[col] && (relres[col] < tol || bn[col] == 0)) { done[col] = 1; status[col] = MLF_CGS_CONVERGED; }
-            if (c->stag_window > 0 && !done[col]) {
+            if (!done[col] && !provisional && (relres[col] < tol || bn[col] == 0)) {
+                done[col] = 1;
+                status[col] = MLF_CGS_CONVERGED;
+            }
+            if (c->stag_window > 0 && !done[col] && !provisional) {
                 if (relres[col] < sbest[col]) {
                     sbest[col] = relres[col];
                     sbest_it[col] = iters[col];

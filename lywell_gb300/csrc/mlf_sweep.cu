@@ -123,9 +123,13 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
     int bsel = block;
     if (bsel <= 0) {
         // autotuned block: candidates up to the sweep length
+        // modes 3 and 4: blocks small enough that every column sweeps a run of
+        // at least four angles, so that most blocks start from extrapolated
+        // warm starts
         std::vector<int> cand;
+        const int bcap = mode >= 3 ? std::max(8, nang / 4) : nang;
         for (int b : {8, 16, 32, 64, 128})
-            if (b <= nang) cand.push_back(b);
+            if (b <= bcap) cand.push_back(b);
         if (cand.empty()) cand.push_back(nang);
         int cols = 0;
         if ((st = autotune_block(c, cand.data(), (int)cand.size(), &bsel, &cols, nullptr, nullptr))) return st;
