@@ -249,7 +249,10 @@ def batched_rcs_722(seq_angles=3, block=0, maxit=4000):
     torch.cuda.synchronize()
     t_pre = time.time() - t0
     t0 = time.time()
-    tune = m.autotune_block() if block <= 0 else dict(block=block, tile_cols=0, per_rhs_ms={})
+    # blocks of at most a quarter of the 361 angles of a sweep, so that every
+    # column sweeps a run of at least four angles from extrapolated warm starts
+    tune = (m.autotune_block(candidates=(8, 16, 32, 64)) if block <= 0
+            else dict(block=block, tile_cols=0, per_rhs_ms={}))
     t_tune = time.time() - t0
     B = int(tune["block"])
     nang = 361
@@ -452,7 +455,7 @@ def learned_at_scale(steps=3000, seed=0):
     lp.apply_to(m)
     t_inst = time.time() - t1
     t1 = time.time()
-    tune = m.autotune_block()
+    tune = m.autotune_block(candidates=(8, 16, 32, 64))   # runs of at least four angles per column
     t_tune = time.time() - t1
     B = int(tune["block"])
     torch.cuda.synchronize()
