@@ -69,130 +69,6 @@ __global__ void k_lp_dense(int N, const double* __restrict__ t_baric, const doub
     }
 }
 
-// Rows of inv(Z[S2, S2]) for the own bases of box b, on the near pattern
-// (FP32 Gaussian elimination with partial pivoting on A^T, one CTA per box).
-__global__ void __launch_bounds__(256) k_ring_inverse32(int b0, int nb, const long long* __restrict__ ring_off,
-                                                        const int* __restrict__ ring_len,
-                                                        const int* __restrict__ ring_bases,
-                                                        const int* __restrict__ box_ptr, const int* __restrict__ perm,
-                                                        const float2* __restrict__ Zd, int N,
-                                                        const int* __restrict__ ia, const int* __restrict__ ja,
-                                                        size_t slab, float2* __restrict__ work,
-                                                        float2* __restrict__ M2, int* __restrict__ bad) {
-    const int b = b0 + blockIdx.x;
-    if (b >= nb) return;
-    const int tid = threadIdx.x, bd = blockDim.x;
-    const int n = ring_len[b];
-    const int* S = ring_bases + ring_off[b];
-    const int nown = box_ptr[b + 1] - box_ptr[b];
-    float2* At = work + (size_t)blockIdx.x * slab;
-    float2* X = At + (size_t)n * n;
-    for (size_t e = tid; e < (size_t)n * n; e += bd) {
-        const int pos = (int)(e / n), r = (int)(e - (size_t)pos * n);
-        At[e] = Zd[(size_t)S[r] * N + S[pos]];
-    }
-    for (int e = tid; e < n * nown; e += bd) X[e] = make_float2(0.f, 0.f);
-    __syncthreads();
-    for (int i = tid; i < nown; i += bd) {
-        const int pos = find_sorted(S, n, perm[box_ptr[b] + i]);
-        X[(size_t)pos * nown + i] = make_float2(1.f, 0.f);
-    }
-    __shared__ float s_val[8];
-    __shared__ int s_idx[8];
-    __shared__ int s_piv, s_sing;
-    if (tid == 0) s_sing = 0;
-    __syncthreads();
-    for (int k = 0; k < n; ++k) {
-        float best = -1.f;
-        int bi = n;
-        for (int i = k + tid; i < n; i += bd) {
-            const float2 a = At[(size_t)i * n + k];
-            const float v = a.x * a.x + a.y * a.y;
-            if (v > best) { best = v; bi = i; }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const float ov = __shfl_xor_sync(0xffffffff, best, o);
-            const int oi = __shfl_xor_sync(0xffffffff, bi, o);
-            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-        }
-        if ((tid & 31) == 0) { s_val[tid >> 5] = best; s_idx[tid >> 5] = bi; }
-        __syncthreads();
-        if (tid == 0) {
-            float bv = s_val[0];
-            int bx = s_idx[0];
-            for (int w = 1; w < bd / 32; ++w)
-                if (s_val[w] > bv || (s_val[w] == bv && s_idx[w] < bx)) { bv = s_val[w]; bx = s_idx[w]; }
-            s_piv = bx;
-            if (!(bv > 0.f)) s_sing = 1;
-        }
-        __syncthreads();
-        if (s_sing) break;
-        const int piv = s_piv;
-        if (piv != k) {
-            for (int j = tid; j < n; j += bd) {
-                const float2 t = At[(size_t)k * n + j];
-                At[(size_t)k * n + j] = At[(size_t)piv * n + j];
-                At[(size_t)piv * n + j] = t;
-            }
-            for (int j = tid; j < nown; j += bd) {
-                const float2 t = X[(size_t)k * nown + j];
-                X[(size_t)k * nown + j] = X[(size_t)piv * nown + j];
-                X[(size_t)piv * nown + j] = t;
-            }
-        }
-        __syncthreads();
-        const float2 d = At[(size_t)k * n + k];
-        for (int i = k + 1 + tid; i < n; i += bd) At[(size_t)i * n + k] = cdivf(At[(size_t)i * n + k], d);
-        __syncthreads();
-        const int rows = n - k - 1, wcols = (n - k - 1) + nown;
-        for (long long e = tid; e < (long long)rows * wcols; e += bd) {
-            const int i = k + 1 + (int)(e / wcols), jj = (int)(e % wcols);
-            const float2 f = At[(size_t)i * n + k];
-            float2* dst;
-            float2 src;
-            if (jj < n - k - 1) {
-                dst = &At[(size_t)i * n + k + 1 + jj];
-                src = At[(size_t)k * n + k + 1 + jj];
-            } else {
-                dst = &X[(size_t)i * nown + (jj - (n - k - 1))];
-                src = X[(size_t)k * nown + (jj - (n - k - 1))];
-            }
-            float2 v = *dst;
-            v.x -= f.x * src.x - f.y * src.y;
-            v.y -= f.x * src.y + f.y * src.x;
-            *dst = v;
-        }
-        __syncthreads();
-    }
-    if (s_sing) {
-        if (tid == 0) atomicMin(bad, b + 1);
-        return;
-    }
-    for (int k = n - 1; k >= 0; --k) {
-        const float2 d = At[(size_t)k * n + k];
-        for (int j = tid; j < nown; j += bd) X[(size_t)k * nown + j] = cdivf(X[(size_t)k * nown + j], d);
-        __syncthreads();
-        for (int e = tid; e < k * nown; e += bd) {
-            const int i = e / nown, j = e % nown;
-            const float2 f = At[(size_t)i * n + k];
-            const float2 s = X[(size_t)k * nown + j];
-            float2 v = X[(size_t)i * nown + j];
-            v.x -= f.x * s.x - f.y * s.y;
-            v.y -= f.x * s.y + f.y * s.x;
-            X[(size_t)i * nown + j] = v;
-        }
-        __syncthreads();
-    }
-    // own row i, near column ja[q]: X[pos(ja[q]) * nown + i]
-    for (int i = 0; i < nown; ++i) {
-        const int g = perm[box_ptr[b] + i];
-        for (int q = ia[g] + tid; q < ia[g + 1]; q += bd) {
-            const int pos = find_sorted(S, n, ja[q]);
-            M2[q] = pos >= 0 ? X[(size_t)pos * nown + i] : make_float2(0.f, 0.f);
-        }
-    }
-}
-
 // s_m = 1/sqrt(Z_mm) from the near CSR diagonal
 __global__ void k_lp_scale(int N, const int* __restrict__ ia, const int* __restrict__ ja, const float2* __restrict__ Z,
                            float2* __restrict__ s) {
@@ -353,7 +229,6 @@ static int lp_ring_targets(Ctx* c, const LpHost& H, float2* M2, int* bad_box) {
         nmax = std::max(nmax, (size_t)len[b]);
         ownmax = std::max(ownmax, (size_t)(c->box_ptr[b + 1] - c->box_ptr[b]));
     }
-    const size_t slab = nmax * nmax + nmax * ownmax;
     size_t fre = 0, tot = 0;
     CK(cudaMemGetInfo(&fre, &tot));
     const size_t zbytes = (size_t)N * N * sizeof(float2);
@@ -361,44 +236,31 @@ static int lp_ring_targets(Ctx* c, const LpHost& H, float2* M2, int* bad_box) {
         c->err = "not enough device memory for the 2-ring targets";
         return MLF_E_NOMEM;
     }
-    const size_t budget = std::min<size_t>((fre - zbytes - ((size_t)1 << 30)) / 2, (size_t)16 << 30);
-    const int batch = (int)std::max<size_t>(1, std::min<size_t>(nb, budget / (slab * sizeof(float2))));
-    float2 *Zd = nullptr, *work = nullptr;
+    float2* Zd = nullptr;
     long long* doff = nullptr;
-    int *dlen = nullptr, *dbases = nullptr, *dbad = nullptr;
+    int *dlen = nullptr, *dbases = nullptr;
     int st = MLF_OK;
     auto fail = [&](int code) { st = code; };
     if (!cuda_ok(c, cudaMalloc(&Zd, zbytes), "alloc") ||
-        !cuda_ok(c, cudaMalloc(&work, slab * batch * sizeof(float2)), "alloc") ||
         !cuda_ok(c, cudaMalloc(&doff, off.size() * sizeof(long long)), "alloc") ||
         !cuda_ok(c, cudaMalloc(&dlen, len.size() * sizeof(int)), "alloc") ||
-        !cuda_ok(c, cudaMalloc(&dbases, std::max<size_t>(bases.size(), 1) * sizeof(int)), "alloc") ||
-        !cuda_ok(c, cudaMalloc(&dbad, sizeof(int)), "alloc"))
+        !cuda_ok(c, cudaMalloc(&dbases, std::max<size_t>(bases.size(), 1) * sizeof(int)), "alloc"))
         fail(MLF_E_CUDA);
     if (!st) {
-        const int big = 0x7fffffff;
         if (!cuda_ok(c, cudaMemcpy(doff, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice), "copy") ||
             !cuda_ok(c, cudaMemcpy(dlen, len.data(), len.size() * sizeof(int), cudaMemcpyHostToDevice), "copy") ||
-            !cuda_ok(c, cudaMemcpy(dbases, bases.data(), bases.size() * sizeof(int), cudaMemcpyHostToDevice), "copy") ||
-            !cuda_ok(c, cudaMemcpy(dbad, &big, sizeof(int), cudaMemcpyHostToDevice), "copy"))
+            !cuda_ok(c, cudaMemcpy(dbases, bases.data(), bases.size() * sizeof(int), cudaMemcpyHostToDevice), "copy"))
             fail(MLF_E_CUDA);
     }
     if (!st) {
         const double c72 = (double)(1.0f / 72.0f);
         k_lp_dense<<<N, 256, 0, c->stream>>>(N, c->dt_baric, c->dt_baric_sub, c->dp_coord, c->de_t, c->de_po,
                                              c->de_long, c->ph.w, c->ph.w * c->ph.smue, c72, Zd);
-        for (int b0 = 0; b0 < nb && !st; b0 += batch) {
-            k_ring_inverse32<<<std::min(batch, nb - b0), 256, 0, c->stream>>>(
-                b0, nb, doff, dlen, dbases, c->dbox_ptr, c->dperm, Zd, N, c->dia, c->dja, slab, work, M2, dbad);
-            if (!cuda_ok(c, cudaGetLastError(), "ring inverse")) fail(MLF_E_CUDA);
-        }
-        int hbad = 0;
-        if (!st && (!cuda_ok(c, cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "copy") ||
-                    !cuda_ok(c, cudaStreamSynchronize(c->stream), "ring inverse")))
-            fail(MLF_E_CUDA);
-        *bad_box = hbad == 0x7fffffff ? 0 : hbad;
+        if (!cuda_ok(c, cudaGetLastError(), "dense Z")) fail(MLF_E_CUDA);
     }
-    for (void* p : {(void*)Zd, (void*)work, (void*)doff, (void*)dlen, (void*)dbases, (void*)dbad})
+    // blocked FP32 LU per box over its 2-ring list (mlf_nbhd_lu.cu)
+    if (!st) st = ring_inverse_lu32(c, Zd, doff, dlen, dbases, len, (int)nmax, (int)ownmax, M2, bad_box);
+    for (void* p : {(void*)Zd, (void*)doff, (void*)dlen, (void*)dbases})
         if (p) cudaFree(p);
     return st;
 }

@@ -29,6 +29,10 @@
 // Persistent CTAs (two per SM) take boxes from an atomic counter, largest
 // neighbourhoods first, so large and small neighbourhoods balance over the GPU.
 //
+// The same kernel computes the learned preconditioner's training targets
+// (mlf_learned.cu): rows of the inverse over each box's 2-ring (125-box)
+// neighbourhood, the system taken from a dense Z.
+//
 // FP32 with partial pivoting leaves the preconditioner's rows within ~1e-5 of
 // the FP64 ones (tested); a preconditioner only has to be close, and the
 // solves' residual test stays FP64.
@@ -80,6 +84,19 @@ __device__ __forceinline__ int bsearch_cols(const int* S, int n, int v) {
 // overlap the FMAs.  Warp w owns columns 8w .. 8w+7 of a tile and each lane
 // rows lane and lane + 32: the U values are warp-wide broadcasts and the D
 // accesses coalesced.  The caller synchronises before; this ends synchronised.
+// The 2-ring variant (training targets of the learned preconditioner): the
+// system comes from a dense Z (complex(4), row-major N x N) over each box's
+// sorted 2-ring list, and the rows go to M2 on the near pattern.  Zd null:
+// the near-list variant.
+struct LuRing {
+    const float2* Zd = nullptr;
+    int N = 0;
+    const long long* off = nullptr;
+    const int* len = nullptr;
+    const int* bases = nullptr;
+    float2* M2 = nullptr;
+};
+
 struct LuTiles {
     float2 L[LU_T][LU_P + 1];
     float2 U[2][LU_P][LU_T + 1];
@@ -177,7 +194,7 @@ __global__ void __launch_bounds__(LU_THREADS, 2)
     k_nbhd_lu32(int nb, const int* __restrict__ box_ptr, const int* __restrict__ box_bases,
                 const int* __restrict__ ia, const int* __restrict__ ja, const float2* __restrict__ Z, size_t slab,
                 float2* __restrict__ work, double2* __restrict__ M, const int* __restrict__ order,
-                int* __restrict__ next_box, int* __restrict__ bad) {
+                int* __restrict__ next_box, int* __restrict__ bad, const LuRing ring) {
     __shared__ LuTiles sm;
     __shared__ float s_val[LU_THREADS / 32];
     __shared__ int s_idx[LU_THREADS / 32];
@@ -195,17 +212,27 @@ __global__ void __launch_bounds__(LU_THREADS, 2)
         const int b = s_b;
         if (b >= nb) break;
         const int m0 = box_bases[box_ptr[b]], nown = box_ptr[b + 1] - box_ptr[b];
-        const int n = ia[m0 + 1] - ia[m0];
-        const int* S = ja + ia[m0];
+        // the neighbourhood: the near list (the CSR row of the box's bases) or the 2-ring list
+        const int n = ring.Zd ? ring.len[b] : ia[m0 + 1] - ia[m0];
+        const int* S = ring.Zd ? ring.bases + ring.off[b] : ja + ia[m0];
         float2* X = A + (size_t)n * n;
         // A^T column r = row S[r] of Z restricted to S; X = the own bases' unit columns
-        for (size_t e = tid; e < (size_t)n * n + (size_t)n * nown; e += LU_THREADS) A[e] = make_float2(0.f, 0.f);
-        __syncthreads();
-        for (int r = wid; r < n; r += LU_THREADS / 32) {
-            const int m = S[r];
-            for (int q = ia[m] + lane; q < ia[m + 1]; q += 32) {
-                const int pos = bsearch_cols(S, n, ja[q]);
-                if (pos >= 0) A[(size_t)r * n + pos] = Z[q];
+        if (ring.Zd) {
+            for (size_t e = tid; e < (size_t)n * n; e += LU_THREADS) {
+                const int r = (int)(e / n), pos = (int)(e - (size_t)r * n);
+                A[e] = ring.Zd[(size_t)S[r] * ring.N + S[pos]];
+            }
+            for (size_t e = tid; e < (size_t)n * nown; e += LU_THREADS) X[e] = make_float2(0.f, 0.f);
+            __syncthreads();
+        } else {
+            for (size_t e = tid; e < (size_t)n * n + (size_t)n * nown; e += LU_THREADS) A[e] = make_float2(0.f, 0.f);
+            __syncthreads();
+            for (int r = wid; r < n; r += LU_THREADS / 32) {
+                const int m = S[r];
+                for (int q = ia[m] + lane; q < ia[m + 1]; q += 32) {
+                    const int pos = bsearch_cols(S, n, ja[q]);
+                    if (pos >= 0) A[(size_t)r * n + pos] = Z[q];
+                }
             }
         }
         for (int cc = tid; cc < nown; cc += LU_THREADS) {
@@ -381,20 +408,30 @@ __global__ void __launch_bounds__(LU_THREADS, 2)
             for (int r0 = 0; r0 < k0; r0 += LU_T)
                 lu_strip_update(sm, A, X, n, kb, k0, 0, k0, 0, 0, 0, r0, k0, nown);
         }
-        // ---- M rows of the own bases: M[ia[g] + j] = X(j, own index)
+        // ---- rows of the own bases: M[ia[g] + j] = X(j, own index) over the near
+        // list, or (2-ring) the entries of the near pattern inside the ring list
         for (int cc = 0; cc < nown; ++cc) {
             const int g = box_bases[box_ptr[b] + cc];
-            double2* row = M + ia[g];
             const float2* col = X + (size_t)cc * n;
-            for (int j = tid; j < n; j += LU_THREADS) row[j] = make_double2((double)col[j].x, (double)col[j].y);
+            if (ring.Zd) {
+                for (int q = ia[g] + tid; q < ia[g + 1]; q += LU_THREADS) {
+                    const int pos = bsearch_cols(S, n, ja[q]);
+                    ring.M2[q] = pos >= 0 ? col[pos] : make_float2(0.f, 0.f);
+                }
+            } else {
+                double2* row = M + ia[g];
+                for (int j = tid; j < n; j += LU_THREADS) row[j] = make_double2((double)col[j].x, (double)col[j].y);
+            }
         }
         __syncthreads();
     }
 }
 
-// Every box's rows of the neighbourhood inverse into c->dMinv (near CSR
-// pattern, allocated by the caller); *bad_box as mlf_nearinv.
-int nbhd_inverse_lu32(Ctx* c, int nmax, int nownmax, int* bad_box) {
+// Every box's rows of the inverse over its neighbourhood: ring null: the near
+// list, into c->dMinv (near CSR pattern, allocated by the caller); ring given:
+// the 2-ring lists (len[b] unknowns each, the host copy ring_len), into
+// ring->M2.  *bad_box as mlf_nearinv.
+int blocked_inverse_rows(Ctx* c, int nmax, int nownmax, const LuRing* ring, const int* ring_len, int* bad_box) {
     DevScope ds;
     const int nb = (int)c->box_ptr.size() - 1;
     const size_t slab = (size_t)nmax * nmax + (size_t)nmax * nownmax;
@@ -406,11 +443,10 @@ int nbhd_inverse_lu32(Ctx* c, int nmax, int nownmax, int* bad_box) {
     const size_t cap = (fr / 2) / (slab * sizeof(float2));
     const int grid = (int)std::max<size_t>(1, std::min<size_t>({(size_t)2 * nsm, (size_t)nb, cap}));
     // boxes by decreasing neighbourhood size, so that the largest do not finish last
+    auto nsize = [&](int b) { return ring ? ring_len[b] : c->near_ptr[b + 1] - c->near_ptr[b]; };
     std::vector<int> order(nb);
     for (int b = 0; b < nb; ++b) order[b] = b;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b2) {
-        return c->near_ptr[a + 1] - c->near_ptr[a] > c->near_ptr[b2 + 1] - c->near_ptr[b2];
-    });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b2) { return nsize(a) > nsize(b2); });
     float2* work = nullptr;
     int *dctr = nullptr, *dbad = nullptr, *dorder = nullptr;
     CK(ds.alloc(&work, slab * grid * sizeof(float2)));
@@ -420,14 +456,31 @@ int nbhd_inverse_lu32(Ctx* c, int nmax, int nownmax, int* bad_box) {
     dbad = dctr + 1;
     const int init[2] = {0, 0x7fffffff};
     CK(cudaMemcpyAsync(dctr, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
+    const LuRing none{};
     k_nbhd_lu32<<<grid, LU_THREADS, 0, c->stream>>>(nb, c->dbox_ptr, c->dperm, c->dia, c->dja, c->dZ, slab, work,
-                                                    c->dMinv, dorder, dctr, dbad);
+                                                    c->dMinv, dorder, dctr, dbad, ring ? *ring : none);
     CK(cudaGetLastError());
     int hbad = 0;
     CK(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     *bad_box = hbad == 0x7fffffff ? 0 : hbad;
     return MLF_OK;
+}
+
+int nbhd_inverse_lu32(Ctx* c, int nmax, int nownmax, int* bad_box) {
+    return blocked_inverse_rows(c, nmax, nownmax, nullptr, nullptr, bad_box);
+}
+
+int ring_inverse_lu32(Ctx* c, const float2* Zd, const long long* off, const int* len, const int* bases,
+                      const std::vector<int>& len_host, int nmax, int nownmax, float2* M2, int* bad_box) {
+    LuRing r;
+    r.Zd = Zd;
+    r.N = c->N;
+    r.off = off;
+    r.len = len;
+    r.bases = bases;
+    r.M2 = M2;
+    return blocked_inverse_rows(c, nmax, nownmax, &r, len_host.data(), bad_box);
 }
 
 }  // namespace mlf
