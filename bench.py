@@ -383,8 +383,9 @@ def learned_heldout_123k(steps=3000, seed=0):
     set-up + solve + two bistatic cuts; compared with ILU0 (the reference's
     preconditioner, CGS capped at 300 iterations), no preconditioner (capped
     at 3000) and the exact neighbourhood inverse M1 the network corrects.
-    The learned solve falls back to ILU0 if it has not converged within the
-    unpreconditioned iteration count."""
+    The learned preconditioner is run with mixed GMRES-IR and with FP64 CGS,
+    the latter falling back to ILU0 (capped at 300 iterations) if it has not
+    converged within the unpreconditioned iteration count."""
     import torch
     from lywell_gb300 import MLFMA, RWG, meshes
     from lywell_gb300.learned import solve_with_fallback, train
@@ -445,13 +446,13 @@ def learned_heldout_123k(steps=3000, seed=0):
     out, ts = timed(lambda: m.solve(b, errmax=1e-4, maxit=3000, precond="nearinv", mixed=True))
     finish("mixed_exact_M1", t_m1, out, ts)
     (_, t_inst) = timed(lambda: lp.apply_to(m))
-    out, ts = timed(lambda: solve_with_fallback(m, b, lp, plain_iters=plain, install_first=False))
+    out, ts = timed(lambda: m.solve(b, errmax=1e-4, maxit=3000, precond="nearinv", mixed=True))
+    finish("mixed_learned", t_m1 + t_inst, out, ts)
+    # FP64 CGS with the ILU0 fallback; the fallback solve is capped like the ILU0 run above
+    out, ts = timed(lambda: solve_with_fallback(m, b, lp, plain_iters=plain, install_first=False, maxit=300))
     used = out["used"]
-    finish("fp64_cgs_learned", t_m1 + t_inst, out, ts)
-    res["fp64_cgs_learned"]["used"] = used
-    if used == "learned":
-        out, ts = timed(lambda: m.solve(b, errmax=1e-4, maxit=3000, precond="nearinv", mixed=True))
-        finish("mixed_learned", t_m1 + t_inst, out, ts)
+    finish("fp64_cgs_learned_with_fallback", t_m1 + t_inst, out, ts)
+    res["fp64_cgs_learned_with_fallback"]["used"] = used
     base = ref["fp64_cgs_exact_M1"]
     for k in res:
         res[k]["rcs_db_maxdiff_vs_exact_M1"] = (float(np.abs(ref[k] - base).max())
