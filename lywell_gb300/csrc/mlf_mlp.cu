@@ -1,5 +1,7 @@
 // Small MLP for the learned near-field preconditioner: hand-written forward,
-// backward and Adam kernels.
+// backward and Adam kernels.  The forward of inference runs on tcgen05 tensor
+// cores (BF16 operands, FP32 accumulation in TMEM); training's forward and
+// backward run on FP32 FMAs over the same BF16 values.
 //
 // Network: 16 inputs -> 128 (ReLU) -> 128 (ReLU) -> 2 outputs, one token per
 // row.  Parameters are kept as an FP32 master copy (Adam state beside it) and
@@ -14,6 +16,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -22,6 +25,7 @@
 #include <vector>
 
 #include "../../include/lywell_mlfma.h"
+#include "mlf_tcgen05.h"
 
 namespace mlp {
 
@@ -37,6 +41,7 @@ struct Net {
     float *G = nullptr, *M1 = nullptr, *M2 = nullptr;
     float* norm = nullptr;         // mu[16], sd[16]
     double* dloss = nullptr;
+    int* derr = nullptr;           // set when a tensor-core forward CTA gave up a wait
     int adam_t = 0;
     std::string err;
 };
@@ -128,18 +133,179 @@ __device__ void forward_tile(Smem& s, const float* __restrict__ X, const float* 
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(256) k_mlp_forward(long long ntok, const float* __restrict__ X,
-                                                     const float* __restrict__ norm,
-                                                     const __nv_bfloat16* __restrict__ Pb, float* __restrict__ Y) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    Smem& s = *reinterpret_cast<Smem*>(smraw);
-    load_weights(s, Pb);
-    for (long long t0 = (long long)blockIdx.x * TT; t0 < ntok; t0 += (long long)gridDim.x * TT) {
-        const int nt = (int)((ntok - t0) < TT ? (ntok - t0) : TT);
-        forward_tile(s, X, norm, t0, nt);
-        if (threadIdx.x < nt * OUT) Y[t0 * OUT + threadIdx.x] = s.out[threadIdx.x];
-        __syncthreads();
+// ---------------------------------------------------------------------------
+// Forward on the fifth-generation tensor cores (inference: mlf_mlp_forward, and
+// so mlf_lp_install).  One tile = 128 tokens = the MMA's M; layer 1 (K = 16)
+// and layer 2 (K = 128) are tcgen05.mma .kind::f16 with BF16 operands and FP32
+// accumulators in TMEM (D1 in columns 0..127, D2 in 128..255); layer 3 (two
+// outputs) is a per-token dot product in registers.  Operands are written by
+// the threads into K-major 128-byte-swizzled tiles: A = the token rows (inputs
+// normalised and rounded to BF16; then H1), B = W^T (row n = neuron n's
+// weights).  Thread t owns token t: it writes its operand row and reads its
+// TMEM lane back.  The arithmetic is the CUDA-core path's -- BF16 values, FP32
+// sums, H1 and H2 rounded to BF16 -- in another summation order.
+// ---------------------------------------------------------------------------
+constexpr int TQ = 128;
+constexpr uint32_t MLP_SPIN = 1u << 20;   // mbarrier polls before a wait gives up
+
+struct TcMlpSmem {
+    alignas(1024) unsigned char X[TQ * 128];        // layer-1 A: 16 BF16 inputs per token (32 of 128 bytes used)
+    alignas(1024) unsigned char H1[2 * TQ * 128];   // layer-2 A: 128 BF16 per token, two K-blocks of 64
+    alignas(1024) unsigned char W1t[H * 128];       // layer-1 B: W1^T, 16 BF16 per neuron
+    alignas(1024) unsigned char W2t[2 * H * 128];   // layer-2 B: W2^T, two K-blocks
+    float b1[H], b2[H], W3[H * OUT], b3[OUT], mu[IN], sd[IN];
+    uint64_t bar;
+    uint32_t tmem;
+    int fail;
+};
+
+__device__ __forceinline__ uint32_t pack_bf2(float a, float b) {
+    const __nv_bfloat162 p = __floats2bfloat162_rn(a, b);   // a at the lower address
+    return *reinterpret_cast<const uint32_t*>(&p);
+}
+
+__global__ void __launch_bounds__(TQ, 2) k_mlp_forward_tc(long long ntok, const float* __restrict__ X,
+                                                         const float* __restrict__ norm,
+                                                         const __nv_bfloat16* __restrict__ Pb, float* __restrict__ Y,
+                                                         int* __restrict__ err) {
+    namespace tc = mlf::tc;
+    extern __shared__ unsigned char mlp_raw[];
+    const uint32_t raw = tc::smem_u32(mlp_raw);
+    TcMlpSmem& s = *reinterpret_cast<TcMlpSmem*>(mlp_raw + (((raw + 1023u) & ~1023u) - raw));
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // B operands (thread = neuron n), biases, the output layer, the normalisation
+    for (int c = 0; c < 2; ++c) {
+        uint32_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int k = c * 8 + 2 * q;
+            w[q] = pack_bf2(__bfloat162float(Pb[OW1 + k * H + tid]), __bfloat162float(Pb[OW1 + (k + 1) * H + tid]));
+        }
+        *reinterpret_cast<uint4*>(s.W1t + tc::sw128_offset(tid, c)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
+    for (int c = 0; c < 16; ++c) {
+        uint32_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int k = c * 8 + 2 * q;
+            w[q] = pack_bf2(__bfloat162float(Pb[OW2 + k * H + tid]), __bfloat162float(Pb[OW2 + (k + 1) * H + tid]));
+        }
+        *reinterpret_cast<uint4*>(s.W2t + (c >> 3) * (H * 128) + tc::sw128_offset(tid, c & 7)) =
+            make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    s.b1[tid] = __bfloat162float(Pb[OB1 + tid]);
+    s.b2[tid] = __bfloat162float(Pb[OB2 + tid]);
+    s.W3[2 * tid] = __bfloat162float(Pb[OW3 + 2 * tid]);
+    s.W3[2 * tid + 1] = __bfloat162float(Pb[OW3 + 2 * tid + 1]);
+    if (tid < OUT) s.b3[tid] = __bfloat162float(Pb[OB3 + tid]);
+    if (tid < IN) {
+        s.mu[tid] = norm[tid];
+        s.sd[tid] = norm[IN + tid];
+    }
+    if (tid == 0) {
+        tc::mbar_init(&s.bar, 1);
+        s.fail = 0;
+        tc::fence_barrier_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&s.tmem, 256);
+        tc::tmem_relinquish();
+    }
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    tc::tc_fence_after_sync();
+    const uint32_t tmem = s.tmem, lane_base = (uint32_t)(32 * warp) << 16;
+    const uint32_t idesc = tc::instr_desc_f32acc(tc::FMT_BF16, TQ, H);
+    const uint32_t aX = tc::smem_u32(s.X), aH = tc::smem_u32(s.H1), aW1 = tc::smem_u32(s.W1t),
+                   aW2 = tc::smem_u32(s.W2t);
+    uint32_t phase = 0;
+    for (long long t0 = (long long)blockIdx.x * TQ; t0 < ntok; t0 += (long long)gridDim.x * TQ) {
+        const long long tok = t0 + tid;
+        const bool live = tok < ntok;
+        {   // layer-1 operand row of this token
+            uint32_t w[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                float a = 0.f, b = 0.f;
+                if (live) {
+                    a = (X[tok * IN + 2 * q] - s.mu[2 * q]) / s.sd[2 * q];
+                    b = (X[tok * IN + 2 * q + 1] - s.mu[2 * q + 1]) / s.sd[2 * q + 1];
+                }
+                w[q] = pack_bf2(a, b);
+            }
+            *reinterpret_cast<uint4*>(s.X + tc::sw128_offset(tid, 0)) = make_uint4(w[0], w[1], w[2], w[3]);
+            *reinterpret_cast<uint4*>(s.X + tc::sw128_offset(tid, 1)) = make_uint4(w[4], w[5], w[6], w[7]);
+        }
+        tc::fence_proxy_async_smem();
+        tc::tc_fence_before_sync();   // the previous tile's TMEM reads are done
+        __syncthreads();
+        if (tid == 0) {
+            tc::tc_fence_after_sync();
+            tc::mma_f16(tmem, tc::kmajor_sw128_desc(aX), tc::kmajor_sw128_desc(aW1), idesc, 0);
+            tc::mma_commit(&s.bar);
+            if (!tc::mbar_wait(&s.bar, phase, MLP_SPIN)) s.fail = 1;
+        }
+        phase ^= 1;
+        __syncthreads();
+        tc::tc_fence_after_sync();
+        if (s.fail) break;
+        // H1 = relu(D1 + b1) in BF16, this token's row of the layer-2 operand
+        for (int c0 = 0; c0 < H; c0 += 32) {
+            float v[32];
+            tc::tmem_ld_32x32b_x32(tmem + lane_base + (uint32_t)c0, v);
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int k = cc * 8 + 2 * q;
+                    w[q] = pack_bf2(fmaxf(v[k] + s.b1[c0 + k], 0.f), fmaxf(v[k + 1] + s.b1[c0 + k + 1], 0.f));
+                }
+                const int c = (c0 >> 3) + cc;   // 16-byte chunk 0..15 of the row
+                *reinterpret_cast<uint4*>(s.H1 + (c >> 3) * (TQ * 128) + tc::sw128_offset(tid, c & 7)) =
+                    make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+        tc::fence_proxy_async_smem();
+        tc::tc_fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc::tc_fence_after_sync();
+#pragma unroll
+            for (int kb = 0; kb < 2; ++kb)
+#pragma unroll
+                for (int q = 0; q < 4; ++q)   // K steps of 16 BF16 = 32 bytes of the 128-byte rows
+                    tc::mma_f16(tmem + 128, tc::kmajor_sw128_desc(aH + kb * (TQ * 128) + 32 * q),
+                                tc::kmajor_sw128_desc(aW2 + kb * (H * 128) + 32 * q), idesc, (kb | q) != 0);
+            tc::mma_commit(&s.bar);
+            if (!tc::mbar_wait(&s.bar, phase, MLP_SPIN)) s.fail = 1;
+        }
+        phase ^= 1;
+        __syncthreads();
+        tc::tc_fence_after_sync();
+        if (s.fail) break;
+        // out = W3^T H2 + b3, H2 = relu(D2 + b2) rounded to BF16
+        float o0 = s.b3[0], o1 = s.b3[1];
+        for (int c0 = 0; c0 < H; c0 += 32) {
+            float v[32];
+            tc::tmem_ld_32x32b_x32(tmem + 128 + lane_base + (uint32_t)c0, v);
+#pragma unroll
+            for (int k = 0; k < 32; ++k) {
+                const float h = bf(fmaxf(v[k] + s.b2[c0 + k], 0.f));
+                o0 = fmaf(h, s.W3[(c0 + k) * OUT], o0);
+                o1 = fmaf(h, s.W3[(c0 + k) * OUT + 1], o1);
+            }
+        }
+        if (live) {
+            Y[tok * OUT] = o0;
+            Y[tok * OUT + 1] = o1;
+        }
+    }
+    if (tid == 0 && s.fail) atomicExch(err, 1);
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 256);
 }
 
 // Forward + loss + backward over tokens idx[0..ntok) (idx NULL: 0..ntok-1);
@@ -363,9 +529,11 @@ int mlf_mlp_create(mlf_mlp** out, int device, unsigned long long seed) {
         !ok(n, cudaMalloc(&n->M1, NPARAM * sizeof(float)), "alloc") ||
         !ok(n, cudaMalloc(&n->M2, NPARAM * sizeof(float)), "alloc") ||
         !ok(n, cudaMalloc(&n->norm, 2 * IN * sizeof(float)), "alloc") ||
-        !ok(n, cudaMalloc(&n->dloss, sizeof(double)), "alloc"))
+        !ok(n, cudaMalloc(&n->dloss, sizeof(double)), "alloc") ||
+        !ok(n, cudaMalloc(&n->derr, sizeof(int)), "alloc") || !ok(n, cudaMemset(n->derr, 0, sizeof(int)), "memset"))
         return fail(MLF_E_CUDA);
-    if (!ok(n, cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(Smem)),
+    if (!ok(n, cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(TcMlpSmem) + 1024)),
             "smem") ||
         !ok(n, cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(Smem)), "smem"))
         return fail(MLF_E_CUDA);
@@ -398,7 +566,7 @@ void mlf_mlp_free(mlf_mlp* h) {
     Net* n = &h->n;
     cudaSetDevice(n->dev);
     for (void* p : {(void*)n->P, (void*)n->Pb, (void*)n->G, (void*)n->M1, (void*)n->M2, (void*)n->norm,
-                    (void*)n->dloss})
+                    (void*)n->dloss, (void*)n->derr})
         if (p) cudaFree(p);
     if (n->stream) cudaStreamDestroy(n->stream);
     delete h;
@@ -439,9 +607,24 @@ int mlf_mlp_forward(mlf_mlp* h, const float* X, long long ntok, float* Y, void* 
     Net* n = &h->n;
     NCK(cudaSetDevice(n->dev));
     cudaStream_t s = stream ? (cudaStream_t)stream : n->stream;
-    if (ntok) k_mlp_forward<<<grid_for(ntok), 256, sizeof(Smem), s>>>(ntok, X, n->norm, n->Pb, Y);
+    if (ntok) {
+        int nsm = 0;
+        NCK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, n->dev));
+        const long long tiles = (ntok + TQ - 1) / TQ;
+        const int grid = (int)std::min<long long>(tiles, 2LL * nsm);
+        k_mlp_forward_tc<<<grid, TQ, sizeof(TcMlpSmem) + 1024, s>>>(ntok, X, n->norm, n->Pb, Y, n->derr);
+    }
     NCK(cudaGetLastError());
-    if (!stream) NCK(cudaStreamSynchronize(s));
+    if (!stream) {
+        NCK(cudaStreamSynchronize(s));
+        int e = 0;
+        NCK(cudaMemcpy(&e, n->derr, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e) {
+            cudaMemset(n->derr, 0, sizeof(int));
+            n->err = "tensor-core forward: an mbarrier wait gave up";
+            return MLF_E_CUDA;
+        }
+    }
     return MLF_OK;
 }
 

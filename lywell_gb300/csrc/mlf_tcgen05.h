@@ -43,6 +43,11 @@ MLF_HD constexpr uint64_t smem_desc(uint32_t addr, uint32_t lbo_bytes, uint32_t 
 // 8 TF32 values inside the 128-byte row moves the start address by 32 bytes.
 MLF_HD constexpr uint64_t kmajor_sw128_desc(uint32_t addr) { return smem_desc(addr, 16, 1024, SWIZZLE_128B); }
 
+// Byte offset of 16-byte chunk c (0..7) of row r in such a tile, for operands
+// written by threads rather than TMA: the 128-byte swizzle places the chunk at
+// c XOR (r mod 8) within its row (the tile 1024-byte aligned).
+MLF_HD constexpr uint32_t sw128_offset(uint32_t r, uint32_t c) { return r * 128u + ((c ^ (r & 7u)) << 4); }
+
 // ---- instruction descriptor of tcgen05.mma .kind::tf32 / .kind::f16 (32 bits)
 //   [0,2) sparsity selector, [2] sparse, [3] saturate   (all 0: dense)
 //   [4,6)   D format: 0 F16, 1 F32
@@ -136,6 +141,20 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64
         " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
+}
+// The same with BF16 (or F16, per the instruction descriptor) operands, .kind::f16.
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// make this thread's generic-proxy shared-memory writes visible to the async
+// proxy (tcgen05.mma operands written with st.shared)
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 // The mbarrier receives one arrival when every tcgen05.mma this thread issued
 // before has completed (their shared-memory operands are then free).

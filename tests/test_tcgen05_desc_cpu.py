@@ -30,6 +30,8 @@ int main() {
     std::printf("%08x\n", instr_desc_f32acc(FMT_TF32, 64, 8));
     std::printf("%d %d %d %d %d\n", valid_shape(128, 160), valid_shape(128, 8), valid_shape(64, 8),
                 valid_shape(128, 272), valid_shape(256, 64));
+    std::printf("%u %u %u %u\n", sw128_offset(0, 0), sw128_offset(1, 0), sw128_offset(9, 3), sw128_offset(7, 7));
+    std::printf("%08x\n", instr_desc_f32acc(FMT_BF16, 128, 128));
     return 0;
 }
 """
@@ -73,3 +75,14 @@ def test_instruction_descriptor(encodings):
 
 def test_valid_shapes(encodings):
     assert encodings[6].split() == ["1", "0", "1", "0", "0"]
+
+
+def test_sw128_chunk_offsets(encodings):
+    # row 0 chunk 0 in place; row 1 chunk 0 -> chunk 1 (128 + 16); row 9 (atom 1, row 1 of
+    # it) chunk 3 -> chunk 2 (9 * 128 + 32); row 7 chunk 7 -> chunk 0 (7 * 128)
+    assert encodings[7].split() == ["0", "144", "1184", "896"]
+
+
+def test_instruction_descriptor_bf16_square(encodings):
+    # BF16 A and B (1 << 7, 1 << 10), F32 D, N = 128 (16 << 17), M = 128 (8 << 24)
+    assert int(encodings[8], 16) == (1 << 4) | (1 << 7) | (1 << 10) | (16 << 17) | (8 << 24)
