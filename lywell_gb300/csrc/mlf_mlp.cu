@@ -135,13 +135,13 @@ __device__ void forward_tile(Smem& s, const float* __restrict__ X, const float* 
 
 // ---------------------------------------------------------------------------
 // Forward on the fifth-generation tensor cores (inference: mlf_mlp_forward, and
-// so mlf_lp_install).  One tile = 128 tokens = the MMA's M; layer 1 (K = 16)
-// and layer 2 (K = 128) are tcgen05.mma .kind::f16 with BF16 operands and FP32
-// accumulators in TMEM (D1 in columns 0..127, D2 in 128..255); layer 3 (two
-// outputs) is a per-token dot product in registers.  Operands are written by
-// the threads into K-major 128-byte-swizzled tiles: A = the token rows (inputs
-// normalised and rounded to BF16; then H1), B = W^T (row n = neuron n's
-// weights).  Thread t owns token t: it writes its operand row and reads its
+// so mlf_lp_install).  One tile = 128 tokens = the MMA's M.  The 128 x 128
+// hidden layer, 86 % of the flops, is tcgen05.mma .kind::f16: A = H1 (BF16,
+// 128 tokens x 128), B = W2^T (BF16, row n = neuron n's weights), both written
+// by the threads into K-major 128-byte-swizzled tiles, FP32 accumulator in
+// TMEM.  Layer 1 (K = 16, on FP32 normalised inputs, which BF16 operands
+// would round) and layer 3 (two outputs) are per-token FP32 dot products in
+// registers.  Thread t owns token t: it writes its row of H1 and reads its
 // TMEM lane back.  The arithmetic is the CUDA-core path's -- BF16 values, FP32
 // sums, H1 and H2 rounded to BF16 -- in another summation order.
 // ---------------------------------------------------------------------------
@@ -149,11 +149,9 @@ constexpr int TQ = 128;
 constexpr uint32_t MLP_SPIN = 1u << 20;   // mbarrier polls before a wait gives up
 
 struct TcMlpSmem {
-    alignas(1024) unsigned char X[TQ * 128];        // layer-1 A: 16 BF16 inputs per token (32 of 128 bytes used)
     alignas(1024) unsigned char H1[2 * TQ * 128];   // layer-2 A: 128 BF16 per token, two K-blocks of 64
-    alignas(1024) unsigned char W1t[H * 128];       // layer-1 B: W1^T, 16 BF16 per neuron
     alignas(1024) unsigned char W2t[2 * H * 128];   // layer-2 B: W2^T, two K-blocks
-    float b1[H], b2[H], W3[H * OUT], b3[OUT], mu[IN], sd[IN];
+    float W1[IN * H], b1[H], b2[H], W3[H * OUT], b3[OUT], mu[IN], sd[IN];
     uint64_t bar;
     uint32_t tmem;
     int fail;
@@ -173,16 +171,8 @@ __global__ void __launch_bounds__(TQ, 2) k_mlp_forward_tc(long long ntok, const 
     const uint32_t raw = tc::smem_u32(mlp_raw);
     TcMlpSmem& s = *reinterpret_cast<TcMlpSmem*>(mlp_raw + (((raw + 1023u) & ~1023u) - raw));
     const int tid = threadIdx.x, warp = tid >> 5;
-    // B operands (thread = neuron n), biases, the output layer, the normalisation
-    for (int c = 0; c < 2; ++c) {
-        uint32_t w[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int k = c * 8 + 2 * q;
-            w[q] = pack_bf2(__bfloat162float(Pb[OW1 + k * H + tid]), __bfloat162float(Pb[OW1 + (k + 1) * H + tid]));
-        }
-        *reinterpret_cast<uint4*>(s.W1t + tc::sw128_offset(tid, c)) = make_uint4(w[0], w[1], w[2], w[3]);
-    }
+    // layer-2 B operand (thread = neuron n), layer 1, biases, the output layer, the normalisation
+    for (int q = tid; q < IN * H; q += TQ) s.W1[q] = __bfloat162float(Pb[OW1 + q]);
     for (int c = 0; c < 16; ++c) {
         uint32_t w[4];
 #pragma unroll
@@ -208,7 +198,7 @@ __global__ void __launch_bounds__(TQ, 2) k_mlp_forward_tc(long long ntok, const 
         tc::fence_barrier_init();
     }
     if (warp == 0) {
-        tc::tmem_alloc(&s.tmem, 256);
+        tc::tmem_alloc(&s.tmem, 128);
         tc::tmem_relinquish();
     }
     tc::fence_proxy_async_smem();
@@ -217,58 +207,32 @@ __global__ void __launch_bounds__(TQ, 2) k_mlp_forward_tc(long long ntok, const 
     tc::tc_fence_after_sync();
     const uint32_t tmem = s.tmem, lane_base = (uint32_t)(32 * warp) << 16;
     const uint32_t idesc = tc::instr_desc_f32acc(tc::FMT_BF16, TQ, H);
-    const uint32_t aX = tc::smem_u32(s.X), aH = tc::smem_u32(s.H1), aW1 = tc::smem_u32(s.W1t),
-                   aW2 = tc::smem_u32(s.W2t);
+    const uint32_t aH = tc::smem_u32(s.H1), aW2 = tc::smem_u32(s.W2t);
     uint32_t phase = 0;
     for (long long t0 = (long long)blockIdx.x * TQ; t0 < ntok; t0 += (long long)gridDim.x * TQ) {
         const long long tok = t0 + tid;
         const bool live = tok < ntok;
-        {   // layer-1 operand row of this token
-            uint32_t w[8];
+        // layer 1 (K = 16) in FP32 on the token's normalised inputs; H1 = relu(.)
+        // rounded to BF16, this token's row of the layer-2 operand
+        float xn[IN];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                float a = 0.f, b = 0.f;
-                if (live) {
-                    a = (X[tok * IN + 2 * q] - s.mu[2 * q]) / s.sd[2 * q];
-                    b = (X[tok * IN + 2 * q + 1] - s.mu[2 * q + 1]) / s.sd[2 * q + 1];
-                }
-                w[q] = pack_bf2(a, b);
-            }
-            *reinterpret_cast<uint4*>(s.X + tc::sw128_offset(tid, 0)) = make_uint4(w[0], w[1], w[2], w[3]);
-            *reinterpret_cast<uint4*>(s.X + tc::sw128_offset(tid, 1)) = make_uint4(w[4], w[5], w[6], w[7]);
+        for (int i = 0; i < IN; ++i) xn[i] = live ? (X[tok * IN + i] - s.mu[i]) / s.sd[i] : 0.f;
+        for (int c = 0; c < 16; ++c) {   // 16-byte chunk c = neurons 8c .. 8c+7
+            float acc[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc[u] = s.b1[8 * c + u];
+#pragma unroll
+            for (int i = 0; i < IN; ++i)
+#pragma unroll
+                for (int u = 0; u < 8; ++u) acc[u] = fmaf(xn[i], s.W1[i * H + 8 * c + u], acc[u]);
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) w[q] = pack_bf2(fmaxf(acc[2 * q], 0.f), fmaxf(acc[2 * q + 1], 0.f));
+            *reinterpret_cast<uint4*>(s.H1 + (c >> 3) * (TQ * 128) + tc::sw128_offset(tid, c & 7)) =
+                make_uint4(w[0], w[1], w[2], w[3]);
         }
         tc::fence_proxy_async_smem();
         tc::tc_fence_before_sync();   // the previous tile's TMEM reads are done
-        __syncthreads();
-        if (tid == 0) {
-            tc::tc_fence_after_sync();
-            tc::mma_f16(tmem, tc::kmajor_sw128_desc(aX), tc::kmajor_sw128_desc(aW1), idesc, 0);
-            tc::mma_commit(&s.bar);
-            if (!tc::mbar_wait(&s.bar, phase, MLP_SPIN)) s.fail = 1;
-        }
-        phase ^= 1;
-        __syncthreads();
-        tc::tc_fence_after_sync();
-        if (s.fail) break;
-        // H1 = relu(D1 + b1) in BF16, this token's row of the layer-2 operand
-        for (int c0 = 0; c0 < H; c0 += 32) {
-            float v[32];
-            tc::tmem_ld_32x32b_x32(tmem + lane_base + (uint32_t)c0, v);
-#pragma unroll
-            for (int cc = 0; cc < 4; ++cc) {
-                uint32_t w[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int k = cc * 8 + 2 * q;
-                    w[q] = pack_bf2(fmaxf(v[k] + s.b1[c0 + k], 0.f), fmaxf(v[k + 1] + s.b1[c0 + k + 1], 0.f));
-                }
-                const int c = (c0 >> 3) + cc;   // 16-byte chunk 0..15 of the row
-                *reinterpret_cast<uint4*>(s.H1 + (c >> 3) * (TQ * 128) + tc::sw128_offset(tid, c & 7)) =
-                    make_uint4(w[0], w[1], w[2], w[3]);
-            }
-        }
-        tc::fence_proxy_async_smem();
-        tc::tc_fence_before_sync();
         __syncthreads();
         if (tid == 0) {
             tc::tc_fence_after_sync();
@@ -276,7 +240,7 @@ __global__ void __launch_bounds__(TQ, 2) k_mlp_forward_tc(long long ntok, const 
             for (int kb = 0; kb < 2; ++kb)
 #pragma unroll
                 for (int q = 0; q < 4; ++q)   // K steps of 16 BF16 = 32 bytes of the 128-byte rows
-                    tc::mma_f16(tmem + 128, tc::kmajor_sw128_desc(aH + kb * (TQ * 128) + 32 * q),
+                    tc::mma_f16(tmem, tc::kmajor_sw128_desc(aH + kb * (TQ * 128) + 32 * q),
                                 tc::kmajor_sw128_desc(aW2 + kb * (H * 128) + 32 * q), idesc, (kb | q) != 0);
             tc::mma_commit(&s.bar);
             if (!tc::mbar_wait(&s.bar, phase, MLP_SPIN)) s.fail = 1;
@@ -289,7 +253,7 @@ __global__ void __launch_bounds__(TQ, 2) k_mlp_forward_tc(long long ntok, const 
         float o0 = s.b3[0], o1 = s.b3[1];
         for (int c0 = 0; c0 < H; c0 += 32) {
             float v[32];
-            tc::tmem_ld_32x32b_x32(tmem + 128 + lane_base + (uint32_t)c0, v);
+            tc::tmem_ld_32x32b_x32(tmem + lane_base + (uint32_t)c0, v);
 #pragma unroll
             for (int k = 0; k < 32; ++k) {
                 const float h = bf(fmaxf(v[k] + s.b2[c0 + k], 0.f));
@@ -305,7 +269,7 @@ __global__ void __launch_bounds__(TQ, 2) k_mlp_forward_tc(long long ntok, const 
     if (tid == 0 && s.fail) atomicExch(err, 1);
     tc::tc_fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 256);
+    if (warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
 // Forward + loss + backward over tokens idx[0..ntok) (idx NULL: 0..ntok-1);
