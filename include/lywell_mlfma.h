@@ -272,6 +272,10 @@ int mlf_autotune_block(mlf_ctx* ctx, const int* candidates, int ncand, int* best
  *       leaf boxes of a few tens of bases), the leaf receive by one CTA per
  *       box with the box's fields in shared memory,
  *   3 = warp engine with the leaf receive also one warp per basis,
+ *   4 = box-block GEMMs on the fifth-generation tensor cores (tcgen05.mma,
+ *       3xTF32, accumulators in tensor memory, operands staged by TMA): the
+ *       near field, the leaf aggregation and receive, and the near-pattern
+ *       preconditioner, 64 columns per tile,
  *  -1 = by the mean leaf-box size: 2 below 48 bases per box, else 1 (the
  *       default).
  * cols = box-block tile width 8, 32 or 64 (0: by the block's width).

@@ -266,7 +266,10 @@ int blk_engine_of(const Ctx* c);   // the engine in force (resolves -1)
 inline bool warp_engine(int e) { return e == 2 || e == 3; }
 // tensor-core engine (mlf_tc.cu)
 int device_blocks_ready(Ctx* c);   // box-pair blocks of the near field built
-int device_near_tc(Ctx* c, const float2* xs, int ld, int nrhs, double2* y, cudaStream_t s);
+int device_near_tc(Ctx* c, const float2* xs, int ld, int nrhs, double2* y, cudaStream_t s, bool x_packed = false);
+int device_agg_tc(Ctx* c, const float2* R, int K, const float2* xs, int nrhs, float2* C, cudaStream_t s);
+int device_recv_tc(Ctx* c, const float2* R, int K, const float2* A, float facy, int nrhs, int ld, double2* y,
+                   cudaStream_t s);
 int device_near_pattern_tc(Ctx* c, const float2* Mblk, const float2* xs, int nrhs, float2* out, cudaStream_t s);
 void tc_drop_precond(Ctx* c);      // drop the preconditioner's tensor-core operand (its blocks changed)
 int tc_check(Ctx* c);              // MLF_E_CUDA if a tensor-core CTA gave up a wait since the last check

@@ -374,8 +374,10 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
         // blocks of columns: box-sorted row-major copy, then per-box GEMMs
         // (or one warp per basis for small boxes)
         if ((st = device_blk_pack(c, x, x32, ld, nrhs, c->m32.xT, s))) return st;
-        st = warp_engine(blk_engine_of(c)) ? device_agg_warp32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s)
-                                   : device_agg_blocks32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s);
+        const int eng = blk_engine_of(c);
+        st = warp_engine(eng) ? device_agg_warp32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s)
+             : eng == 4       ? device_agg_tc(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s)
+                              : device_agg_blocks32(c, c->m32.R, leaf.K, c->m32.xT, nrhs, c->m32.lv[nl].C, s);
         if (st) return st;
     }
     if (prof) cudaEventRecord(c->ev[1], s);
@@ -452,9 +454,15 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
                                               c->m32.xT, nrhs, ld, y, s)))
                 return st;
         } else {
-            if ((st = device_recv_blocks32(c, c->m32.R, leaf.K, (nl == 3 ? c->m32.lv[nl].B : c->m32.lv[nl].A), facy, nrhs, ld, y, s))) return st;
-            st = blk_engine_of(c) == 4 ? device_near_tc(c, c->m32.xT, ld, nrhs, y, s)
-                                       : device_near_blocks32(c, c->m32.xT, ld, nrhs, y, s);
+            const float2* Aleaf = nl == 3 ? c->m32.lv[nl].B : c->m32.lv[nl].A;
+            if (blk_engine_of(c) == 4) {
+                // the X operand was packed by the aggregation of this product
+                if ((st = device_recv_tc(c, c->m32.R, leaf.K, Aleaf, facy, nrhs, ld, y, s))) return st;
+                st = device_near_tc(c, c->m32.xT, ld, nrhs, y, s, true);
+            } else {
+                if ((st = device_recv_blocks32(c, c->m32.R, leaf.K, Aleaf, facy, nrhs, ld, y, s))) return st;
+                st = device_near_blocks32(c, c->m32.xT, ld, nrhs, y, s);
+            }
             if (st) return st;
         }
     }

@@ -86,6 +86,15 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
 }
+// one arrival of this thread (release: its earlier shared-memory writes are
+// visible to whoever observes the phase complete)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// barrier among nthreads threads (a multiple of 32: whole warps) of the CTA, id 1..15
+__device__ __forceinline__ void named_bar_sync(uint32_t id, uint32_t nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
 // Wait for the phase with the given parity to complete; gives up after
 // max_iter polls (each poll may itself suspend for a bounded time) and
 // returns false then.

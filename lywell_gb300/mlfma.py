@@ -343,8 +343,8 @@ class MLFMA:
         """Multi-column engine of the batched FP32 operator and preconditioner:
         1 box blocks on tensor cores (3xTF32 mma.sync), 0 box blocks on FP32
         FMA, 2 warp per basis (receive per box), 3 warp per basis throughout,
-        4 box blocks with the near field on tcgen05 (3xTF32, TMEM
-        accumulators, TMA-staged operands), -1 by leaf-box size; tile width
+        4 box blocks on tcgen05 (near field, leaf aggregation and receive;
+        3xTF32, TMEM accumulators, TMA-staged operands), -1 by leaf-box size; tile width
         cols 8, 32, 64 (0: by block width)."""
         _check(load().mlf_set_block_engine(self._h, int(engine), int(cols)), self._h)
 

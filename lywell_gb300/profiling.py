@@ -5,7 +5,7 @@
 
 fp32: the batched FP32 operator (mlf_matvec32_device) on `nrhs` random
 columns with a chosen multi-column engine (-1 automatic, 0 FMA box blocks,
-1 mma.sync box blocks, 2/3 warp engine, 4 tcgen05 near field) and tile
+1 mma.sync box blocks, 2/3 warp engine, 4 tcgen05 box blocks) and tile
 width; fp64: the FP64 matvec (mlf_matvec_device) on one column.  Each prints
 one JSON line: time per call (CUDA events over `steps` calls after two
 warm-up calls) and the per-stage times of one more call.

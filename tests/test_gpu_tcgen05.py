@@ -1,10 +1,13 @@
-"""The tcgen05 near-field engine (block engine 4) against the mma.sync box-block
-engine (engine 1) and the FP64 operator.
+"""The tcgen05 engine (block engine 4: near field, leaf aggregation and leaf
+receive on tcgen05.mma) against the mma.sync box-block engine (engine 1) and
+the FP64 operator.
 
 Workloads: a 30 720-RWG prolate spheroid at the 722-RHS workload's mesh
 density (icosphere-5, semi-axes 1.5 x 0.375 x 0.375 lambda, about 145 bases
 per 0.25 lambda leaf box), and the same body with 0.5 lambda leaf boxes
-(several hundred bases per box: boxes split over tiles of at most 256 rows).
+(several hundred bases per box: boxes split over tiles of at most 160 rows).
+The aggregation splits the 2K directions of a leaf box (324 with 0.25 lambda
+leaves) over tiles of at most 160 as well.
 
 Tolerances: the 3xTF32 products of both tensor-core engines drop the lo x lo
 term, so a batched column agrees with the other engine's to 5e-6 relative,
