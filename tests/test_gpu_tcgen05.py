@@ -9,11 +9,14 @@ per 0.25 lambda leaf box), and the same body with 0.5 lambda leaf boxes
 The aggregation splits the 2K directions of a leaf box (324 with 0.25 lambda
 leaves) over tiles of at most 160 as well.
 
-Tolerances: the 3xTF32 products of both tensor-core engines drop the lo x lo
-term, so a batched column agrees with the other engine's to 5e-6 relative,
-and with the FP64 operator to the FP32 operator's own accuracy: 2e-5 with
-0.25 lambda leaves, 1e-4 with 0.5 lambda leaves (larger sampling grids and
-longer FP32 translation sums; measured 8e-5 with either engine).
+Tolerances: engine 4 splits each FP32 operand of the near field and the
+aggregation into scaled FP16 hi and lo parts (22 significant bits, as the
+3xTF32 split of the receive and of engine 1) and drops the lo x lo term.
+Against the FP64 operator both engines stay within the FP32 operator's own
+accuracy: 2e-5 with 0.25 lambda leaves, 1e-4 with 0.5 lambda leaves (larger
+sampling grids and longer FP32 translation sums).  Measured on the 30 720-RWG
+spheroid: engine 4 1.0e-5 and 4.5e-5, engine 1 1.8e-5 and 7.7e-5, so the two
+engines differ by up to 7.7e-6 and 3.3e-5; the same bounds apply between them.
 """
 import numpy as np
 import pytest
@@ -47,11 +50,14 @@ def test_tc_engine_matches_mma_engine(spheroid, nrhs):
     Y4b = m.matvec32(X)
     m.set_block_engine(-1)
     assert np.array_equal(Y4, Y4b)            # deterministic: each output written by one CTA
+    tol = 2e-5 if side == 0.25 else 1e-4
     worst = max(_rel(Y4[:, k], Y1[:, k]) for k in range(nrhs))
-    print(f"nrhs {nrhs}: tcgen05 vs mma.sync worst column {worst:.2e}")
-    assert worst < 5e-6
-    for k in sorted({0, nrhs - 1}):
-        assert _rel(Y4[:, k], m.matvec(X[:, k])) < (2e-5 if side == 0.25 else 1e-4)
+    e64 = {k: (_rel(Y4[:, k], m.matvec(X[:, k])), _rel(Y1[:, k], m.matvec(X[:, k]))) for k in sorted({0, nrhs - 1})}
+    print(f"nrhs {nrhs}: tcgen05 vs mma.sync worst column {worst:.2e}; vs FP64 (tcgen05, mma.sync) "
+          + " ".join(f"{a:.2e}/{b:.2e}" for a, b in e64.values()))
+    assert worst < tol
+    for a, b in e64.values():
+        assert a < tol and b < tol
 
 
 def test_tc_engine_mixed_solve(spheroid):
