@@ -314,7 +314,7 @@ __global__ void k_tc_fill_rr(int K2, const int* __restrict__ box_ptr, const int*
 //   TCM_RECV      y(basis, col) = j facy sum_q conj R(basis, q) A(q, col, i)
 // The aggregation takes the near field's packed X operand (the box's own
 // chunks); the receive stages raw rows of the A field (64 columns x 16
-// directions, unswizzled) by TMA and warps 2-3 expand them in shared memory
+// directions, 128-byte swizzled) by TMA and warps 2-3 expand them in shared memory
 // into the [re, -im] / [im, re] row pairs, split into TF32 hi and lo.
 //
 // Persistent: one CTA per SM walks the work items q = blockIdx.x + k gridDim.x,
@@ -534,23 +534,30 @@ __global__ void __launch_bounds__(256, 1)
                     }
                     tc::mbar_wait(&full[s], par, TC_SPIN);   // complete already: acquires the landed bytes
                     unsigned char* st = ring + (size_t)s * TC_STAGE_BYTES;
-                    const float4* src = reinterpret_cast<const float4*>(st + TC_ABYTES + cl * 128);
+                    // the raw rows arrive 128-byte swizzled: chunk k of row cl sits at
+                    // k ^ (cl & 7), so the 8 lanes of a shared-memory wavefront read 8
+                    // different bank groups
                     float4 v[8];
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) v[k] = src[k];
+                    for (int k = 0; k < 8; ++k)
+                        v[k] = *reinterpret_cast<const float4*>(st + TC_ABYTES + tc::sw128_offset(cl, k));
                     tc::named_bar_sync(1, 64);   // every raw row is read before the lo tile overwrites them
+                    // rows 2cl and 2cl+1 place chunk k at k ^ (2cl & 7) (resp. +1): lanes
+                    // with cl & 4 take the chunks in the order k ^ 1 so that the 8 lanes
+                    // of a wavefront again store to 8 different bank groups
+                    const int flip = (cl >> 2) & 1;
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) {   // 16-byte chunk k: complex values 2k, 2k+1
-                        const float4 w = v[k];
-                        const float4 ev = make_float4(w.x, -w.y, w.z, -w.w), od = make_float4(w.y, w.x, w.w, w.z);
-                        const float4 eh = make_float4(tc::tf32_rna(ev.x), tc::tf32_rna(ev.y), tc::tf32_rna(ev.z),
-                                                      tc::tf32_rna(ev.w));
-                        const float4 oh = make_float4(tc::tf32_rna(od.x), tc::tf32_rna(od.y), tc::tf32_rna(od.z),
-                                                      tc::tf32_rna(od.w));
-                        const float4 el = make_float4(tc::tf32_rna(ev.x - eh.x), tc::tf32_rna(ev.y - eh.y),
-                                                      tc::tf32_rna(ev.z - eh.z), tc::tf32_rna(ev.w - eh.w));
-                        const float4 ol = make_float4(tc::tf32_rna(od.x - oh.x), tc::tf32_rna(od.y - oh.y),
-                                                      tc::tf32_rna(od.z - oh.z), tc::tf32_rna(od.w - oh.w));
+                    for (int kk = 0; kk < 8; ++kk) {   // 16-byte chunk k: complex values 2k, 2k+1
+                        const int k = kk ^ flip;
+                        const float4 w = flip ? v[kk ^ 1] : v[kk];
+                        // row 2cl: (re, -im) pairs; row 2cl+1: (im, re) -- the same values, so
+                        // its hi and lo parts follow from row 2cl's (the rounding is symmetric)
+                        const float4 eh = make_float4(tc::tf32_rna(w.x), tc::tf32_rna(-w.y), tc::tf32_rna(w.z),
+                                                      tc::tf32_rna(-w.w));
+                        const float4 el = make_float4(tc::tf32_rna(w.x - eh.x), tc::tf32_rna(-w.y - eh.y),
+                                                      tc::tf32_rna(w.z - eh.z), tc::tf32_rna(-w.w - eh.w));
+                        const float4 oh = make_float4(-eh.y, eh.x, -eh.w, eh.z);
+                        const float4 ol = make_float4(-el.y, el.x, -el.w, el.z);
                         const uint32_t oe = tc::sw128_offset(2 * cl, k), oo = tc::sw128_offset(2 * cl + 1, k);
                         *reinterpret_cast<float4*>(st + oe) = eh;
                         *reinterpret_cast<float4*>(st + oo) = oh;
@@ -1029,8 +1036,8 @@ int device_recv_tc(Ctx* c, const float2* R, int K, const float2* A, float facy, 
     TcState* t = c->tc;
     const int nb = (int)c->box_ptr.size() - 1;
     CUtensorMap raw;
-    if ((st = make_map_2d(c, &raw, reinterpret_cast<const float*>(A), 2LL * K2, (long long)nb * nrhs,
-                          (long long)K2 * (long long)sizeof(float2), 2 * TC_KCH, TC_COLS, CU_TENSOR_MAP_SWIZZLE_NONE)))
+    if ((st = make_map_2d(c, &raw, A, 2LL * K2, (long long)nb * nrhs, (long long)K2 * (long long)sizeof(float2),
+                          2 * TC_KCH, TC_COLS, CU_TENSOR_MAP_SWIZZLE_128B)))
         return st;
     TcArgs a = tc_args(c, nrhs);
     a.zrow = t->drbase;
