@@ -249,6 +249,13 @@ int mlf_set_translation_group(mlf_ctx* ctx, int boxes, int cols);
  * orthogonalisation, wall total}.  No counterpart in the reference. */
 int mlf_solve_times(mlf_ctx* ctx, double* out4);
 
+/* The same phases and more, out[0..n-1] of {preconditioner, FP32 operator,
+ * orthogonalisation, wall total, FP64 residuals (the outer checks), the
+ * provisional FP32 residual of a warm start (ms), outer steps}; n <= 7.
+ * The residual phases are timed on the host between stream
+ * synchronisations.  No counterpart in the reference. */
+int mlf_solve_phases(mlf_ctx* ctx, double* out, int n);
+
 /* Autotuner for batched solves: times the FP32 operator on each candidate
  * block of right-hand sides (candidates[ncand], 1..4096) with each
  * multi-column engine -- both box-block GEMM engines at the tile widths 8, 32

@@ -45,6 +45,7 @@ SIGNATURES = {
     "mlf_set_basis_precision": (C.c_int, [vp, C.c_int]),
     "mlf_set_translation_group": (C.c_int, [vp, C.c_int, C.c_int]),
     "mlf_solve_times": (C.c_int, [vp, vp]),
+    "mlf_solve_phases": (C.c_int, [vp, vp, C.c_int]),
     "mlf_precond_apply32": (C.c_int, [vp, vp, vp, C.c_int]),
     "mlf_autotune_block": (C.c_int, [vp, vp, C.c_int, vp, vp, vp, vp]),
     "mlf_set_block_engine": (C.c_int, [vp, C.c_int, C.c_int]),

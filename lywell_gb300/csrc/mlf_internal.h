@@ -147,9 +147,11 @@ struct Ctx {
     int blk_cols = 0;                 // box-block tile width: 0 = by nrhs, else 8, 32 or 64 (autotuner)
     int blk_engine = -1;              // multi-column engine: 0 box-block FP32 FMA, 1 box-block mma.sync
                                       // 3xTF32, 2 warp per basis with a per-box receive, 3 warp per basis
-                                      // throughout, 4 box blocks with the near field on tcgen05 (3xTF32,
-                                      // TMEM accumulators) and the rest as 1; -1 by mean leaf-box size
+                                      // throughout, 4 box blocks on tcgen05 (near field, leaf
+                                      // aggregation and receive); -1 by mean leaf-box size
     TcState* tc = nullptr;            // engine 4's operand layouts and tensor maps, built on first use
+    void* mix_ws = nullptr;           // workspace of the mixed-precision solve (Krylov basis and vectors),
+    size_t mix_ws_bytes = 0;          //   kept between solves, grown on demand
     int* djas = nullptr;              // near CSR columns as box-sorted positions (warp engine)
     float2* dZblk = nullptr;
     long long* dblk_off = nullptr;
@@ -207,7 +209,8 @@ struct Ctx {
     // mixed solve phases, accumulated while profiling: preconditioner,
     // FP32 operator, orthogonalisation, total
     cudaEvent_t sev[4]{};
-    double solve_ms[4]{};
+    double solve_ms[7]{};             // last profiled mixed solve: precond, FP32 operator, orthogonalisation,
+                                      // wall total, FP64 residuals, provisional FP32 residual (ms), outer steps
 };
 
 // host set-up (mlf_setup.cpp)
@@ -292,6 +295,8 @@ int device_excitation(Ctx* c, const double* dirs, const double2* pols, double2 c
                       double2* b);
 int device_rcs(Ctx* c, const double2* I, const double2* pol, double2 ctte, const double* th,
                const double* ph, int nang, double* sigma);
+int device_rcs_cols(Ctx* c, const double2* X, size_t ldx, int ncol, const double2* pols, double2 ctte,
+                    const double* th, const double* ph, double* sigma);
 
 bool cuda_ok(Ctx* c, cudaError_t e, const char* what);
 

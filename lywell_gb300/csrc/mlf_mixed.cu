@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <memory>
 #include <type_traits>
 #include <vector>
 
@@ -477,7 +478,9 @@ static int matvec32_core(Ctx* c, const double2* x, const float2* x32, double2* y
 
 void mixed_free(Ctx* c) {
     auto F = [](void* p) { if (p) cudaFree(p); };
-    F(c->m32.R); F(c->m32.xf); F(c->m32.xT);
+    F(c->m32.R); F(c->m32.xf); F(c->m32.xT); F(c->mix_ws);
+    c->mix_ws = nullptr;
+    c->mix_ws_bytes = 0;
     for (int n = 0; n < 32; ++n) {
         Mixed32::Lv& M = c->m32.lv[n];
         F(M.T); F(M.wq); F(M.shift); F(M.C); F(M.B); F(M.A);
@@ -804,7 +807,6 @@ static int apply_precond64(Ctx* c, int precond, int nrhs, const double2* in, dou
 template <class BT>
 static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
                          int* iters, double* relres, int precond, int* status, double inner_tol, int* outer) {
-    DevScope ds;
     const int N = c->N;
     // restart length: the one set, else 1600 while the basis fits in 16 GB,
     // down to 800 for wide blocks (a cold solve of the bench workloads takes
@@ -820,18 +822,43 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
     float2 *w32 = nullptr, *t32 = nullptr;
     double2 *w = nullptr, *r = nullptr, *t64 = nullptr, *partial = nullptr, *dred = nullptr;
     double* dscale = nullptr;
-    CK(ds.alloc(&V, (size_t)(m + 1) * V1 * sizeof(BT)));
-    CK(ds.alloc(&w32, V1 * sizeof(float2)));
-    CK(ds.alloc(&t32, V1 * sizeof(float2)));
-    CK(ds.alloc(&w, V1 * sizeof(double2)));
-    CK(ds.alloc(&r, V1 * sizeof(double2)));
-    CK(ds.alloc(&t64, V1 * sizeof(double2)));
     const int md_chunks = (N + 256 * MD_E - 1) / (256 * MD_E);
     int nsm = 0;
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev));
-    CK(ds.alloc(&partial, (size_t)(m + 1) * nrhs * std::max(GM_BLOCKS, md_chunks) * sizeof(double2)));
-    CK(ds.alloc(&dred, (size_t)(m + 1) * nrhs * sizeof(double2)));
-    CK(ds.alloc(&dscale, nrhs * sizeof(double)));
+    // The buffers come from a workspace the context keeps between solves: a
+    // batched sweep solves hundreds of blocks, and allocating and freeing the
+    // Krylov basis (tens of GB for wide blocks) for each took about 0.1 s.
+    {
+        auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+        const size_t sz[9] = {(size_t)(m + 1) * V1 * sizeof(BT), V1 * sizeof(float2), V1 * sizeof(float2),
+                              V1 * sizeof(double2), V1 * sizeof(double2), V1 * sizeof(double2),
+                              (size_t)(m + 1) * nrhs * std::max(GM_BLOCKS, md_chunks) * sizeof(double2),
+                              (size_t)(m + 1) * nrhs * sizeof(double2), nrhs * sizeof(double)};
+        size_t total = 0;
+        for (size_t b : sz) total += al(b);
+        if (c->mix_ws_bytes < total) {
+            if (c->mix_ws) cudaFree(c->mix_ws);
+            c->mix_ws = nullptr;
+            c->mix_ws_bytes = 0;
+            CK(cudaMalloc(&c->mix_ws, total));
+            c->mix_ws_bytes = total;
+        }
+        char* p = static_cast<char*>(c->mix_ws);
+        auto take = [&](int k) {
+            char* q = p;
+            p += al(sz[k]);
+            return static_cast<void*>(q);
+        };
+        V = static_cast<BT*>(take(0));
+        w32 = static_cast<float2*>(take(1));
+        t32 = static_cast<float2*>(take(2));
+        w = static_cast<double2*>(take(3));
+        r = static_cast<double2*>(take(4));
+        t64 = static_cast<double2*>(take(5));
+        partial = static_cast<double2*>(take(6));
+        dred = static_cast<double2*>(take(7));
+        dscale = static_cast<double*>(take(8));
+    }
     if (x0) CK(cudaMemcpyAsync(x, x0, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     else CK(cudaMemsetAsync(x, 0, V1 * sizeof(double2), s));
     const unsigned g = (unsigned)std::min<size_t>((N + 255) / 256, 2048);
@@ -844,16 +871,19 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
     // stagnation: the best FP64 residual of each column and the inner step count that reached it
     std::vector<double> sbest(nrhs, HUGE_VAL);
     std::vector<int> sbest_it(nrhs, 0);
-    std::vector<Cx> H((size_t)nrhs * (m + 1) * m), G((size_t)nrhs * (m + 1)), CS((size_t)nrhs * m), SN((size_t)nrhs * m);
+    // H: per column the (m + 1) x m Hessenberg matrix, left uninitialised (for
+    // wide blocks it spans hundreds of MB of which a cycle touches the first
+    // few hundred columns): every entry is written before it is read
+    std::unique_ptr<Cx[]> H(new Cx[(size_t)nrhs * (m + 1) * m]);
+    std::vector<Cx> G((size_t)nrhs * (m + 1)), CS((size_t)nrhs * m), SN((size_t)nrhs * m);
     auto Hc = [&](int col, int i, int j) -> Cx& { return H[((size_t)col * m + j) * (m + 1) + i]; };
     int st = MLF_OK, k = 0;
     const int max_outer = 1000;
     const bool prof = c->profiling != 0;
     if (prof) {
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < 4; ++q)
             if (!c->sev[q]) CK(cudaEventCreate(&c->sev[q]));
-            c->solve_ms[q] = 0;
-        }
+        for (double& v : c->solve_ms) v = 0;
     }
     const auto t_start = std::chrono::steady_clock::now();
     for (; k < max_outer; ++k) {
@@ -864,16 +894,43 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
         // column is declared converged on it), the FP64 residual after the
         // cycle deciding as always.
         const bool provisional = k == 0 && x0 != nullptr;
+        if (prof) cudaStreamSynchronize(s);
+        const auto t_res = std::chrono::steady_clock::now();
         if (k == 0 && !x0) {
             CK(cudaMemcpyAsync(r, b, V1 * sizeof(double2), cudaMemcpyDeviceToDevice, s));
         } else {
+            // after a check, only the columns still running need a new residual
+            // (a converged column's x and r no longer change): they are gathered
+            // so that the FP64 operator runs on those columns alone
+            std::vector<int> run;
+            if (!provisional)
+                for (int col = 0; col < nrhs; ++col)
+                    if (!done[col]) run.push_back(col);
+            const int nrun = (int)run.size();
             c->mv_prec = provisional ? 1 : 0;
-            st = device_matvec(c, x, t64, nrhs, N, s);
-            c->mv_prec = 0;
-            if (st) break;
-            k_resid<<<4096, 256, 0, s>>>(V1, b, t64, r);
+            if (!provisional && nrun < nrhs) {
+                for (int i = 0; i < nrun && !st; ++i)
+                    if (!cuda_ok(c, cudaMemcpyAsync(w + (size_t)i * N, x + (size_t)run[i] * N, N * sizeof(double2),
+                                                    cudaMemcpyDeviceToDevice, s), "gather"))
+                        st = MLF_E_CUDA;
+                if (!st && nrun) st = device_matvec(c, w, t64, nrun, N, s);
+                c->mv_prec = 0;
+                if (st) break;
+                for (int i = 0; i < nrun; ++i)
+                    k_resid<<<1024, 256, 0, s>>>((size_t)N, b + (size_t)run[i] * N, t64 + (size_t)i * N,
+                                                 r + (size_t)run[i] * N);
+            } else {
+                st = device_matvec(c, x, t64, nrhs, N, s);
+                c->mv_prec = 0;
+                if (st) break;
+                k_resid<<<4096, 256, 0, s>>>(V1, b, t64, r);
+            }
         }
         if ((st = col_norms(c, nrhs, r, partial, dred, hbuf, beta, s))) break;
+        if (prof) {   // col_norms synchronised the stream
+            const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_res).count();
+            c->solve_ms[provisional ? 5 : 4] += ms;
+        }
         bool all = true, budget = false;
         for (int col = 0; col < nrhs; ++col) {
             // a NaN or Inf in b or in the residual ends the column first
@@ -901,7 +958,6 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
         for (int col = 0; col < nrhs; ++col) scl[col] = (!done[col] && beta[col] > 0) ? 1.0 / beta[col] : 0.0;
         CK(cudaMemcpyAsync(dscale, scl.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
         k_colscale_df<BT><<<gc, 256, 0, s>>>(N, r, dscale, V, ss);
-        std::fill(H.begin(), H.end(), cx(0, 0));
         std::fill(G.begin(), G.end(), cx(0, 0));
         for (int col = 0; col < nrhs; ++col) G[(size_t)col * (m + 1)] = cx(done[col] ? 0.0 : beta[col], 0);
         std::vector<int> jcol(nrhs, 0), live(nrhs, 0);
@@ -1038,6 +1094,7 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
     if (prof) {
         cudaStreamSynchronize(s);
         c->solve_ms[3] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+        c->solve_ms[6] = k;
     }
     return st;
 }
@@ -1056,6 +1113,12 @@ using namespace mlf;
 extern "C" int mlf_solve_times(mlf_ctx* h, double* out4) {
     if (!h || !out4) return MLF_E_ARG;
     for (int q = 0; q < 4; ++q) out4[q] = h->c.solve_ms[q];
+    return MLF_OK;
+}
+
+extern "C" int mlf_solve_phases(mlf_ctx* h, double* out, int n) {
+    if (!h || !out || n < 0) return MLF_E_ARG;
+    for (int q = 0; q < n && q < 7; ++q) out[q] = h->c.solve_ms[q];
     return MLF_OK;
 }
 

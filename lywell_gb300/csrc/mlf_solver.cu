@@ -478,11 +478,15 @@ __global__ void k_excitation(int N, int nrhs, const double* __restrict__ dirs, c
     b[(size_t)r * N + i] = make_double2(acc.x * 0.5 * l, acc.y * 0.5 * l);
 }
 
+// One CTA per angle a; the currents of angle a are I + a istride (istride 0:
+// one current vector for every angle) and its polarisation norm den[a].
 __global__ void k_rcs(int N, const double* __restrict__ t_baric, const int* __restrict__ e_t,
-                      const double* __restrict__ e_long, const double2* __restrict__ I, const double* __restrict__ th,
-                      const double* __restrict__ ph, double rx, double ry, double rz, double rzl, double w_smue,
-                      double facE, double den, double* __restrict__ sigma) {
+                      const double* __restrict__ e_long, const double2* __restrict__ Iall, size_t istride,
+                      const double* __restrict__ th, const double* __restrict__ ph, double rx, double ry, double rz,
+                      double rzl, double w_smue, double facE, const double* __restrict__ den,
+                      double* __restrict__ sigma) {
     const int a = blockIdx.x;
+    const double2* __restrict__ I = Iall + (size_t)a * istride;
     double st, ct, sp, cp;
     sincos(th[a], &st, &ct);
     sincos(ph[a], &sp, &cp);
@@ -528,7 +532,7 @@ __global__ void k_rcs(int N, const double* __restrict__ t_baric, const int* __re
             const double ex = -facE * red[2 * d + 1][0], ey = facE * red[2 * d][0];
             s2 += ex * ex + ey * ey;
         }
-        sigma[a] = s2 * 4 * PI * (rzl * rzl) / den;
+        sigma[a] = s2 * 4 * PI * (rzl * rzl) / den[a];
     }
 }
 
@@ -548,11 +552,12 @@ int device_excitation(Ctx* c, const double* dirs, const double2* pols, double2 c
     return MLF_OK;
 }
 
-int device_rcs(Ctx* c, const double2* I, const double2* pol, double2 ctte, const double* th, const double* ph,
-               int nang, double* sigma) {
+// calc_RCS (modRCS.f90:109-153): observation radius from the edge-centre
+// bounding box; calc_E uses the triangle centroids.  Angle a's currents are
+// I + a istride and its polarisation pol + 3 (a pstride).
+static int rcs_launch(Ctx* c, const double2* I, size_t istride, const double2* pol, int pstride, double2 ctte,
+                      const double* th, const double* ph, int nang, double* sigma) {
     DevScope ds;
-    // calc_RCS (modRCS.f90:109-153): observation radius from the edge-centre
-    // bounding box; calc_E uses the triangle centroids
     const int N = c->N;
     const double* ec = c->e_centro.data();
     int lim[6] = {0, 0, 0, 0, 0, 0};
@@ -574,24 +579,41 @@ int device_rcs(Ctx* c, const double2* I, const double2* pol, double2 ctte, const
     if (50 * D > rzl) rzl = 50 * D;
     if (20 * lambda > rzl) rzl = 20 * lambda;
     rzl = rzl * 10;
-    double den = 0;
-    for (int d = 0; d < 3; ++d) {
-        const double vx = pol[d].x * ctte.x - pol[d].y * ctte.y, vy = pol[d].x * ctte.y + pol[d].y * ctte.x;
-        den += vx * vx + vy * vy;
-    }
-    double *dth = nullptr, *dph = nullptr, *dsig = nullptr;
+    std::vector<double> den(nang, 0.0);
+    for (int a = 0; a < nang; ++a)
+        for (int d = 0; d < 3; ++d) {
+            const double2 pv = pol[3 * (size_t)a * pstride + d];
+            const double vx = pv.x * ctte.x - pv.y * ctte.y, vy = pv.x * ctte.y + pv.y * ctte.x;
+            den[a] += vx * vx + vy * vy;
+        }
+    double *dth = nullptr, *dph = nullptr, *dsig = nullptr, *dden = nullptr;
     CK(ds.alloc(&dth, nang * sizeof(double)));
     CK(ds.alloc(&dph, nang * sizeof(double)));
     CK(ds.alloc(&dsig, nang * sizeof(double)));
+    CK(ds.alloc(&dden, nang * sizeof(double)));
     CK(cudaMemcpyAsync(dth, th, nang * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dph, ph, nang * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    k_rcs<<<nang, 256, 0, c->stream>>>(N, c->dt_baric, c->de_t, c->de_long, I, dth, dph, 0.5 * (maxX + minX),
-                                       0.5 * (maxY + minY), 0.5 * (maxZ + minZ), rzl, c->ph.w * c->ph.smue,
-                                       c->ph.w * MU / (4 * PI), den, dsig);
+    CK(cudaMemcpyAsync(dden, den.data(), nang * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    k_rcs<<<nang, 256, 0, c->stream>>>(N, c->dt_baric, c->de_t, c->de_long, I, istride, dth, dph,
+                                       0.5 * (maxX + minX), 0.5 * (maxY + minY), 0.5 * (maxZ + minZ), rzl,
+                                       c->ph.w * c->ph.smue, c->ph.w * MU / (4 * PI), dden, dsig);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(sigma, dsig, nang * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return MLF_OK;
+}
+
+// sigma(theta[a], phi[a]) of one current vector for nang bistatic angles
+int device_rcs(Ctx* c, const double2* I, const double2* pol, double2 ctte, const double* th, const double* ph,
+               int nang, double* sigma) {
+    return rcs_launch(c, I, 0, pol, 0, ctte, th, ph, nang, sigma);
+}
+
+// one angle per column: column q (currents X + q ldx, polarisation pols + 3 q)
+// at (th[q], ph[q]) -- the backscatter of a block of monostatic angles in one launch
+int device_rcs_cols(Ctx* c, const double2* X, size_t ldx, int ncol, const double2* pols, double2 ctte,
+                    const double* th, const double* ph, double* sigma) {
+    return rcs_launch(c, X, ldx, pols, 1, ctte, th, ph, ncol, sigma);
 }
 
 }  // namespace mlf

@@ -173,13 +173,17 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
             if ((st = device_solve_mixed(c, b, x0, tol, maxit, nb, x, it.data(), rr.data(), precond_kind,
                                          stc.data(), 0.9 * tol, &outer)))
                 break;
-            for (int q = 0; q < nb && !st; ++q) {
+            // the block's backscatter in one launch (a CTA per column)
+            std::vector<double> thq(nb, PI / 2.), phq(nb), sq(nb);
+            for (int q = 0; q < nb; ++q) {
                 const int a = q * nrun + k;
-                const double th = PI / 2.;
                 iters[a] = it[q];
                 status_out[a] = stc[q];
-                st = device_rcs(c, x + (size_t)q * N, &pols[3 * q], ctte, &th, &ph[a], 1, &sigma[a]);
+                phq[q] = ph[a];
             }
+            if ((st = device_rcs_cols(c, x, (size_t)N, nb, pols.data(), ctte, thq.data(), phq.data(), sq.data())))
+                break;
+            for (int q = 0; q < nb; ++q) sigma[q * nrun + k] = sq[q];
             if (g2 && k > 0) std::swap(g, g2);   // g2 <- x_{k-1} in this angle's frame
             CK(cudaMemcpyAsync(g, x, nbytes_col * nb, cudaMemcpyDeviceToDevice, c->stream));
             std::copy(dirs.begin(), dirs.begin() + 3 * nb, prev.begin());
@@ -206,10 +210,8 @@ extern "C" int mlf_monostatic(mlf_ctx* h, int nang, const double* phis, int hh, 
                                     &status_out[a0], 0.9 * tol, &outer);
         }
         if (st) break;
-        for (int q = 0; q < nb && !st; ++q) {
-            const double th = PI / 2.;
-            st = device_rcs(c, x + (size_t)q * N, &pols[3 * q], ctte, &th, &ph[a0 + q], 1, &sigma[a0 + q]);
-        }
+        std::vector<double> thq(nb, PI / 2.);
+        st = device_rcs_cols(c, x, (size_t)N, nb, pols.data(), ctte, thq.data(), &ph[a0], &sigma[a0]);
     }
     return st;
 }

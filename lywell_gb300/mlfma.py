@@ -376,6 +376,14 @@ class MLFMA:
         _check(load().mlf_solve_times(self._h, _p(out)), self._h)
         return dict(zip(("precond", "operator", "orthogonalisation", "total"), out.tolist()))
 
+    def solve_phases(self):
+        """mlf_solve_phases: solve_times plus the FP64 residual checks, the
+        provisional FP32 residual of a warm start (ms) and the outer steps."""
+        out = np.zeros(7)
+        _check(load().mlf_solve_phases(self._h, _p(out), 7), self._h)
+        return dict(zip(("precond", "operator", "orthogonalisation", "total", "fp64_residual",
+                         "provisional_residual", "outer"), out.tolist()))
+
     def set_gmres_restart(self, m: int):
         _check(load().mlf_set_gmres_restart(self._h, int(m)), self._h)
 
