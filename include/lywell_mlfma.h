@@ -259,7 +259,8 @@ int mlf_solve_phases(mlf_ctx* ctx, double* out, int n);
 /* Autotuner for batched solves: times the FP32 operator on each candidate
  * block of right-hand sides (candidates[ncand], 1..4096) with each
  * multi-column engine -- both box-block GEMM engines at the tile widths 8, 32
- * and 64 columns, the warp engine and the tcgen05 near field -- and returns
+ * and 64 columns, the warp engine (leaf boxes under 96 bases on average) and
+ * the tcgen05 engine (16 bases or more) -- and returns
  * the smallest block whose time per right-hand side is within 5 % of the
  * best, with its tile width (0 for a single column or the warp engine) and
  * engine (best_engine, optional: 1 tensor cores (mma.sync), 0 FP32 FMA, 2 or

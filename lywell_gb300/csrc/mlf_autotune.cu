@@ -6,6 +6,10 @@
 // engine, and the box blocks with the near field on tcgen05 -- one FP32
 // operator application on B random columns is timed with CUDA events (two
 // warm-up calls, three timed).
+// Engines far outside their range are not timed: the warp engines when leaf
+// boxes hold 96 bases or more on average (twice the size below which they
+// are the default), the tcgen05 engine below 16 (its tiles pad a box to 16
+// rows and its chunks to 32 bases).
 // The choice minimises operator time per right-hand side; a smaller block is
 // kept when it is within 5 % of the best (it retires columns sooner and holds
 // a smaller Krylov basis).  No counterpart in the reference, whose monostatic
@@ -55,6 +59,8 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
     *best_cols = 0;
     std::vector<std::pair<double, int>> per(ncand);
     std::vector<int> colsel(ncand, 0), engsel(ncand, 1);
+    const long long nbox = std::max<long long>(1, (long long)c->box_ptr.size() - 1);
+    const double mean_box = (double)c->N / (double)nbox;
     for (int q = 0; q < ncand && !st; ++q) {
         const int B = cand[q];
         double tq = 1e300;
@@ -64,6 +70,8 @@ int autotune_block(Ctx* c, const int* cand, int ncand, int* best_block, int* bes
             // with its per-box and its per-basis receive, then the tcgen05 near field
             const int wv = var % 3, eng = var >= 6 ? var - 4 : 1 - var / 3;
             if (B == 1 && var) break;   // one column uses the CSR kernels
+            if ((eng == 2 || eng == 3) && mean_box >= 96.0) continue;
+            if (eng == 4 && mean_box < 16.0) continue;
             if (eng < 2 && wv > 0 && widths[wv - 1] >= B) continue;   // a narrower tile already covers the block
             c->blk_cols = eng >= 2 ? 0 : widths[wv];
             c->blk_engine = eng;

@@ -2,17 +2,21 @@
 
   python -m lywell_gb300.profiling fp32 --mesh spheroid5 --nrhs 64 --engine 4 --steps 5
   python -m lywell_gb300.profiling fp64 --mesh sphere5 --steps 5
+  python -m lywell_gb300.profiling nearinv --mesh spheroid4 --steps 1
 
 fp32: the batched FP32 operator (mlf_matvec32_device) on `nrhs` random
 columns with a chosen multi-column engine (-1 automatic, 0 FMA box blocks,
 1 mma.sync box blocks, 2/3 warp engine, 4 tcgen05 box blocks) and tile
 width; fp64: the FP64 matvec (mlf_matvec_device) on one column.  Each prints
 one JSON line: time per call (CUDA events over `steps` calls after two
-warm-up calls) and the per-stage times of one more call.
+warm-up calls) and the per-stage times of one more call.  nearinv: the
+27-box neighbourhood-inverse set-up (mlf_nearinv, the blocked FP32 LU for
+large neighbourhoods), one untimed call and `steps` timed ones, with the
+neighbourhood sizes.
 
-Meshes: spheroid5 = 30 720-RWG prolate spheroid with the 722-RHS workload's
-mesh density (icosphere-5, semi-axes 1.5 x 0.375 x 0.375 lambda, ~145 bases
-per leaf box); spheroid6 = the 122 880-RWG spheroid of that workload
+Meshes: spheroid4 / spheroid5 = 7 680 / 30 720-RWG prolate spheroids with
+the 722-RHS workload's mesh density (icosphere-4 / -5, semi-axes 0.75 x
+0.1875 x 0.1875 / 1.5 x 0.375 x 0.375 lambda, ~145 bases per leaf box); spheroid6 = the 122 880-RWG spheroid of that workload
 (3 x 0.75 x 0.75 lambda); sphere5 / sphere6 = the r = 3 / 6 lambda
 icospheres (30 720 / 122 880 RWG, ~7-11 bases per leaf box).  Leaf boxes of
 0.25 lambda, lambda = 1 m.
@@ -25,7 +29,7 @@ import json
 
 import numpy as np
 
-MESHES = ("spheroid5", "spheroid6", "sphere5", "sphere6")
+MESHES = ("spheroid4", "spheroid5", "spheroid6", "sphere5", "sphere6")
 
 
 def make_mesh(name):
@@ -36,6 +40,8 @@ def make_mesh(name):
         return meshes.icosphere(5, 3.0)
     if name == "spheroid6":
         return meshes.spheroid(6, (3.0, 0.75, 0.75), noise=0.01, seed=1234)
+    if name == "spheroid4":
+        return meshes.spheroid(4, (0.75, 0.1875, 0.1875), noise=0.0025, seed=1234)
     return meshes.spheroid(5, (1.5, 0.375, 0.375), noise=0.005, seed=1234)
 
 
@@ -80,16 +86,41 @@ def run(kind, mesh, nrhs=64, steps=5, engine=-1, cols=0):
     return out
 
 
+def run_nearinv(mesh, steps=1):
+    import time
+    import torch
+    from . import MLFMA, RWG
+
+    m = MLFMA(RWG(make_mesh(mesh)), lam=1.0, ladomax=0.25)
+    assert m.nearinv() == 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        assert m.nearinv() == 0
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    ia, _, _ = m.near_csr()
+    rows = np.diff(np.asarray(ia))
+    out = {"profile": "neighbourhood inverse", "mesh": mesh, "N": m.N, "near_nnz": m.nnz,
+           "neighbourhood_mean": float(rows.mean()), "neighbourhood_max": int(rows.max()),
+           "seconds_per_call": dt}
+    m.close()
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("kind", choices=["fp32", "fp64"])
+    ap.add_argument("kind", choices=["fp32", "fp64", "nearinv"])
     ap.add_argument("--mesh", default="spheroid5", choices=MESHES)
     ap.add_argument("--nrhs", type=int, default=64)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--engine", type=int, default=-1)
     ap.add_argument("--cols", type=int, default=0)
     a = ap.parse_args(argv)
-    print(json.dumps(run(a.kind, a.mesh, a.nrhs, a.steps, a.engine, a.cols)), flush=True)
+    if a.kind == "nearinv":
+        print(json.dumps(run_nearinv(a.mesh, a.steps)), flush=True)
+    else:
+        print(json.dumps(run(a.kind, a.mesh, a.nrhs, a.steps, a.engine, a.cols)), flush=True)
 
 
 if __name__ == "__main__":

@@ -11,7 +11,7 @@ solve's.
 import numpy as np
 import pytest
 
-from lywell_gb300 import MLFMA, RWG, ajustar_polariz, direction, meshes
+from lywell_gb300 import MLFMA, RWG, _capi, ajustar_polariz, direction, meshes
 from oracle import core
 from oracle.rwg import RWG as ORWG
 
@@ -203,9 +203,7 @@ def test_autotune_block_covers_all_engines(ico4):
     _, m, _ = ico4
     res = m.autotune_block((4, 8, 16))
     assert res["block"] in (4, 8, 16)
-    assert res["engine"] in ("FP32 FMA", "tensor cores (3xTF32 mma.sync)", "warp per basis",
-                             "warp per basis, per-basis receive",
-                             "tensor cores (3xTF32 tcgen05 near field, TMEM accumulators)")
+    assert res["engine"] in _capi.ENGINES.values()
     assert all(t > 0 for t in res["per_rhs_ms"].values())
     rng = np.random.default_rng(77)
     X = rng.standard_normal((m.N, res["block"])) + 1j * rng.standard_normal((m.N, res["block"]))
