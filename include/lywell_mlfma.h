@@ -312,6 +312,17 @@ int mlf_nearinv(mlf_ctx* ctx, int* bad_box);
  * unknowns per neighbourhood, FP32 above.  No counterpart in the reference. */
 int mlf_set_nearinv_precision(mlf_ctx* ctx, int bits);
 
+/* The FP32 LU gives each box one CTA, so the largest neighbourhoods would set
+ * the set-up time alone.  Boxes of at least min_unknowns unknowns whose work
+ * (n^3) exceeds the remaining boxes' share per CTA are factorised on many CTAs
+ * each instead (panel on one CTA; row swaps, U12 and the trailing update over
+ * the GPU), on side streams next to the one-CTA-per-box kernel.
+ * min_unknowns = 0 turns this off; the default is 1024.  mlf_get_lu_split
+ * reads the setting and how many boxes took the many-CTA path in the last
+ * build.  No counterpart in the reference. */
+int mlf_set_lu_split(mlf_ctx* ctx, int min_unknowns);
+int mlf_get_lu_split(mlf_ctx* ctx, int* min_unknowns, int* last_big_boxes);
+
 /* Same with each box's own bases as the neighbourhood (block Jacobi on the
  * near field): cheaper where leaf boxes hold many bases and near lists run
  * into the thousands.  Replaces any previous mlf_nearinv result. */

@@ -46,6 +46,8 @@ SIGNATURES = {
     "mlf_set_translation_group": (C.c_int, [vp, C.c_int, C.c_int]),
     "mlf_solve_times": (C.c_int, [vp, vp]),
     "mlf_solve_phases": (C.c_int, [vp, vp, C.c_int]),
+    "mlf_set_lu_split": (C.c_int, [vp, C.c_int]),
+    "mlf_get_lu_split": (C.c_int, [vp, vp, vp]),
     "mlf_precond_apply32": (C.c_int, [vp, vp, vp, C.c_int]),
     "mlf_autotune_block": (C.c_int, [vp, vp, C.c_int, vp, vp, vp, vp]),
     "mlf_set_block_engine": (C.c_int, [vp, C.c_int, C.c_int]),

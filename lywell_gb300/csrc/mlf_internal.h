@@ -150,6 +150,8 @@ struct Ctx {
                                       // throughout, 4 box blocks on tcgen05 (near field, leaf
                                       // aggregation and receive); -1 by mean leaf-box size
     TcState* tc = nullptr;            // engine 4's operand layouts and tensor maps, built on first use
+    int lu_big_min = 1024;            // neighbourhood inverse: smallest box for the many-CTA LU (0: none)
+    int lu_big_last = 0;              //   boxes that took it in the last build
     void* mix_ws = nullptr;           // workspace of the mixed-precision solve (Krylov basis and vectors),
     size_t mix_ws_bytes = 0;          //   kept between solves, grown on demand
     int* djas = nullptr;              // near CSR columns as box-sorted positions (warp engine)
@@ -246,7 +248,8 @@ int nbhd_inverse_lu32(Ctx* c, int nmax, int nownmax, int* bad_box);   // blocked
 // the same over 2-ring lists (dense Z, N x N row-major complex(4)): rows of the
 // own bases on the near pattern into M2 (the learned preconditioner's targets)
 int ring_inverse_lu32(Ctx* c, const float2* Zd, const long long* off, const int* len, const int* bases,
-                      const std::vector<int>& len_host, int nmax, int nownmax, float2* M2, int* bad_box);
+                      const std::vector<int>& len_host, const std::vector<long long>& off_host, int nmax,
+                      int nownmax, float2* M2, int* bad_box);
 int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s);
 int device_matvec32_from32(Ctx* c, const float2* x32, double2* y, int nrhs, cudaStream_t s);
 int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStream_t s);

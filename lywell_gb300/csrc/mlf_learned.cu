@@ -259,7 +259,7 @@ static int lp_ring_targets(Ctx* c, const LpHost& H, float2* M2, int* bad_box) {
         if (!cuda_ok(c, cudaGetLastError(), "dense Z")) fail(MLF_E_CUDA);
     }
     // blocked FP32 LU per box over its 2-ring list (mlf_nbhd_lu.cu)
-    if (!st) st = ring_inverse_lu32(c, Zd, doff, dlen, dbases, len, (int)nmax, (int)ownmax, M2, bad_box);
+    if (!st) st = ring_inverse_lu32(c, Zd, doff, dlen, dbases, len, off, (int)nmax, (int)ownmax, M2, bad_box);
     for (void* p : {(void*)Zd, (void*)doff, (void*)dlen, (void*)dbases})
         if (p) cudaFree(p);
     return st;

@@ -268,6 +268,18 @@ class MLFMA:
         """Elimination of nearinv(): 64 FP64, 32 blocked FP32 LU, 0 by size (FP64 up to 768 unknowns)."""
         _check(load().mlf_set_nearinv_precision(self._h, int(bits)), self._h)
 
+    def set_lu_split(self, min_unknowns: int = 1024):
+        """mlf_set_lu_split: boxes of at least min_unknowns unknowns that would
+        dominate the neighbourhood inverse's set-up are factorised on many CTAs
+        each (0: never)."""
+        _check(load().mlf_set_lu_split(self._h, int(min_unknowns)), self._h)
+
+    def lu_split(self):
+        """(min_unknowns, boxes on the many-CTA path in the last build)."""
+        a, b = C.c_int(), C.c_int()
+        _check(load().mlf_get_lu_split(self._h, C.byref(a), C.byref(b)), self._h)
+        return a.value, b.value
+
     def precond_apply(self, y, precond="nearinv"):
         if isinstance(precond, str):
             precond = PRECOND[precond]

@@ -10,7 +10,9 @@ blocked LU is practical.
 
 Tolerances: FP32 elimination with partial pivoting, 1e-4 relative to the
 FP64 rows (measured a few 1e-6); numpy inverses in FP64 of the same
-complex(4) blocks, 1e-4.
+complex(4) blocks, 1e-4.  The many-CTA path for the largest neighbourhoods
+(mlf_set_lu_split) runs the same tiles in the same order as the one-CTA
+kernel, so its rows are compared bit for bit.
 """
 import time
 
@@ -52,9 +54,37 @@ def test_blocked_fp32_matches_fp64_elimination(gpu_lib):
     m.close()
 
 
-def test_large_neighbourhoods_against_numpy(gpu_lib):
+@pytest.fixture(scope="module")
+def spheroid30k(gpu_lib):
     tris = meshes.spheroid(5, (1.5, 0.375, 0.375), noise=0.005, seed=1234)
     m = MLFMA(RWG(tris), lam=1.0, ladomax=0.25)
+    yield m
+    m.close()
+
+
+def test_many_cta_boxes_match_one_cta_kernel(spheroid30k):
+    """The largest neighbourhoods factorised on many CTAs each give the same
+    rows, bit for bit, as the one-CTA-per-box kernel (on this mesh of about 200
+    boxes, fewer than two per SM, every box qualifies)."""
+    m = spheroid30k
+    m.set_lu_split(0)
+    t0 = time.time()
+    assert m.nearinv() == 0
+    t_one = time.time() - t0
+    v_one = m.nearinv_values()
+    m.set_lu_split(1024)
+    t0 = time.time()
+    assert m.nearinv() == 0
+    t_split = time.time() - t0
+    nbig = m.lu_split()[1]
+    v_split = m.nearinv_values()
+    print(f"spheroid 30720 RWG: one CTA per box {t_one:.2f} s; {nbig} boxes on many CTAs {t_split:.2f} s")
+    assert nbig > 0
+    assert np.array_equal(v_split.view(np.float64), v_one.view(np.float64))
+
+
+def test_large_neighbourhoods_against_numpy(spheroid30k):
+    m = spheroid30k
     t0 = time.time()
     assert m.nearinv() == 0
     t_lu = time.time() - t0
@@ -79,4 +109,3 @@ def test_large_neighbourhoods_against_numpy(gpu_lib):
     for r in rows:
         got = M[ia[r]:ia[r + 1]]
         assert _rel(got, inv[pos[r]]) < 1e-4, r
-    m.close()
