@@ -314,7 +314,7 @@ int mlf_set_nearinv_precision(mlf_ctx* ctx, int bits);
 
 /* The FP32 LU gives each box one CTA, so the largest neighbourhoods would set
  * the set-up time alone.  Boxes of at least min_unknowns unknowns whose work
- * (n^3) exceeds the remaining boxes' share per CTA are factorised on many CTAs
+ * (n^3) exceeds three times the remaining boxes' share per CTA are factorised on many CTAs
  * each instead (panel on one CTA; row swaps, U12 and the trailing update over
  * the GPU), on side streams next to the one-CTA-per-box kernel.
  * min_unknowns = 0 turns this off; the default is 1024.  mlf_get_lu_split

@@ -56,6 +56,7 @@ constexpr int LU_T = 64;          // GEMM tile rows and columns
 constexpr int LU_THREADS = 256;
 constexpr int LU_BIG_MAX = 512;       // boxes at most on the many-CTA path
 constexpr int LU_BIG_STREAMS = 8;     // large boxes in flight at once
+constexpr double LU_BIG_FACTOR = 3.0; // a box goes to the many-CTA path above this many CTA shares
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -620,7 +621,7 @@ static int big_box_launch(Ctx* c, const LuRing& ring, int b, int n, int nown, co
 // ring->M2.  *bad_box as mlf_nearinv.
 //
 // A box's elimination costs ~n^3.  The persistent kernel gives each box one
-// CTA, so a box whose work exceeds an average CTA's share of the rest would
+// CTA, so a box whose work exceeds a few average CTA shares of the rest would
 // set the finishing time alone (on the 722-RHS workload's spheroid the
 // largest neighbourhoods, 5648 unknowns, took most of the set-up).  Those
 // boxes, largest first, run instead on many CTAs each (k_lub_*), on a few side
@@ -636,13 +637,15 @@ static int blocked_inverse_rows(Ctx* c, int nmax, int nownmax, const LuRing* rin
     std::vector<int> order(nb);
     for (int b = 0; b < nb; ++b) order[b] = b;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b2) { return nsize(a) > nsize(b2); });
-    // the large boxes: a prefix of the order, while a box's work exceeds the
-    // remaining work's share per CTA of the persistent kernel
+    // the large boxes: a prefix of the order, while a box's work exceeds three
+    // times the remaining work's share per CTA of the persistent kernel (the
+    // many-CTA path serialises each box's panels; measured on the 122 880-RWG
+    // spheroid: 128 boxes on it at once the share, 1.79 s; its 32 largest, 1.44 s)
     std::vector<double> tail(nb + 1, 0.0);
     for (int k = nb - 1; k >= 0; --k) tail[k] = tail[k + 1] + std::pow((double)nsize(order[k]), 3.0);
     int nbig = 0;
     while (c->lu_big_min > 0 && nbig < nb && nbig < LU_BIG_MAX && nsize(order[nbig]) >= c->lu_big_min &&
-           std::pow((double)nsize(order[nbig]), 3.0) > tail[nbig] / (2.0 * nsm))
+           std::pow((double)nsize(order[nbig]), 3.0) > LU_BIG_FACTOR * tail[nbig] / (2.0 * nsm))
         ++nbig;
     const int nsmall = nb - nbig;
     int *dctr = nullptr, *dbad = nullptr, *dorder = nullptr;

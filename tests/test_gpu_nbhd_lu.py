@@ -64,8 +64,7 @@ def spheroid30k(gpu_lib):
 
 def test_many_cta_boxes_match_one_cta_kernel(spheroid30k):
     """The largest neighbourhoods factorised on many CTAs each give the same
-    rows, bit for bit, as the one-CTA-per-box kernel (on this mesh of about 200
-    boxes, fewer than two per SM, every box qualifies)."""
+    rows, bit for bit, as the one-CTA-per-box kernel."""
     m = spheroid30k
     m.set_lu_split(0)
     t0 = time.time()
