@@ -83,7 +83,7 @@ FLAG_DENSE_MOM = 2
 FLAG_FMM = 4
 PRECOND = {"none": 0, "ilu0": 1, "nearinv": 2}
 ENGINES = {0: "FP32 FMA", 1: "tensor cores (3xTF32 mma.sync)", 2: "warp per basis", 3: "warp per basis, per-basis receive",
-           4: "tensor cores (3xTF32 tcgen05 near field, aggregation and receive; TMEM accumulators)"}
+           4: "tensor cores (tcgen05: FP16-split near field and aggregation, 3xTF32 receive; TMEM accumulators)"}
 
 _lib = None
 
