@@ -11,9 +11,10 @@
 // Refinement (mode 1 of mlf_solve): r = b - A64 x in FP64; one restart cycle
 // of right-preconditioned GMRES(m) solves A d = r with an FP32 inner loop
 // (operator, preconditioner, Krylov basis and Gram-Schmidt in float) until its
-// residual estimate drops below inner_tol ||b|| or m steps; x += M^-1 V y in
-// FP64; stop when the FP64 residual ||b - A64 x|| < tol ||b||.  The FP64 residual decides, so the result
-// meets the same stopping test as the plain FP64 solve.
+// residual estimate drops below inner_tol ||b|| or m steps; x += M^-1 V y,
+// accumulated in FP64; stop when the FP64 residual ||b - A64 x|| < tol ||b||.
+// The FP64 residual decides, so the result meets the same stopping test as
+// the plain FP64 solve.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -802,7 +803,7 @@ static int apply_precond64(Ctx* c, int precond, int nrhs, const double2* in, dou
 // Iterative refinement: r = b - A64 x (FP64); one cycle of right-preconditioned
 // GMRES(m) with an all-FP32 inner loop (basis, Gram-Schmidt, preconditioner,
 // operator; Hessenberg and Givens on the host in double); d = V y in double;
-// x += M^-1 d with the FP64 preconditioner.
+// x += M^-1 d (the neighbourhood inverse in FP32 as in the cycle, ILU0 in FP64).
 // BT: the Krylov basis storage, float2 or __half2 (mlf_set_basis_precision).
 template <class BT>
 static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs, double2* x,
@@ -1082,7 +1083,19 @@ static int solve_mixed_t(Ctx* c, const double2* b, const double2* x0, double tol
         if (jmax == 0) break;
         CK(cudaMemcpyAsync(dred, y.data(), (size_t)jmax * nrhs * sizeof(double2), cudaMemcpyHostToDevice, s));
         k_combine32<BT><<<gc, 256, 0, s>>>(N, nrhs, jmax, V, V1, ls, dred, w);
-        if ((st = apply_precond64(c, precond, nrhs, w, t64, s))) break;
+        if (precond == 2 && f32) {
+            // the correction through the FP32 neighbourhood inverse the cycle itself
+            // used (the FP64 apply of a 64-column block costs ~0.12 s on GB300's
+            // FP64 units; the FP32 one changes the correction by ~1e-6 relative,
+            // and the FP64 residual still decides).  With the FP16 basis the FP64
+            // apply stays: a 3-column solve on that basis then ran into its step
+            // limit, which it meets with the FP64 apply.
+            k_d2f_m<<<4096, 256, 0, s>>>(V1, w, w32);
+            if ((st = device_nearinv_apply32(c, w32, t32, nrhs, s))) break;
+            k_f2d_m<<<4096, 256, 0, s>>>(V1, t32, t64);
+        } else if ((st = apply_precond64(c, precond, nrhs, w, t64, s))) {
+            break;
+        }
         k_axpy1<<<4096, 256, 0, s>>>(V1, t64, x);
         CK(cudaGetLastError());
     }
