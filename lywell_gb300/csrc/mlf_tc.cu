@@ -411,6 +411,10 @@ __global__ void __launch_bounds__(256, 1)
             tc::tma_prefetch_desc(&mblo);
             tc::tma_prefetch_desc(&mxhi);
             if (!RAW) tc::tma_prefetch_desc(&mxlo);
+            // the B operands stream through once (evicted first from L2); the X
+            // operand, read again by the CTAs of every target box near its source
+            // box, keeps the normal policy, as does everything after this kernel
+            const uint64_t pol_b = tc::l2_evict_first();
             uint32_t g = 0;
             bool ok = true;
             for (int q = blockIdx.x; q < nitems && ok; q += gridDim.x) {
@@ -448,12 +452,16 @@ __global__ void __launch_bounds__(256, 1)
                         zr = a.zrow[i] + cI * a.K2 + r0;
                     } else {
                         // raw field rows (box i, columns of this tile) into the lo tile's first 8 KB
-                        tc::tma_load_2d(st + TC_ABYTES, &mxhi, 2 * TC_KCH * cI, i * a.nrhs + ct * TC_COLS, &full[s]);
+                        tc::tma_load_2d_hint(st + TC_ABYTES, &mxhi, 2 * TC_KCH * cI, i * a.nrhs + ct * TC_COLS,
+                                             &full[s], pol_b);
                         zr = a.zrow[i] + cI * ni + r0;
                     }
                     for (int qq = 0; qq < nB; qq += TC_ZBOX) {
-                        tc::tma_load_2d(st + 2 * TC_ABYTES + qq * 128, &mbhi, 0, zr + qq, &full[s]);
-                        tc::tma_load_2d(st + 2 * TC_ABYTES + TC_BBYTES + qq * 128, &mblo, 0, zr + qq, &full[s]);
+                        // the aggregation's and receive's pattern operands are read by the
+                        // tiles of one box (and the column tiles) only: streamed too
+                        tc::tma_load_2d_hint(st + 2 * TC_ABYTES + qq * 128, &mbhi, 0, zr + qq, &full[s], pol_b);
+                        tc::tma_load_2d_hint(st + 2 * TC_ABYTES + TC_BBYTES + qq * 128, &mblo, 0, zr + qq, &full[s],
+                                             pol_b);
                     }
                 }
             }
