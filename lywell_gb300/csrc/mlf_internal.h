@@ -244,12 +244,12 @@ int device_ilu_solve(Ctx* c, const double2* y, double2* x, cudaStream_t s);
 int device_cgs(Ctx* c, const double2* b, const double2* x0, double tol, int maxit, int nrhs,
                double2* x, int* iters, double* relres, int precond, int* status);
 int device_nearinv_setup(Ctx* c, int* bad_box, int own_only);
-int nbhd_inverse_lu32(Ctx* c, int nmax, int nownmax, int* bad_box);   // blocked FP32 LU (mlf_nbhd_lu.cu)
+int nbhd_inverse_lu32(Ctx* c, int nownmax, int* bad_box);   // blocked FP32 LU (mlf_nbhd_lu.cu)
 // the same over 2-ring lists (dense Z, N x N row-major complex(4)): rows of the
 // own bases on the near pattern into M2 (the learned preconditioner's targets)
 int ring_inverse_lu32(Ctx* c, const float2* Zd, const long long* off, const int* len, const int* bases,
-                      const std::vector<int>& len_host, const std::vector<long long>& off_host, int nmax,
-                      int nownmax, float2* M2, int* bad_box);
+                      const std::vector<int>& len_host, const std::vector<long long>& off_host, int nownmax,
+                      float2* M2, int* bad_box);
 int device_matvec32(Ctx* c, const double2* x, double2* y, int nrhs, int ld, cudaStream_t s);
 int device_matvec32_from32(Ctx* c, const float2* x32, double2* y, int nrhs, cudaStream_t s);
 int device_nearinv_apply32(Ctx* c, const float2* y, float2* x, int nrhs, cudaStream_t s);

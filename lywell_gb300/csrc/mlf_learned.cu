@@ -211,7 +211,7 @@ static int lp_ring_targets(Ctx* c, const LpHost& H, float2* M2, int* bad_box) {
     for (int b = 0; b < nb; ++b) at.emplace(key(H.cell[3 * b], H.cell[3 * b + 1], H.cell[3 * b + 2]), b);
     std::vector<long long> off(nb + 1, 0);
     std::vector<int> len(nb), bases;
-    size_t nmax = 0, ownmax = 0;
+    size_t ownmax = 0;
     for (int b = 0; b < nb; ++b) {
         const size_t start = bases.size();
         for (int dx = -2; dx <= 2; ++dx)
@@ -226,7 +226,6 @@ static int lp_ring_targets(Ctx* c, const LpHost& H, float2* M2, int* bad_box) {
         std::sort(bases.begin() + start, bases.end());
         len[b] = (int)(bases.size() - start);
         off[b + 1] = (long long)bases.size();
-        nmax = std::max(nmax, (size_t)len[b]);
         ownmax = std::max(ownmax, (size_t)(c->box_ptr[b + 1] - c->box_ptr[b]));
     }
     size_t fre = 0, tot = 0;
@@ -259,7 +258,7 @@ static int lp_ring_targets(Ctx* c, const LpHost& H, float2* M2, int* bad_box) {
         if (!cuda_ok(c, cudaGetLastError(), "dense Z")) fail(MLF_E_CUDA);
     }
     // blocked FP32 LU per box over its 2-ring list (mlf_nbhd_lu.cu)
-    if (!st) st = ring_inverse_lu32(c, Zd, doff, dlen, dbases, len, off, (int)nmax, (int)ownmax, M2, bad_box);
+    if (!st) st = ring_inverse_lu32(c, Zd, doff, dlen, dbases, len, off, (int)ownmax, M2, bad_box);
     for (void* p : {(void*)Zd, (void*)doff, (void*)dlen, (void*)dbases})
         if (p) cudaFree(p);
     return st;

@@ -626,7 +626,7 @@ static int big_box_launch(Ctx* c, const LuRing& ring, int b, int n, int nown, co
 // largest neighbourhoods, 5648 unknowns, took most of the set-up).  Those
 // boxes, largest first, run instead on many CTAs each (k_lub_*), on a few side
 // streams concurrently with the persistent kernel over the others.
-static int blocked_inverse_rows(Ctx* c, int nmax, int nownmax, const LuRing* ring, const int* ring_len,
+static int blocked_inverse_rows(Ctx* c, int nownmax, const LuRing* ring, const int* ring_len,
                                 const long long* ring_off, int* bad_box) {
     DevScope ds;
     const int nb = (int)c->box_ptr.size() - 1;
@@ -708,13 +708,13 @@ static int blocked_inverse_rows(Ctx* c, int nmax, int nownmax, const LuRing* rin
     return MLF_OK;
 }
 
-int nbhd_inverse_lu32(Ctx* c, int nmax, int nownmax, int* bad_box) {
-    return blocked_inverse_rows(c, nmax, nownmax, nullptr, nullptr, nullptr, bad_box);
+int nbhd_inverse_lu32(Ctx* c, int nownmax, int* bad_box) {
+    return blocked_inverse_rows(c, nownmax, nullptr, nullptr, nullptr, bad_box);
 }
 
 int ring_inverse_lu32(Ctx* c, const float2* Zd, const long long* off, const int* len, const int* bases,
-                      const std::vector<int>& len_host, const std::vector<long long>& off_host, int nmax,
-                      int nownmax, float2* M2, int* bad_box) {
+                      const std::vector<int>& len_host, const std::vector<long long>& off_host, int nownmax,
+                      float2* M2, int* bad_box) {
     LuRing r;
     r.Zd = Zd;
     r.N = c->N;
@@ -722,7 +722,7 @@ int ring_inverse_lu32(Ctx* c, const float2* Zd, const long long* off, const int*
     r.len = len;
     r.bases = bases;
     r.M2 = M2;
-    return blocked_inverse_rows(c, nmax, nownmax, &r, len_host.data(), off_host.data(), bad_box);
+    return blocked_inverse_rows(c, nownmax, &r, len_host.data(), off_host.data(), bad_box);
 }
 
 }  // namespace mlf

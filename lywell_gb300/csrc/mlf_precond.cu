@@ -373,7 +373,7 @@ int device_nearinv_setup(Ctx* c, int* bad_box, int own_only) {
     CK(cudaMalloc(&c->dMinv, std::max<long long>(total, 1) * sizeof(double2)));
     // large neighbourhoods: the blocked FP32 LU (mlf_nbhd_lu.cu)
     if (!own_only && (c->nearinv_bits == 32 || (c->nearinv_bits == 0 && nmax > NBI_FP64_MAX))) {
-        const int st = nbhd_inverse_lu32(c, nmax, nownmax, bad_box);
+        const int st = nbhd_inverse_lu32(c, nownmax, bad_box);
         if (st) return st;
         c->nearinv_ok = *bad_box == 0;
         return MLF_OK;
