@@ -8,9 +8,10 @@ installed preconditioner is M = M1 + gamma * tscale * net(tokens): the same
 pattern and apply cost as M1, still linear.  Training, inference and
 gradients run in the library's own CUDA kernels (mlf_mlp_*); tokens and the
 2-ring targets come from mlf_lp_tokens; gamma is chosen from CGS traces on
-the training bodies; solve_with_fallback switches to ILU0 when the learned
-solve has not converged within the unpreconditioned iteration count, measured
-by the true FP64 MLFMA residual.  Device buffers are torch CUDA tensors
+the training bodies, and only when it beats M1 by a margin there (else 0: M1
+itself); solve_with_fallback solves again with the base M1, then with ILU0,
+when the learned solve has not converged within the unpreconditioned
+iteration count, measured by the true FP64 MLFMA residual.  Device buffers are torch CUDA tensors
 (memory only).  No counterpart in the reference.
 """
 from __future__ import annotations
@@ -133,6 +134,10 @@ class LearnedPreconditioner:
     def apply_to(self, m) -> int:
         return install(m, self.net, self.gamma * self.tscale)
 
+    def remove_from(self, m) -> int:
+        """Back to the exact neighbourhood inverse M1 (kept under the correction)."""
+        return install(m, self.net, 0.0)
+
 
 def _cgs_iters(m, b, errmax, maxit):
     out = m.cgs(b, errmax=errmax, maxit=maxit, precond="nearinv")
@@ -140,12 +145,16 @@ def _cgs_iters(m, b, errmax, maxit):
 
 
 def train(contexts, excitations, steps=4000, batch=8192, lr=1e-3, seed=0, gammas=(0.25, 0.5, 0.75, 1.0),
-          errmax=1e-4, maxit=3000):
+          errmax=1e-4, maxit=3000, margin=0.95):
     """Train on the 2-ring targets of `contexts` (MLFMA objects whose exact
     neighbourhood inverse is built) with the library's kernels, then pick the
     damping gamma from CGS traces on the same bodies: the gamma whose
     iteration count, relative to the exact neighbourhood inverse's, is lowest
-    on average (0 = no correction if none helps)."""
+    on average, provided that average is below `margin` (0 = no correction
+    otherwise).  On bodies where M1 is already strong the traces differ by a
+    few per cent, and such a gamma did not carry over: on a held-out 123k-RWG
+    superellipsoid a gamma 4 % ahead of M1 on its training bodies left the
+    solve short of convergence."""
     import torch
     Xs, Ts = [], []
     for m in contexts:
@@ -163,7 +172,7 @@ def train(contexts, excitations, steps=4000, batch=8192, lr=1e-3, seed=0, gammas
     del X, T, Xs, Ts
     base = [_cgs_iters(m, b, errmax, maxit) for m, b in zip(contexts, excitations)]
     trace = {"exact": base}
-    best_g, best_r = 0.0, 1.0
+    best_g, best_r = 0.0, margin
     for g in gammas:
         its = []
         for m, b in zip(contexts, excitations):
@@ -183,17 +192,29 @@ def solve_with_fallback(m, b, lp: LearnedPreconditioner, plain_iters: int, errma
                         install_first=True):
     """CGS with the learned preconditioner, checked against the true FP64 MLFMA
     residual; if it has not converged within `plain_iters` iterations (the
-    count of the solve without a preconditioner), solve again with ILU0, the
-    reference's preconditioner.  install_first=False when lp is already
-    installed on m.  Returns the result dict with 'used'."""
+    count of the solve without a preconditioner), solve again with the exact
+    neighbourhood inverse M1 the correction was built on (when the correction
+    is not zero), then with ILU0, the reference's preconditioner.
+    install_first=False when lp is already installed on m.  Returns the
+    result dict with 'used'."""
     if install_first:
         lp.apply_to(m)
-    out = m.cgs(b, errmax=errmax, maxit=plain_iters, precond="nearinv")
-    rel = float(np.linalg.norm(m.matvec(out["x"]) - b) / np.linalg.norm(b))
-    if out["status"] == "converged" and rel < errmax * 1.01:
-        out["used"] = "learned"
+
+    def accepted(out):
+        rel = float(np.linalg.norm(m.matvec(out["x"]) - b) / np.linalg.norm(b))
         out["true_relres"] = rel
+        return out["status"] == "converged" and rel < errmax * 1.01
+
+    out = m.cgs(b, errmax=errmax, maxit=plain_iters, precond="nearinv")
+    if accepted(out):
+        out["used"] = "learned"
         return out
+    if getattr(lp, "gamma", 1.0) != 0.0 and hasattr(lp, "remove_from"):
+        lp.remove_from(m)
+        out = m.cgs(b, errmax=errmax, maxit=plain_iters, precond="nearinv")
+        if accepted(out):
+            out["used"] = "neighbourhood inverse"
+            return out
     ierr = m.ilu0()
     out = m.cgs(b, errmax=errmax, maxit=maxit, precond="ilu0" if ierr == 0 else "none")
     out["used"] = "ilu0" if ierr == 0 else "none"

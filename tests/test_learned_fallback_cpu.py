@@ -3,7 +3,8 @@ operator records the calls that solve_with_fallback makes.
 
 The rule: keep the learned solve when it converged within the
 unpreconditioned iteration count AND its true residual ||b - Z x|| / ||b||
-meets the tolerance; otherwise solve again with ILU0 (the reference's
+meets the tolerance; otherwise solve again with the exact neighbourhood
+inverse M1 under the correction (same test), then with ILU0 (the reference's
 preconditioner, crear_precond main.f90:851-902), or without a preconditioner
 when ILU0 meets a zero pivot."""
 import numpy as np
@@ -15,12 +16,17 @@ from lywell_gb300.learned import solve_with_fallback
 class FakeOperator:
     """Z = 2 I.  cgs() returns the scripted result for each preconditioner."""
 
-    def __init__(self, n, learned_status="converged", learned_x_scale=1.0, ilu0_ierr=0):
+    def __init__(self, n, learned_status="converged", learned_x_scale=1.0, ilu0_ierr=0, m1_status=None,
+                 m1_x_scale=None):
         self.n = n
         self.calls = []
         self.learned_status = learned_status
         self.learned_x_scale = learned_x_scale
         self.ilu0_ierr = ilu0_ierr
+        # the base M1 fails the same way unless told
+        self.m1_status = m1_status or learned_status
+        self.m1_x_scale = learned_x_scale if m1_x_scale is None else m1_x_scale
+        self.m1 = False                                # the correction removed
 
     def matvec(self, x):
         return 2.0 * x
@@ -31,6 +37,9 @@ class FakeOperator:
 
     def cgs(self, b, errmax=1e-4, maxit=1000, precond=0):
         self.calls.append(("cgs", precond, maxit))
+        if precond == "nearinv" and self.m1:
+            self.calls[-1] = ("cgs", "m1", maxit)
+            return dict(x=self.m1_x_scale * b / 2.0, iters=min(maxit, 9), relres=0.0, status=self.m1_status)
         if precond == "nearinv":
             return dict(x=self.learned_x_scale * b / 2.0, iters=min(maxit, 7), relres=0.0,
                         status=self.learned_status)
@@ -38,11 +47,18 @@ class FakeOperator:
 
 
 class FakeLearned:
-    def __init__(self):
+    def __init__(self, gamma=0.5):
         self.installed = 0
+        self.gamma = gamma
 
     def apply_to(self, m):
         self.installed += 1
+        m.m1 = False
+        return 0
+
+    def remove_from(self, m):
+        m.calls.append("remove")
+        m.m1 = True
         return 0
 
 
@@ -64,8 +80,24 @@ def test_falls_back_to_ilu0_past_the_plain_count(b):
     m, lp = FakeOperator(50, learned_status="maxit"), FakeLearned()
     out = solve_with_fallback(m, b, lp, plain_iters=1, maxit=900)
     assert out["used"] == "ilu0"
-    assert m.calls == [("cgs", "nearinv", 1), "ilu0", ("cgs", "ilu0", 900)]
+    assert m.calls == [("cgs", "nearinv", 1), "remove", ("cgs", "m1", 1), "ilu0", ("cgs", "ilu0", 900)]
     assert out["true_relres"] < 1e-15
+
+
+def test_falls_back_to_m1_first(b):
+    m, lp = FakeOperator(50, learned_status="maxit", m1_status="converged", m1_x_scale=1.0), FakeLearned()
+    out = solve_with_fallback(m, b, lp, plain_iters=30)
+    assert out["used"] == "neighbourhood inverse"
+    assert m.calls == [("cgs", "nearinv", 30), "remove", ("cgs", "m1", 30)]
+    assert out["true_relres"] < 1e-15
+
+
+def test_no_m1_retry_without_a_correction(b):
+    # gamma = 0: the learned solve already was the M1 solve
+    m, lp = FakeOperator(50, learned_status="maxit"), FakeLearned(gamma=0.0)
+    out = solve_with_fallback(m, b, lp, plain_iters=1, maxit=900)
+    assert out["used"] == "ilu0"
+    assert "remove" not in m.calls
 
 
 def test_falls_back_when_true_residual_misses(b):
