@@ -2,6 +2,7 @@
 symbol include/lywell_mlfma.h declares, validates arguments on the host, and
 its RWG builder reproduces the oracle's restatement of the reference bit for
 bit."""
+import ctypes as C
 import os
 import re
 
@@ -36,7 +37,6 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_init_rejects_bad_arguments(lib):
-    import ctypes as C
     h = C.c_void_p()
     rc = lib.mlf_init(C.byref(h), None, 0, None, None, None, None, None, None, None, None, None, 0, 0, None,
                       1.0, 0.5, 0)
@@ -47,6 +47,13 @@ def test_init_rejects_bad_arguments(lib):
 def test_null_context_calls_fail_cleanly(lib):
     assert lib.mlf_matvec(None, None, None, 1, 1) == -1
     assert lib.mlf_cgs(None, None, None, 1e-3, 10, 1, None, None, None, 0, None) == -1
+    # tuning and diagnostics entry points: argument checks before any device work
+    out = (C.c_double * 7)()
+    assert lib.mlf_solve_phases(None, out, 7) == -1
+    assert lib.mlf_set_lu_split(None, 1024) == -1
+    a, b = C.c_int(), C.c_int()
+    assert lib.mlf_get_lu_split(None, C.byref(a), C.byref(b)) == -1
+    assert lib.mlf_set_block_engine(None, 4, 0) == -1
 
 
 @pytest.mark.parametrize("body", ["ico3", "spheroid", "superellipsoid"])
