@@ -144,6 +144,19 @@ def _cgs_iters(m, b, errmax, maxit):
     return int(out["iters"]) if out["status"] == "converged" else maxit + 1
 
 
+def choose_gamma(base, traces, margin=0.95):
+    """The damping factor from CGS iteration counts: `base` the exact M1's count
+    per training body, `traces` {gamma: counts per body}.  The gamma with the
+    lowest mean count relative to M1, if that mean is below `margin`; else 0
+    (M1 itself).  Returns (gamma, its mean ratio)."""
+    best_g, best_r = 0.0, float(margin)
+    for g, its in traces.items():
+        r = float(np.mean([i / b0 for i, b0 in zip(its, base)]))
+        if r < best_r:
+            best_g, best_r = float(g), r
+    return best_g, best_r
+
+
 def train(contexts, excitations, steps=4000, batch=8192, lr=1e-3, seed=0, gammas=(0.25, 0.5, 0.75, 1.0),
           errmax=1e-4, maxit=3000, margin=0.95):
     """Train on the 2-ring targets of `contexts` (MLFMA objects whose exact
@@ -172,7 +185,6 @@ def train(contexts, excitations, steps=4000, batch=8192, lr=1e-3, seed=0, gammas
     del X, T, Xs, Ts
     base = [_cgs_iters(m, b, errmax, maxit) for m, b in zip(contexts, excitations)]
     trace = {"exact": base}
-    best_g, best_r = 0.0, margin
     for g in gammas:
         its = []
         for m, b in zip(contexts, excitations):
@@ -180,9 +192,7 @@ def train(contexts, excitations, steps=4000, batch=8192, lr=1e-3, seed=0, gammas
             its.append(_cgs_iters(m, b, errmax, maxit))
             install(m, net, 0.0)              # back to the exact M1 (kept under the correction)
         trace[g] = its
-        r = float(np.mean([i / b0 for i, b0 in zip(its, base)]))
-        if r < best_r:
-            best_g, best_r = g, r
+    best_g, _ = choose_gamma(base, {g: trace[g] for g in gammas}, margin)
     lp = LearnedPreconditioner(net, tscale, best_g, trace)
     lp.loss_history = hist
     return lp

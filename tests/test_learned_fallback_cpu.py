@@ -1,5 +1,7 @@
-"""Host logic of the learned preconditioner's fallback (no GPU): a stand-in
-operator records the calls that solve_with_fallback makes.
+"""Host logic of the learned preconditioner (no GPU): the fallback, with a
+stand-in operator recording the calls that solve_with_fallback makes, and
+the damping choice from training traces (choose_gamma, fed the iteration
+counts measured on the GB300).
 
 The rule: keep the learned solve when it converged within the
 unpreconditioned iteration count AND its true residual ||b - Z x|| / ||b||
@@ -10,7 +12,7 @@ when ILU0 meets a zero pivot."""
 import numpy as np
 import pytest
 
-from lywell_gb300.learned import solve_with_fallback
+from lywell_gb300.learned import choose_gamma, solve_with_fallback
 
 
 class FakeOperator:
@@ -113,3 +115,25 @@ def test_no_preconditioner_when_ilu0_has_a_zero_pivot(b):
     out = solve_with_fallback(m, b, lp, plain_iters=5)
     assert out["used"] == "none"
     assert m.calls[-1] == ("cgs", "none", 5000)
+
+
+# ---- the damping choice from training traces (CGS iterations per body)
+
+def test_gamma_with_a_clear_gain_is_chosen():
+    # 7680-RWG superellipsoids: M1 1012, 1754, 231; gamma 0.5 a third of that
+    base = [1012, 1754, 231]
+    traces = {0.25: [560, 1122, 230], 0.5: [336, 645, 221], 0.75: [473, 604, 222], 1.0: [3001, 2874, 240]}
+    g, r = choose_gamma(base, traces)
+    assert g == 0.5 and r < 0.6
+
+
+def test_gamma_within_the_margin_falls_back_to_m1():
+    # 30 720-RWG superellipsoids at 60 bases per box: M1 231, 128, 90; the best gamma 4 % ahead
+    base = [231, 128, 90]
+    traces = {0.25: [222, 133, 99], 0.5: [222, 125, 87], 0.75: [222, 125, 85], 1.0: [230, 143, 104]}
+    assert choose_gamma(base, traces)[0] == 0.0
+    assert choose_gamma(base, traces, margin=1.0)[0] == 0.75
+
+
+def test_no_gamma_helps():
+    assert choose_gamma([100, 100], {0.5: [120, 110], 1.0: [150, 101]})[0] == 0.0
