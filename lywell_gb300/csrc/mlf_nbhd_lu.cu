@@ -663,30 +663,37 @@ static int blocked_inverse_rows(Ctx* c, int nownmax, const LuRing* ring, const i
     std::vector<cudaStream_t> bs(nstream, nullptr);
     std::vector<float2*> bslab(nstream, nullptr);
     int* bscr = nullptr;
+    int st = MLF_OK;
     if (nbig) {
         const int n0 = nsize(order[0]);
         const size_t bslab_el = (size_t)n0 * n0 + (size_t)n0 * nownmax;
-        CK(ds.alloc(&bscr, (size_t)nstream * (LU_P + 1) * sizeof(int)));
-        for (int q = 0; q < nstream; ++q) {
-            CK(ds.alloc(&bslab[q], bslab_el * sizeof(float2)));
-            CK(cudaStreamCreateWithFlags(&bs[q], cudaStreamNonBlocking));
-        }
+        if (!cuda_ok(c, ds.alloc(&bscr, (size_t)nstream * (LU_P + 1) * sizeof(int)), "large-box scratch"))
+            st = MLF_E_CUDA;
+        for (int q = 0; q < nstream && !st; ++q)
+            if (!cuda_ok(c, ds.alloc(&bslab[q], bslab_el * sizeof(float2)), "large-box slab") ||
+                !cuda_ok(c, cudaStreamCreateWithFlags(&bs[q], cudaStreamNonBlocking), "large-box stream"))
+                st = MLF_E_CUDA;
     }
-    int st = MLF_OK;
     // the persistent kernel over the other boxes: two CTAs per SM, the slabs
     // within half of the free device memory
-    if (nsmall) {
+    if (nsmall && !st) {
         const int ns0 = nsize(order[nbig]);
         const size_t slab = (size_t)ns0 * ns0 + (size_t)ns0 * nownmax;
         size_t fr = 0, tot = 0;
-        CK(cudaMemGetInfo(&fr, &tot));
-        const size_t cap = (fr / 2) / (slab * sizeof(float2));
-        const int grid = (int)std::max<size_t>(1, std::min<size_t>({(size_t)2 * nsm, (size_t)nsmall, cap}));
         float2* work = nullptr;
-        CK(ds.alloc(&work, slab * grid * sizeof(float2)));
-        k_nbhd_lu32<<<grid, LU_THREADS, 0, c->stream>>>(nsmall, c->dbox_ptr, c->dperm, c->dia, c->dja, c->dZ, slab,
-                                                        work, c->dMinv, dorder, dctr, dbad, rg);
-        if (!cuda_ok(c, cudaGetLastError(), "neighbourhood LU")) st = MLF_E_CUDA;
+        if (!cuda_ok(c, cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo")) {
+            st = MLF_E_CUDA;
+        } else {
+            const size_t cap = (fr / 2) / (slab * sizeof(float2));
+            const int grid = (int)std::max<size_t>(1, std::min<size_t>({(size_t)2 * nsm, (size_t)nsmall, cap}));
+            if (!cuda_ok(c, ds.alloc(&work, slab * grid * sizeof(float2)), "neighbourhood LU slabs")) {
+                st = MLF_E_CUDA;
+            } else {
+                k_nbhd_lu32<<<grid, LU_THREADS, 0, c->stream>>>(nsmall, c->dbox_ptr, c->dperm, c->dia, c->dja, c->dZ,
+                                                                slab, work, c->dMinv, dorder, dctr, dbad, rg);
+                if (!cuda_ok(c, cudaGetLastError(), "neighbourhood LU")) st = MLF_E_CUDA;
+            }
+        }
     }
     for (int k = 0; k < nbig && !st; ++k) {
         const int q = k % nstream, b = order[k];
@@ -696,10 +703,14 @@ static int blocked_inverse_rows(Ctx* c, int nownmax, const LuRing* ring, const i
         st = big_box_launch(c, rg, b, n, nown, S, bslab[q], scr, scr + LU_P, dbad, bs[q]);
     }
     for (int q = 0; q < nstream; ++q) {
+        if (!bs[q]) continue;
         if (!cuda_ok(c, cudaStreamSynchronize(bs[q]), "large-box LU") && !st) st = MLF_E_CUDA;
         cudaStreamDestroy(bs[q]);
     }
-    if (st) return st;
+    if (st) {
+        cudaStreamSynchronize(c->stream);   // the persistent kernel, if launched, ends before its slabs go
+        return st;
+    }
     int hbad = 0;
     CK(cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
