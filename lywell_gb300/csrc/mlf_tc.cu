@@ -733,7 +733,25 @@ void tc_free(Ctx* c) {
 
 // FP16 operand of a matrix on the near pattern (the near field Z or the
 // preconditioner M) from its box-pair blocks: per-row scales, then the rows
+static void tc_operand_free(TcOperand* op) {
+    if (op->hi) cudaFree(op->hi);
+    if (op->lo) cudaFree(op->lo);
+    if (op->rinv) cudaFree(op->rinv);
+    op->hi = op->lo = nullptr;
+    op->rinv = nullptr;
+}
+
+static int tc_near_operand_build(Ctx* c, const float2* blk, TcOperand* op, cudaStream_t s);
+
+// built completely or not at all (a later call would otherwise take a half-built
+// operand for a ready one)
 static int tc_near_operand(Ctx* c, const float2* blk, TcOperand* op, cudaStream_t s) {
+    const int st = tc_near_operand_build(c, blk, op, s);
+    if (st) tc_operand_free(op);
+    return st;
+}
+
+static int tc_near_operand_build(Ctx* c, const float2* blk, TcOperand* op, cudaStream_t s) {
     TcState* t = c->tc;
     const size_t bytes = (size_t)std::max<long long>(t->zrows, 1) * 128;
     CK(cudaMalloc(&op->hi, bytes));
@@ -754,9 +772,18 @@ static int tc_near_operand(Ctx* c, const float2* blk, TcOperand* op, cudaStream_
     return MLF_OK;
 }
 
-// tiles, chunk tables and the Z operand (needs the box-pair blocks)
+static int tc_setup_build(Ctx* c);
+
+// tiles, chunk tables and the Z operand (needs the box-pair blocks); on a
+// failure nothing is kept, so that the next call starts over
 static int tc_setup(Ctx* c) {
     if (c->tc) return MLF_OK;
+    const int st = tc_setup_build(c);
+    if (st) tc_free(c);
+    return st;
+}
+
+static int tc_setup_build(Ctx* c) {
     int st;
     if ((st = device_blocks_ready(c))) return st;
     const int nb = (int)c->box_ptr.size() - 1;
@@ -1061,11 +1088,7 @@ int device_recv_tc(Ctx* c, const float2* R, int K, const float2* A, float facy, 
 void tc_drop_precond(Ctx* c) {
     TcState* t = c->tc;
     if (!t) return;
-    if (t->M.hi) cudaFree(t->M.hi);
-    if (t->M.lo) cudaFree(t->M.lo);
-    if (t->M.rinv) cudaFree(t->M.rinv);
-    t->M.hi = t->M.lo = nullptr;
-    t->M.rinv = nullptr;
+    tc_operand_free(&t->M);
 }
 
 // error flag of the tensor-core kernels since the last check (0: none)
